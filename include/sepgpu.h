@@ -1,0 +1,92 @@
+/*
+ * sepgpu.h - entry points this GPU implementation adds to the sep C API.
+ *
+ * None of these has a counterpart in the reference library; the reference
+ * hot-path calls keep their meaning (see the other headers).  Programs that
+ * only use the reference calls need nothing from this header.
+ *
+ * Residency.  The particle state of a seppart array lives on the GPU from the
+ * first hot-path call on.  The host copy in the array is refreshed at these
+ * observation points: sep_eval_mom(), sep_save_xyz(), sep_gpu_sync() and
+ * every library call that reads particle data on the host.  The sepret and
+ * the sepsys counters are current after every sep_leapfrog().  A program that
+ * writes atoms[i].x/v/f/m/z/type directly after the first hot-path call must
+ * call sep_gpu_invalidate() before the next library call.
+ */
+#ifndef SEP_GB300_SEPGPU_H
+#define SEP_GB300_SEPGPU_H
+
+#include "sepstrct.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* 1 when a CUDA device is usable, else 0. */
+int sep_gpu_available(void);
+
+/* Last device error message (empty when none). */
+const char *sep_gpu_error(void);
+
+/* Observation point: copy the device state into the seppart array. */
+int sep_gpu_sync(seppart *ptr);
+
+/* The seppart array was changed directly on the host: upload it before the
+ * next device call. */
+int sep_gpu_invalidate(seppart *ptr);
+
+/*
+ * Device-resident MD loop: nsteps repetitions of
+ *     sep_reset_retval; sep_reset_force;
+ *     sep_force_pairs(types, cf, fun, opt)   (fun != NULL)
+ *       or sep_force_lj(types, ljparam, opt) (fun == NULL);
+ *     [sep_nosehoover(T0, alpha, tau)]       (nh != 0);
+ *     sep_leapfrog;
+ * captured once in a CUDA graph whose neighbour-list rebuild is a
+ * conditional node decided on the device.  On return ret holds the last
+ * step's values, *alpha the thermostat state and sys the counters, exactly as
+ * after the equivalent call sequence.  Returns 0 on success.
+ */
+int sep_gpu_run(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
+		double (*fun)(double, char), const double *ljparam, double cf,
+		unsigned opt, int nh, double T0, double *alpha, double tau, long nsteps);
+
+/* Lanes per particle in the pair kernels: 1, 2 or 4 (default chosen by size). */
+int sep_gpu_set_tpp(seppart *ptr, int tpp);
+
+/* Diagnostics. */
+typedef struct {
+	long launches;        /* kernel launches issued for this system */
+	long list_builds;     /* neighbour-list builds */
+	int list_capacity;    /* neighbour slots per particle */
+	int list_max;         /* largest neighbour count of the current list */
+	double list_mean;     /* mean neighbour count (full list) */
+	int tpp;
+} sep_gpu_info;
+
+int sep_gpu_info_get(seppart *ptr, sep_gpu_info *info);
+
+/* Unordered neighbour pairs (i < j, user indices, sorted) of the current
+ * full list; returns the count (pairs filled up to cap), negative on error. */
+long sep_gpu_list_pairs(seppart *ptr, int *pairs, long cap);
+
+/* Events on the library's stream, for timing from the caller: record event
+ * e (0..7) / elapsed milliseconds between two recorded events. */
+int sep_gpu_event_record(seppart *ptr, int e);
+int sep_gpu_event_elapsed(seppart *ptr, int e0, int e1, float *ms);
+int sep_gpu_stream_sync(seppart *ptr);
+
+/*
+ * Timing helper: run nsteps steps of the sep_gpu_run loop from the host
+ * (rebuilds outside the timed brackets) and return the mean duration of the
+ * fused step kernel in ms, measured with events around each launch.
+ */
+int sep_gpu_time_step_kernel(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
+			     double (*fun)(double, char), const double *ljparam, double cf,
+			     unsigned opt, int nh, double T0, double *alpha, double tau,
+			     long nsteps, double *ms_per_launch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

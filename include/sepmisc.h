@@ -1,0 +1,84 @@
+/*
+ * sepmisc.h - helper macros, the built-in pair potentials and the small
+ * utilities of the sep C API that the MD-step hot path uses.
+ *
+ * Declarations follow the reference's include/sepmisc.h; each entry names
+ * the line of the reference declaration it stands in for.
+ */
+#ifndef SEP_GB300_SEPMISC_H
+#define SEP_GB300_SEPMISC_H
+
+#include <stdio.h>
+#include <stdlib.h>
+#include <stdarg.h>
+#include <string.h>
+#include <math.h>
+#include <time.h>
+#include <float.h>
+#include "sepdef.h"
+#include "sepstrct.h"
+
+/* Macros programs use (reference include/sepmisc.h:39-95). */
+#define SEP_FLUSH fflush(stdout)
+#define SEP_TICTOC clock_t time_then
+#define SEP_TIC time_then = clock()
+#define SEP_TOC ((int)(1000*(clock()-time_then)/CLOCKS_PER_SEC))%1000
+#define sep_rand() ( rand()/(RAND_MAX+1.0) )
+#define sep_here(x) { printf("%d\n", x); SEP_FLUSH; }
+#define sep_Sq(x) ( (x)*(x) )
+#define sep_Abs(x) ( (x) > 0.0 ? (x) : -(x) )
+/* minimum-image wrap of one component x of a separation in a box of length y */
+#define sep_Wrap(x, y) { if ( (x) > 0.5*(y) ) (x) -= (y); else if ( (x) < -0.5*(y) ) (x) += (y); }
+/* periodic wrap of one position component into [0, y) */
+#define sep_Periodic(x, y) { if ( (x) > (y) ) (x) -= (y); else if ( (x) < 0.0 ) (x) += (y); }
+
+/* Prints "sep-error -> message" and exits with EXIT_FAILURE (reference :101). */
+void sep_error(char *str, ...);
+/* Prints "sep-warning -> message" and continues (reference :108). */
+void sep_warning(char *str, ...);
+
+/*
+ * Built-in pair potentials, f(r^2, 'f') = -dU/dr / r and f(r^2, 'u') = U
+ * (reference :115-136).  Passing one of these to sep_force_pairs() selects the
+ * matching device kernel; any other function is tabulated on the host.
+ */
+double sep_lj(double r2, char opt);
+double sep_lj_shift(double r2, char opt);
+double sep_wca(double r2, char opt);
+double sep_spring_x0(double r2, char opt);
+
+/* Writes the particles of the listed types as xyz text (reference :164). */
+void sep_save_xyz(seppart *ptr, const char *partnames, const char *file,
+		  char *mode, sepsys *sys);
+
+/* Zeroes the forces and sys->max_dist2 (reference :245). */
+void sep_reset_force(seppart *ptr, sepsys *sys);
+/* Zeroes the molecular force matrix (reference :252). */
+void sep_reset_force_mol(sepsys *sys);
+
+/* Counts the particles of one type (reference :285). */
+int sep_count_type(seppart *ptr, char type, int npart);
+
+/* Marks the system as threaded; the GPU path ignores the thread count (reference :303). */
+void sep_set_omp(unsigned nthreads, sepsys *sys);
+/* Sets the neighbour-list skin (reference :311). */
+void sep_set_skin(sepsys *sys, double value);
+
+/* Sets mass or charge of every particle of a type (reference :320-330). */
+void sep_set_charge(seppart *ptr, char type, double z, sepsys sys);
+void sep_set_mass(seppart *ptr, char type, double m, sepsys sys);
+
+/* Removes the centre-of-mass momentum of one type (reference :338). */
+void sep_reset_momentum(seppart *ptr, const char type, sepsys *sys);
+void sep_set_ndof(size_t ndof, sepsys *sys);
+void sep_set_x0(seppart *ptr, int npart);
+void sep_set_xn(seppart *ptr, int npart);
+
+/* Number of linked-list cells along a box edge (reference :431). */
+int sep_nsubbox(double cf, double delta, double lbox);
+double sep_box_length(double dens, int npart, int ndim);
+
+/* Mean momentum per degree of freedom (reference :434). */
+double sep_eval_mom(seppart *ptr, int npart);
+
+#endif

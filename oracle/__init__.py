@@ -1,0 +1,226 @@
+"""CPU oracle for the seplib MD-step hot path -- TEST INFRASTRUCTURE ONLY.
+
+numpy front end to ``oracle/lib/libsepora.so`` (built from sepora.c by
+oracle/Makefile), the FP64 restatement of the reference algorithms that the
+GPU library is checked against.  Only tests/, ``__graft_entry__.smoke()`` and
+bench.py's CPU-baseline leg may import this package; the product never does.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "lib", "libsepora.so")
+REF_LIB = os.path.join(HERE, "_ref", "libsepref.so")
+
+EXCL_NONE, EXCL_BONDS, EXCL_ALLBONDED, EXCL_SAMEMOL = 0, 1, 2, 3
+POT_LJ, POT_LJSHIFT, POT_WCA, POT_LJPARAM = 0, 1, 2, 3
+
+_lib = None
+
+
+def build(ref=False):
+    """Compile the restatement (and, if `ref`, the reference library)."""
+    targets = ["all"] + (["ref"] if ref else [])
+    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        _lib = C.CDLL(LIB)
+        d, dp, ip, lp, up, cp = (C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_int),
+                                 C.POINTER(C.c_long), C.POINTER(C.c_uint), C.c_char_p)
+        _lib.ora_pairs_brute.restype = C.c_long
+        _lib.ora_pairs_brute.argtypes = [C.c_long, dp, dp, d, C.c_int, ip, ip, ip, ip, ip, C.c_long]
+        _lib.ora_pairs_llist.restype = C.c_long
+        _lib.ora_pairs_llist.argtypes = [C.c_long, dp, dp, ip, d, d, C.c_int, ip, ip, ip, ip,
+                                         lp, ip, C.c_long]
+        _lib.ora_pair_forces.restype = None
+        _lib.ora_pair_forces.argtypes = [C.c_long, dp, cp, dp, cp, C.c_int, dp, d, lp, ip, dp, dp, dp]
+        _lib.ora_coulomb_sf.restype = None
+        _lib.ora_coulomb_sf.argtypes = [C.c_long, dp, dp, dp, d, lp, ip, dp, dp, dp]
+        _lib.ora_nosehoover.restype = None
+        _lib.ora_nosehoover.argtypes = [C.c_long, dp, dp, dp, d, dp, d, d]
+        _lib.ora_leapfrog.restype = C.c_int
+        _lib.ora_leapfrog.argtypes = [C.c_long, dp, dp, dp, dp, dp, ip, ip, dp, dp, d, d, dp, dp, dp]
+        _lib.ora_stretch_harmonic.restype = None
+        _lib.ora_stretch_harmonic.argtypes = [C.c_long, up, C.c_int, d, d, dp, dp, dp, dp, dp, dp]
+        _lib.ora_angles.restype = None
+        _lib.ora_angles.argtypes = [C.c_long, up, C.c_int, d, d, C.c_int, dp, dp, dp, dp]
+        _lib.ora_torsion_rb.restype = None
+        _lib.ora_torsion_rb.argtypes = [C.c_long, up, C.c_int, dp, dp, dp, dp, dp]
+        _lib.ora_run_lj.restype = C.c_int
+        _lib.ora_run_lj.argtypes = [C.c_long, dp, dp, dp, cp, dp, C.c_int, dp, d, d, d, C.c_long,
+                                    C.c_int, d, d, dp, C.c_int, dp, dp]
+        _lib.ora_nsubbox.restype = C.c_int
+        _lib.ora_nsubbox.argtypes = [d, d, d]
+    return _lib
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct)) if a is not None else None
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _excl_args(n, molindex, bond, angle, dihed):
+    mi = _i32(molindex if molindex is not None else -np.ones(n))
+    b = _i32(bond if bond is not None else -np.ones((n, 10)))
+    a = _i32(angle if angle is not None else -np.ones((n, 10)))
+    dh = _i32(dihed if dihed is not None else -np.ones((n, 20)))
+    return mi, b, a, dh
+
+
+def pairs_brute(x, L, rlist, excl=EXCL_NONE, molindex=None, bond=None, angle=None, dihed=None):
+    """Sorted (i<j) FP64 pair set within rlist (min image), shape (npairs, 2)."""
+    x = _f64(x); n = len(x); L = _f64(L)
+    mi, b, a, dh = _excl_args(n, molindex, bond, angle, dihed)
+    cap = max(1024, int(n * 80))
+    while True:
+        out = np.empty((cap, 2), np.int32)
+        np_ = lib().ora_pairs_brute(n, _p(x, C.c_double), _p(L, C.c_double), rlist, excl,
+                                    _p(mi, C.c_int), _p(b, C.c_int), _p(a, C.c_int),
+                                    _p(dh, C.c_int), _p(out, C.c_int), cap)
+        if np_ <= cap:
+            return out[:np_]
+        cap = np_
+
+
+def llist(x, L, nsub, cf, skin, excl=EXCL_NONE, molindex=None, bond=None, angle=None, dihed=None):
+    """The reference's linked-cell half list as CSR (start[n+1], nb)."""
+    x = _f64(x); n = len(x); L = _f64(L); ns = _i32(nsub)
+    mi, b, a, dh = _excl_args(n, molindex, bond, angle, dihed)
+    start = np.zeros(n + 1, np.int64)
+    cap = max(1024, int(n * 120))
+    while True:
+        nb = np.empty(cap, np.int32)
+        r = lib().ora_pairs_llist(n, _p(x, C.c_double), _p(L, C.c_double), _p(ns, C.c_int), cf,
+                                  skin, excl, _p(mi, C.c_int), _p(b, C.c_int), _p(a, C.c_int),
+                                  _p(dh, C.c_int), _p(start, C.c_long), _p(nb, C.c_int), cap)
+        if r >= 0:
+            return start, nb[:start[-1]]
+        cap = int(start[-1]) + 16
+
+
+def csr_from_pairs(n, pairs):
+    """CSR half list from an (npairs, 2) array, grouped by the first index."""
+    pairs = np.asarray(pairs)
+    order = np.lexsort((pairs[:, 1], pairs[:, 0]))
+    p = pairs[order]
+    start = np.zeros(n + 1, np.int64)
+    np.add.at(start, p[:, 0] + 1, 1)
+    return np.cumsum(start), _i32(p[:, 1])
+
+
+def pair_forces(x, types_arr, L, types, kind, param, cf, start, nb):
+    """(f (n,3), epot, potP (3,3)) of one pair term over a CSR half list."""
+    x = _f64(x); n = len(x); L = _f64(L)
+    t = np.ascontiguousarray(types_arr, dtype="S1")
+    p = _f64(param if param is not None else np.zeros(4))
+    f = np.zeros((n, 3)); e = C.c_double(0.0); pP = np.zeros(9)
+    lib().ora_pair_forces(n, _p(x, C.c_double), t.ctypes.data_as(C.c_char_p), _p(L, C.c_double),
+                          types.encode() if isinstance(types, str) else types, kind,
+                          _p(p, C.c_double), cf, _p(_as_long(start), C.c_long),
+                          _p(_i32(nb), C.c_int), _p(f, C.c_double), C.byref(e), _p(pP, C.c_double))
+    return f, e.value, pP.reshape(3, 3)
+
+
+def _as_long(a):
+    return np.ascontiguousarray(a, dtype=np.int64)
+
+
+def coulomb_sf(x, z, L, cf, start, nb):
+    x = _f64(x); n = len(x); L = _f64(L); z = _f64(z)
+    f = np.zeros((n, 3)); e = C.c_double(0.0); pP = np.zeros(9)
+    lib().ora_coulomb_sf(n, _p(x, C.c_double), _p(z, C.c_double), _p(L, C.c_double), cf,
+                         _p(_as_long(start), C.c_long), _p(_i32(nb), C.c_int),
+                         _p(f, C.c_double), C.byref(e), _p(pP, C.c_double))
+    return f, e.value, pP.reshape(3, 3)
+
+
+def nosehoover(v, m, f, T0, alpha, tau, dt):
+    """Returns (f_new, alpha_new)."""
+    v = _f64(v); m = _f64(m); f = _f64(f).copy(); a = C.c_double(alpha)
+    lib().ora_nosehoover(len(v), _p(v, C.c_double), _p(m, C.c_double), _p(f, C.c_double),
+                         T0, C.byref(a), tau, dt)
+    return f, a.value
+
+
+class LeapState:
+    """Mutable per-particle state for ora_leapfrog."""
+
+    def __init__(self, x, v, m):
+        n = len(x)
+        self.x = _f64(x).copy(); self.v = _f64(v).copy(); self.m = _f64(m)
+        self.a = np.zeros((n, 3)); self.cn = np.zeros((n, 3), np.int32)
+        self.cr = np.zeros((n, 3), np.int32); self.xn = np.zeros((n, 3))
+
+
+def leapfrog(st, f, L, dt, skin, max_dist2=0.0):
+    """Advance LeapState in place; returns (flag, max_dist2, ekin, kinP)."""
+    md = C.c_double(max_dist2); ek = C.c_double(0.0); kP = np.zeros(9)
+    f = _f64(f); L = _f64(L)
+    flag = lib().ora_leapfrog(len(st.x), _p(st.x, C.c_double), _p(st.v, C.c_double),
+                              _p(f, C.c_double), _p(st.a, C.c_double), _p(st.m, C.c_double),
+                              _p(st.cn, C.c_int), _p(st.cr, C.c_int), _p(st.xn, C.c_double),
+                              _p(L, C.c_double), dt, skin, C.byref(md), C.byref(ek),
+                              _p(kP, C.c_double))
+    return flag, md.value, ek.value, kP.reshape(3, 3)
+
+
+def stretch_harmonic(blist, btype, l0, ks, x, L):
+    x = _f64(x); n = len(x); L = _f64(L); bl = np.ascontiguousarray(blist, np.uint32)
+    f = np.zeros((n, 3)); e = C.c_double(0.0); pP = np.zeros(9); pB = np.zeros(9)
+    lib().ora_stretch_harmonic(len(bl) // 3, _p(bl, C.c_uint), btype, l0, ks, _p(x, C.c_double),
+                               _p(L, C.c_double), _p(f, C.c_double), C.byref(e),
+                               _p(pP, C.c_double), _p(pB, C.c_double))
+    return f, e.value, pP.reshape(3, 3), pB.reshape(3, 3)
+
+
+def angles(alist, atype, angle0, k, cossq, x, L):
+    x = _f64(x); n = len(x); L = _f64(L); al = np.ascontiguousarray(alist, np.uint32)
+    f = np.zeros((n, 3)); e = C.c_double(0.0)
+    lib().ora_angles(len(al) // 4, _p(al, C.c_uint), atype, angle0, k, int(cossq),
+                     _p(x, C.c_double), _p(L, C.c_double), _p(f, C.c_double), C.byref(e))
+    return f, e.value
+
+
+def torsion_rb(dlist, dtype_, g, x, L):
+    x = _f64(x); n = len(x); L = _f64(L); dl = np.ascontiguousarray(dlist, np.uint32)
+    g = _f64(g); f = np.zeros((n, 3)); e = C.c_double(0.0)
+    lib().ora_torsion_rb(len(dl) // 5, _p(dl, C.c_uint), dtype_, _p(g, C.c_double),
+                         _p(x, C.c_double), _p(L, C.c_double), _p(f, C.c_double), C.byref(e))
+    return f, e.value
+
+
+def run_lj(x, v, m, types_arr, L, kind, param, cf, skin, dt, nsteps, nh=False, T0=1.0,
+           tau=1.0, alpha=0.0, nthreads=0, trace=False):
+    """Full LJ loop; returns dict(x, v, alpha, epot, ekin, potP, kinP, nupdate, etot)."""
+    x = _f64(x).copy(); v = _f64(v).copy(); m = _f64(m); L = _f64(L)
+    t = np.ascontiguousarray(types_arr, dtype="S1")
+    p = _f64(param if param is not None else np.zeros(4))
+    a = C.c_double(alpha); out = np.zeros(21)
+    tr = np.zeros(nsteps) if trace else None
+    rc = lib().ora_run_lj(len(x), _p(x, C.c_double), _p(v, C.c_double), _p(m, C.c_double),
+                          t.ctypes.data_as(C.c_char_p), _p(L, C.c_double), kind,
+                          _p(p, C.c_double), cf, skin, dt, nsteps, int(nh), T0, tau, C.byref(a),
+                          nthreads, _p(tr, C.c_double), _p(out, C.c_double))
+    if rc != 0:
+        raise MemoryError("ora_run_lj")
+    return dict(x=x, v=v, alpha=a.value, epot=out[0], ekin=out[1], potP=out[2:11].reshape(3, 3),
+                kinP=out[11:20].reshape(3, 3), nupdate=int(out[20]), etot=tr)
+
+
+def nsubbox(cf, delta, L):
+    return lib().ora_nsubbox(cf, delta, L)

@@ -1,0 +1,578 @@
+/*
+ * sepora.c - CPU ORACLE for the seplib MD-step hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file restates, in plain FP64 C99 on
+ * structure-of-arrays inputs, the algorithms of the reference library's
+ * hot path so that the GPU library can be checked against them.  Nothing in
+ * the product (seplib_gb300/) links or calls it; only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg do.
+ *
+ * Parity is pinned two ways: tests/test_oracle_golden.py checks these
+ * functions against golden vectors produced by the reference library itself
+ * (tests/golden/make_golden.py, which drives oracle/_ref/libsepref.so built
+ * from the reference sources by oracle/Makefile), and, where the reference
+ * sources are present, directly against that library.
+ *
+ * Layout: x, v, f are 3*n doubles, particle-major (x[3*i+k]).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORA_BOND 10
+#define ORA_ANGLE 10
+#define ORA_DIHED 20
+
+/* exclusion rules, see ora_excluded() */
+enum { ORA_EXCL_NONE = 0, ORA_EXCL_BONDS = 1, ORA_EXCL_ALLBONDED = 2, ORA_EXCL_SAMEMOL = 3 };
+
+/* minimum image of one separation component; reference include/sepmisc.h:81-85
+ * (strict comparisons against L/2) */
+static inline double ora_wrap(double d, double L)
+{
+	if (d > 0.5 * L) return d - L;
+	if (d < -0.5 * L) return d + L;
+	return d;
+}
+
+static inline double ora_sep(const double *x, long i, long j, const double L[3], double d[3])
+{
+	double r2 = 0.0;
+	for (int k = 0; k < 3; k++) {
+		d[k] = ora_wrap(x[3 * i + k] - x[3 * j + k], L[k]);
+		r2 += d[k] * d[k];
+	}
+	return r2;
+}
+
+/* membership of j in a -1 terminated partner array of length cap;
+ * equivalent to the reference's pairwise scan in source/sepprfrc.c:703-733 for
+ * the symmetric partner relations the topology reader builds */
+static int ora_in_list(const int *lst, int cap, long j)
+{
+	for (int k = 0; k < cap && lst[k] != -1; k++)
+		if (lst[k] == j) return 1;
+	return 0;
+}
+
+/*
+ * Exclusion predicate.
+ *  ORA_EXCL_BONDS     - sep_bond_share only (source/sepprfrc.c:703-711), used by
+ *                       the brute pair force and the O(N^2) list for SEP_EXCL_BONDED
+ *                       (source/sepprfrc.c:35, :317)
+ *  ORA_EXCL_ALLBONDED - sep_bonded = bond + angle + dihedral partners
+ *                       (source/sepprfrc.c:736-740), used by the linked-cell list
+ *                       (:582) and by the brute SF Coulomb (source/sepcoulomb.c:39)
+ *  ORA_EXCL_SAMEMOL   - same molindex and not -1 (source/sepprfrc.c:38-41, :666)
+ */
+int ora_excluded(int mode, long i, long j, const int *molindex,
+		 const int *bond, const int *angle, const int *dihed)
+{
+	switch (mode) {
+	case ORA_EXCL_BONDS:
+		return ora_in_list(bond + ORA_BOND * i, ORA_BOND, j) ||
+		       ora_in_list(bond + ORA_BOND * j, ORA_BOND, i);
+	case ORA_EXCL_ALLBONDED:
+		return ora_in_list(bond + ORA_BOND * i, ORA_BOND, j) ||
+		       ora_in_list(angle + ORA_ANGLE * i, ORA_ANGLE, j) ||
+		       ora_in_list(dihed + ORA_DIHED * i, ORA_DIHED, j) ||
+		       ora_in_list(bond + ORA_BOND * j, ORA_BOND, i) ||
+		       ora_in_list(angle + ORA_ANGLE * j, ORA_ANGLE, i) ||
+		       ora_in_list(dihed + ORA_DIHED * j, ORA_DIHED, i);
+	case ORA_EXCL_SAMEMOL:
+		return molindex[i] != -1 && molindex[i] == molindex[j];
+	default:
+		return 0;
+	}
+}
+
+/*
+ * All unordered pairs (i < j) closer than rlist under the minimum image,
+ * O(N^2) in FP64.  Restates the brute-force list of source/sepprfrc.c:306-343
+ * (criterion r^2 < (cf+skin)^2).  Returns the number of pairs (the array is
+ * filled up to maxpairs).
+ */
+long ora_pairs_brute(long n, const double *x, const double L[3], double rlist,
+		     int excl, const int *molindex, const int *bond,
+		     const int *angle, const int *dihed, int *pairs, long maxpairs)
+{
+	const double rl2 = rlist * rlist;
+	long np = 0;
+	double d[3];
+	for (long i = 0; i < n - 1; i++)
+		for (long j = i + 1; j < n; j++) {
+			if (excl && ora_excluded(excl, i, j, molindex, bond, angle, dihed))
+				continue;
+			if (ora_sep(x, i, j, L, d) < rl2) {
+				if (np < maxpairs) { pairs[2 * np] = (int)i; pairs[2 * np + 1] = (int)j; }
+				np++;
+			}
+		}
+	return np;
+}
+
+/* number of cells along an edge: floor(L/(cf+delta)) (source/sepmisc.c sep_nsubbox,
+ * called with delta = 0.25 by sep_sys_setup, source/sepinit.c:249-276) */
+int ora_nsubbox(double cf, double delta, double L)
+{
+	return (int)floor(L / (cf + delta));
+}
+
+/*
+ * Half neighbour list from a linked-cell list, as the reference builds it
+ * (source/sepprfrc.c:394-415 cell list, :419-513 list build):
+ *  - cell of a particle: (int)(x/lsub) per axis, lsub = L/nsub fixed at setup;
+ *  - head/next linked cells, filled in particle order so a cell is walked
+ *    from its highest index down;
+ *  - each particle of cell m1 scans the 14-cell half stencil; a partner j2
+ *    is kept when (m1 != m2 || j2 > j1) and r^2 < (cf+skin)^2.
+ * The per-particle lists are returned in the reference's order in a CSR
+ * (start[n+1], nb[]).  Because the cell edge is fixed at setup while the skin
+ * may grow later (sep_set_skin), pairs with l_cell < r < cf+skin in
+ * non-adjacent cells are missed exactly as in the reference.
+ * Returns the number of pairs, or -1 when maxpairs is too small.
+ */
+long ora_pairs_llist(long n, const double *x, const double L[3], const int nsub[3],
+		     double cf, double skin, int excl, const int *molindex,
+		     const int *bond, const int *angle, const int *dihed,
+		     long *start, int *nb, long maxpairs)
+{
+	static const int ox[14] = {0, 1, 1, 0, -1, 0, 1, 1, 0, -1, -1, -1, 0, 1};
+	static const int oy[14] = {0, 0, 1, 1, 1, 0, 0, 1, 1, 1, 0, -1, -1, -1};
+	static const int oz[14] = {0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1, 1};
+	const long nc2 = (long)nsub[0] * nsub[1], nc3 = nc2 * nsub[2];
+	const double rl2 = (cf + skin) * (cf + skin);
+	double lsub[3];
+	for (int k = 0; k < 3; k++) lsub[k] = L[k] / nsub[k];
+
+	long *head = malloc(sizeof(long) * nc3), *next = malloc(sizeof(long) * n);
+	int **tmp = malloc(sizeof(int *) * n);
+	long *cnt = calloc(n, sizeof(long)), *cap = malloc(sizeof(long) * n);
+	for (long c = 0; c < nc3; c++) head[c] = -1;
+	for (long i = 0; i < n; i++) {
+		long c = (long)(x[3 * i] / lsub[0]) + (long)(x[3 * i + 1] / lsub[1]) * nsub[0] +
+			 (long)(x[3 * i + 2] / lsub[2]) * nc2;
+		if (c < 0 || c >= nc3) c = c < 0 ? 0 : nc3 - 1;
+		next[i] = head[c];
+		head[c] = i;
+		cap[i] = 64;
+		tmp[i] = malloc(sizeof(int) * cap[i]);
+	}
+	for (int cz = 0; cz < nsub[2]; cz++)
+		for (int cy = 0; cy < nsub[1]; cy++)
+			for (int cx = 0; cx < nsub[0]; cx++) {
+				long m1 = cz * nc2 + (long)cy * nsub[0] + cx;
+				for (long j1 = head[m1]; j1 != -1; j1 = next[j1]) {
+					for (int s = 0; s < 14; s++) {
+						int mx = cx + ox[s], my = cy + oy[s], mz = cz + oz[s];
+						if (mx == nsub[0]) mx = 0; else if (mx == -1) mx = nsub[0] - 1;
+						if (my == nsub[1]) my = 0; else if (my == -1) my = nsub[1] - 1;
+						if (mz == nsub[2]) mz = 0;
+						long m2 = mz * nc2 + (long)my * nsub[0] + mx;
+						for (long j2 = head[m2]; j2 != -1; j2 = next[j2]) {
+							if (!(m1 != m2 || j2 > j1)) continue;
+							if (excl && ora_excluded(excl, j1, j2, molindex, bond, angle, dihed))
+								continue;
+							double d[3];
+							if (ora_sep(x, j1, j2, L, d) < rl2) {
+								if (cnt[j1] == cap[j1]) {
+									cap[j1] *= 2;
+									tmp[j1] = realloc(tmp[j1], sizeof(int) * cap[j1]);
+								}
+								tmp[j1][cnt[j1]++] = (int)j2;
+							}
+						}
+					}
+				}
+			}
+	long total = 0;
+	for (long i = 0; i < n; i++) {
+		start[i] = total;
+		for (long k = 0; k < cnt[i]; k++) {
+			if (total < maxpairs) nb[total] = tmp[i][k];
+			total++;
+		}
+		free(tmp[i]);
+	}
+	start[n] = total;
+	free(tmp); free(cnt); free(cap); free(head); free(next);
+	return total <= maxpairs ? total : -1;
+}
+
+/*
+ * Pair-potential kinds.  ORA_POT_LJ*: the built-in callbacks of
+ * source/sepmisc.c:115-165 (unit sigma/epsilon; shift 0, SEP_LJCF2 or 1.0);
+ * ORA_POT_LJPARAM: the inlined Lennard-Jones of sep_force_lj with
+ * p = {cf, eps, sigma, aw} (source/sepprfrc.c:782-1000), whose force factor
+ * is 48 eps (s^6)(s^6 - aw/2) * sigma^2/r^2 with s = sigma/r, and whose shift is
+ * 4 eps ((sigma/cf)^12 - aw (sigma/cf)^6).
+ */
+enum { ORA_POT_LJ = 0, ORA_POT_LJSHIFT = 1, ORA_POT_WCA = 2, ORA_POT_LJPARAM = 3 };
+#define ORA_LJCF2 0.016316891136
+
+static inline void ora_pot(int kind, const double *p, double r2, double *ft, double *u)
+{
+	if (kind == ORA_POT_LJPARAM) {
+		const double eps = p[1], sigma = p[2], aw = p[3], cf = p[0];
+		const double shift = 4.0 * eps * (pow(sigma / cf, 12.) - aw * pow(sigma / cf, 6.));
+		double rri = sigma * sigma / r2, rri3 = rri * rri * rri;
+		*ft = 48.0 * eps * rri3 * (rri3 - 0.5 * aw) * rri;
+		*u = 4.0 * eps * rri3 * (rri3 - aw) - shift;
+		return;
+	}
+	double rri = 1.0 / r2, rri3 = rri * rri * rri;
+	*ft = 48.0 * rri3 * (rri3 - 0.5) * rri;
+	*u = 4.0 * rri3 * (rri3 - 1.0);
+	if (kind == ORA_POT_LJSHIFT) *u += ORA_LJCF2;
+	else if (kind == ORA_POT_WCA) *u += 1.0;
+}
+
+static inline int ora_typematch(char ti, char tj, const char *types)
+{
+	return (ti == types[0] && tj == types[1]) || (ti == types[1] && tj == types[0]);
+}
+
+/*
+ * Pair forces over a CSR half list (or any unordered pair list): for every
+ * listed pair with matching types and r^2 < cf^2 add f = ft r to i and -f to
+ * j, sum the energy and the configurational tensor pot_P[k][kk] += f_k r_kk
+ * (source/sepprfrc.c:94-224 and :782-923).  `epot` receives the plain sum;
+ * whether the caller assigns or adds it is the caller's business.
+ */
+void ora_pair_forces(long n, const double *x, const char *type, const double L[3],
+		     const char *types, int kind, const double *p, double cf,
+		     const long *start, const int *nb, double *f, double *epot, double *potP)
+{
+	const double cf2 = cf * cf;
+	double e = 0.0;
+	for (long i = 0; i < n; i++) {
+		if (type[i] != types[0] && type[i] != types[1]) continue;
+		for (long s = start[i]; s < start[i + 1]; s++) {
+			long j = nb[s];
+			if (!ora_typematch(type[i], type[j], types)) continue;
+			double d[3], r2 = ora_sep(x, i, j, L, d), ft, u;
+			if (r2 >= cf2) continue;
+			ora_pot(kind, p, r2, &ft, &u);
+			for (int k = 0; k < 3; k++) {
+				double fk = ft * d[k];
+				f[3 * i + k] += fk;
+				f[3 * j + k] -= fk;
+				for (int kk = 0; kk < 3; kk++) potP[3 * k + kk] += fk * d[kk];
+			}
+			e += u;
+		}
+	}
+	*epot = e;
+}
+
+/*
+ * Shifted-force Coulomb over a CSR half list (source/sepcoulomb.c:96-160):
+ * particles with |z| < DBL_EPSILON are skipped; ft = zi zj (1/r^2 - 1/cf^2)/r,
+ * u = zi zj (1/r + (r - cf)/cf^2 - 1/cf).  The serial reference adds the full
+ * energy; its OpenMP variant halves it (source/sepcoulomb.c:226-227), which
+ * this oracle does not reproduce.
+ */
+void ora_coulomb_sf(long n, const double *x, const double *z, const double L[3], double cf,
+		    const long *start, const int *nb, double *f, double *ecoul, double *potP)
+{
+	const double cf2 = cf * cf, icf2 = 1.0 / cf2, icf = 1.0 / cf;
+	double e = 0.0;
+	for (long i = 0; i < n; i++) {
+		if (fabs(z[i]) < 2.220446049250313e-16) continue;
+		for (long s = start[i]; s < start[i + 1]; s++) {
+			long j = nb[s];
+			double d[3], r2 = ora_sep(x, i, j, L, d);
+			if (r2 >= cf2) continue;
+			double zz = z[i] * z[j], r = sqrt(r2);
+			double ft = zz * (1.0 / r2 - icf2) / r;
+			for (int k = 0; k < 3; k++) {
+				double fk = ft * d[k];
+				f[3 * i + k] += fk;
+				f[3 * j + k] -= fk;
+				for (int kk = 0; kk < 3; kk++) potP[3 * k + kk] += fk * d[kk];
+			}
+			e += zz * (1.0 / r + (r - cf) * icf2 - icf);
+		}
+	}
+	*ecoul = e;
+}
+
+/*
+ * Nose-Hoover friction (source/sepintgr.c:149-168): ekin = sum m v^2 / (2n),
+ * T = 0.666667 ekin, alpha += dt/tau^2 (T/T0 - 1), f -= alpha m v.
+ */
+void ora_nosehoover(long n, const double *v, const double *m, double *f,
+		    double T0, double *alpha, double tau, double dt)
+{
+	double ek = 0.0;
+	for (long i = 0; i < n; i++)
+		for (int k = 0; k < 3; k++) ek += v[3 * i + k] * v[3 * i + k] * m[i];
+	ek = 0.5 * ek / n;
+	double T = 0.666667 * ek;
+	*alpha = *alpha + dt / (tau * tau) * (T / T0 - 1.0);
+	for (long i = 0; i < n; i++)
+		for (int k = 0; k < 3; k++) f[3 * i + k] -= *alpha * m[i] * v[3 * i + k];
+}
+
+/*
+ * Leap-frog step with periodic wrap and the skin test
+ * (source/sepintgr.c:18-40 sep_periodic, :42-88 sep_leapfrog):
+ * a = f/m; v += a dt; x += v dt; vt = v - a dt/2 enters ekin and kin_P; a
+ * coordinate above L or below 0 is moved by one box length with the crossing
+ * counters updated; d^2 = |x + cross_neighb L - xn|^2 feeds max_dist2; when
+ * sqrt(max_dist2) > skin/2 the update flag is raised, the counter incremented,
+ * xn = x and cross_neighb = 0.  Returns 1 when an update was flagged.
+ * ekin receives 0.5 sum m vt^2 (added), kinP accumulates.
+ */
+int ora_leapfrog(long n, double *x, double *v, const double *f, double *a, const double *m,
+		 int *cross_neighb, int *crossings, double *xn, const double L[3],
+		 double dt, double skin, double *max_dist2, double *ekin, double *kinP)
+{
+	double sum = 0.0;
+	for (long i = 0; i < n; i++) {
+		double vt[3], d2 = 0.0;
+		for (int k = 0; k < 3; k++) {
+			long q = 3 * i + k;
+			a[q] = f[q] / m[i];
+			v[q] += a[q] * dt;
+			x[q] += v[q] * dt;
+			vt[k] = v[q] - 0.5 * a[q] * dt;
+			sum += vt[k] * vt[k] * m[i];
+		}
+		for (int k = 0; k < 3; k++) {
+			long q = 3 * i + k;
+			if (x[q] > L[k]) { x[q] -= L[k]; cross_neighb[q]++; crossings[q]++; }
+			else if (x[q] < 0.0) { x[q] += L[k]; cross_neighb[q]--; crossings[q]--; }
+			double r = (x[q] + cross_neighb[q] * L[k]) - xn[q];
+			d2 += r * r;
+		}
+		if (d2 > *max_dist2) *max_dist2 = d2;
+		for (int k = 0; k < 3; k++)
+			for (int kk = 0; kk < 3; kk++) kinP[3 * k + kk] += vt[k] * vt[kk] * m[i];
+	}
+	int flag = 0;
+	if (sqrt(*max_dist2) > 0.5 * skin) {
+		flag = 1;
+		memcpy(xn, x, sizeof(double) * 3 * n);
+		memset(cross_neighb, 0, sizeof(int) * 3 * n);
+	}
+	*ekin += 0.5 * sum;
+	return flag;
+}
+
+/* harmonic bonds of one type (source/sepmol.c:372-415) */
+void ora_stretch_harmonic(long nb, const unsigned *blist, int type, double l0, double ks,
+			  const double *x, const double L[3], double *f, double *epot,
+			  double *potP, double *potPbond)
+{
+	for (long b = 0; b < nb; b++) {
+		if ((int)blist[3 * b + 2] != type) continue;
+		long i = blist[3 * b], j = blist[3 * b + 1];
+		double d[3], r2 = ora_sep(x, i, j, L, d), r = sqrt(r2);
+		double ft = -ks * (r - l0) / r;
+		for (int k = 0; k < 3; k++) {
+			double fk = ft * d[k];
+			f[3 * i + k] += fk;
+			f[3 * j + k] -= fk;
+			for (int kk = 0; kk < 3; kk++) {
+				potP[3 * k + kk] += fk * d[kk];
+				potPbond[3 * k + kk] += fk * d[kk];
+			}
+		}
+		*epot += 0.5 * ks * (r - l0) * (r - l0);
+	}
+}
+
+/* bond vectors r_ab and r_bc with the minimum image (source/sepmol.c:438-444) */
+static void ora_two_vectors(const double *x, long a, long b, long c, const double L[3],
+			    double d1[3], double d2[3])
+{
+	for (int k = 0; k < 3; k++) {
+		d1[k] = ora_wrap(x[3 * b + k] - x[3 * a + k], L[k]);
+		d2[k] = ora_wrap(x[3 * c + k] - x[3 * b + k], L[k]);
+	}
+}
+
+/*
+ * Angles of one type.  cossq != 0: sep_angle_cossq (source/sepmol.c:418-466),
+ * prefactor -k (cos - cos(pi - angle0)); otherwise sep_angle_harmonic
+ * (:469-517), prefactor -k (theta - angle0) with theta = pi - acos(c12/cD).
+ * Both apply the prefactor to the same cosine-gradient vectors, exactly as
+ * the reference does (for the harmonic form that is not the gradient of its
+ * energy; the difference is a factor 1/sin(theta)).  No virial contribution.
+ */
+void ora_angles(long na, const unsigned *alist, int type, double angle0, double kang,
+		int cossq, const double *x, const double L[3], double *f, double *epot)
+{
+	const double pi = 3.14159265358979;
+	const double c0 = cos(pi - angle0);
+	for (long t = 0; t < na; t++) {
+		if ((int)alist[4 * t + 3] != type) continue;
+		long a = alist[4 * t], b = alist[4 * t + 1], c = alist[4 * t + 2];
+		double d1[3], d2[3];
+		ora_two_vectors(x, a, b, c, L, d1, d2);
+		double c11 = d1[0] * d1[0] + d1[1] * d1[1] + d1[2] * d1[2];
+		double c12 = d1[0] * d2[0] + d1[1] * d2[1] + d1[2] * d2[2];
+		double c22 = d2[0] * d2[0] + d2[1] * d2[1] + d2[2] * d2[2];
+		double cD = sqrt(c11 * c22), cc = c12 / cD, pref;
+		if (cossq) {
+			pref = -kang * (cc - c0);
+			*epot += 0.5 * kang * (cc - c0) * (cc - c0);
+		} else {
+			double th = pi - acos(cc);
+			pref = -kang * (th - angle0);
+			*epot += 0.5 * kang * (th - angle0) * (th - angle0);
+		}
+		for (int k = 0; k < 3; k++) {
+			double f1 = pref * ((c12 / c11) * d1[k] - d2[k]) / cD;
+			double f2 = pref * (d1[k] - (c12 / c22) * d2[k]) / cD;
+			f[3 * a + k] += f1;
+			f[3 * b + k] += -f1 - f2;
+			f[3 * c + k] += f2;
+		}
+	}
+}
+
+/* Ryckaert-Bellemans torsions of one type in Rapaport's form
+ * (source/sepmol.c:520-587); no virial contribution */
+void ora_torsion_rb(long nd, const unsigned *dlist, int type, const double g[6],
+		    const double *x, const double L[3], double *f, double *epot)
+{
+	for (long t = 0; t < nd; t++) {
+		if ((int)dlist[5 * t + 4] != type) continue;
+		long a = dlist[5 * t], b = dlist[5 * t + 1], c = dlist[5 * t + 2], dd = dlist[5 * t + 3];
+		double r1[3], r2[3], r3[3];
+		for (int k = 0; k < 3; k++) {
+			r1[k] = ora_wrap(x[3 * b + k] - x[3 * a + k], L[k]);
+			r2[k] = ora_wrap(x[3 * c + k] - x[3 * b + k], L[k]);
+			r3[k] = ora_wrap(x[3 * dd + k] - x[3 * c + k], L[k]);
+		}
+#define ORA_DOT(u, w) ((u)[0] * (w)[0] + (u)[1] * (w)[1] + (u)[2] * (w)[2])
+		double c11 = ORA_DOT(r1, r1), c12 = ORA_DOT(r1, r2), c13 = ORA_DOT(r1, r3);
+		double c22 = ORA_DOT(r2, r2), c23 = ORA_DOT(r2, r3), c33 = ORA_DOT(r3, r3);
+#undef ORA_DOT
+		double cA = c13 * c22 - c12 * c23;
+		double cB1 = c11 * c22 - c12 * c12, cB2 = c22 * c33 - c23 * c23;
+		double cD = sqrt(cB1 * cB2), cc = cA / cD;
+		double pref = -(g[1] + (2. * g[2] + (3. * g[3] + (4. * g[4] + 5. * g[5] * cc) * cc) * cc) * cc);
+		double t1 = cA, t2 = c11 * c23 - c12 * c13, t3 = -cB1;
+		double t4 = cB2, t5 = c13 * c23 - c12 * c33, t6 = -cA;
+		double cR1 = c12 / c22, cR2 = c23 / c22;
+		for (int k = 0; k < 3; k++) {
+			double f1 = pref * c22 * (t1 * r1[k] + t2 * r2[k] + t3 * r3[k]) / (cD * cB1);
+			double f2 = pref * c22 * (t4 * r1[k] + t5 * r2[k] + t6 * r3[k]) / (cD * cB2);
+			f[3 * a + k] += f1;
+			f[3 * b + k] += -(1.0 + cR1) * f1 + cR2 * f2;
+			f[3 * c + k] += cR1 * f1 - (1.0 + cR2) * f2;
+			f[3 * dd + k] += f2;
+		}
+		*epot += g[0] + (g[1] + (g[2] + (g[3] + (g[4] + g[5] * cc) * cc) * cc) * cc) * cc;
+	}
+}
+
+/*
+ * Complete plain-LJ loop, used for energy-drift references and as the timed
+ * CPU baseline: per step reset, linked-cell half-list rebuild when flagged,
+ * pair forces with Newton's third law (OpenMP over i with a per-thread force
+ * array, as the reference's threaded path at source/sepprfrc.c:108-150),
+ * optional Nose-Hoover, leap-frog.  The rebuild uses the reference's cell
+ * grid rule (nsub from cf + 0.25) and 14-cell stencil via ora_pairs_llist.
+ * kind/p select the potential as in ora_pair_forces.  etot_trace (optional,
+ * nsteps entries) receives (epot + ekin)/n per step; the final epot, ekin,
+ * pot_P, kin_P are written to out[0], out[1], out[2..10], out[11..19];
+ * out[20] = number of list updates.  nthreads <= 0 uses the OpenMP default.
+ * Returns 0, or -1 on allocation failure.
+ */
+int ora_run_lj(long n, double *x, double *v, const double *m, const char *type,
+	       const double L[3], int kind, const double *p, double cf, double skin,
+	       double dt, long nsteps, int nh, double T0, double tau, double *alpha,
+	       int nthreads, double *etot_trace, double *out)
+{
+#ifdef _OPENMP
+	if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+	(void)nthreads;
+#endif
+	int nsub[3];
+	for (int k = 0; k < 3; k++) nsub[k] = ora_nsubbox(cf, 0.25, L[k]);
+	double *f = calloc(3 * n, sizeof(double)), *a = calloc(3 * n, sizeof(double));
+	double *xn = calloc(3 * n, sizeof(double));
+	int *cn = calloc(3 * n, sizeof(int)), *cr = calloc(3 * n, sizeof(int));
+	long *start = malloc(sizeof(long) * (n + 1));
+	long maxp = n * 200 + 1000;
+	int *nb = malloc(sizeof(int) * maxp);
+	if (!f || !a || !xn || !cn || !cr || !start || !nb) return -1;
+	const char types[2] = {type[0], type[0]};
+	int flag = 1;
+	unsigned nupd = 0;
+	double epot = 0, ekin = 0, potP[9], kinP[9];
+	for (long step = 0; step < nsteps; step++) {
+		double maxd2 = 0.0;
+		memset(f, 0, sizeof(double) * 3 * n);
+		memset(potP, 0, sizeof potP);
+		memset(kinP, 0, sizeof kinP);
+		ekin = 0.0;
+		if (flag) {
+			long np = ora_pairs_llist(n, x, L, nsub, cf, skin, 0, NULL, NULL, NULL, NULL,
+						  start, nb, maxp);
+			if (np < 0) {
+				maxp = start[n] + 1000;
+				nb = realloc(nb, sizeof(int) * maxp);
+				ora_pairs_llist(n, x, L, nsub, cf, skin, 0, NULL, NULL, NULL, NULL,
+						start, nb, maxp);
+			}
+			flag = 0;
+		}
+		/* threaded Newton-3 force loop with a private force array per thread */
+		double e = 0.0, pP[9] = {0};
+		const double cf2 = cf * cf;
+#pragma omp parallel
+		{
+			double *fl = calloc(3 * n, sizeof(double));
+			double el = 0.0, pl[9] = {0};
+#pragma omp for schedule(dynamic, 64)
+			for (long i = 0; i < n; i++) {
+				for (long s = start[i]; s < start[i + 1]; s++) {
+					long j = nb[s];
+					if (!ora_typematch(type[i], type[j], types)) continue;
+					double d[3], r2 = ora_sep(x, i, j, L, d), ft, u;
+					if (r2 >= cf2) continue;
+					ora_pot(kind, p, r2, &ft, &u);
+					for (int k = 0; k < 3; k++) {
+						double fk = ft * d[k];
+						fl[3 * i + k] += fk;
+						fl[3 * j + k] -= fk;
+						for (int kk = 0; kk < 3; kk++) pl[3 * k + kk] += fk * d[kk];
+					}
+					el += u;
+				}
+			}
+#pragma omp critical
+			{
+				for (long q = 0; q < 3 * n; q++) f[q] += fl[q];
+				for (int k = 0; k < 9; k++) pP[k] += pl[k];
+				e += el;
+			}
+			free(fl);
+		}
+		epot = e;
+		memcpy(potP, pP, sizeof pP);
+		if (nh) ora_nosehoover(n, v, m, f, T0, alpha, tau, dt);
+		if (ora_leapfrog(n, x, v, f, a, m, cn, cr, xn, L, dt, skin, &maxd2, &ekin, kinP)) {
+			flag = 1;
+			nupd++;
+		}
+		if (etot_trace) etot_trace[step] = (epot + ekin) / n;
+	}
+	if (out) {
+		out[0] = epot;
+		out[1] = ekin;
+		for (int k = 0; k < 9; k++) { out[2 + k] = potP[k]; out[11 + k] = kinP[k]; }
+		out[20] = nupd;
+	}
+	free(f); free(a); free(xn); free(cn); free(cr); free(start); free(nb);
+	return 0;
+}

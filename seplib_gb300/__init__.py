@@ -1,0 +1,60 @@
+"""seplib_gb300 -- GB300-native implementation of seplib's MD-step hot path.
+
+The product is ``lib/libsep.so``: the sep C API (reference include/sep.h)
+implemented as a C99 host layer over hand-written sm_103a CUDA kernels.
+This package builds it (``build.build()``) and binds it with ctypes
+(``load()``), for Python callers and the test suite.  There is no CPU
+fallback: ``load()`` raises when the library has not been built, and the
+library itself exits through sep_error when no GPU is present.
+"""
+import ctypes as C
+import os
+
+from . import sepapi
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libsep.so")
+
+_lib = None
+
+
+class GpuInfo(C.Structure):
+    """``sep_gpu_info`` (include/sepgpu.h)."""
+    _fields_ = [("launches", C.c_long), ("list_builds", C.c_long), ("list_capacity", C.c_int),
+                ("list_max", C.c_int), ("list_mean", C.c_double), ("tpp", C.c_int)]
+
+
+_GPU_SIGNATURES = {
+    "sep_gpu_available": (C.c_int, []),
+    "sep_gpu_error": (C.c_char_p, []),
+    "sep_gpu_sync": (C.c_int, [sepapi.PART_P]),
+    "sep_gpu_invalidate": (C.c_int, [sepapi.PART_P]),
+    "sep_gpu_run": (C.c_int, [sepapi.PART_P, sepapi.SYS_P, sepapi.RET_P, C.c_char_p, C.c_void_p,
+                             sepapi.D_P, C.c_double, C.c_uint, C.c_int, C.c_double, sepapi.D_P,
+                             C.c_double, C.c_long]),
+    "sep_gpu_set_tpp": (C.c_int, [sepapi.PART_P, C.c_int]),
+    "sep_gpu_info_get": (C.c_int, [sepapi.PART_P, C.POINTER(GpuInfo)]),
+    "sep_gpu_list_pairs": (C.c_long, [sepapi.PART_P, C.POINTER(C.c_int), C.c_long]),
+    "sep_gpu_event_record": (C.c_int, [sepapi.PART_P, C.c_int]),
+    "sep_gpu_event_elapsed": (C.c_int, [sepapi.PART_P, C.c_int, C.c_int, C.POINTER(C.c_float)]),
+    "sep_gpu_stream_sync": (C.c_int, [sepapi.PART_P]),
+    "sep_gpu_time_step_kernel": (C.c_int, [sepapi.PART_P, sepapi.SYS_P, sepapi.RET_P, C.c_char_p,
+                                          C.c_void_p, sepapi.D_P, C.c_double, C.c_uint, C.c_int,
+                                          C.c_double, sepapi.D_P, C.c_double, C.c_long, sepapi.D_P]),
+}
+
+
+def load():
+    """ctypes handle to libsep.so with every prototype attached."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libsep.so is not built (%s); run seplib_gb300.build.build()" % LIB_PATH)
+        lib = C.CDLL(LIB_PATH)
+        sepapi.bind(lib)
+        for name, (res, args) in _GPU_SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib

@@ -1,0 +1,201 @@
+// dev_common.cuh - internals shared by the sepdev translation units.
+//
+// Number formats (chosen for GB300, whose FP64 rate is 1/64 of FP32):
+//  * position component k: unsigned 64-bit fixed point X = frac * 2^64 with
+//    frac = x / L_k in [0, 1).  The high word (x_hi) is what the pair kernels
+//    read; (int)(x_hi_i - x_hi_j) is the minimum-image separation in units of
+//    L_k / 2^32 because two's-complement wrap-around is the periodic boundary.
+//    The integrator adds v dt in this format, so the position update keeps
+//    more than FP64 resolution (L / 2^64) without a single FP64 instruction.
+//  * velocity: float-float (hi + lo, ~48-bit mantissa).
+//  * per-pair force, energy and virial: FP32.
+//  * sums over particles: FP32 within a warp (<= 32 particles), then exact
+//    64-bit fixed point (scale 2^32) through integer atomics, so every total is
+//    independent of scheduling order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "../sepdev.h"
+
+#define SEPDEV_NEV 8
+#define SEPDEV_MAXTAB 4
+
+struct sepdev {
+	long n;
+	int device;
+	cudaStream_t st;
+	cudaEvent_t ev[SEPDEV_NEV];
+
+	double L[3];
+	float fscale[3];        // L_k / 2^32
+	double vscale_hi[3], vscale_lo[3];  // unused placeholder for alignment
+
+	// particle state in cell order
+	int4 *pos[2];           // x_hi, y_hi, z_hi, type id
+	int cur;
+	uint4 *xlo, *xlo_b;     // low words, .w = 0
+	float4 *vhi, *vhi_b;    // velocity hi, .w = mass
+	float4 *vlo, *vlo_b;    // velocity lo, .w = 1/mass
+	float4 *frc, *frc_b;    // force, .w = per-particle pair energy
+	int4 *xn;               // high words at the last list build
+	int4 *cross, *cross_b;  // crossings since the start
+	int4 *cbase, *cbase_b;  // crossings at the last skin-triggered build
+	int *gid, *gid_b;       // user index of each slot
+	int *inv;               // slot of each user index
+	float *charge, *charge_b;
+	int *mol, *mol_b;
+	int has_charge;
+
+	// cell list
+	int ncell[3];
+	long ncells, cap_cells;
+	int *cellof;            // cell of each slot (old order)
+	int *celloff;           // rank inside the cell
+	int *cellcount;
+	int *cellstart;         // ncells + 1
+	int *perm;              // new slot -> old slot
+
+	// neighbour list: tiles of 32/tpp particles, each tile maxnb*(32/tpp) ints
+	int *nl;
+	int *ncnt;
+	int maxnb, tpp;
+	size_t cap_nl;
+	double rlist;
+	int excl;
+	int list_valid;
+
+	// exclusions (user indices, CSR)
+	int *exb_start, *exb_idx, *exa_start, *exa_idx;
+	int has_excl;
+
+	// topology (user indices) and per-atom incidence CSR
+	int nbond, nangle, ndihed;
+	uint4 *bonds;           // a b type -
+	uint4 *angles;          // a b c type
+	uint4 *diheds_abcd;     // a b c d
+	int *dihed_type;
+	int *inc_start;         // n+1, per user atom
+	int *inc_term;          // encoded term: kind<<30 | role<<28 | index
+	float *term_out;        // per-term observable (length / angle)
+	size_t term_out_cap;
+
+	// tabulated potentials
+	float2 *tab[SEPDEV_MAXTAB];
+	int tab_n[SEPDEV_MAXTAB];
+	float tab_r2min[SEPDEV_MAXTAB], tab_idr2[SEPDEV_MAXTAB];
+
+	// reductions
+	long long *slots;       // device, nslots * SLOT_FIELDS
+	long long *h_slots;     // pinned mirror
+	unsigned *flags;        // device status word [0] overflow, [1] max count, [2..3] scratch
+	unsigned *h_flags;      // pinned mirror
+	int nslots;
+
+	sepdev_pairset *d_ps;   // device copy of the current pair set
+
+	// graph runner state
+	void *runner;
+
+	long launches;
+};
+
+#define FX_SCALE 4294967296.0f      // 2^32
+#define FX_ISCALE (1.0 / 4294967296.0)
+
+// ---- error handling -------------------------------------------------------
+extern "C" void sepdev_set_error(const char *what, cudaError_t e);
+#define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { \
+	sepdev_set_error(#call, e_); return SEPDEV_ECUDA; } } while (0)
+#define CKL(d) do { (d)->launches++; cudaError_t e_ = cudaGetLastError(); \
+	if (e_ != cudaSuccess) { sepdev_set_error("kernel launch", e_); return SEPDEV_ECUDA; } } while (0)
+
+// ---- small device helpers -------------------------------------------------
+// reciprocal: hardware approximation refined by one Newton step, which
+// removes the approximation's bias (the result is within ~0.5 ulp)
+__device__ __forceinline__ float fast_rcp(float x)
+{
+	float r;
+	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+	const float e = fmaf(-x, r, 1.0f);
+	return fmaf(r, e, r);
+}
+
+// minimum-image separation component from two high words
+__device__ __forceinline__ float sep_hi(int a, int b, float s)
+{
+	return (float)(a - b) * s;
+}
+
+// float-float: (hi, lo) + q, returns renormalised pair
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float q)
+{
+	float s = hi + q;
+	float bp = s - hi;
+	float e = (hi - (s - bp)) + (q - bp);   // two-sum error
+	e += lo;
+	float h2 = s + e;
+	lo = e - (h2 - s);
+	hi = h2;
+}
+
+// 64-bit fixed-point increment round((hi + lo) * (shi + slo)) with
+// |result| < 2^62; exact product of the high parts via FMA
+__device__ __forceinline__ long long ff_mul_fix(float hi, float lo, float shi, float slo)
+{
+	float p = hi * shi;
+	float e = fmaf(hi, shi, -p);
+	float r = e + (hi * slo + lo * shi);
+	return __float2ll_rn(p) + __float2ll_rn(r);
+}
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31; }
+
+// Warp sum of NV floats, result valid in lane 0.
+template <int NV>
+__device__ __forceinline__ void warp_sum(float (&v)[NV])
+{
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+		for (int k = 0; k < NV; k++) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+}
+
+// Block reduction of NV floats: base[fld[k]] += sum v[k] through 64-bit
+// fixed-point atomics (FP32 inside each warp, exact integer sums above), plus
+// an optional max of a non-negative float into base[maxfld] (maxfld < 0: none).
+// Must be called by all threads of the block, once per kernel.
+template <int NV>
+__device__ __forceinline__ void block_to_slot(float (&v)[NV], const int (&fld)[NV],
+					      long long *base, float maxval, int maxfld)
+{
+	__shared__ long long red[32][NV];
+	__shared__ unsigned redm[32];
+	warp_sum<NV>(v);
+	const unsigned mx = __reduce_max_sync(0xffffffffu, __float_as_uint(maxval));
+	const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+	if (lane_id() == 0) {
+#pragma unroll
+		for (int k = 0; k < NV; k++) red[w][k] = __float2ll_rn(v[k] * FX_SCALE);
+		redm[w] = mx;
+	}
+	__syncthreads();
+	if (w == 0) {
+#pragma unroll
+		for (int k = 0; k < NV; k++) {
+			long long s = (int)lane_id() < nw ? red[lane_id()][k] : 0ll;
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+			if (lane_id() == 0 && s != 0)
+				atomicAdd((unsigned long long *)&base[fld[k]], (unsigned long long)s);
+		}
+		if (maxfld >= 0) {
+			unsigned m = (int)lane_id() < nw ? redm[lane_id()] : 0u;
+			m = __reduce_max_sync(0xffffffffu, m);
+			if (lane_id() == 0 && m)
+				atomicMax((unsigned long long *)&base[maxfld], (unsigned long long)m);
+		}
+	}
+}
+
+static inline int grid_for(long n, int block) { return (int)((n + block - 1) / block); }

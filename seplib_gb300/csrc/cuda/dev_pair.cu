@@ -1,0 +1,393 @@
+// dev_pair.cu - pair forces, Nose-Hoover friction and leap-frog.
+//
+// Reference semantics restated here:
+//   pair force      source/sepprfrc.c:94-224 (generic callback) and :782-923
+//                   (inlined LJ); per pair ft(r^2), f = ft r, U, f_k r_kk
+//   SF Coulomb      source/sepcoulomb.c:96-160
+//   Nose-Hoover     source/sepintgr.c:149-168 (alpha computed by the caller)
+//   leap-frog       source/sepintgr.c:18-88
+//
+// GB300 design:
+//   * FULL neighbour list: each particle sums all its pair forces itself, so
+//     no atomics touch the force array; energies and virials are halved.
+//   * TPP lanes per particle (1, 2 or 4) walk its list in warp tiles: lane
+//     (p, q) of a warp reads entry s*32 + p*TPP + q, so each list load of a
+//     warp is one coalesced 128-byte line.
+//   * j positions are 16-byte int4 gathers through the read-only path;
+//     separations are int32 differences of fixed-point high words
+//     (minimum image by wrap-around) converted to FP32.
+//   * the fused step kernel computes the force of particle i from the
+//     positions of step t (buffer cur) and immediately integrates i into
+//     buffer cur^1, so one launch and one pass over the particle state per
+//     MD step suffice.
+#include <math.h>
+#include <string.h>
+#include "dev_common.cuh"
+
+#include "dev_pair.cuh"
+
+enum { VAR_SINGLE = 0, VAR_GENERAL = 1, VAR_GENERAL_COUL = 2 };
+
+__device__ __forceinline__ void lj_eval(float r2, float sig2, float eps48, float eps4, float awh,
+					float aw, float ushift, float &ft, float &u)
+{
+	const float s2 = sig2 * fast_rcp(r2);
+	const float s6 = s2 * s2 * s2;
+	ft = eps48 * s6 * (s6 - awh) * s2;   // the reference multiplies by sigma^2/r^2
+	u = eps4 * s6 * (s6 - aw) + ushift;
+}
+
+__device__ __forceinline__ void tab_eval(const float2 *__restrict__ t, int nt, float r2min,
+					 float idr2, float r2, float &ft, float &u)
+{
+	float xk = (r2 - r2min) * idr2;
+	xk = fminf(fmaxf(xk, 0.f), (float)(nt - 1) - 1e-3f);
+	const int k = (int)xk;
+	const float w = xk - (float)k;
+	const float2 a = __ldg(&t[k]), b = __ldg(&t[k + 1]);
+	ft = a.x + w * (b.x - a.x);
+	u = a.y + w * (b.y - a.y);
+}
+
+// Integrate particle i (leap-frog, optional friction) and return its kinetic
+// contributions; F is the total force before friction.
+__device__ __forceinline__ void integrate(long i, float fx, float fy, float fz, float ei,
+					  const int4 pi, const PairArgs &a, float alpha, int4 *pos_out,
+					  float &ek, float (&kp)[6], float &sv2, float &d2)
+{
+	float4 vh = a.vhi[i], vl = a.vlo[i];
+	const uint4 lo = a.xlo[i];
+	const float m = vh.w, im = vl.w;
+	if (a.nh) {
+		const float am = alpha * m;
+		fx -= am * vh.x; fy -= am * vh.y; fz -= am * vh.z;
+	}
+	a.frc[i] = make_float4(fx, fy, fz, ei);
+	// a dt with dt carried to ~48 bits, so the velocity and position updates
+	// use the same time step
+	const float ax = fx * im, ay = fy * im, az = fz * im;
+	const float qx = fmaf(ax, a.dt, ax * a.dt_lo), qy = fmaf(ay, a.dt, ay * a.dt_lo),
+		    qz = fmaf(az, a.dt, az * a.dt_lo);
+	ff_add(vh.x, vl.x, qx);
+	ff_add(vh.y, vl.y, qy);
+	ff_add(vh.z, vl.z, qz);
+	const float tx = vh.x - 0.5f * qx, ty = vh.y - 0.5f * qy, tz = vh.z - 0.5f * qz;
+	ek = m * (tx * tx + ty * ty + tz * tz);
+	kp[0] = m * tx * tx; kp[1] = m * tx * ty; kp[2] = m * tx * tz;
+	kp[3] = m * ty * ty; kp[4] = m * ty * tz; kp[5] = m * tz * tz;
+	sv2 = m * (vh.x * vh.x + vh.y * vh.y + vh.z * vh.z);
+	const long long ix = ff_mul_fix(vh.x, vl.x, a.shi[0], a.slo[0]);
+	const long long iy = ff_mul_fix(vh.y, vl.y, a.shi[1], a.slo[1]);
+	const long long iz = ff_mul_fix(vh.z, vl.z, a.shi[2], a.slo[2]);
+	const unsigned long long X0 = ((unsigned long long)(unsigned)pi.x << 32) | lo.x;
+	const unsigned long long Y0 = ((unsigned long long)(unsigned)pi.y << 32) | lo.y;
+	const unsigned long long Z0 = ((unsigned long long)(unsigned)pi.z << 32) | lo.z;
+	const unsigned long long X1 = X0 + (unsigned long long)ix;
+	const unsigned long long Y1 = Y0 + (unsigned long long)iy;
+	const unsigned long long Z1 = Z0 + (unsigned long long)iz;
+	const int cx = (ix > 0 && X1 < X0) ? 1 : ((ix < 0 && X1 > X0) ? -1 : 0);
+	const int cy = (iy > 0 && Y1 < Y0) ? 1 : ((iy < 0 && Y1 > Y0) ? -1 : 0);
+	const int cz = (iz > 0 && Z1 < Z0) ? 1 : ((iz < 0 && Z1 > Z0) ? -1 : 0);
+	if (cx | cy | cz) {
+		int4 c = a.cross[i];
+		c.x += cx; c.y += cy; c.z += cz;
+		a.cross[i] = c;
+	}
+	const int4 po = make_int4((int)(unsigned)(X1 >> 32), (int)(unsigned)(Y1 >> 32),
+				  (int)(unsigned)(Z1 >> 32), pi.w);
+	pos_out[i] = po;
+	a.xlo[i] = make_uint4((unsigned)X1, (unsigned)Y1, (unsigned)Z1, 0u);
+	a.vhi[i] = vh;
+	a.vlo[i] = vl;
+	const int4 xn = a.xn[i];
+	const float dx = sep_hi(po.x, xn.x, a.fs[0]);
+	const float dy = sep_hi(po.y, xn.y, a.fs[1]);
+	const float dz = sep_hi(po.z, xn.z, a.fs[2]);
+	d2 = dx * dx + dy * dy + dz * dz;
+}
+
+template <int TPP, int VAR, bool FUSED>
+__global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
+{
+	constexpr int P = 32 / TPP;
+	constexpr int NCH = VAR == VAR_SINGLE ? 1 : 4;
+	extern __shared__ sepdev_pot spot[];
+	if (a.flags && (a.flags[0] & 1u)) return;    // list overflow: leave the state untouched
+	int ntypes = 1;
+	if (VAR != VAR_SINGLE) {
+		ntypes = a.ps->ntypes;
+		for (int k = threadIdx.x; k < ntypes * ntypes; k += blockDim.x) spot[k] = a.ps->pot[k];
+		__syncthreads();
+	}
+	const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	const long i = g / TPP;
+	const int q = (int)(g % TPP);
+	const bool act = i < n;
+	float fx = 0.f, fy = 0.f, fz = 0.f;
+	float e[NCH];
+#pragma unroll
+	for (int c = 0; c < NCH; c++) e[c] = 0.f;
+	float ec = 0.f;
+	float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f, w4 = 0.f, w5 = 0.f;
+	int4 pi = make_int4(0, 0, 0, 0);
+	if (act) {
+		pi = a.pos[i];
+		const int cnt = a.ncnt[i];
+		const int *base = a.nl + (i / P) * (long)a.maxnb * P + (i % P) * TPP + q;
+		float qi = 0.f;
+		bool coul_i = false;
+		if (VAR == VAR_GENERAL_COUL) {
+			qi = a.charge[i];
+			coul_i = fabsf(qi) >= 2.220446049250313e-16f;
+		}
+		const float sx = a.fs[0], sy = a.fs[1], sz = a.fs[2];
+#pragma unroll 4
+		for (int k = q; k < cnt; k += TPP) {
+			const int j = __ldg(base + (k / TPP) * 32);
+			const int4 pj = __ldg(&a.pos[j]);
+			const float dx = sep_hi(pi.x, pj.x, sx);
+			const float dy = sep_hi(pi.y, pj.y, sy);
+			const float dz = sep_hi(pi.z, pj.z, sz);
+			const float r2 = dx * dx + dy * dy + dz * dz;
+			float ft = 0.f;
+			if (VAR == VAR_SINGLE) {
+				if (r2 < a.rc2) {
+					float u;
+					lj_eval(r2, a.sig2, a.eps48, a.eps4, a.awh, a.aw, a.ushift, ft, u);
+					e[0] += u;
+				}
+			} else {
+				const sepdev_pot &pp = spot[pi.w * ntypes + pj.w];
+				if (pp.kind != SEPDEV_POT_OFF && r2 < pp.rc2) {
+					float u;
+					if (pp.kind == SEPDEV_POT_LJ)
+						lj_eval(r2, pp.sig2, pp.eps48, pp.eps4, pp.awh, pp.aw, pp.ushift, ft, u);
+					else
+						tab_eval(a.tab[pp.table], a.tab_n[pp.table], a.tab_r2min[pp.table],
+							 a.tab_idr2[pp.table], r2, ft, u);
+#pragma unroll
+					for (int c = 0; c < NCH; c++) e[c] += (pp.chan == c) ? u : 0.f;
+				}
+				if (VAR == VAR_GENERAL_COUL && coul_i && r2 < a.ps->coul_rc2) {
+					const float qq = qi * __ldg(&a.charge[j]);
+					const float ir = rsqrtf(r2), r = r2 * ir, ir2 = ir * ir;
+					ft += qq * (ir2 - a.ps->coul_irc2) * ir;
+					ec += qq * (ir + (r - a.ps->coul_rc) * a.ps->coul_irc2 - a.ps->coul_irc);
+				}
+			}
+			const float gx = ft * dx, gy = ft * dy, gz = ft * dz;
+			fx += gx; fy += gy; fz += gz;
+			w0 += gx * dx; w1 += gx * dy; w2 += gx * dz;
+			w3 += gy * dy; w4 += gy * dz; w5 += gz * dz;
+		}
+	}
+	// per-particle totals across the TPP lanes of particle i
+	float etot = ec;
+#pragma unroll
+	for (int c = 0; c < NCH; c++) etot += e[c];
+#pragma unroll
+	for (int o = TPP / 2; o > 0; o >>= 1) {
+		fx += __shfl_xor_sync(0xffffffffu, fx, o);
+		fy += __shfl_xor_sync(0xffffffffu, fy, o);
+		fz += __shfl_xor_sync(0xffffffffu, fz, o);
+		etot += __shfl_xor_sync(0xffffffffu, etot, o);
+	}
+	float ek = 0.f, kp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, sv2 = 0.f, d2 = 0.f;
+	if (act && q == 0) {
+		if (a.accumulate) {
+			const float4 fo = a.frc[i];
+			fx += fo.x; fy += fo.y; fz += fo.z;
+		}
+		if (FUSED) {
+			const float alpha = a.alpha_dev ? (float)*a.alpha_dev : a.alpha;
+			integrate(i, fx, fy, fz, 0.5f * etot, pi, a, alpha, a.pos_out, ek, kp, sv2, d2);
+		} else {
+			a.frc[i] = make_float4(fx, fy, fz, 0.5f * etot);
+		}
+	}
+	// reductions: pair terms (halved for the full list) into pslot, kinetic into lslot
+	long long *ps = a.slots + (long)a.pslot * SLOT_FIELDS;
+	if (!FUSED) {
+		float v[NCH + 7];
+		int fld[NCH + 7];
+#pragma unroll
+		for (int c = 0; c < NCH; c++) { v[c] = 0.5f * e[c]; fld[c] = SLOT_EPOT0 + c; }
+		v[NCH] = 0.5f * ec; fld[NCH] = SLOT_ECOUL;
+		v[NCH + 1] = 0.5f * w0; v[NCH + 2] = 0.5f * w1; v[NCH + 3] = 0.5f * w2;
+		v[NCH + 4] = 0.5f * w3; v[NCH + 5] = 0.5f * w4; v[NCH + 6] = 0.5f * w5;
+#pragma unroll
+		for (int k = 0; k < 6; k++) fld[NCH + 1 + k] = SLOT_POTP + k;
+		block_to_slot<NCH + 7>(v, fld, ps, 0.f, -1);
+	} else {
+		long long *ls = a.slots + (long)a.lslot * SLOT_FIELDS;
+		const long long off = ls - ps;
+		float v[NCH + 15];
+		int fld[NCH + 15];
+#pragma unroll
+		for (int c = 0; c < NCH; c++) { v[c] = 0.5f * e[c]; fld[c] = SLOT_EPOT0 + c; }
+		v[NCH] = 0.5f * ec; fld[NCH] = SLOT_ECOUL;
+		v[NCH + 1] = 0.5f * w0; v[NCH + 2] = 0.5f * w1; v[NCH + 3] = 0.5f * w2;
+		v[NCH + 4] = 0.5f * w3; v[NCH + 5] = 0.5f * w4; v[NCH + 6] = 0.5f * w5;
+#pragma unroll
+		for (int k = 0; k < 6; k++) fld[NCH + 1 + k] = SLOT_POTP + k;
+		v[NCH + 7] = ek; fld[NCH + 7] = (int)off + SLOT_EKIN;
+#pragma unroll
+		for (int k = 0; k < 6; k++) { v[NCH + 8 + k] = kp[k]; fld[NCH + 8 + k] = (int)off + SLOT_KINP + k; }
+		v[NCH + 14] = sv2; fld[NCH + 14] = (int)off + SLOT_SUMV2;
+		block_to_slot<NCH + 15>(v, fld, ps, d2, (int)off + SLOT_MAXD2);
+	}
+}
+
+// Standalone leap-frog on the stored forces (in-place position update).
+__global__ void __launch_bounds__(256) k_leapfrog(long n, PairArgs a)
+{
+	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	float ek = 0.f, kp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, sv2 = 0.f, d2 = 0.f;
+	if (i < n) {
+		const float4 f = a.frc[i];
+		const float alpha = a.alpha_dev ? (float)*a.alpha_dev : a.alpha;
+		integrate(i, f.x, f.y, f.z, f.w, a.pos[i], a, alpha, (int4 *)a.pos, ek, kp, sv2, d2);
+	}
+	float v[8] = {ek, kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], sv2};
+	const int fld[8] = {SLOT_EKIN, SLOT_KINP, SLOT_KINP + 1, SLOT_KINP + 2, SLOT_KINP + 3,
+			    SLOT_KINP + 4, SLOT_KINP + 5, SLOT_SUMV2};
+	block_to_slot<8>(v, fld, a.slots + (long)a.lslot * SLOT_FIELDS, d2, SLOT_MAXD2);
+}
+
+__global__ void k_friction(long n, float alpha, const float4 *__restrict__ vhi, float4 *frc)
+{
+	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const float4 v = vhi[i];
+	float4 f = frc[i];
+	const float am = alpha * v.w;
+	f.x -= am * v.x; f.y -= am * v.y; f.z -= am * v.z;
+	frc[i] = f;
+}
+
+// ---- host side -----------------------------------------------------------------
+
+static bool single_variant(const sepdev_pairset *ps)
+{
+	return ps->ntypes == 1 && !ps->coulomb && ps->pot[0].kind == SEPDEV_POT_LJ &&
+	       ps->pot[0].chan == 0;
+}
+
+void sepdev_fill_args(sepdev *d, PairArgs &a, const sepdev_pairset *ps, double dt, int nh,
+		      double alpha, int accumulate, int pslot, int lslot, int parity)
+{
+	memset(&a, 0, sizeof a);
+	a.pos = d->pos[parity];
+	a.pos_out = d->pos[parity ^ 1];
+	a.xlo = d->xlo; a.vhi = d->vhi; a.vlo = d->vlo; a.frc = d->frc;
+	a.xn = d->xn; a.cross = d->cross;
+	a.nl = d->nl; a.ncnt = d->ncnt; a.maxnb = d->maxnb;
+	a.charge = d->charge;
+	for (int k = 0; k < 3; k++) {
+		a.fs[k] = d->fscale[k];
+		const double S = dt * 18446744073709551616.0 / d->L[k];
+		a.shi[k] = (float)S;
+		a.slo[k] = (float)(S - (double)a.shi[k]);
+	}
+	a.ps = d->d_ps;
+	if (ps) {
+		const sepdev_pot &p0 = ps->pot[0];
+		a.rc2 = p0.rc2; a.eps48 = p0.eps48; a.eps4 = p0.eps4; a.sig2 = p0.sig2;
+		a.aw = p0.aw; a.awh = p0.awh; a.ushift = p0.ushift;
+	}
+	for (int t = 0; t < SEPDEV_MAXTAB; t++) {
+		a.tab[t] = d->tab[t]; a.tab_n[t] = d->tab_n[t];
+		a.tab_r2min[t] = d->tab_r2min[t]; a.tab_idr2[t] = d->tab_idr2[t];
+	}
+	a.dt = (float)dt;
+	a.dt_lo = (float)(dt - (double)a.dt);
+	a.alpha = (float)alpha;
+	a.nh = nh;
+	a.accumulate = accumulate;
+	a.slots = d->slots;
+	a.pslot = pslot;
+	a.lslot = lslot;
+	a.flags = NULL;
+}
+
+static int upload_pairset(sepdev *d, const sepdev_pairset *ps)
+{
+	CK(cudaMemcpyAsync(d->d_ps, ps, sizeof(sepdev_pairset), cudaMemcpyHostToDevice, d->st));
+	return SEPDEV_OK;
+}
+
+template <int TPP, bool FUSED>
+static void launch_tpp(sepdev *d, int var, const PairArgs &a, size_t shm)
+{
+	const int B = 256;
+	const int grid = grid_for(d->n * TPP, B);
+	if (var == VAR_SINGLE)
+		k_pair<TPP, VAR_SINGLE, FUSED><<<grid, B, 0, d->st>>>(d->n, a);
+	else if (var == VAR_GENERAL)
+		k_pair<TPP, VAR_GENERAL, FUSED><<<grid, B, shm, d->st>>>(d->n, a);
+	else
+		k_pair<TPP, VAR_GENERAL_COUL, FUSED><<<grid, B, shm, d->st>>>(d->n, a);
+}
+
+int sepdev_launch_pair(sepdev *d, const sepdev_pairset *ps, PairArgs &a, bool fused)
+{
+	const int var = single_variant(ps) ? VAR_SINGLE : (ps->coulomb ? VAR_GENERAL_COUL : VAR_GENERAL);
+	const size_t shm = sizeof(sepdev_pot) * ps->ntypes * ps->ntypes;
+	switch (d->tpp) {
+	case 1: fused ? launch_tpp<1, true>(d, var, a, shm) : launch_tpp<1, false>(d, var, a, shm); break;
+	case 2: fused ? launch_tpp<2, true>(d, var, a, shm) : launch_tpp<2, false>(d, var, a, shm); break;
+	default: fused ? launch_tpp<4, true>(d, var, a, shm) : launch_tpp<4, false>(d, var, a, shm); break;
+	}
+	CKL(d);
+	return SEPDEV_OK;
+}
+
+extern "C" int sepdev_pair_forces(sepdev *d, const sepdev_pairset *ps, int accumulate, int slot)
+{
+	if (!d->list_valid || slot < 0 || slot >= d->nslots) return SEPDEV_EINVAL;
+	int rc;
+	if ((rc = upload_pairset(d, ps))) return rc;
+	PairArgs a;
+	sepdev_fill_args(d, a, ps, 0.0, 0, 0.0, accumulate, slot, slot, d->cur);
+	return sepdev_launch_pair(d, ps, a, false);
+}
+
+extern "C" int sepdev_step(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
+			   int nh, double alpha, int pair_slot, int lf_slot)
+{
+	if (!d->list_valid || pair_slot < 0 || pair_slot >= d->nslots || lf_slot < 0 ||
+	    lf_slot >= d->nslots)
+		return SEPDEV_EINVAL;
+	int rc;
+	if ((rc = upload_pairset(d, ps))) return rc;
+	PairArgs a;
+	sepdev_fill_args(d, a, ps, dt, nh, alpha, accumulate, pair_slot, lf_slot, d->cur);
+	if ((rc = sepdev_launch_pair(d, ps, a, true))) return rc;
+	d->cur ^= 1;
+	return SEPDEV_OK;
+}
+
+extern "C" int sepdev_leapfrog(sepdev *d, double dt, int nh, double alpha, int slot)
+{
+	if (slot < 0 || slot >= d->nslots) return SEPDEV_EINVAL;
+	PairArgs a;
+	sepdev_fill_args(d, a, NULL, dt, nh, alpha, 0, slot, slot, d->cur);
+	const int B = 256;
+	k_leapfrog<<<grid_for(d->n, B), B, 0, d->st>>>(d->n, a);
+	CKL(d);
+	return SEPDEV_OK;
+}
+
+extern "C" int sepdev_friction(sepdev *d, double alpha)
+{
+	const int B = 256;
+	k_friction<<<grid_for(d->n, B), B, 0, d->st>>>(d->n, (float)alpha, d->vhi, d->frc);
+	CKL(d);
+	return SEPDEV_OK;
+}
+
+extern "C" int sepdev_zero_forces(sepdev *d)
+{
+	CK(cudaMemsetAsync(d->frc, 0, sizeof(float4) * d->n, d->st));
+	return SEPDEV_OK;
+}

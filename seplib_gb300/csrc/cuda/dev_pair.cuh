@@ -1,0 +1,37 @@
+// dev_pair.cuh - argument block of the pair / step kernels (shared with the graph runner).
+#pragma once
+#include "dev_common.cuh"
+
+struct PairArgs {
+	const int4 *pos;
+	int4 *pos_out;
+	uint4 *xlo;
+	float4 *vhi, *vlo, *frc;
+	const int4 *xn;
+	int4 *cross;
+	const int *nl, *ncnt;
+	int maxnb;
+	const float *charge;
+	float fs[3];
+	const sepdev_pairset *ps;
+	// single-potential fast path
+	float rc2, eps48, eps4, sig2, aw, awh, ushift;
+	// tables
+	const float2 *tab[SEPDEV_MAXTAB];
+	float tab_r2min[SEPDEV_MAXTAB], tab_idr2[SEPDEV_MAXTAB];
+	int tab_n[SEPDEV_MAXTAB];
+	// integration
+	float dt, dt_lo;            // dt as float plus its rounding remainder
+	float shi[3], slo[3];
+	float alpha;
+	const double *alpha_dev;   // when set, alpha is read from device memory
+	int nh, accumulate;
+	long long *slots;
+	int pslot, lslot;
+	const unsigned *flags;
+};
+
+
+void sepdev_fill_args(sepdev *d, PairArgs &a, const sepdev_pairset *ps, double dt, int nh,
+		      double alpha, int accumulate, int pslot, int lslot, int parity);
+int sepdev_launch_pair(sepdev *d, const sepdev_pairset *ps, PairArgs &a, bool fused);

@@ -1,0 +1,241 @@
+/*
+ * sep_api_gpu.c - the entry points this implementation adds (include/sepgpu.h).
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include "sep_rt.h"
+
+void rt_pairset(rt_ctx *c, sepdev_pairset *ps);
+
+int sep_gpu_available(void)
+{
+	return sepdev_device_count() > 0;
+}
+
+const char *sep_gpu_error(void)
+{
+	return sepdev_last_error();
+}
+
+int sep_gpu_sync(seppart *ptr)
+{
+	rt_ctx *c = rt_get(ptr, __func__);
+	rt_need_host(c);
+	return 0;
+}
+
+int sep_gpu_invalidate(seppart *ptr)
+{
+	rt_ctx *c = rt_get(ptr, __func__);
+	rt_flush(c);
+	c->host_valid = 1;
+	c->dev_valid = 0;
+	c->forces_zero = 0;
+	return 0;
+}
+
+int sep_gpu_set_tpp(seppart *ptr, int tpp)
+{
+	rt_ctx *c = rt_get(ptr, __func__);
+	if (tpp != 1 && tpp != 2 && tpp != 4) return -1;
+	c->tpp = tpp;
+	if (c->dev) {
+		rt_flush(c);
+		extern int sepdev_set_tpp(sepdev *d, int tpp);
+		sepdev_set_tpp(c->dev, tpp);
+		c->list_stale = 1;
+	}
+	return 0;
+}
+
+int sep_gpu_info_get(seppart *ptr, sep_gpu_info *info)
+{
+	rt_ctx *c = rt_get(ptr, __func__);
+	memset(info, 0, sizeof *info);
+	info->list_builds = c->nbuild;
+	if (!c->dev) return 0;
+	info->launches = sepdev_launch_count(c->dev);
+	int mx = 0, cap = 0;
+	double mean = 0.0;
+	if (!c->list_stale) sepdev_list_stats(c->dev, &mx, &mean, &cap);
+	info->list_capacity = cap;
+	info->list_max = mx;
+	info->list_mean = mean;
+	extern int sepdev_get_tpp(sepdev *d);
+	info->tpp = sepdev_get_tpp(c->dev);
+	return 0;
+}
+
+long sep_gpu_list_pairs(seppart *ptr, int *pairs, long cap)
+{
+	rt_ctx *c = rt_get(ptr, __func__);
+	if (!c->dev || c->list_stale) return -1;
+	return sepdev_list_pairs(c->dev, pairs, cap);
+}
+
+int sep_gpu_event_record(seppart *ptr, int e)
+{
+	rt_ctx *c = rt_get(ptr, __func__);
+	if (!c->dev) return -1;
+	return sepdev_event_record(c->dev, e);
+}
+
+int sep_gpu_event_elapsed(seppart *ptr, int e0, int e1, float *ms)
+{
+	rt_ctx *c = rt_get(ptr, __func__);
+	if (!c->dev) return -1;
+	return sepdev_event_elapsed(c->dev, e0, e1, ms);
+}
+
+int sep_gpu_stream_sync(seppart *ptr)
+{
+	rt_ctx *c = rt_get(ptr, __func__);
+	if (!c->dev) return 0;
+	return sepdev_sync(c->dev);
+}
+
+/* Set up the single pair term of a device loop, as the first iteration's
+ * sep_force_pairs / sep_force_lj call would. */
+static rt_ctx *loop_setup(seppart *ptr, sepsys *sys, const char *types,
+			  double (*fun)(double, char), const double *ljparam, double cf,
+			  unsigned opt, sepdev_pairset *ps)
+{
+	rt_ctx *c = rt_get(ptr, "sep_gpu_run");
+	const double rc = fun ? cf : ljparam[0];
+	if (rc > sys->cf) sep_error("cutoff for an interaction cannot be larger than maximum cutoff");
+	rt_need_device(c, sys);
+	rt_flush(c);
+	rt_prepare_list(c, sys, opt, 1);
+	/* one pending term describes the loop's pair force */
+	rt_term *T = &c->terms[0];
+	memset(T, 0, sizeof *T);
+	if (fun) {
+		T->rc = cf; T->eps = 1.0; T->sigma = 1.0; T->aw = 1.0;
+		if (fun == sep_lj_shift) { T->kind = SEPDEV_POT_LJ; T->ushift = SEP_LJCF2; }
+		else if (fun == sep_lj) { T->kind = SEPDEV_POT_LJ; }
+		else if (fun == sep_wca) { T->kind = SEPDEV_POT_LJ; T->ushift = 1.0; }
+		else sep_error("sep_gpu_run: only sep_lj, sep_lj_shift, sep_wca or LJ parameters");
+	} else {
+		T->kind = SEPDEV_POT_LJ;
+		T->rc = ljparam[0]; T->eps = ljparam[1]; T->sigma = ljparam[2]; T->aw = ljparam[3];
+		T->ushift = -4.0 * T->eps * (pow(T->sigma / T->rc, 12.) - T->aw * pow(T->sigma / T->rc, 6.));
+	}
+	T->t0 = types[0];
+	T->t1 = types[1];
+	c->nterms = 1;
+	c->coul_on = 0;
+	rt_pairset(c, ps);
+	c->nterms = 0;
+	return c;
+}
+
+/* results of a device loop into sys and ret, as after the last sep_leapfrog */
+static void loop_finish(rt_ctx *c, sepsys *sys, sepret *ret, const double *s, long nsteps,
+			long ntrig, int last_trig)
+{
+	sep_reset_retval(ret);
+	ret->epot = s[SLOT_EPOT0];
+	ret->ekin = 0.5 * s[SLOT_EKIN];
+	const double *P = s + SLOT_POTP, *K = s + SLOT_KINP;
+	const int map[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+	for (int k = 0; k < 3; k++)
+		for (int kk = 0; kk < 3; kk++) {
+			ret->pot_P[k][kk] = P[map[k][kk]];
+			ret->kin_P[k][kk] = K[map[k][kk]];
+		}
+	sys->max_dist2 = s[SLOT_MAXD2];
+	sys->nupdate_neighb += (unsigned)ntrig;
+	sys->tnow += nsteps * sys->dt;
+	if (last_trig) {
+		sys->neighb_flag = 1;
+		c->list_stale = 1;
+		c->trigger_next = 1;
+	} else if (sys->neighb_update != SEP_BRUTE && ntrig > 0) {
+		sys->neighb_flag = 0;
+	}
+	c->pending_trigger = 0;
+	c->host_valid = 0;
+	c->forces_zero = 0;
+	c->friction = 0;
+}
+
+int sep_gpu_run(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
+		double (*fun)(double, char), const double *ljparam, double cf, unsigned opt,
+		int nh, double T0, double *alpha, double tau, long nsteps)
+{
+	if (nsteps <= 0) return 0;
+	sepdev_pairset ps;
+	rt_ctx *c = loop_setup(ptr, sys, types, fun, ljparam, cf, opt, &ps);
+	sepdev_runcfg cfg;
+	memset(&cfg, 0, sizeof cfg);
+	cfg.dt = sys->dt;
+	cfg.skin = sys->skin;
+	cfg.nh = nh;
+	cfg.T0 = T0;
+	cfg.tau = tau;
+	cfg.force_trigger = c->pending_trigger;
+	if (!c->sumv2_valid) {
+		rt_check(sepdev_sumv2(c->dev, &c->sumv2), "kinetic sum");
+		c->sumv2_valid = 1;
+	}
+	double a = alpha ? *alpha : 0.0, last[SLOT_FIELDS];
+	if (nh) {
+		/* the first step's thermostat update, exactly as sep_nosehoover */
+		const double ekin = 0.5 * c->sumv2 / sys->npart;
+		const double temp = 0.666667 * ekin;
+		a = a + sys->dt / (tau * tau) * (temp / T0 - 1.0);
+	}
+	long ntrig = 0;
+	int lt = 0;
+	rt_check(sepdev_run(c->dev, &ps, &cfg, nsteps, &a, &c->sumv2, last, &ntrig, &lt), "device loop");
+	if (alpha && nh) *alpha = a;
+	c->nbuild += ntrig;
+	loop_finish(c, sys, ret, last, nsteps, ntrig, lt);
+	return 0;
+}
+
+int sep_gpu_time_step_kernel(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
+			     double (*fun)(double, char), const double *ljparam, double cf,
+			     unsigned opt, int nh, double T0, double *alpha, double tau,
+			     long nsteps, double *ms_per_launch)
+{
+	double total = 0.0;
+	long timed = 0;
+	for (long s = 0; s < nsteps; s++) {
+		sepdev_pairset ps;
+		rt_ctx *c = loop_setup(ptr, sys, types, fun, ljparam, cf, opt, &ps);
+		if (nh) {
+			const double ekin = 0.5 * c->sumv2 / sys->npart;
+			const double temp = 0.666667 * ekin;
+			*alpha = *alpha + sys->dt / (tau * tau) * (temp / T0 - 1.0);
+		}
+		const int slot = rt_new_slot(c), lf = rt_new_slot(c);
+		rt_check(sepdev_event_record(c->dev, 0), "event");
+		rt_check(sepdev_step(c->dev, &ps, 0, sys->dt, nh, nh ? *alpha : 0.0, slot, lf), "step");
+		rt_check(sepdev_event_record(c->dev, 1), "event");
+		float ms = 0.f;
+		rt_check(sepdev_event_elapsed(c->dev, 0, 1, &ms), "event");
+		total += ms;
+		timed++;
+		sep_reset_retval(ret);
+		rt_add_op(c, ret, OP_PAIR_ASSIGN, slot, 0);
+		rt_add_op(c, ret, OP_VIRIAL, slot, 0);
+		rt_add_op(c, ret, OP_KIN, lf, 0);
+		sys->max_dist2 = 0.0;
+		rt_read_slots(c, sys, lf);
+		if (sqrt(sys->max_dist2) > sys->skin * 0.5 || c->pending_trigger) {
+			sys->neighb_flag = 1;
+			sys->nupdate_neighb++;
+			c->list_stale = 1;
+			c->trigger_next = 1;
+			c->pending_trigger = 0;
+		}
+		sys->tnow += sys->dt;
+		c->host_valid = 0;
+		c->forces_zero = 0;
+	}
+	if (ms_per_launch) *ms_per_launch = timed ? total / timed : 0.0;
+	return 0;
+}

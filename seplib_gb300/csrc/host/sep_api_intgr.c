@@ -1,0 +1,80 @@
+/*
+ * sep_api_intgr.c - Nose-Hoover thermostat and leap-frog of the sep C API.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include "sep_rt.h"
+
+/* Nose-Hoover (source/sepintgr.c:149-168).  The thermostat update itself is
+ * scalar and done here in FP64 from the device's sum m v^2; the friction
+ * f -= alpha m v is deferred to the next force materialisation, normally the
+ * fused leap-frog kernel. */
+void sep_nosehoover(seppart *ptr, double temp0, double *alpha, const double tau, sepsys *sys)
+{
+	rt_ctx *c = rt_get(ptr, __func__);
+	double sv2;
+	if (c->dev && c->dev_valid) {
+		if (!c->sumv2_valid) {
+			rt_check(sepdev_sumv2(c->dev, &c->sumv2), "kinetic sum");
+			c->sumv2_valid = 1;
+		}
+		sv2 = c->sumv2;
+	} else {
+		sv2 = 0.0;
+		for (long i = 0; i < sys->npart; i++)
+			for (int k = 0; k < 3; k++) sv2 += ptr[i].v[k] * ptr[i].v[k] * ptr[i].m;
+	}
+	const double ekin = 0.5 * sv2 / sys->npart;
+	const double temp = 0.666667 * ekin;
+	*alpha = *alpha + sys->dt / (tau * tau) * (temp / temp0 - 1.0);
+	if (c->dev && c->dev_valid) {
+		c->friction = 1;
+		c->friction_alpha += *alpha;
+		c->host_valid = 0;
+	} else {
+		for (long i = 0; i < sys->npart; i++)
+			for (int k = 0; k < 3; k++) ptr[i].f[k] -= *alpha * ptr[i].m * ptr[i].v[k];
+	}
+}
+
+/* Leap-frog (source/sepintgr.c:42-88).  Pending pair terms, friction and the
+ * integration run as one fused kernel; the step's sums are read back and
+ * applied to retval and sys before returning, so the program sees the
+ * reference's values after every call. */
+void sep_leapfrog(seppart *ptr, sepsys *sys, sepret *retval)
+{
+	rt_ctx *c = rt_get(ptr, __func__);
+	rt_need_device(c, sys);
+	int lf;
+	if (c->pass_slot >= 0) {
+		sepdev_pairset ps;
+		extern void rt_pairset(rt_ctx *c, sepdev_pairset *ps);
+		rt_pairset(c, &ps);
+		lf = rt_new_slot(c);
+		rt_check(sepdev_step(c->dev, &ps, !c->forces_zero, sys->dt, c->friction,
+				     c->friction_alpha, c->pass_slot, lf), "fused step");
+		c->nterms = 0;
+		c->coul_on = 0;
+		c->pass_slot = -1;
+	} else {
+		if (c->forces_zero) rt_check(sepdev_zero_forces(c->dev), "force reset");
+		lf = rt_new_slot(c);
+		rt_check(sepdev_leapfrog(c->dev, sys->dt, c->friction, c->friction_alpha, lf), "leap-frog");
+	}
+	c->forces_zero = 0;
+	c->friction = 0;
+	c->friction_alpha = 0.0;
+	c->host_valid = 0;
+	rt_add_op(c, retval, OP_KIN, lf, 0);
+	rt_read_slots(c, sys, lf);
+	if (sqrt(sys->max_dist2) > sys->skin * 0.5 || c->pending_trigger) {
+		sys->neighb_flag = 1;
+		sys->nupdate_neighb++;
+		c->list_stale = 1;
+		c->trigger_next = 1;
+		c->pending_trigger = 0;
+	}
+	sys->tnow += sys->dt;
+}

@@ -1,0 +1,203 @@
+/*
+ * sepdev.h - C ABI between the C99 host layer (the csrc/host sources) and the
+ * CUDA device layer (the csrc/cuda sources).  Plain pointers and sizes only.
+ *
+ * One sepdev context holds one particle system resident on the GPU:
+ *   - positions as 64-bit fixed-point fractions of the box edge, split in a
+ *     32-bit high word (packed with the type id in an int4, double-buffered,
+ *     read by the pair kernels) and a 32-bit low word;
+ *   - velocities as float-float pairs (hi + lo), mass and 1/mass packed in the
+ *     fourth lanes;
+ *   - forces as float4 (xyz + per-particle pair energy);
+ *   - everything stored in cell order (a spatial sort refreshed at every
+ *     neighbour-list build), with gid[] mapping a slot to the user index.
+ * Reductions (energies, virial, kinetic tensor) land in "slots" of 64-bit
+ * fixed-point accumulators (scale 2^32), read back in one copy.
+ */
+#ifndef SEPDEV_H
+#define SEPDEV_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sepdev sepdev;
+
+/* status codes (0 = success) */
+#define SEPDEV_OK            0
+#define SEPDEV_ECUDA        -1   /* CUDA runtime error, message in sepdev_last_error() */
+#define SEPDEV_ENOMEM       -2
+#define SEPDEV_EINVAL       -3
+#define SEPDEV_EOVERFLOW    -4   /* neighbour list capacity exceeded */
+#define SEPDEV_ENODEV       -5   /* no CUDA device */
+
+#define SEPDEV_MAXTYPES 16
+#define SEPDEV_MAXCHAN   4
+
+/* fields of one accumulator slot (int64, value * 2^32) */
+enum {
+	SLOT_EPOT0 = 0,        /* energy channels 0..3 */
+	SLOT_ECOUL = 4,
+	SLOT_POTP = 5,         /* pot_P: 6 entries xx xy xz yy yz zz (9 reserved) */
+	SLOT_POTPB = 14,       /* pot_P_bond: 6 entries (9 reserved) */
+	SLOT_EKIN = 23,        /* sum m vt^2 (leap-frog kinetic term, before the 1/2) */
+	SLOT_KINP = 24,        /* 6 entries xx xy xz yy yz zz */
+	SLOT_SUMV2 = 30,       /* sum m v^2 after the step (for the next Nose-Hoover call) */
+	SLOT_MAXD2 = 31,       /* max squared displacement since the last build, float bits */
+	SLOT_FIELDS = 32
+};
+
+/* exclusion modes for the list build (see the oracle's ora_excluded) */
+enum { SEPDEV_EXCL_NONE = 0, SEPDEV_EXCL_BONDS = 1, SEPDEV_EXCL_ALLBONDED = 2,
+       SEPDEV_EXCL_SAMEMOL = 3 };
+
+/* pair-potential kinds */
+enum { SEPDEV_POT_OFF = 0, SEPDEV_POT_LJ = 1, SEPDEV_POT_TABLE = 2 };
+
+/*
+ * Pair interaction table for one force pass: for every ordered type pair
+ * (ti, tj) one potential.  LJ: ft = eps48 s6 (s6 - awh) sig2/r^2 with
+ * s6 = (sig2/r^2)^3, u = eps4 s6 (s6 - aw) + ushift, cut at rc2.
+ * TABLE: tabulated ft(r^2) and u(r^2) on a uniform r^2 grid.
+ */
+typedef struct {
+	int kind;
+	int chan;              /* energy channel 0..3 */
+	float rc2;
+	float eps48, eps4, sig2, aw, awh;
+	float ushift;
+	int table;             /* index of the table for SEPDEV_POT_TABLE */
+} sepdev_pot;
+
+typedef struct {
+	int ntypes;
+	int nchan;                                  /* energy channels in use */
+	sepdev_pot pot[SEPDEV_MAXTYPES * SEPDEV_MAXTYPES];
+	int coulomb;                                /* shifted-force Coulomb on */
+	float coul_rc2, coul_irc2, coul_irc, coul_rc;
+} sepdev_pairset;
+
+/* ---- context ---- */
+int sepdev_create(sepdev **out, long n);
+void sepdev_destroy(sepdev *d);
+const char *sepdev_last_error(void);
+int sepdev_device_count(void);
+
+/*
+ * Upload the full state (user order).  x, v: 3n doubles; m, z: n doubles;
+ * type_id, molindex: n ints; crossings, cross_neighb: 3n ints; L: 3 doubles.
+ * The internal order is reset to the user order and the list marked stale.
+ */
+int sepdev_upload(sepdev *d, const double *x, const double *v, const double *f,
+		  const double *m, const double *z, const int *type_id, const int *molindex,
+		  const int *crossings, const int *cross_neighb, const double *L);
+
+/* Download to user order.  Any pointer may be NULL.  xn receives the
+ * positions at the last list build. */
+int sepdev_download(sepdev *d, double *x, double *v, double *f, int *crossings,
+		    int *cross_neighb, double *xn);
+
+/* Sum of m v^2 over the current velocities (one reduction, synchronous). */
+int sepdev_sumv2(sepdev *d, double *out);
+
+/* Exclusion partner lists in user order: two CSR tables, partners by user
+ * index; `bonds` = direct bonds, `all` = bond+angle+dihedral partners. */
+int sepdev_set_exclusions(sepdev *d, const int *bond_start, const int *bond_idx,
+			  const int *all_start, const int *all_idx);
+
+/* Tabulated potential: nt points, ft and u at r2 = r2min + k*dr2. */
+int sepdev_set_table(sepdev *d, int table, int nt, double r2min, double dr2,
+		     const float *ft, const float *u);
+
+/* ---- accumulator slots ---- */
+int sepdev_slots_reset(sepdev *d);              /* zero all slots (async) */
+int sepdev_slots_read(sepdev *d, int nslots, double *out, unsigned *flags);
+	/* synchronous: out[nslots*SLOT_FIELDS] as doubles (MAXD2 decoded), flags = status word */
+
+/* ---- neighbour list ---- */
+/* Rebuild the cell order and the full neighbour list with cut-off rlist.
+ * trigger != 0 marks a skin-triggered rebuild (crossing base reset). */
+int sepdev_build_list(sepdev *d, double rlist, int excl, int trigger);
+/* Pair set of the current list, user indices, i<j, unique: returns count,
+ * fills up to cap pairs (2 ints each).  Test and diagnostics helper. */
+long sepdev_list_pairs(sepdev *d, int *pairs, long cap);
+int sepdev_list_stats(sepdev *d, int *maxcount, double *meancount, int *capacity);
+
+/* ---- forces and integration ---- */
+/*
+ * Pair forces of `ps` over the current list.  accumulate != 0 adds to the
+ * stored forces, otherwise overwrites them.  Energies go to slot `slot`
+ * channels, virial to its POTP entries.
+ */
+int sepdev_pair_forces(sepdev *d, const sepdev_pairset *ps, int accumulate, int slot);
+
+/*
+ * Leap-frog (source/sepintgr.c:42-88 semantics) on the stored forces.
+ * nh != 0 subtracts alpha m v first and stores the modified force.
+ * Kinetic terms, sum m v^2 and the displacement maximum go to `slot`.
+ */
+int sepdev_leapfrog(sepdev *d, double dt, int nh, double alpha, int slot);
+
+/* Fused pair forces + optional Nose-Hoover friction + leap-frog in one kernel. */
+int sepdev_step(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
+		int nh, double alpha, int pair_slot, int lf_slot);
+
+/* f -= alpha m v on the stored forces. */
+int sepdev_friction(sepdev *d, double alpha);
+
+/* Set stored forces to zero. */
+int sepdev_zero_forces(sepdev *d);
+
+/* ---- bonded terms ---- */
+/* Topology in user indices: nb bonds (a,b,type), na angles (a,b,c,type),
+ * nd dihedrals (a,b,c,d,type). */
+int sepdev_set_topology(sepdev *d, int nb, const unsigned *blist, int na,
+			const unsigned *alist, int nd, const unsigned *dlist);
+int sepdev_bonds(sepdev *d, int type, double l0, double k, int slot);
+int sepdev_angles(sepdev *d, int type, double theta0, double k, int cossq, int slot);
+int sepdev_torsions(sepdev *d, int type, const double g[6], int slot);
+/* per-term observables of the last call of each kind (0 bond lengths,
+ * 1 angles, 2 dihedral angles), in topology order */
+int sepdev_term_values(sepdev *d, int kind, double *out);
+
+/* ---- timing and multi-step ---- */
+int sepdev_sync(sepdev *d);
+/* events on the context stream: record into slot e (0..7), elapsed ms */
+int sepdev_event_record(sepdev *d, int e);
+int sepdev_event_elapsed(sepdev *d, int e0, int e1, float *ms);
+
+/*
+ * Run nsteps of {pair forces, [Nose-Hoover], leap-frog} entirely on the
+ * device, rebuilding the list when the skin test fires.  The loop is one
+ * CUDA graph (WHILE node over two unrolled steps, each behind an IF node that
+ * holds the captured list rebuild); a one-thread kernel after each step
+ * updates the thermostat and decides the rebuild.  The list must be valid on
+ * entry.  alpha: in, the thermostat value the first step uses (already
+ * advanced by the caller); out, the value the last step used, as
+ * sep_nosehoover leaves it; sumv2: sum m v^2 in/out; last: the final step's
+ * slot values (SLOT_FIELDS doubles); ntrig: skin-triggered updates;
+ * last_trig: whether the final step requested an update.
+ */
+typedef struct {
+	double dt, skin;
+	int nh;
+	double T0, tau;
+	int force_trigger;     /* report an update after the first step */
+} sepdev_runcfg;
+
+int sepdev_run(sepdev *d, const sepdev_pairset *ps, const sepdev_runcfg *cfg, long nsteps,
+	       double *alpha, double *sumv2, double *last, long *ntrig, int *last_trig);
+
+/* lanes per particle in the pair kernels (1, 2, 4); invalidates the list */
+int sepdev_set_tpp(sepdev *d, int tpp);
+int sepdev_get_tpp(sepdev *d);
+
+/* kernel launches issued by this context so far (all kinds) */
+long sepdev_launch_count(sepdev *d);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

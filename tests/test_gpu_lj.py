@@ -1,0 +1,161 @@
+"""Parity of the GPU plain-LJ path with the FP64 oracle (sepora.c).
+
+Bars: neighbour pair set identical to the FP64 brute-force set except for
+pairs within 1e-6 sigma of rc+skin; single-step forces within 1e-5 relative
+L2 (over all particles) of FP64; energies and virial within 1e-6 relative;
+NVE energy drift over 1e4 steps no worse than 2x the oracle's.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from seplib_gb300 import configs as cfg
+from seplib_gb300 import sepapi as A
+from sephelp import Handle, boundary_mask, gpu_pairs, pairset, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-5      # relative L2 of the force field, FP32 pair maths vs FP64
+ENERGY_TOL = 1e-6     # relative, sums are 64-bit fixed point above warp level
+
+
+def small():
+    return cfg.plain_lj_small(seed=1)
+
+
+def oracle_forces(ora, s, cf=2.5, kind=None, param=None):
+    kind = ora.POT_LJSHIFT if kind is None else kind
+    pairs = ora.pairs_brute(s.x, s.L, cf)
+    st, nb = ora.csr_from_pairs(s.n, pairs)
+    return ora.pair_forces(s.x, s.types, s.L, "AA", kind, param, cf, st, nb)
+
+
+def test_pair_set_matches_fp64(gpu_lib, ora):
+    s = small()
+    h = Handle(gpu_lib, s, skin=0.5)
+    h.forces()
+    got = gpu_pairs(gpu_lib, h.atoms, 200000)
+    ref = ora.pairs_brute(s.x, s.L, 3.0)
+    near = boundary_mask(s.x, s.L, ref, 3.0)
+    assert pairset(ref[~near]) - pairset(got) == set()
+    extra = pairset(got) - pairset(ref)
+    gnear = boundary_mask(s.x, s.L, got, 3.0)
+    assert extra <= pairset(got[gnear])
+    h.close()
+
+
+def test_single_step_forces(gpu_lib, ora):
+    s = small()
+    # perturb the lattice so forces are not all zero
+    rng = np.random.default_rng(7)
+    s.x = np.mod(s.x + rng.normal(0, 0.05, s.x.shape), s.L)
+    h = Handle(gpu_lib, s, skin=0.5)
+    h.forces()
+    h.sync()
+    f, e, pP = oracle_forces(ora, s)
+    assert rel_l2(h.view["f"], f) < FORCE_TOL
+    assert abs(h.ret.epot - e) < ENERGY_TOL * abs(e)
+    assert np.allclose(np.array(h.ret.pot_P), pP, rtol=1e-5, atol=1e-6 * np.abs(pP).max())
+    h.close()
+
+
+def test_force_lj_param_form(gpu_lib, ora):
+    s = small()
+    rng = np.random.default_rng(8)
+    s.x = np.mod(s.x + rng.normal(0, 0.05, s.x.shape), s.L)
+    h = Handle(gpu_lib, s, skin=0.5)
+    p = (C.c_double * 4)(2.5, 1.3, 1.05, 1.0)
+    gpu_lib.sep_reset_retval(C.byref(h.ret))
+    gpu_lib.sep_reset_force(h.atoms, C.byref(h.sys))
+    gpu_lib.sep_force_lj(h.atoms, b"AA", p, C.byref(h.sys), C.byref(h.ret), A.SEP_ALL)
+    h.sync()
+    f, e, _ = oracle_forces(ora, s, kind=ora.POT_LJPARAM, param=np.array(p[:]))
+    assert rel_l2(h.view["f"], f) < FORCE_TOL
+    # epsilon = 1.3 and sigma^2 = 1.1025 are not FP32 numbers: their rounding
+    # shifts every pair term by ~1e-7, and the net energy here cancels to
+    # ~1% of the summed magnitudes, so the bar is relative to sum |u_ij|
+    assert abs(h.ret.epot - e) < ENERGY_TOL * abs_pair_energy(ora, s, np.array(p[:]))
+    h.close()
+
+
+def abs_pair_energy(ora, s, p):
+    pairs = ora.pairs_brute(s.x, s.L, p[0])
+    d = s.x[pairs[:, 0]] - s.x[pairs[:, 1]]
+    d -= s.L * np.round(d / s.L)
+    s6 = (p[2] ** 2 / (d * d).sum(1)) ** 3
+    shift = 4 * p[1] * ((p[2] / p[0]) ** 12 - p[3] * (p[2] / p[0]) ** 6)
+    return float(np.abs(4 * p[1] * s6 * (s6 - p[3]) - shift).sum())
+
+
+def oracle_run(ora, s, nsteps, nh=False, skin=0.5, T0=1.0, tau=10.0, alpha=0.0):
+    return ora.run_lj(s.x, s.v, s.m, s.types, s.L, ora.POT_LJSHIFT, None, 2.5, skin, 0.005,
+                      nsteps, nh=nh, T0=T0, tau=tau, alpha=alpha)
+
+
+@pytest.mark.parametrize("nh", [False, True])
+def test_short_trajectory(gpu_lib, ora, nh):
+    s = small()
+    h = Handle(gpu_lib, s, skin=0.5)
+    nsteps = 20
+    for _ in range(nsteps):
+        h.step(nh=(1.0, 10.0) if nh else None)
+    h.sync()
+    r = oracle_run(ora, s, nsteps, nh=nh)
+    assert np.abs(h.view["v"] - r["v"]).max() < 1e-5
+    dx = h.view["x"] - r["x"]
+    dx -= s.L * np.round(dx / s.L)
+    assert np.abs(dx).max() < 1e-6
+    assert abs(h.ret.epot - r["epot"]) < 1e-5 * abs(r["epot"])
+    assert abs(h.ret.ekin - r["ekin"]) < 1e-5 * abs(r["ekin"])
+    # entries are sums of +-m v_k v_kk terms: tolerance scaled to the diagonal
+    kscale = np.abs(np.diag(r["kinP"])).max()
+    assert np.abs(np.array(h.ret.kin_P) - r["kinP"]).max() < 1e-6 * kscale
+    assert h.sys.nupdate_neighb == r["nupdate"]
+    if nh:
+        assert abs(h.alpha.value - r["alpha"]) < 1e-6 * max(1e-3, abs(r["alpha"]))
+    h.close()
+
+
+def test_graph_loop_equals_api_loop(gpu_lib):
+    """sep_gpu_run must reproduce the C-API loop bit for bit."""
+    s = small()
+    a = Handle(gpu_lib, s, skin=0.5)
+    b = Handle(gpu_lib, s, skin=0.5)
+    nsteps = 37
+    for _ in range(nsteps):
+        a.step(nh=(1.0, 10.0))
+    rc = gpu_lib.sep_gpu_run(b.atoms, C.byref(b.sys), C.byref(b.ret), b"AA", b.fun(), None, 2.5,
+                             A.SEP_ALL, 1, 1.0, C.byref(b.alpha), 10.0, nsteps)
+    assert rc == 0
+    a.sync(); b.sync()
+    assert np.array_equal(a.view["x"], b.view["x"])
+    assert np.array_equal(a.view["v"], b.view["v"])
+    assert a.alpha.value == b.alpha.value
+    assert a.ret.epot == b.ret.epot and a.ret.ekin == b.ret.ekin
+    assert a.sys.nupdate_neighb == b.sys.nupdate_neighb
+    a.close(); b.close()
+
+
+def test_nve_drift(gpu_lib, ora):
+    """Energy drift over 1e4 NVE steps of the N=1000 workload.  Truncation at
+    rc makes the total energy a random walk whose drift varies by a factor of
+    several between initial conditions, so the bar compares the mean |drift|
+    over four seeds: GPU <= 2x oracle."""
+    chunks, per = 100, 100
+    t = np.arange(chunks)
+    dg, dr = [], []
+    for seed in (1, 2, 3, 4):
+        s = cfg.plain_lj_small(seed=seed)
+        h = Handle(gpu_lib, s, skin=0.5)
+        et = []
+        for _ in range(chunks):
+            gpu_lib.sep_gpu_run(h.atoms, C.byref(h.sys), C.byref(h.ret), b"AA", h.fun(), None,
+                                2.5, A.SEP_ALL, 0, 1.0, None, 1.0, per)
+            et.append((h.ret.epot + h.ret.ekin) / s.n)
+        h.close()
+        r = ora.run_lj(s.x, s.v, s.m, s.types, s.L, ora.POT_LJSHIFT, None, 2.5, 0.5, 0.005,
+                       chunks * per, trace=True)
+        dg.append(abs(np.polyfit(t, np.asarray(et), 1)[0]) * chunks)
+        dr.append(abs(np.polyfit(t, r["etot"][per - 1::per], 1)[0]) * chunks)
+    assert np.mean(dg) <= 2.0 * np.mean(dr), (dg, dr)
