@@ -1,0 +1,324 @@
+"""Benchmark of the seplib MD-step hot path on GB300.
+
+Workload (one "step" = one MD step of the whole system):
+  plain LJ NVT, N = 4*ncell^3 atoms on an fcc lattice (ncell=40: N=256000) at
+  rho*=0.8442, Maxwell-Boltzmann velocities at T*=1.0 (seeded); Nose-Hoover
+  T0=1.0, Q=10; shifted LJ rc=2.5; skin 0.3; dt=0.005; FP32 pair forces,
+  64-bit fixed-point positions, FP64-exact sums.
+
+Printed JSON line (rank 0):
+  value   particle-steps/s of the device-resident loop (sep_gpu_run, one CUDA
+          graph; state resident in HBM), timed with CUDA events on the
+          library's stream, max over ranks;
+  e2e     the same metric through the reference-facing C API, prgs-style
+          loop (sep_reset_retval, sep_reset_force, sep_force_pairs,
+          sep_nosehoover, sep_leapfrog) starting from host seppart arrays:
+          the host->device upload, every per-step copy and the final
+          device->host download are inside the timed region;
+  roofline  the fused step kernel: algorithmic bytes per launch
+          N*(4*nbar_f + 128), nbar_f = 4/3 pi (rc+skin)^3 rho, divided by its
+          mean launch duration (events around each launch);
+  cpu_baseline  the CPU oracle (FP64 restatement of the reference's threaded
+          linked-cell path) on a bounded sample of the same workload.
+
+`--impl reference` times that CPU path alone (the reference sources cannot
+be built on the GPU host, so the oracle port stands in for them).
+Multi-GPU: independent replicas, one per rank (the system does not shard).
+"""
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+RHO, TEMP, RC, SKIN, DT, T0, TAU = 0.8442, 1.0, 2.5, 0.3, 0.005, 1.0, 10.0
+L2_BYTES = 129 * 2 ** 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=200)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ncell", type=int, default=40, help="fcc cells per edge (40: N=256000)")
+    ap.add_argument("--cpu-steps", type=int, default=0, help="oracle steps for cpu_baseline (0: auto)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--tpp", type=int, default=0)
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        # one GPU per rank: the library uses the first visible device
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload_config(args, n):
+    nbar = 4.0 / 3.0 * math.pi * (RC + SKIN) ** 3 * RHO
+    return {
+        "workload": "plain LJ NVT fcc %d^3 cells, N=%d, rho*=%.4f, T*=%.1f, Nose-Hoover T0=%.1f Q=%.0f, "
+                    "shifted LJ rc=%.1f, skin %.1f, dt=%.3f" % (args.ncell, n, RHO, TEMP, T0, TAU, RC, SKIN, DT),
+        "n_particles": n, "rc": RC, "skin": SKIN, "dt": DT, "ensemble": "NVT Nose-Hoover",
+        "nbar_full_list": round(nbar, 2),
+        "algorithmic_bytes_per_particle_step": round(4 * nbar + 128, 1),
+        "parallelism": "replicas (one independent system per GPU)",
+    }
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.p = None
+        self.path = os.path.join(HERE, "gpurun_out", "clocks_bench.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.fh = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                       "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return None
+        time.sleep(0.25)
+        self.p.terminate()
+        self.p.wait()
+        self.fh.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1])); mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def new_system(lib, s):
+    from seplib_gb300 import sepapi as A
+    atoms = lib.sep_init(s.n, A.SEP_NEIGHB)
+    v = A.parts_view(atoms, s.n)
+    v["x"], v["v"], v["m"], v["type"] = s.x, s.v, s.m, s.types
+    sys_ = lib.sep_sys_setup(s.L[0], s.L[1], s.L[2], RC, DT, s.n, A.SEP_LLIST_NEIGHBLIST)
+    lib.sep_set_skin(C.byref(sys_), SKIN)
+    return atoms, sys_
+
+
+def cpu_leg(s, steps, threads):
+    """time the oracle's threaded LJ loop on a sample of the workload"""
+    import oracle
+    oracle.build()
+    t0 = time.perf_counter()
+    oracle.run_lj(s.x, s.v, s.m, s.types, s.L, oracle.POT_LJSHIFT, None, RC, SKIN, DT, steps,
+                  nh=True, T0=T0, tau=TAU, alpha=0.0, nthreads=threads)
+    el = time.perf_counter() - t0
+    return s.n * steps / el, el
+
+
+def run_reference(args, rank, world):
+    from seplib_gb300 import configs
+    if rank != 0:
+        return
+    s = configs.plain_lj_large(args.ncell, seed=2)
+    threads = os.cpu_count() or 1
+    steps = max(1, args.cpu_steps or max(3, min(args.steps, 40)))
+    cpu_leg(s, max(1, args.warmup // 100), threads)        # warm-up (page-in, thread pool)
+    val, el = cpu_leg(s, steps, threads)
+    line = {"metric": "particle-steps/s", "value": val, "unit": "particle-steps/s", "n_gpus": 0,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded fcc lattice, Maxwell-Boltzmann velocities)",
+            "config": workload_config(args, s.n), "impl": "reference",
+            "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                             "sample": "%d MD steps of the full N=%d system" % (steps, s.n)},
+            "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    rank, world = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    from seplib_gb300 import build, configs, load, sepapi as A, GpuInfo
+    build.build()
+    lib = load()
+    if not lib.sep_gpu_available():
+        raise SystemExit("no CUDA device visible")
+    s = configs.plain_lj_large(args.ncell, seed=2 + rank)
+    n = s.n
+    fun = A.fun_ptr(lib, "sep_lj_shift")
+
+    # ---- device-resident loop (value) ----
+    atoms, sys_ = new_system(lib, s)
+    if args.tpp:
+        lib.sep_gpu_set_tpp(atoms, args.tpp)
+    ret = A.SepRet()
+    alpha = C.c_double(0.0)
+    run = lambda k: lib.sep_gpu_run(atoms, C.byref(sys_), C.byref(ret), b"AA", fun, None, RC,
+                                    A.SEP_ALL, 1, T0, C.byref(alpha), TAU, k)
+    assert run(max(3, args.warmup)) == 0
+    lib.sep_gpu_stream_sync(atoms)
+    info0 = GpuInfo()
+    lib.sep_gpu_info_get(atoms, C.byref(info0))
+    upd0 = sys_.nupdate_neighb
+    clocks = Clocks()
+    clocks.start()
+    barrier(world)
+    lib.sep_gpu_stream_sync(atoms)
+    lib.sep_gpu_event_record(atoms, 2)
+    assert run(args.steps) == 0
+    lib.sep_gpu_event_record(atoms, 3)
+    ms = C.c_float()
+    lib.sep_gpu_event_elapsed(atoms, 2, 3, C.byref(ms))
+    lib.sep_gpu_stream_sync(atoms)
+    barrier(world)
+    clk = clocks.stop()
+    t_dev = allmax(world, ms.value / 1e3)
+    rebuilds = sys_.nupdate_neighb - upd0
+    epot_pp = ret.epot / n
+    temp = 2.0 * ret.ekin / (3.0 * n)
+    value = world * n * args.steps / t_dev
+
+    # ---- roofline of the fused step kernel ----
+    mspl = C.c_double()
+    lib.sep_gpu_time_step_kernel(atoms, C.byref(sys_), C.byref(ret), b"AA", fun, None, RC, A.SEP_ALL,
+                                 1, T0, C.byref(alpha), TAU, 50, C.byref(mspl))
+    info = GpuInfo()
+    lib.sep_gpu_info_get(atoms, C.byref(info))
+    lib.sep_close(atoms, n)
+    nbar = 4.0 / 3.0 * math.pi * (RC + SKIN) ** 3 * RHO
+    alg_bytes = n * (4 * nbar + 128)
+    achieved = alg_bytes / (mspl.value / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    rebuild_bytes = n * (4 * nbar + 64)
+    achieved_step = n * (4 * nbar + 128 + (4 * nbar + 64) * rebuilds / args.steps) * args.steps / t_dev / 1e9
+
+    # ---- end to end through the sep C API with host buffers ----
+    atoms, sys_ = new_system(lib, s)
+    ret = A.SepRet()
+    alpha = C.c_double(0.0)
+    nh_alpha = C.byref(alpha)
+
+    def api_steps(k):
+        for _ in range(k):
+            lib.sep_reset_retval(C.byref(ret))
+            lib.sep_reset_force(atoms, C.byref(sys_))
+            lib.sep_force_pairs(atoms, b"AA", RC, fun, C.byref(sys_), C.byref(ret), A.SEP_ALL)
+            lib.sep_nosehoover(atoms, T0, nh_alpha, TAU, C.byref(sys_))
+            lib.sep_leapfrog(atoms, C.byref(sys_), C.byref(ret))
+
+    api_steps(max(3, args.warmup // 10))      # warm the path (context, list, caches)
+    lib.sep_gpu_sync(atoms)
+    lib.sep_gpu_invalidate(atoms)             # next call uploads the host arrays again
+    e_steps = args.steps
+    barrier(world)
+    t0 = time.perf_counter()
+    api_steps(e_steps)
+    lib.sep_gpu_sync(atoms)                   # device -> host download of x, v, f, ...
+    t_e2e = allmax(world, time.perf_counter() - t0)
+    lib.sep_close(atoms, n)
+    state_bytes = n * (16 + 16 + 16 + 16 + 16 + 4 + 4 + 16 + 16)   # what upload/download move
+    h2d = (state_bytes + 8 * 4 * n) / e_steps + 16
+    d2h = (state_bytes + 4 * n) / e_steps + 2 * 8 * 32 + 16
+    e2e_val = world * n * e_steps / t_e2e
+
+    # ---- CPU baseline (rank 0, N=1) ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        steps = args.cpu_steps or 100
+        cval, el = cpu_leg(s, steps, threads)
+        cpu = {"value": cval, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+               "sample": "%d MD steps of the full N=%d system (oracle port of the reference's "
+                         "threaded linked-cell LJ path, FP64), %.1f s" % (steps, n, el)}
+
+    wset = n * (16 * 2 + 16 * 4 + 16 + 4) + n * info.list_capacity * 4
+    if rank == 0:
+        cfgd = workload_config(args, n)
+        cfgd["l2"] = "no flush; per-step working set %.0f MB vs %d MB L2" % (wset / 2 ** 20, L2_BYTES // 2 ** 20)
+        cfgd["tpp"] = info.tpp
+        cfgd["list_mean_full"] = round(info.list_mean, 2)
+        cfgd["list_rebuilds_in_timed_steps"] = rebuilds
+        cfgd["final_state"] = {"epot_per_particle": epot_pp, "temperature": temp}
+        line = {
+            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 pair / fixed-point x / f64-exact sums",
+            "data": "synthetic (seeded fcc lattice, Maxwell-Boltzmann velocities)",
+            "config": cfgd,
+            "e2e": {"value": e2e_val, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": e_steps,
+                    "path": "sep C API prgs-style loop, host seppart arrays, upload+download timed"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                         "kernel": "k_pair<fused step>", "kernel_ms": mspl.value,
+                         "bytes_per_launch": alg_bytes,
+                         "whole_step_achieved_incl_rebuild": achieved_step},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": 2 * args.steps + 7 * rebuilds,
+        }
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -93,9 +93,15 @@ struct sepdev {
 	int nslots;
 
 	sepdev_pairset *d_ps;   // device copy of the current pair set
+	sepdev_pairset h_ps;    // what d_ps holds (uploads are skipped when unchanged)
+	int ps_valid;
 
 	// graph runner state
 	void *runner;
+
+	// kernel variants chosen by the tuner (SEPLIB_LJ_VARIANT overrides)
+	int lj_variant;
+	int nsm;
 
 	long launches;
 };
@@ -149,6 +155,50 @@ __device__ __forceinline__ long long ff_mul_fix(float hi, float lo, float shi, f
 	return __float2ll_rn(p) + __float2ll_rn(r);
 }
 
+// ---- packed FP32 pairs (f32x2 instructions of sm_100-family GPUs) --------
+// Two floats in one 64-bit register; one instruction operates on both.
+typedef unsigned long long f2_t;
+__device__ __forceinline__ f2_t f2_pack(float a, float b)
+{
+	f2_t r;
+	asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+	return r;
+}
+__device__ __forceinline__ void f2_unpack(f2_t r, float &a, float &b)
+{
+	asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c)
+{
+	f2_t d;
+	asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+	return d;
+}
+__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b)
+{
+	f2_t d;
+	asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+	return d;
+}
+__device__ __forceinline__ f2_t f2_add(f2_t a, f2_t b)
+{
+	f2_t d;
+	asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+	return d;
+}
+__device__ __forceinline__ f2_t f2_sub(f2_t a, f2_t b)
+{
+	f2_t d;
+	asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+	return d;
+}
+__device__ __forceinline__ float f2_sum(f2_t r)
+{
+	float a, b;
+	f2_unpack(r, a, b);
+	return a + b;
+}
+
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31; }
 
 // Warp sum of NV floats, result valid in lane 0.
@@ -196,6 +246,16 @@ __device__ __forceinline__ void block_to_slot(float (&v)[NV], const int (&fld)[N
 				atomicMax((unsigned long long *)&base[maxfld], (unsigned long long)m);
 		}
 	}
+}
+
+// Neighbour-list layout (one lane per particle): particle i is lane
+// p = i % 32 of tile t = i / 32; its entry k lives at
+//     nl[t*maxnb*32 + (k/4)*128 + p*4 + (k%4)]
+// so a lane's next four neighbours are one 16-byte load and a warp's batch
+// of four is one contiguous 512-byte read.  maxnb is a multiple of 8.
+__host__ __device__ __forceinline__ long nl_index(long i, int k, int maxnb)
+{
+	return (i >> 5) * (long)maxnb * 32 + (long)(k >> 2) * 128 + (i & 31) * 4 + (k & 3);
 }
 
 static inline int grid_for(long n, int block) { return (int)((n + block - 1) / block); }

@@ -76,19 +76,6 @@ __global__ void k_scatter(long n, const int *__restrict__ cellof, const int *__r
 	if (s < n) perm[start[cellof[s]] + celloff[s]] = (int)s;
 }
 
-__global__ void k_cellsort(long m, const int *__restrict__ start, const int *__restrict__ gid,
-			   int *__restrict__ perm)
-{
-	long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
-	if (c >= m) return;
-	int lo = start[c], hi = start[c + 1];
-	for (int a = lo + 1; a < hi; a++) {
-		int v = perm[a], key = gid[v], b = a - 1;
-		while (b >= lo && gid[perm[b]] > key) { perm[b + 1] = perm[b]; b--; }
-		perm[b + 1] = v;
-	}
-}
-
 struct GatherArgs {
 	const int *perm;
 	const int4 *pos; int4 *pos_o;
@@ -150,79 +137,231 @@ struct BuildArgs {
 	const int *exs, *exi;   // CSR for the active exclusion mode
 };
 
-template <int TPP>
-__global__ void __launch_bounds__(128) k_build(long n, BuildArgs a)
+// Tile-staged list build: one warp per tile of 32 consecutive particles (in
+// cell order a tile covers a short run of cells along x).  For each row run
+// of the tile the warp stages the candidates of the deduplicated 3x3
+// neighbouring rows over the x range [first cell - 1, last cell + 1] with
+// coalesced loads (a cell row is one contiguous range of the sorted
+// particles), converted once into FP32 offsets from the run's first
+// particle; candidates farther than rlist from the bounding box of the run's
+// particles are dropped and the rest compacted into shared memory, where
+// every lane of the run tests them (broadcast reads).  Candidates outside a
+// lane's own 27 cells are at least one cell edge (>= rlist) away and fail the
+// distance test.
+// Accepted entries go to a per-warp shared ring of BT_RING rows ([row][lane],
+// conflict-free) with a branch-free append; complete four-entry groups are
+// written out as 16-byte stores whenever the next chunk could wrap the ring
+// onto entries not yet written.
+#define BT_WARPS 4
+#define BT_CAP 32      // staged candidates per chunk
+#define BT_RING 64     // ring rows per warp (power of two)
+
+__device__ __forceinline__ int wrapc(int c, int n) { return c < 0 ? c + n : (c >= n ? c - n : c); }
+
+__device__ __forceinline__ float warp_min_f(float v, unsigned mask)
 {
-	long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-	if (i >= n) return;
-	constexpr int P = 32 / TPP;
-	const int4 pi = a.pos[i];
-	const int cx = (int)__umulhi((unsigned)pi.x, (unsigned)a.nc[0]);
-	const int cy = (int)__umulhi((unsigned)pi.y, (unsigned)a.nc[1]);
-	const int cz = (int)__umulhi((unsigned)pi.z, (unsigned)a.nc[2]);
-	int *base = a.nl + (i / P) * (long)a.maxnb * P + (i % P) * TPP;
-	const int gi = a.gid[i], mi = a.mol[i];
-	int cnt = 0;
-	const int lo0 = a.nc[0] >= 3 ? -1 : 0, hi0 = a.nc[0] >= 2 ? 1 : 0;
-	const int lo1 = a.nc[1] >= 3 ? -1 : 0, hi1 = a.nc[1] >= 2 ? 1 : 0;
-	const int lo2 = a.nc[2] >= 3 ? -1 : 0, hi2 = a.nc[2] >= 2 ? 1 : 0;
-	for (int oz = lo2; oz <= hi2; oz++) {
-		int zz = cz + oz; zz += (zz < 0) ? a.nc[2] : 0; zz -= (zz >= a.nc[2]) ? a.nc[2] : 0;
-		for (int oy = lo1; oy <= hi1; oy++) {
-			int yy = cy + oy; yy += (yy < 0) ? a.nc[1] : 0; yy -= (yy >= a.nc[1]) ? a.nc[1] : 0;
-			const int row = a.nc[0] * (yy + a.nc[1] * zz);
-			for (int ox = lo0; ox <= hi0; ox++) {
-				int xx = cx + ox; xx += (xx < 0) ? a.nc[0] : 0; xx -= (xx >= a.nc[0]) ? a.nc[0] : 0;
-				const int c = xx + row;
-				const int jb = a.cellstart[c], je = a.cellstart[c + 1];
-				for (int j = jb; j < je; j++) {
-					if (j == (int)i) continue;
-					const int4 pj = __ldg(&a.pos[j]);
-					const float dx = sep_hi(pi.x, pj.x, a.fs[0]);
-					const float dy = sep_hi(pi.y, pj.y, a.fs[1]);
-					const float dz = sep_hi(pi.z, pj.z, a.fs[2]);
-					const float r2 = dx * dx + dy * dy + dz * dz;
-					if (r2 >= a.rl2) continue;
-					if (a.excl == SEPDEV_EXCL_SAMEMOL) {
-						if (mi != -1 && mi == a.mol[j]) continue;
-					} else if (a.excl != SEPDEV_EXCL_NONE) {
-						const int gj = a.gid[j];
-						if (in_csr(a.exs, a.exi, gi, gj) || in_csr(a.exs, a.exi, gj, gi)) continue;
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(mask, v, o));
+	return v;
+}
+
+__device__ __forceinline__ float warp_max_f(float v, unsigned mask)
+{
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(mask, v, o));
+	return v;
+}
+
+__global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles(long n, BuildArgs a)
+{
+	__shared__ float4 sp_all[BT_WARPS][BT_CAP];
+	__shared__ int ring_all[BT_WARPS][BT_RING * 32];
+	const unsigned FULL = 0xffffffffu;
+	const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	float4 *sp = sp_all[w];
+	int *ring = ring_all[w];
+	const long i0 = ((long)blockIdx.x * BT_WARPS + w) * 32;
+	if (i0 >= n) return;
+	const long i = i0 + lane;
+	const bool act = i < n;
+	const int4 pi = a.pos[act ? i : i0];
+	const int nc0 = a.nc[0], nc1 = a.nc[1], nc2 = a.nc[2];
+	const int cx = (int)__umulhi((unsigned)pi.x, (unsigned)nc0);
+	const int cy = (int)__umulhi((unsigned)pi.y, (unsigned)nc1);
+	const int cz = (int)__umulhi((unsigned)pi.z, (unsigned)nc2);
+	const int row = cy + nc1 * cz;
+	int4 *gbase = (int4 *)(a.nl + nl_index(i, 0, a.maxnb));   // this lane's group 0
+	const int gi = act ? a.gid[i] : -1, mi = act ? a.mol[i] : -1;
+	const int lo1 = nc1 >= 3 ? -1 : 0, hi1 = nc1 >= 2 ? 1 : 0;
+	const int lo2 = nc2 >= 3 ? -1 : 0, hi2 = nc2 >= 2 ? 1 : 0;
+	const int cap = a.maxnb;
+	const float rl = sqrtf(a.rl2);
+	int cnt = 0, flushed = 0;     // entries found / entries written out (multiple of 4)
+	bool me = false, local = false;
+	float mx = 0.f, my = 0.f, mz = 0.f;
+	float bx0 = 0.f, bx1 = 0.f, by0 = 0.f, by1 = 0.f, bz0 = 0.f, bz1 = 0.f;
+	int4 ref = pi;
+	auto excluded = [&](int j) -> bool {
+		if (a.excl == SEPDEV_EXCL_SAMEMOL) return mi != -1 && mi == a.mol[j];
+		const int gj = a.gid[j];
+		return in_csr(a.exs, a.exi, gi, gj) || in_csr(a.exs, a.exi, gj, gi);
+	};
+	auto flush = [&]() {
+		const int top = cnt < cap ? cnt : cap;
+		const int g0 = flushed >> 2, g1 = (top + 3) >> 2;
+		const int gmin = __reduce_min_sync(FULL, act ? g0 : 0x7fffffff);
+		const int gmax = __reduce_max_sync(FULL, act ? g1 : 0);
+		for (int g = gmin; g < gmax; g++) {
+			if (act && g >= g0 && g < g1) {
+				const int r = (4 * g) & (BT_RING - 1);
+				gbase[g * 32] = make_int4(ring[r * 32 + lane], ring[(r + 1) * 32 + lane],
+							  ring[(r + 2) * 32 + lane], ring[(r + 3) * 32 + lane]);
+			}
+		}
+		flushed = top & ~3;
+	};
+	auto test = [&](int fill) {
+		__syncwarp();
+		// entries not yet written out must stay in the ring through this chunk
+		const int span = __reduce_max_sync(FULL, act ? cnt - flushed : 0);
+		if (span + fill > BT_RING) flush();
+		if (me) {
+			if (local && a.excl == SEPDEV_EXCL_NONE) {
+#pragma unroll 4
+				for (int c = 0; c < fill; c++) {
+					const float4 q = sp[c];
+					const float dx = mx - q.x, dy = my - q.y, dz = mz - q.z;
+					const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+					const int j = __float_as_int(q.w);
+					const bool hit = (r2 < a.rl2) & (j != (int)i);
+					ring[(cnt & (BT_RING - 1)) * 32 + lane] = j;
+					cnt += hit ? 1 : 0;
+				}
+			} else {
+				for (int c = 0; c < fill; c++) {
+					const float4 q = sp[c];
+					const int j = __float_as_int(q.w);
+					float dx, dy, dz;
+					if (local) { dx = mx - q.x; dy = my - q.y; dz = mz - q.z; }
+					else {
+						dx = sep_hi(pi.x, __float_as_int(q.x), a.fs[0]);
+						dy = sep_hi(pi.y, __float_as_int(q.y), a.fs[1]);
+						dz = sep_hi(pi.z, __float_as_int(q.z), a.fs[2]);
 					}
-					if (cnt < a.maxnb) base[(cnt / TPP) * 32 + (cnt % TPP)] = j;
+					if (!(dx * dx + dy * dy + dz * dz < a.rl2) || j == (int)i) continue;
+					if (a.excl != SEPDEV_EXCL_NONE && excluded(j)) continue;
+					ring[(cnt & (BT_RING - 1)) * 32 + lane] = j;
 					cnt++;
 				}
 			}
 		}
+		__syncwarp();
+	};
+	unsigned todo = __ballot_sync(FULL, act);
+	while (todo) {
+		const int leader = __ffs(todo) - 1;
+		const int rrow = __shfl_sync(FULL, row, leader);
+		const unsigned mine = __ballot_sync(FULL, act && row == rrow);
+		todo &= ~mine;
+		me = (mine >> lane) & 1u;
+		const int xlo = __shfl_sync(FULL, cx, __ffs(mine) - 1);
+		const int xhi = __shfl_sync(FULL, cx, 31 - __clz(mine));
+		const int ry = rrow % nc1, rz = rrow / nc1;
+		// the staged region spans (xhi - xlo + 3) x 3 x 3 cells; when that is
+		// under half the box on every axis, separations need no wrapping
+		local = 2 * (xhi - xlo + 3) < nc0 && 6 < nc1 && 6 < nc2;
+		ref.x = __shfl_sync(FULL, pi.x, leader);
+		ref.y = __shfl_sync(FULL, pi.y, leader);
+		ref.z = __shfl_sync(FULL, pi.z, leader);
+		mx = sep_hi(pi.x, ref.x, a.fs[0]);
+		my = sep_hi(pi.y, ref.y, a.fs[1]);
+		mz = sep_hi(pi.z, ref.z, a.fs[2]);
+		// bounding box of the run's particles, widened by rlist at use
+		bx0 = warp_min_f(me ? mx : 3.0e38f, FULL); bx1 = warp_max_f(me ? mx : -3.0e38f, FULL);
+		by0 = warp_min_f(me ? my : 3.0e38f, FULL); by1 = warp_max_f(me ? my : -3.0e38f, FULL);
+		bz0 = warp_min_f(me ? mz : 3.0e38f, FULL); bz1 = warp_max_f(me ? mz : -3.0e38f, FULL);
+		int sA0, sA1, sB0 = 0, sB1 = 0;
+		if (xhi - xlo + 3 >= nc0) { sA0 = 0; sA1 = nc0; }
+		else {
+			const int s0 = xlo - 1, s1 = xhi + 2;
+			if (s0 < 0) { sA0 = s0 + nc0; sA1 = nc0; sB1 = s1; }
+			else if (s1 > nc0) { sA0 = s0; sA1 = nc0; sB1 = s1 - nc0; }
+			else { sA0 = s0; sA1 = s1; }
+		}
+		int fill = 0;
+		for (int oz = lo2; oz <= hi2; oz++) {
+			const int zz = wrapc(rz + oz, nc2);
+			for (int oy = lo1; oy <= hi1; oy++) {
+				const int yy = wrapc(ry + oy, nc1);
+				const int rb = nc0 * (yy + nc1 * zz);
+				for (int sg = 0; sg < 2; sg++) {
+					const int c0 = sg ? sB0 : sA0, c1 = sg ? sB1 : sA1;
+					if (c1 <= c0) continue;
+					const int jb = a.cellstart[rb + c0], je = a.cellstart[rb + c1];
+					for (int jj = jb; jj < je; jj += 32) {
+						const int take = min(32, je - jj);
+						if (fill + take > BT_CAP) { test(fill); fill = 0; }
+						bool keep = lane < take;
+						float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+						if (keep) {
+							const int4 pj = a.pos[jj + lane];
+							if (local) {
+								q = make_float4(sep_hi(pj.x, ref.x, a.fs[0]), sep_hi(pj.y, ref.y, a.fs[1]),
+										sep_hi(pj.z, ref.z, a.fs[2]), __int_as_float(jj + lane));
+								const float ex = fmaxf(fmaxf(bx0 - q.x, q.x - bx1), 0.f);
+								const float ey = fmaxf(fmaxf(by0 - q.y, q.y - by1), 0.f);
+								const float ez = fmaxf(fmaxf(bz0 - q.z, q.z - bz1), 0.f);
+								keep = ex < rl && ey < rl && ez < rl &&
+								       fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < a.rl2;
+							} else {
+								q = make_float4(__int_as_float(pj.x), __int_as_float(pj.y),
+										__int_as_float(pj.z), __int_as_float(jj + lane));
+							}
+						}
+						const unsigned kb = __ballot_sync(FULL, keep);
+						if (keep) sp[fill + __popc(kb & ((1u << lane) - 1u))] = q;
+						fill += __popc(kb);
+					}
+				}
+			}
+		}
+		test(fill);
 	}
-	a.ncnt[i] = cnt < a.maxnb ? cnt : a.maxnb;
-	if (cnt > a.maxnb) atomicOr(&a.flags[0], 1u);
-	atomicMax(&a.flags[1], (unsigned)cnt);
+	__syncwarp();
+	flush();
+	if (act) {
+		a.ncnt[i] = cnt < cap ? cnt : cap;
+		if (cnt > cap) atomicOr(&a.flags[0], 1u);
+	}
+	const unsigned mxc = __reduce_max_sync(FULL, act ? (unsigned)cnt : 0u);
+	if (lane == 0) atomicMax(&a.flags[1], mxc);
 }
 
-static int grow(sepdev *d, void **p, size_t bytes, size_t *cap)
+// Deterministic order inside each cell: one warp per cell ranks its members
+// by user index with shuffles (cells of more than 32 fall back to a serial
+// insertion sort in lane 0).
+__global__ void k_cellsort_w(long m, const int *__restrict__ start, const int *__restrict__ gid,
+			     int *__restrict__ perm)
 {
-	if (*p && *cap >= bytes) return SEPDEV_OK;
-	if (*p) cudaFree(*p);
-	*p = NULL;
-	cudaError_t e = cudaMalloc(p, bytes);
-	if (e != cudaSuccess) { sepdev_set_error("cudaMalloc(list)", e); *cap = 0; return SEPDEV_ENOMEM; }
-	*cap = bytes;
-	(void)d;
-	return SEPDEV_OK;
-}
-
-static int launch_build(sepdev *d, const BuildArgs &a)
-{
-	const int B = 128;
-	switch (d->tpp) {
-	case 1: k_build<1><<<grid_for(d->n, B), B, 0, d->st>>>(d->n, a); break;
-	case 2: k_build<2><<<grid_for(d->n, B), B, 0, d->st>>>(d->n, a); break;
-	case 4: k_build<4><<<grid_for(d->n, B), B, 0, d->st>>>(d->n, a); break;
-	default: k_build<8><<<grid_for(d->n, B), B, 0, d->st>>>(d->n, a); break;
+	const long c = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+	const int lane = threadIdx.x & 31;
+	if (c >= m) return;
+	const int lo = start[c], cnt = start[c + 1] - lo;
+	if (cnt <= 1) return;
+	if (cnt <= 32) {
+		const int v = lane < cnt ? perm[lo + lane] : 0;
+		const int key = lane < cnt ? gid[v] : 0x7fffffff;
+		int rank = 0;
+		for (int l = 0; l < cnt; l++) rank += (__shfl_sync(0xffffffffu, key, l) < key);
+		__syncwarp();
+		if (lane < cnt) perm[lo + rank] = v;
+	} else if (lane == 0) {
+		for (int x = lo + 1; x < lo + cnt; x++) {
+			int v = perm[x], key = gid[v], b = x - 1;
+			while (b >= lo && gid[perm[b]] > key) { perm[b + 1] = perm[b]; b--; }
+			perm[b + 1] = v;
+		}
 	}
-	CKL(d);
-	return SEPDEV_OK;
 }
 
 // Copy the gathered arrays back into the primary buffers, so buffer
@@ -254,6 +393,26 @@ __global__ void k_copyback(long n, CopyArgs a)
 	a.gid_d[t] = a.gid_s[t];
 	a.chg_d[t] = a.chg_s[t];
 	a.mol_d[t] = a.mol_s[t];
+}
+
+static int grow(sepdev *d, void **p, size_t bytes, size_t *cap)
+{
+	if (*p && *cap >= bytes) return SEPDEV_OK;
+	if (*p) cudaFree(*p);
+	*p = NULL;
+	cudaError_t e = cudaMalloc(p, bytes);
+	if (e != cudaSuccess) { sepdev_set_error("cudaMalloc(list)", e); *cap = 0; return SEPDEV_ENOMEM; }
+	*cap = bytes;
+	(void)d;
+	return SEPDEV_OK;
+}
+
+static int launch_build(sepdev *d, const BuildArgs &a)
+{
+	const int grid = grid_for((d->n + 31) / 32, BT_WARPS);
+	k_build_tiles<<<grid, BT_WARPS * 32, 0, d->st>>>(d->n, a);
+	CKL(d);
+	return SEPDEV_OK;
 }
 
 // Cell grid for cut-off rlist: edge >= rlist, total cells bounded by 2n + 64.
@@ -294,7 +453,7 @@ int sepdev_sort_async(sepdev *d, int parity, int trigger)
 	CKL(d);
 	k_scatter<<<grid_for(n, B), B, 0, d->st>>>(n, d->cellof, d->celloff, d->cellstart, d->perm);
 	CKL(d);
-	k_cellsort<<<grid_for(d->ncells, B), B, 0, d->st>>>(d->ncells, d->cellstart, d->gid, d->perm);
+	k_cellsort_w<<<grid_for(d->ncells * 32, B), B, 0, d->st>>>(d->ncells, d->cellstart, d->gid, d->perm);
 	CKL(d);
 	GatherArgs g;
 	const int o = parity ^ 1;
@@ -331,10 +490,9 @@ int sepdev_sort_async(sepdev *d, int parity, int trigger)
 
 static int list_capacity(sepdev *d, int maxnb)
 {
-	const int P = 32 / d->tpp;
 	maxnb = ((maxnb + 7) / 8) * 8;
-	const size_t tiles = (size_t)((d->n + P - 1) / P);
-	const size_t bytes = tiles * (size_t)P * (size_t)maxnb * sizeof(int);
+	const size_t tiles = (size_t)((d->n + 31) / 32);
+	const size_t bytes = tiles * 32 * (size_t)maxnb * sizeof(int);
 	int rc = grow(d, (void **)&d->nl, bytes, &d->cap_nl);
 	if (rc) return rc;
 	d->maxnb = maxnb;
@@ -430,9 +588,7 @@ extern "C" long sepdev_list_pairs(sepdev *d, int *pairs, long cap)
 {
 	if (!d->list_valid) return -1;
 	const long n = d->n;
-	const int P = 32 / d->tpp;
-	const size_t tiles = (size_t)((n + P - 1) / P);
-	const size_t len = tiles * P * (size_t)d->maxnb;
+	const size_t len = (size_t)((n + 31) / 32) * 32 * (size_t)d->maxnb;
 	int *nl = (int *)malloc(sizeof(int) * len), *cnt = (int *)malloc(sizeof(int) * n);
 	int *gid = (int *)malloc(sizeof(int) * n);
 	if (!nl || !cnt || !gid) { free(nl); free(cnt); free(gid); return -2; }
@@ -442,10 +598,9 @@ extern "C" long sepdev_list_pairs(sepdev *d, int *pairs, long cap)
 	if (cudaStreamSynchronize(d->st) != cudaSuccess) { free(nl); free(cnt); free(gid); return -3; }
 	long np = 0;
 	for (long i = 0; i < n; i++) {
-		const int *base = nl + (i / P) * (size_t)d->maxnb * P + (i % P) * d->tpp;
 		for (int k = 0; k < cnt[i]; k++) {
-			int j = base[(k / d->tpp) * 32 + (k % d->tpp)];
-			int gi = gid[i], gj = gid[j];
+			const int j = nl[nl_index(i, k, d->maxnb)];
+			const int gi = gid[i], gj = gid[j];
 			if (gi < gj) {
 				if (np < cap) { pairs[2 * np] = gi; pairs[2 * np + 1] = gj; }
 				np++;
@@ -459,10 +614,7 @@ extern "C" long sepdev_list_pairs(sepdev *d, int *pairs, long cap)
 
 extern "C" int sepdev_set_tpp(sepdev *d, int tpp)
 {
-	if (tpp != 1 && tpp != 2 && tpp != 4) return SEPDEV_EINVAL;
-	d->tpp = tpp;
-	d->list_valid = 0;
-	return SEPDEV_OK;
+	return tpp == 1 ? SEPDEV_OK : SEPDEV_EINVAL;
 }
 
-extern "C" int sepdev_get_tpp(sepdev *d) { return d->tpp; }
+extern "C" int sepdev_get_tpp(sepdev *d) { (void)d; return 1; }

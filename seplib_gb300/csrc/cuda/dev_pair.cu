@@ -106,10 +106,9 @@ __device__ __forceinline__ void integrate(long i, float fx, float fy, float fz, 
 	d2 = dx * dx + dy * dy + dz * dz;
 }
 
-template <int TPP, int VAR, bool FUSED>
+template <int VAR, bool FUSED>
 __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 {
-	constexpr int P = 32 / TPP;
 	constexpr int NCH = VAR == VAR_SINGLE ? 1 : 4;
 	extern __shared__ sepdev_pot spot[];
 	if (a.flags && (a.flags[0] & 1u)) return;    // list overflow: leave the state untouched
@@ -119,9 +118,7 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 		for (int k = threadIdx.x; k < ntypes * ntypes; k += blockDim.x) spot[k] = a.ps->pot[k];
 		__syncthreads();
 	}
-	const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
-	const long i = g / TPP;
-	const int q = (int)(g % TPP);
+	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
 	const bool act = i < n;
 	float fx = 0.f, fy = 0.f, fz = 0.f;
 	float e[NCH];
@@ -133,7 +130,7 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 	if (act) {
 		pi = a.pos[i];
 		const int cnt = a.ncnt[i];
-		const int *base = a.nl + (i / P) * (long)a.maxnb * P + (i % P) * TPP + q;
+		const int *base = a.nl + nl_index(i, 0, a.maxnb);
 		float qi = 0.f;
 		bool coul_i = false;
 		if (VAR == VAR_GENERAL_COUL) {
@@ -142,8 +139,8 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 		}
 		const float sx = a.fs[0], sy = a.fs[1], sz = a.fs[2];
 #pragma unroll 4
-		for (int k = q; k < cnt; k += TPP) {
-			const int j = __ldg(base + (k / TPP) * 32);
+		for (int k = 0; k < cnt; k++) {
+			const int j = __ldg(base + (k >> 2) * 128 + (k & 3));
 			const int4 pj = __ldg(&a.pos[j]);
 			const float dx = sep_hi(pi.x, pj.x, sx);
 			const float dy = sep_hi(pi.y, pj.y, sy);
@@ -181,19 +178,11 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 			w3 += gy * dy; w4 += gy * dz; w5 += gz * dz;
 		}
 	}
-	// per-particle totals across the TPP lanes of particle i
 	float etot = ec;
 #pragma unroll
 	for (int c = 0; c < NCH; c++) etot += e[c];
-#pragma unroll
-	for (int o = TPP / 2; o > 0; o >>= 1) {
-		fx += __shfl_xor_sync(0xffffffffu, fx, o);
-		fy += __shfl_xor_sync(0xffffffffu, fy, o);
-		fz += __shfl_xor_sync(0xffffffffu, fz, o);
-		etot += __shfl_xor_sync(0xffffffffu, etot, o);
-	}
 	float ek = 0.f, kp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, sv2 = 0.f, d2 = 0.f;
-	if (act && q == 0) {
+	if (act) {
 		if (a.accumulate) {
 			const float4 fo = a.frc[i];
 			fx += fo.x; fy += fo.y; fz += fo.z;
@@ -235,6 +224,102 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 		for (int k = 0; k < 6; k++) { v[NCH + 8 + k] = kp[k]; fld[NCH + 8 + k] = (int)off + SLOT_KINP + k; }
 		v[NCH + 14] = sv2; fld[NCH + 14] = (int)off + SLOT_SUMV2;
 		block_to_slot<NCH + 15>(v, fld, ps, d2, (int)off + SLOT_MAXD2);
+	}
+}
+
+// Fast path for one Lennard-Jones potential on all pairs (the plain-LJ
+// workload).  A lane owns one particle and consumes its neighbour list in
+// batches of four: one 16-byte load brings the next four indices (the
+// following batch is already in flight while the current one is computed),
+// then four independent position gathers, then branch-free pair maths with
+// the cut-off as a mask.  For a cubic box the box scale is folded out of the
+// pair loop: separations stay in fixed-point units (L/2^32) and the
+// per-particle sums are rescaled once.
+template <bool FUSED, bool CUBIC, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_lj(long n, PairArgs a)
+{
+	if (a.flags && (a.flags[0] & 1u)) return;
+	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	const bool act = i < n;
+	const float u = a.fs[0];
+	const float sx = CUBIC ? 1.f : a.fs[0], sy = CUBIC ? 1.f : a.fs[1], sz = CUBIC ? 1.f : a.fs[2];
+	const float rc2 = CUBIC ? a.rc2 / (u * u) : a.rc2;
+	const float sig2 = CUBIC ? a.sig2 / (u * u) : a.sig2;
+	const float eps48 = a.eps48, eps4 = a.eps4, awh = a.awh, aw = a.aw;
+	float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f, nin = 0.f;
+	float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f, w4 = 0.f, w5 = 0.f;
+	int4 pi = make_int4(0, 0, 0, 0);
+	if (act) {
+		pi = a.pos[i];
+		const int cnt = a.ncnt[i];
+		const int4 *lp = (const int4 *)(a.nl + nl_index(i, 0, a.maxnb));
+		const int nb = (cnt + 3) >> 2;
+		int4 jn = nb > 0 ? __ldg(lp) : make_int4(0, 0, 0, 0);
+		for (int s0 = 0; s0 < nb; s0++) {
+			const int4 jc = jn;
+			if (s0 + 1 < nb) jn = __ldg(lp + (s0 + 1) * 32);
+			const int rem = cnt - 4 * s0;
+			const int j[4] = {jc.x, rem > 1 ? jc.y : (int)i, rem > 2 ? jc.z : (int)i,
+					  rem > 3 ? jc.w : (int)i};
+			int4 pj[4];
+#pragma unroll
+			for (int b = 0; b < 4; b++) pj[b] = __ldg(&a.pos[j[b]]);
+#pragma unroll
+			for (int b = 0; b < 4; b++) {
+				const float dx = (float)(pi.x - pj[b].x) * sx;
+				const float dy = (float)(pi.y - pj[b].y) * sy;
+				const float dz = (float)(pi.z - pj[b].z) * sz;
+				const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+				const bool in = (b < rem) && (r2 < rc2);
+				// pairs outside the cut-off get s2 = 0, which zeroes their
+				// force and energy; the shift is added per hit at the end
+				const float s2 = in ? sig2 * fast_rcp(r2) : 0.f;
+				const float s6 = s2 * s2 * s2;
+				const float ft = eps48 * s6 * (s6 - awh) * s2;
+				e = fmaf(eps4 * s6, s6 - aw, e);
+				nin += in ? 1.f : 0.f;
+				const float gx = ft * dx, gy = ft * dy, gz = ft * dz;
+				fx += gx; fy += gy; fz += gz;
+				w0 = fmaf(gx, dx, w0); w1 = fmaf(gx, dy, w1); w2 = fmaf(gx, dz, w2);
+				w3 = fmaf(gy, dy, w3); w4 = fmaf(gy, dz, w4); w5 = fmaf(gz, dz, w5);
+			}
+		}
+	}
+	e = fmaf(nin, a.ushift, e);
+	if (CUBIC) {
+		fx *= u; fy *= u; fz *= u;
+		const float u2 = u * u;
+		w0 *= u2; w1 *= u2; w2 *= u2; w3 *= u2; w4 *= u2; w5 *= u2;
+	}
+	const float etot = e;
+	float ek = 0.f, kp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, sv2 = 0.f, d2 = 0.f;
+	if (act) {
+		if (a.accumulate) {
+			const float4 fo = a.frc[i];
+			fx += fo.x; fy += fo.y; fz += fo.z;
+		}
+		if (FUSED) {
+			const float alpha = a.alpha_dev ? (float)*a.alpha_dev : a.alpha;
+			integrate(i, fx, fy, fz, 0.5f * etot, pi, a, alpha, a.pos_out, ek, kp, sv2, d2);
+		} else {
+			a.frc[i] = make_float4(fx, fy, fz, 0.5f * etot);
+		}
+	}
+	long long *ps = a.slots + (long)a.pslot * SLOT_FIELDS;
+	if (!FUSED) {
+		float v[7] = {0.5f * e, 0.5f * w0, 0.5f * w1, 0.5f * w2, 0.5f * w3, 0.5f * w4, 0.5f * w5};
+		const int fld[7] = {SLOT_EPOT0, SLOT_POTP, SLOT_POTP + 1, SLOT_POTP + 2, SLOT_POTP + 3,
+				    SLOT_POTP + 4, SLOT_POTP + 5};
+		block_to_slot<7>(v, fld, ps, 0.f, -1);
+	} else {
+		const int off = (int)((long)(a.lslot - a.pslot) * SLOT_FIELDS);
+		float v[15] = {0.5f * e, 0.5f * w0, 0.5f * w1, 0.5f * w2, 0.5f * w3, 0.5f * w4, 0.5f * w5,
+			       ek, kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], sv2};
+		const int fld[15] = {SLOT_EPOT0, SLOT_POTP, SLOT_POTP + 1, SLOT_POTP + 2, SLOT_POTP + 3,
+				     SLOT_POTP + 4, SLOT_POTP + 5, off + SLOT_EKIN, off + SLOT_KINP,
+				     off + SLOT_KINP + 1, off + SLOT_KINP + 2, off + SLOT_KINP + 3,
+				     off + SLOT_KINP + 4, off + SLOT_KINP + 5, off + SLOT_SUMV2};
+		block_to_slot<15>(v, fld, ps, d2, off + SLOT_MAXD2);
 	}
 }
 
@@ -310,34 +395,40 @@ void sepdev_fill_args(sepdev *d, PairArgs &a, const sepdev_pairset *ps, double d
 	a.flags = NULL;
 }
 
-static int upload_pairset(sepdev *d, const sepdev_pairset *ps)
+int sepdev_upload_pairset(sepdev *d, const sepdev_pairset *ps)
 {
-	CK(cudaMemcpyAsync(d->d_ps, ps, sizeof(sepdev_pairset), cudaMemcpyHostToDevice, d->st));
+	if (d->ps_valid && memcmp(&d->h_ps, ps, sizeof *ps) == 0) return SEPDEV_OK;
+	d->h_ps = *ps;
+	CK(cudaMemcpyAsync(d->d_ps, &d->h_ps, sizeof(sepdev_pairset), cudaMemcpyHostToDevice, d->st));
+	d->ps_valid = 1;
 	return SEPDEV_OK;
 }
 
-template <int TPP, bool FUSED>
-static void launch_tpp(sepdev *d, int var, const PairArgs &a, size_t shm)
+template <bool FUSED>
+static void launch_fused(sepdev *d, int var, const PairArgs &a, size_t shm)
 {
 	const int B = 256;
-	const int grid = grid_for(d->n * TPP, B);
-	if (var == VAR_SINGLE)
-		k_pair<TPP, VAR_SINGLE, FUSED><<<grid, B, 0, d->st>>>(d->n, a);
+	const int grid = grid_for(d->n, B);
+	const bool cubic = d->L[0] == d->L[1] && d->L[1] == d->L[2];
+	if (var == VAR_SINGLE && cubic) {
+		switch (d->lj_variant) {
+		case 1: k_lj<FUSED, true, 5><<<grid, B, 0, d->st>>>(d->n, a); break;
+		default: k_lj<FUSED, true, 4><<<grid, B, 0, d->st>>>(d->n, a); break;
+		}
+	} else if (var == VAR_SINGLE)
+		k_lj<FUSED, false, 4><<<grid, B, 0, d->st>>>(d->n, a);
 	else if (var == VAR_GENERAL)
-		k_pair<TPP, VAR_GENERAL, FUSED><<<grid, B, shm, d->st>>>(d->n, a);
+		k_pair<VAR_GENERAL, FUSED><<<grid, B, shm, d->st>>>(d->n, a);
 	else
-		k_pair<TPP, VAR_GENERAL_COUL, FUSED><<<grid, B, shm, d->st>>>(d->n, a);
+		k_pair<VAR_GENERAL_COUL, FUSED><<<grid, B, shm, d->st>>>(d->n, a);
 }
 
 int sepdev_launch_pair(sepdev *d, const sepdev_pairset *ps, PairArgs &a, bool fused)
 {
 	const int var = single_variant(ps) ? VAR_SINGLE : (ps->coulomb ? VAR_GENERAL_COUL : VAR_GENERAL);
 	const size_t shm = sizeof(sepdev_pot) * ps->ntypes * ps->ntypes;
-	switch (d->tpp) {
-	case 1: fused ? launch_tpp<1, true>(d, var, a, shm) : launch_tpp<1, false>(d, var, a, shm); break;
-	case 2: fused ? launch_tpp<2, true>(d, var, a, shm) : launch_tpp<2, false>(d, var, a, shm); break;
-	default: fused ? launch_tpp<4, true>(d, var, a, shm) : launch_tpp<4, false>(d, var, a, shm); break;
-	}
+	if (fused) launch_fused<true>(d, var, a, shm);
+	else launch_fused<false>(d, var, a, shm);
 	CKL(d);
 	return SEPDEV_OK;
 }
@@ -346,7 +437,7 @@ extern "C" int sepdev_pair_forces(sepdev *d, const sepdev_pairset *ps, int accum
 {
 	if (!d->list_valid || slot < 0 || slot >= d->nslots) return SEPDEV_EINVAL;
 	int rc;
-	if ((rc = upload_pairset(d, ps))) return rc;
+	if ((rc = sepdev_upload_pairset(d, ps))) return rc;
 	PairArgs a;
 	sepdev_fill_args(d, a, ps, 0.0, 0, 0.0, accumulate, slot, slot, d->cur);
 	return sepdev_launch_pair(d, ps, a, false);
@@ -359,7 +450,7 @@ extern "C" int sepdev_step(sepdev *d, const sepdev_pairset *ps, int accumulate, 
 	    lf_slot >= d->nslots)
 		return SEPDEV_EINVAL;
 	int rc;
-	if ((rc = upload_pairset(d, ps))) return rc;
+	if ((rc = sepdev_upload_pairset(d, ps))) return rc;
 	PairArgs a;
 	sepdev_fill_args(d, a, ps, dt, nh, alpha, accumulate, pair_slot, lf_slot, d->cur);
 	if ((rc = sepdev_launch_pair(d, ps, a, true))) return rc;

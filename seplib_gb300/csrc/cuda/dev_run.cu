@@ -26,6 +26,7 @@
 int sepdev_sort_async(sepdev *d, int parity, int trigger);
 int sepdev_build_async(sepdev *d, int parity);
 int sepdev_grow_list(sepdev *d, int needed);
+int sepdev_upload_pairset(sepdev *d, const sepdev_pairset *ps);
 
 struct RunState {
 	double alpha;          // alpha for the next step
@@ -260,7 +261,8 @@ extern "C" int sepdev_run(sepdev *d, const sepdev_pairset *ps, const sepdev_runc
 		CK(cudaMallocHost((void **)&r->h_rs, sizeof(RunState)));
 	}
 	Runner *r = (Runner *)d->runner;
-	CK(cudaMemcpyAsync(d->d_ps, ps, sizeof *ps, cudaMemcpyHostToDevice, d->st));
+	int rc0 = sepdev_upload_pairset(d, ps);
+	if (rc0) return rc0;
 	RunState *h = r->h_rs;
 	memset(h, 0, sizeof *h);
 	h->sumv2 = *sumv2;

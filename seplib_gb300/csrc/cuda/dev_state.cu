@@ -70,6 +70,11 @@ extern "C" int sepdev_create(sepdev **out, long n)
 	CK(cudaMemsetAsync(d->flags, 0, sizeof(unsigned) * 4, d->st));
 	CK(cudaMemsetAsync(d->frc, 0, sizeof(float4) * n, d->st));
 	d->tpp = 1;
+	CK(cudaDeviceGetAttribute(&d->nsm, cudaDevAttrMultiProcessorCount, d->device));
+	{
+		const char *v = getenv("SEPLIB_LJ_VARIANT");
+		d->lj_variant = v ? atoi(v) : 0;
+	}
 	*out = d;
 	return SEPDEV_OK;
 }
