@@ -19,6 +19,9 @@ class Handle:
         self.view["m"] = s.m
         self.view["z"] = s.z
         self.view["type"] = s.types
+        # the reference's sep_init leaves xn unset; a fresh allocation holds
+        # zeros, a recycled one the previous run's values.  Define it.
+        self.view["xn"] = 0.0
         self.sys = lib.sep_sys_setup(s.L[0], s.L[1], s.L[2], cf, dt, s.n, update)
         if skin is not None:
             lib.sep_set_skin(C.byref(self.sys), skin)

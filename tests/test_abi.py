@@ -1,0 +1,64 @@
+"""The C ABI boundary: every entry point declared in include/*.h is exported
+by libsep.so, the structures have the reference's byte layout, and the
+reference's own example programs compile and link unchanged."""
+import glob
+import os
+import re
+import subprocess
+
+import pytest
+
+from seplib_gb300 import sepapi as A
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+INC = os.path.join(ROOT, "include")
+LIBDIR = os.path.join(ROOT, "seplib_gb300", "lib")
+REF_PRGS = "/root/reference/prgs"
+REF_INC = "/root/reference/include"
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(INC, "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b(sep_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert len(names) > 50
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_struct_layout(tmp_path):
+    src = tmp_path / "lay.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "sep.h"\n'
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(seppart), '
+                   'sizeof(sepsys), sizeof(sepret), offsetof(seppart, xn), '
+                   'offsetof(sepsys, molptr), offsetof(sepret, pot_P), sizeof(sepmolinfo));return 0;}')
+    exe = tmp_path / "lay"
+    subprocess.run(["gcc", "-std=c99", "-I", INC, str(src), "-o", str(exe)], check=True)
+    vals = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    # the reference's LP64 layout
+    assert vals == [568, 168, 1000, 400, 160, 184, 120]
+    assert A.C.sizeof(A.SepPart) == 568 and A.C.sizeof(A.SepSys) == 168
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_PRGS), reason="reference programs not present")
+@pytest.mark.parametrize("prg", ["prg0.c", "prg4.c"])
+@pytest.mark.parametrize("headers", ["ours", "reference"])
+def test_reference_programs_link_unchanged(lib, tmp_path, prg, headers):
+    """prgs/prg0.c and prgs/prg4.c compile against these headers (or the
+    reference's own) and link against libsep.so without a source change."""
+    inc = INC if headers == "ours" else REF_INC
+    exe = tmp_path / prg.replace(".c", "")
+    cmd = ["gcc", "-std=c99", "-fgnu89-inline", "-DCOMPLEX", "-w", "-I", inc,
+           os.path.join(REF_PRGS, prg), "-o", str(exe), "-L", LIBDIR,
+           "-Wl,-rpath," + LIBDIR, "-Wl,--no-undefined", "-lsep", "-lm"]
+    subprocess.run(cmd, check=True)
+    assert exe.exists()

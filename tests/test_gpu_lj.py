@@ -159,3 +159,35 @@ def test_nve_drift(gpu_lib, ora):
         dg.append(abs(np.polyfit(t, np.asarray(et), 1)[0]) * chunks)
         dr.append(abs(np.polyfit(t, r["etot"][per - 1::per], 1)[0]) * chunks)
     assert np.mean(dg) <= 2.0 * np.mean(dr), (dg, dr)
+
+
+def test_c_program_through_the_api(gpu_lib, ora, tmp_path):
+    """a C program using only the sep API runs on the GPU library and agrees
+    with the oracle started from the state it saved"""
+    import os
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.join(root, "seplib_gb300", "lib")
+    exe = tmp_path / "lj_loop"
+    subprocess.run(["gcc", "-std=c99", "-O2", "-I", os.path.join(root, "include"),
+                    os.path.join(root, "tests", "c", "lj_loop.c"), "-o", str(exe), "-L", libdir,
+                    "-Wl,-rpath," + libdir, "-lsep", "-lm"], check=True)
+    xyz = tmp_path / "init.xyz"
+    out = subprocess.run([str(exe), str(xyz), "200"], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    epot, ekin, alpha, nupd, mom, p, x0 = out.stdout.split()
+    lines = xyz.read_text().split("\n")
+    n = int(lines[0])
+    L = np.array([float(t) for t in lines[1].split()])
+    data = np.array([[float(t) for t in ln.split()[1:]] for ln in lines[2:2 + n]])
+    x, v = data[:, 0:3], data[:, 3:6]
+    # sep_save_xyz writes the box with %f: take the exact box from the density
+    L[:] = (n / 0.8442) ** (1.0 / 3.0)
+    r = ora.run_lj(x, v, np.ones(n), np.full(n, b"A", "S1"), L, ora.POT_LJSHIFT, None, 2.5, 0.5,
+                   0.005, 200, nh=True, T0=1.0, tau=10.0)
+    assert abs(float(epot) - r["epot"]) < 1e-4 * abs(r["epot"])
+    assert abs(float(ekin) - r["ekin"]) < 1e-4 * abs(r["ekin"])
+    assert abs(float(alpha) - r["alpha"]) < 1e-4 * max(1e-3, abs(r["alpha"]))
+    assert int(nupd) == r["nupdate"]
+    # FP32 force sums conserve momentum to the accumulation round-off
+    assert abs(float(mom)) < 1e-7
