@@ -86,6 +86,39 @@ int sep_gpu_time_step_kernel(seppart *ptr, sepsys *sys, sepret *ret, const char 
 			     unsigned opt, int nh, double T0, double *alpha, double tau,
 			     long nsteps, double *ms_per_launch);
 
+/*
+ * Lennard-Jones forces for callers that may not allocate device memory.
+ * No counterpart in the reference: it is an addition of this library.
+ *
+ * Who needs it: host programs that give all device memory to their own pool
+ * allocator at start-up and forbid any allocation outside it, and loops
+ * where the device-wide synchronisation of cudaMalloc/cudaFree is too
+ * costly.  This call allocates nothing (no cudaMalloc, no library routine
+ * that allocates): its working memory is a fixed array of about 5 MB inside
+ * the library, sized for at most 131072 particles and 65536 linked cells
+ * (cells of edge >= cf per box side).  Larger inputs return an error before
+ * any work is issued.
+ *
+ * It computes what sep_force_lj computes for one particle type and SEP_ALL:
+ * param = {cf, eps, sigma, aw} (as in sep_force_lj), shifted so the pair
+ * energy is zero at cf.  x (3n doubles, x0 y0 z0 x1 ...) is read from device
+ * memory; f (3n doubles, overwritten, not added to) and *epot (the total pair
+ * energy) are written to device memory.  L (3 box lengths) and param are
+ * host arrays.  All work is queued on `stream` (a cudaStream_t; NULL is the
+ * legacy default stream) and the call returns without waiting.
+ *
+ * The fixed array is shared by every call and keeps the last call's
+ * contents; each call clears what it needs.  Calls whose work overlaps on
+ * the GPU (different streams, or several host threads) race on it and give
+ * wrong results: order them on one stream.  The first call on each device,
+ * with that device current, looks up the array's address and keeps it;
+ * make that first call before any stream capture.
+ *
+ * Returns 0, or a negative code with the message in sep_gpu_error().
+ */
+int sep_gpu_lj_forces_noalloc(const double *x, long n, const double *L, const double *param,
+			      double *f, double *epot, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
