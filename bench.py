@@ -41,6 +41,7 @@ sys.path.insert(0, HERE)
 
 RHO, TEMP, RC, SKIN, DT, T0, TAU = 0.8442, 1.0, 2.5, 0.3, 0.005, 1.0, 10.0
 L2_BYTES = 129 * 2 ** 20
+FLUSH_BYTES = 256 * 2 ** 20     # written between timed steps: about twice the L2
 
 
 def parse():
@@ -197,7 +198,7 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
-    from seplib_gb300 import build, configs, load, sepapi as A, GpuInfo
+    from seplib_gb300 import build, configs, load, sepapi as A, GpuInfo, GpuTiming
     build.build()
     lib = load()
     if not lib.sep_gpu_available():
@@ -207,48 +208,65 @@ def main():
     fun = A.fun_ptr(lib, "sep_lj_shift")
 
     # ---- device-resident loop (value) ----
-    atoms, sys_ = new_system(lib, s)
-    if args.tpp:
-        lib.sep_gpu_set_tpp(atoms, args.tpp)
-    ret = A.SepRet()
-    alpha = C.c_double(0.0)
-    run = lambda k: lib.sep_gpu_run(atoms, C.byref(sys_), C.byref(ret), b"AA", fun, None, RC,
-                                    A.SEP_ALL, 1, T0, C.byref(alpha), TAU, k)
-    assert run(max(3, args.warmup)) == 0
-    lib.sep_gpu_stream_sync(atoms)
-    info0 = GpuInfo()
-    lib.sep_gpu_info_get(atoms, C.byref(info0))
-    upd0 = sys_.nupdate_neighb
+    # sep_gpu_run_timed: sep_gpu_run's device work in unrolled graphs, an L2
+    # flush (FLUSH_BYTES written, outside the spans) before every step, one
+    # CUDA event pair per step.  Each measurement runs on a fresh copy of the
+    # system over the same trajectory segment: steps [W, W + K) after W
+    # warm-up steps (the loops are bitwise identical, so are the segments).
+    def segment(mode):
+        atoms, sys_ = new_system(lib, s)
+        if args.tpp:
+            lib.sep_gpu_set_tpp(atoms, args.tpp)
+        ret = A.SepRet()
+        alpha = C.c_double(0.0)
+        args_run = (atoms, C.byref(sys_), C.byref(ret), b"AA", fun, None, RC, A.SEP_ALL, 1, T0,
+                    C.byref(alpha), TAU)
+        assert lib.sep_gpu_run(*args_run, max(3, args.warmup)) == 0
+        lib.sep_gpu_stream_sync(atoms)
+        upd0 = sys_.nupdate_neighb
+        barrier(world)
+        if mode == "graph":
+            # the production loop: one graph with a WHILE node, no flush
+            lib.sep_gpu_event_record(atoms, 2)
+            assert lib.sep_gpu_run(*args_run, args.steps) == 0
+            lib.sep_gpu_event_record(atoms, 3)
+            msf = C.c_float()
+            lib.sep_gpu_event_elapsed(atoms, 2, 3, C.byref(msf))
+            ms = msf.value
+        else:
+            tm = GpuTiming(flush_bytes=FLUSH_BYTES, kernel_spans=1 if mode == "kernel" else 0)
+            rc = lib.sep_gpu_run_timed(*args_run, args.steps, C.byref(tm))
+            assert rc == 0, lib.sep_gpu_error()
+            ms = tm.ms_kernel if mode == "kernel" else tm.ms_steps
+        lib.sep_gpu_stream_sync(atoms)
+        barrier(world)
+        info = GpuInfo()
+        lib.sep_gpu_info_get(atoms, C.byref(info))
+        out = dict(ms=ms, rebuilds=sys_.nupdate_neighb - upd0, epot=ret.epot, ekin=ret.ekin, info=info)
+        lib.sep_close(atoms, n)
+        return out
+
     clocks = Clocks()
     clocks.start()
-    barrier(world)
-    lib.sep_gpu_stream_sync(atoms)
-    lib.sep_gpu_event_record(atoms, 2)
-    assert run(args.steps) == 0
-    lib.sep_gpu_event_record(atoms, 3)
-    ms = C.c_float()
-    lib.sep_gpu_event_elapsed(atoms, 2, 3, C.byref(ms))
-    lib.sep_gpu_stream_sync(atoms)
-    barrier(world)
+    seg = segment("steps")
+    segk = segment("kernel")
     clk = clocks.stop()
-    t_dev = allmax(world, ms.value / 1e3)
-    rebuilds = sys_.nupdate_neighb - upd0
-    epot_pp = ret.epot / n
-    temp = 2.0 * ret.ekin / (3.0 * n)
+    segg = segment("graph")
+    t_dev = allmax(world, seg["ms"] / 1e3)
+    t_kernel = allmax(world, segk["ms"] / 1e3)
+    rebuilds = seg["rebuilds"]
+    epot_pp = seg["epot"] / n
+    temp = 2.0 * seg["ekin"] / (3.0 * n)
     value = world * n * args.steps / t_dev
+    graph_loop_pss = n * args.steps / (segg["ms"] / 1e3)
+    info = seg["info"]
 
-    # ---- roofline of the fused step kernel ----
-    mspl = C.c_double()
-    lib.sep_gpu_time_step_kernel(atoms, C.byref(sys_), C.byref(ret), b"AA", fun, None, RC, A.SEP_ALL,
-                                 1, T0, C.byref(alpha), TAU, 50, C.byref(mspl))
-    info = GpuInfo()
-    lib.sep_gpu_info_get(atoms, C.byref(info))
-    lib.sep_close(atoms, n)
+    # ---- roofline of the fused step kernel (its own timed pass, same segment) ----
     nbar = 4.0 / 3.0 * math.pi * (RC + SKIN) ** 3 * RHO
     alg_bytes = n * (4 * nbar + 128)
-    achieved = alg_bytes / (mspl.value / 1e3) / 1e9
+    kernel_ms = 1e3 * t_kernel / args.steps
+    achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
-    rebuild_bytes = n * (4 * nbar + 64)
     achieved_step = n * (4 * nbar + 128 + (4 * nbar + 64) * rebuilds / args.steps) * args.steps / t_dev / 1e9
 
     # ---- end to end through the sep C API with host buffers ----
@@ -270,10 +288,16 @@ def main():
     lib.sep_gpu_invalidate(atoms)             # next call uploads the host arrays again
     e_steps = args.steps
     barrier(world)
+    t_e2e = 0.0
+    for _ in range(e_steps):
+        lib.sep_gpu_flush_l2(atoms, FLUSH_BYTES)   # untimed; the step's readback is synchronous
+        t0 = time.perf_counter()
+        api_steps(1)
+        t_e2e += time.perf_counter() - t0
     t0 = time.perf_counter()
-    api_steps(e_steps)
     lib.sep_gpu_sync(atoms)                   # device -> host download of x, v, f, ...
-    t_e2e = allmax(world, time.perf_counter() - t0)
+    t_e2e += time.perf_counter() - t0
+    t_e2e = allmax(world, t_e2e)
     lib.sep_close(atoms, n)
     state_bytes = n * (16 + 16 + 16 + 16 + 16 + 4 + 4 + 16 + 16)   # what upload/download move
     h2d = (state_bytes + 8 * 4 * n) / e_steps + 16
@@ -293,7 +317,12 @@ def main():
     wset = n * (16 * 2 + 16 * 4 + 16 + 4) + n * info.list_capacity * 4
     if rank == 0:
         cfgd = workload_config(args, n)
-        cfgd["l2"] = "no flush; per-step working set %.0f MB vs %d MB L2" % (wset / 2 ** 20, L2_BYTES // 2 ** 20)
+        cfgd["l2"] = ("flushed: %d MiB written before every timed step, outside the timed spans "
+                      "(per-step working set %.0f MiB, L2 %d MiB)" % (FLUSH_BYTES >> 20, wset / 2 ** 20,
+                                                                  L2_BYTES >> 20))
+        cfgd["graph_loop_no_flush"] = {
+            "value": graph_loop_pss, "unit": "particle-steps/s", "list_rebuilds": segg["rebuilds"],
+            "what": "sep_gpu_run, one CUDA graph with a WHILE node, L2 not flushed (production loop)"}
         cfgd["tpp"] = info.tpp
         cfgd["list_mean_full"] = round(info.list_mean, 2)
         cfgd["list_rebuilds_in_timed_steps"] = rebuilds
@@ -310,12 +339,15 @@ def main():
                     "path": "sep C API prgs-style loop, host seppart arrays, upload+download timed"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
-                         "kernel": "k_pair<fused step>", "kernel_ms": mspl.value,
+                         "kernel": "k_lj<fused step>", "kernel_ms": kernel_ms,
                          "bytes_per_launch": alg_bytes,
                          "whole_step_achieved_incl_rebuild": achieved_step},
             "cpu_baseline": cpu,
             "clocks": clk,
-            "gpu_launches": 2 * args.steps + 7 * rebuilds,
+            # per step: k_lj (fused force + integration + decision); per 64
+            # steps: k_setif; per rebuild: k_bin, k_scan, k_scatter,
+            # k_cellsort_w, k_gather, k_copyback, k_build_tiles
+            "gpu_launches": args.steps + (args.steps + 63) // 64 + 7 * rebuilds,
         }
         print(json.dumps(line))
 

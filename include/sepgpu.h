@@ -87,6 +87,32 @@ int sep_gpu_time_step_kernel(seppart *ptr, sepsys *sys, sepret *ret, const char 
 			     long nsteps, double *ms_per_launch);
 
 /*
+ * Timing helper: sep_gpu_run's loop (same arguments, same results) arranged
+ * for measurement.  Before every step the library writes tm->flush_bytes to
+ * a buffer of its own (on its stream, outside the timed spans) so that no
+ * step finds the previous step's data in L2.  One pair of CUDA events per
+ * step brackets either the whole step (list rebuild when due, fused
+ * force + integration kernel, loop decision) or, with kernel_spans set, the
+ * fused kernel alone; the summed device times come back in tm.
+ */
+typedef struct {
+	long flush_bytes;      /* in: bytes written between steps (0: no flush) */
+	int kernel_spans;      /* in: 0: time each step; 1: time each fused step kernel */
+	double ms_steps;       /* out: summed device time of the steps (kernel_spans == 0) */
+	double ms_kernel;      /* out: summed device time of the kernels (kernel_spans == 1) */
+	long launches;         /* out: steps launched */
+	long overflows;        /* out: neighbour-list regrowths (outside the spans) */
+} sep_gpu_timing;
+
+int sep_gpu_run_timed(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
+		      double (*fun)(double, char), const double *ljparam, double cf, unsigned opt,
+		      int nh, double T0, double *alpha, double tau, long nsteps, sep_gpu_timing *tm);
+
+/* Write `bytes` to a library-owned device buffer on the library's stream and
+ * wait for it: evicts the L2 cache between timed calls. */
+int sep_gpu_flush_l2(seppart *ptr, long bytes);
+
+/*
  * Lennard-Jones forces for callers that may not allocate device memory.
  * No counterpart in the reference: it is an addition of this library.
  *

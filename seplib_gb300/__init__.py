@@ -24,6 +24,12 @@ class GpuInfo(C.Structure):
                 ("list_max", C.c_int), ("list_mean", C.c_double), ("tpp", C.c_int)]
 
 
+class GpuTiming(C.Structure):
+    """``sep_gpu_timing`` (include/sepgpu.h)."""
+    _fields_ = [("flush_bytes", C.c_long), ("kernel_spans", C.c_int), ("ms_steps", C.c_double),
+                ("ms_kernel", C.c_double), ("launches", C.c_long), ("overflows", C.c_long)]
+
+
 _GPU_SIGNATURES = {
     "sep_gpu_available": (C.c_int, []),
     "sep_gpu_error": (C.c_char_p, []),
@@ -41,6 +47,10 @@ _GPU_SIGNATURES = {
     "sep_gpu_time_step_kernel": (C.c_int, [sepapi.PART_P, sepapi.SYS_P, sepapi.RET_P, C.c_char_p,
                                           C.c_void_p, sepapi.D_P, C.c_double, C.c_uint, C.c_int,
                                           C.c_double, sepapi.D_P, C.c_double, C.c_long, sepapi.D_P]),
+    "sep_gpu_run_timed": (C.c_int, [sepapi.PART_P, sepapi.SYS_P, sepapi.RET_P, C.c_char_p, C.c_void_p,
+                                   sepapi.D_P, C.c_double, C.c_uint, C.c_int, C.c_double, sepapi.D_P,
+                                   C.c_double, C.c_long, C.POINTER(GpuTiming)]),
+    "sep_gpu_flush_l2": (C.c_int, [sepapi.PART_P, C.c_long]),
 }
 
 

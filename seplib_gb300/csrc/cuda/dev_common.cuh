@@ -99,6 +99,10 @@ struct sepdev {
 	// graph runner state
 	void *runner;
 
+	// L2 flush buffer of the timing helpers (allocated on first use)
+	void *flush_buf;
+	size_t flush_bytes;
+
 	// kernel variants chosen by the tuner (SEPLIB_LJ_VARIANT overrides)
 	int lj_variant;
 	int nsm;

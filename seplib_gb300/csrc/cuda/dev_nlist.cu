@@ -563,10 +563,12 @@ int sepdev_grow_list(sepdev *d, int needed)
 
 extern "C" int sepdev_list_stats(sepdev *d, int *maxcount, double *meancount, int *capacity)
 {
+	if (!d->list_valid || !d->ncnt) return SEPDEV_EINVAL;
 	int *h = (int *)malloc(sizeof(int) * d->n);
 	if (!h) return SEPDEV_ENOMEM;
-	CK(cudaMemcpyAsync(h, d->ncnt, sizeof(int) * d->n, cudaMemcpyDeviceToHost, d->st));
-	CK(cudaStreamSynchronize(d->st));
+	cudaError_t e = cudaMemcpyAsync(h, d->ncnt, sizeof(int) * d->n, cudaMemcpyDeviceToHost, d->st);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(d->st);
+	if (e != cudaSuccess) { free(h); sepdev_set_error("list stats", e); return SEPDEV_ECUDA; }
 	long s = 0; int mx = 0;
 	for (long i = 0; i < d->n; i++) { s += h[i]; if (h[i] > mx) mx = h[i]; }
 	free(h);

@@ -111,7 +111,11 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 {
 	constexpr int NCH = VAR == VAR_SINGLE ? 1 : 4;
 	extern __shared__ sepdev_pot spot[];
-	if (a.flags && (a.flags[0] & 1u)) return;    // list overflow: leave the state untouched
+	if (FUSED) step_decide_entry(a.dec);
+	if (a.flags && (a.flags[0] & 1u)) {           // list overflow: leave the state untouched
+		if (FUSED) step_decide_skip(a.dec);
+		return;
+	}
 	int ntypes = 1;
 	if (VAR != VAR_SINGLE) {
 		ntypes = a.ps->ntypes;
@@ -224,6 +228,7 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 		for (int k = 0; k < 6; k++) { v[NCH + 8 + k] = kp[k]; fld[NCH + 8 + k] = (int)off + SLOT_KINP + k; }
 		v[NCH + 14] = sv2; fld[NCH + 14] = (int)off + SLOT_SUMV2;
 		block_to_slot<NCH + 15>(v, fld, ps, d2, (int)off + SLOT_MAXD2);
+		step_decide_exit(a.dec);
 	}
 }
 
@@ -238,7 +243,11 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 template <bool FUSED, bool CUBIC, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_lj(long n, PairArgs a)
 {
-	if (a.flags && (a.flags[0] & 1u)) return;
+	if (FUSED) step_decide_entry(a.dec);
+	if (a.flags && (a.flags[0] & 1u)) {
+		if (FUSED) step_decide_skip(a.dec);
+		return;
+	}
 	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
 	const bool act = i < n;
 	const float u = a.fs[0];
@@ -320,6 +329,7 @@ __global__ void __launch_bounds__(256, MINB) k_lj(long n, PairArgs a)
 				     off + SLOT_KINP + 1, off + SLOT_KINP + 2, off + SLOT_KINP + 3,
 				     off + SLOT_KINP + 4, off + SLOT_KINP + 5, off + SLOT_SUMV2};
 		block_to_slot<15>(v, fld, ps, d2, off + SLOT_MAXD2);
+		step_decide_exit(a.dec);
 	}
 }
 
@@ -393,6 +403,7 @@ void sepdev_fill_args(sepdev *d, PairArgs &a, const sepdev_pairset *ps, double d
 	a.pslot = pslot;
 	a.lslot = lslot;
 	a.flags = NULL;
+	memset(&a.dec, 0, sizeof a.dec);
 }
 
 int sepdev_upload_pairset(sepdev *d, const sepdev_pairset *ps)

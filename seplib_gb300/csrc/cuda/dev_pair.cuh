@@ -1,6 +1,7 @@
 // dev_pair.cuh - argument block of the pair / step kernels (shared with the graph runner).
 #pragma once
 #include "dev_common.cuh"
+#include "dev_decide.cuh"
 
 struct PairArgs {
 	const int4 *pos;
@@ -29,6 +30,7 @@ struct PairArgs {
 	long long *slots;
 	int pslot, lslot;
 	const unsigned *flags;
+	DecideArgs dec;            // graph loop: decision at the end of a fused step
 };
 
 

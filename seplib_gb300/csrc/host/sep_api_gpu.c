@@ -59,7 +59,7 @@ int sep_gpu_info_get(seppart *ptr, sep_gpu_info *info)
 	info->launches = sepdev_launch_count(c->dev);
 	int mx = 0, cap = 0;
 	double mean = 0.0;
-	if (!c->list_stale) sepdev_list_stats(c->dev, &mx, &mean, &cap);
+	sepdev_list_stats(c->dev, &mx, &mean, &cap);   /* the last list built */
 	info->list_capacity = cap;
 	info->list_max = mx;
 	info->list_mean = mean;
@@ -193,6 +193,63 @@ int sep_gpu_run(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
 	if (alpha && nh) *alpha = a;
 	c->nbuild += ntrig;
 	loop_finish(c, sys, ret, last, nsteps, ntrig, lt);
+	return 0;
+}
+
+int sep_gpu_run_timed(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
+		      double (*fun)(double, char), const double *ljparam, double cf, unsigned opt,
+		      int nh, double T0, double *alpha, double tau, long nsteps, sep_gpu_timing *tm)
+{
+	if (!tm) return -1;
+	sepdev_timing t;
+	memset(&t, 0, sizeof t);
+	t.flush_bytes = tm->flush_bytes;
+	t.kernel_spans = tm->kernel_spans;
+	if (nsteps <= 0) {
+		tm->ms_steps = tm->ms_kernel = 0.0;
+		tm->launches = tm->overflows = 0;
+		return 0;
+	}
+	sepdev_pairset ps;
+	rt_ctx *c = loop_setup(ptr, sys, types, fun, ljparam, cf, opt, &ps);
+	sepdev_runcfg cfg;
+	memset(&cfg, 0, sizeof cfg);
+	cfg.dt = sys->dt;
+	cfg.skin = sys->skin;
+	cfg.nh = nh;
+	cfg.T0 = T0;
+	cfg.tau = tau;
+	cfg.force_trigger = c->pending_trigger;
+	if (!c->sumv2_valid) {
+		rt_check(sepdev_sumv2(c->dev, &c->sumv2), "kinetic sum");
+		c->sumv2_valid = 1;
+	}
+	double a = alpha ? *alpha : 0.0, last[SLOT_FIELDS];
+	if (nh) {
+		const double ekin = 0.5 * c->sumv2 / sys->npart;
+		const double temp = 0.666667 * ekin;
+		a = a + sys->dt / (tau * tau) * (temp / T0 - 1.0);
+	}
+	long ntrig = 0;
+	int lt = 0;
+	rt_check(sepdev_run_timed(c->dev, &ps, &cfg, nsteps, &a, &c->sumv2, last, &ntrig, &lt, &t),
+		 "timed device loop");
+	if (alpha && nh) *alpha = a;
+	c->nbuild += ntrig + t.overflows;
+	loop_finish(c, sys, ret, last, nsteps, ntrig, lt);
+	tm->ms_steps = t.ms_steps;
+	tm->ms_kernel = t.ms_kernel;
+	tm->launches = t.launches;
+	tm->overflows = t.overflows;
+	return 0;
+}
+
+int sep_gpu_flush_l2(seppart *ptr, long bytes)
+{
+	rt_ctx *c = rt_find(ptr);
+	if (!c || !c->dev || bytes <= 0) return -1;
+	rt_check(sepdev_flush_l2(c->dev, (size_t)bytes, 7u), "L2 flush");
+	rt_check(sepdev_sync(c->dev), "L2 flush");
 	return 0;
 }
 

@@ -171,9 +171,10 @@ int sepdev_event_elapsed(sepdev *d, int e0, int e1, float *ms);
 /*
  * Run nsteps of {pair forces, [Nose-Hoover], leap-frog} entirely on the
  * device, rebuilding the list when the skin test fires.  The loop is one
- * CUDA graph (WHILE node over two unrolled steps, each behind an IF node that
- * holds the captured list rebuild); a one-thread kernel after each step
- * updates the thermostat and decides the rebuild.  The list must be valid on
+ * CUDA graph (WHILE node over eight unrolled steps, each behind an IF node
+ * that holds the captured list rebuild); at the end of each fused step the
+ * last block to finish updates the thermostat and decides the rebuild.
+ * Steps beyond a multiple of eight run singly.  The list must be valid on
  * entry.  alpha: in, the thermostat value the first step uses (already
  * advanced by the caller); out, the value the last step used, as
  * sep_nosehoover leaves it; sumv2: sum m v^2 in/out; last: the final step's
@@ -189,6 +190,28 @@ typedef struct {
 
 int sepdev_run(sepdev *d, const sepdev_pairset *ps, const sepdev_runcfg *cfg, long nsteps,
 	       double *alpha, double *sumv2, double *last, long *ntrig, int *last_trig);
+
+/*
+ * The same loop for measurement: graphs of up to 64 unrolled steps with an
+ * L2 flush of flush_bytes before every step, outside the timed spans, and
+ * one pair of CUDA events per step (around the step, or around its fused
+ * step kernel).  Results and outputs as sepdev_run.
+ */
+typedef struct {
+	long flush_bytes;      /* in: bytes written between steps (0: no flush) */
+	int kernel_spans;      /* in: 0: events around each step; 1: around each fused step kernel */
+	double ms_steps;       /* out: summed device time of the steps (kernel_spans == 0) */
+	double ms_kernel;      /* out: summed device time of the fused step kernel (kernel_spans == 1) */
+	long launches;         /* out: steps launched (skipped ones included) */
+	long overflows;        /* out: list overflows recovered outside the spans */
+} sepdev_timing;
+
+int sepdev_run_timed(sepdev *d, const sepdev_pairset *ps, const sepdev_runcfg *cfg, long nsteps,
+		     double *alpha, double *sumv2, double *last, long *ntrig, int *last_trig,
+		     sepdev_timing *tm);
+
+/* queue a write of `bytes` (rounded down to 16) to a context-owned buffer */
+int sepdev_flush_l2(sepdev *d, size_t bytes, unsigned tag);
 
 /* lanes per particle in the pair kernels (1, 2, 4); invalidates the list */
 int sepdev_set_tpp(sepdev *d, int tpp);

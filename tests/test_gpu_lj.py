@@ -137,6 +137,49 @@ def test_graph_loop_equals_api_loop(gpu_lib):
     a.close(); b.close()
 
 
+def test_timed_loop_equals_graph_loop(gpu_lib):
+    """sep_gpu_run_timed (unrolled graphs, L2 flushed between steps) must
+    give sep_gpu_run's results bit for bit.  301 steps: sep_gpu_run takes 37
+    loop iterations of 8 plus 5 single steps; the timed runs take 150 and 151
+    steps (64-step graphs plus remainders, odd counts) and include list
+    rebuilds."""
+    from seplib_gb300 import GpuTiming
+    s = small()
+    a = Handle(gpu_lib, s, skin=0.3)
+    b = Handle(gpu_lib, s, skin=0.3)
+    nsteps = 301
+    for h in (a, b):           # build the list and take one step through the API
+        h.step(nh=(1.0, 10.0))
+    rc = gpu_lib.sep_gpu_run(a.atoms, C.byref(a.sys), C.byref(a.ret), b"AA", a.fun(), None, 2.5,
+                             A.SEP_ALL, 1, 1.0, C.byref(a.alpha), 10.0, nsteps)
+    assert rc == 0
+    # step spans for the first part, kernel spans for the rest
+    tms = []
+    for k, part in ((0, 150), (1, nsteps - 150)):
+        tm = GpuTiming(flush_bytes=64 << 20, kernel_spans=k)
+        rc = gpu_lib.sep_gpu_run_timed(b.atoms, C.byref(b.sys), C.byref(b.ret), b"AA", b.fun(), None,
+                                       2.5, A.SEP_ALL, 1, 1.0, C.byref(b.alpha), 10.0, part,
+                                       C.byref(tm))
+        assert rc == 0, gpu_lib.sep_gpu_error()
+        assert tm.launches == part and tm.overflows == 0
+        tms.append(tm)
+    assert tms[0].ms_steps > 0 and tms[0].ms_kernel == 0
+    assert tms[1].ms_kernel > 0 and tms[1].ms_steps == 0
+    assert tms[1].ms_kernel / (nsteps - 150) < tms[0].ms_steps / 150
+    a.sync(); b.sync()
+    assert a.sys.nupdate_neighb == b.sys.nupdate_neighb and a.sys.nupdate_neighb > 1
+    assert np.array_equal(a.view["x"], b.view["x"])
+    assert np.array_equal(a.view["v"], b.view["v"])
+    assert a.alpha.value == b.alpha.value
+    assert a.ret.epot == b.ret.epot and a.ret.ekin == b.ret.ekin
+    # both continue identically through the API afterwards
+    for h in (a, b):
+        h.step(nh=(1.0, 10.0))
+    a.sync(); b.sync()
+    assert np.array_equal(a.view["x"], b.view["x"])
+    a.close(); b.close()
+
+
 def test_nve_drift(gpu_lib, ora):
     """Energy drift over 1e4 NVE steps of the N=1000 workload.  Truncation at
     rc makes the total energy a random walk whose drift varies by a factor of
