@@ -42,6 +42,10 @@ sys.path.insert(0, HERE)
 RHO, TEMP, RC, SKIN, DT, T0, TAU = 0.8442, 1.0, 2.5, 0.3, 0.005, 1.0, 10.0
 L2_BYTES = 129 * 2 ** 20
 FLUSH_BYTES = 256 * 2 ** 20     # written between timed steps: about twice the L2
+# DRAM bytes (read + write) per launch of the fused step kernel, from one ncu
+# capture of this workload after an L2 flush (profiles/k_lj_fcc256000.md);
+# keyed by fcc cells per edge
+K_LJ_TRAFFIC = {40: 105.6e6}
 
 
 def parse():
@@ -338,7 +342,8 @@ def main():
                     "d2h_bytes_per_step": d2h, "steps": e_steps,
                     "path": "sep C API prgs-style loop, host seppart arrays, upload+download timed"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                         "frac": achieved / peak, "traffic": K_LJ_TRAFFIC.get(args.ncell),
+                         "traffic_unit": "bytes per launch", "peak_source": peak_kind,
                          "kernel": "k_lj<fused step>", "kernel_ms": kernel_ms,
                          "bytes_per_launch": alg_bytes,
                          "whole_step_achieved_incl_rebuild": achieved_step},

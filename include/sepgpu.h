@@ -45,7 +45,9 @@ int sep_gpu_invalidate(seppart *ptr);
  * captured once in a CUDA graph whose neighbour-list rebuild is a
  * conditional node decided on the device.  On return ret holds the last
  * step's values, *alpha the thermostat state and sys the counters, exactly as
- * after the equivalent call sequence.  Returns 0 on success.
+ * after the equivalent call sequence.  Energy and virial are accumulated on
+ * the last step only, since no earlier step's sepret can be read.  Returns 0
+ * on success.
  */
 int sep_gpu_run(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
 		double (*fun)(double, char), const double *ljparam, double cf,
@@ -79,7 +81,9 @@ int sep_gpu_stream_sync(seppart *ptr);
 /*
  * Timing helper: run nsteps steps of the sep_gpu_run loop from the host
  * (rebuilds outside the timed brackets) and return the mean duration of the
- * fused step kernel in ms, measured with events around each launch.
+ * fused step kernel in ms, measured with events around each launch.  As with
+ * sep_gpu_run, ret reports the last step (energy and virial are only
+ * accumulated there).
  */
 int sep_gpu_time_step_kernel(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
 			     double (*fun)(double, char), const double *ljparam, double cf,

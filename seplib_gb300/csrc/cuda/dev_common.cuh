@@ -103,6 +103,10 @@ struct sepdev {
 	void *flush_buf;
 	size_t flush_bytes;
 
+	// pinned host staging of uploads and downloads (kept between calls)
+	void *stage;
+	size_t stage_bytes;
+
 	// kernel variants chosen by the tuner (SEPLIB_LJ_VARIANT overrides)
 	int lj_variant;
 	int nsm;

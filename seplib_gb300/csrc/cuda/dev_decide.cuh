@@ -17,6 +17,7 @@ struct RunState {
 	long long remaining;   // loop iterations left
 	long long done;        // steps completed
 	long long ntrig;       // skin-triggered updates
+	long long total;       // steps in this call (the last one produces the observables)
 	int force_trig;        // report an update after the next step
 	int last_trig;         // the last completed step reported an update
 	int abort;
@@ -87,6 +88,15 @@ __device__ __forceinline__ void decide_warp(const DecideArgs &a)
 			cudaGraphSetConditional(a.h_while, rs->remaining > 0 ? 1u : 0u);
 		}
 	}
+}
+
+// Whether this step's energy and virial are observed: in the device loop
+// only the last step of a call reports them (sep_gpu_run returns the last
+// step's sepret); every other step needs forces, the kinetic sum and the
+// displacement only.  Without a decision (API path) every step reports.
+__device__ __forceinline__ bool step_observed(const DecideArgs &a)
+{
+	return !a.rs || a.rs->done + 1 >= a.rs->total;
 }
 
 // In a step kernel with a decision attached: on entry (before anything can

@@ -48,25 +48,58 @@ __global__ void k_bin(long n, const int4 *__restrict__ pos, int ncx, int ncy, in
 	}
 }
 
-// exclusive scan of count[0..m) into start[0..m], one block of 1024 threads
-__global__ void k_scan(long m, const int *__restrict__ count, int *__restrict__ start)
+// exclusive scan of count[0..m) into start[0..m], one block of 1024 threads.
+// The counts are taken in tiles of 1024 (one per thread, coalesced); up to
+// SCAN_REG tiles are loaded together so their latencies overlap, then each
+// tile is scanned with warp shuffles plus one pass over the 32 warp totals,
+// carrying the running sum from tile to tile.
+#define SCAN_REG 16
+__global__ void __launch_bounds__(1024) k_scan(long m, const int *__restrict__ count, int *__restrict__ start)
 {
-	__shared__ int part[1024];
-	const long chunk = (m + blockDim.x - 1) / blockDim.x;
-	const long lo = threadIdx.x * chunk, hi = min(m, lo + chunk);
-	int s = 0;
-	for (long k = lo; k < hi; k++) s += count[k];
-	part[threadIdx.x] = s;
-	__syncthreads();
-	for (int off = 1; off < (int)blockDim.x; off <<= 1) {
-		int v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
-		__syncthreads();
-		part[threadIdx.x] += v;
-		__syncthreads();
+	__shared__ int wsum[32];
+	__shared__ int carry_s;
+	const unsigned FULL = 0xffffffffu;
+	const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+	if (t == 0) carry_s = 0;
+	for (long base = 0; base < m; base += 1024L * SCAN_REG) {
+		int v[SCAN_REG];
+#pragma unroll
+		for (int r = 0; r < SCAN_REG; r++) {
+			const long k = base + (long)r * 1024 + t;
+			v[r] = k < m ? __ldg(count + k) : 0;
+		}
+#pragma unroll
+		for (int r = 0; r < SCAN_REG; r++) {
+			if (base + (long)r * 1024 >= m) continue;       // uniform over the block
+			int x = v[r];
+#pragma unroll
+			for (int o = 1; o < 32; o <<= 1) {
+				const int y = __shfl_up_sync(FULL, x, o);
+				if (lane >= o) x += y;
+			}
+			__syncthreads();                                // wsum / carry_s of the last tile are consumed
+			if (lane == 31) wsum[w] = x;
+			__syncthreads();
+			if (w == 0) {
+				int ws = wsum[lane];
+#pragma unroll
+				for (int o = 1; o < 32; o <<= 1) {
+					const int y = __shfl_up_sync(FULL, ws, o);
+					if (lane >= o) ws += y;
+				}
+				wsum[lane] = ws;                        // inclusive over warps
+			}
+			__syncthreads();
+			const int carry = carry_s;
+			const int excl = carry + (w ? wsum[w - 1] : 0) + x - v[r];
+			const long k = base + (long)r * 1024 + t;
+			if (k < m) start[k] = excl;
+			__syncthreads();
+			if (t == 1023) carry_s = carry + wsum[31];
+		}
 	}
-	int run = threadIdx.x ? part[threadIdx.x - 1] : 0;
-	for (long k = lo; k < hi; k++) { start[k] = run; run += count[k]; }
-	if (threadIdx.x == blockDim.x - 1) start[m] = part[threadIdx.x];
+	__syncthreads();
+	if (t == 0) start[m] = carry_s;
 }
 
 __global__ void k_scatter(long n, const int *__restrict__ cellof, const int *__restrict__ celloff,

@@ -240,7 +240,103 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 // the cut-off as a mask.  For a cubic box the box scale is folded out of the
 // pair loop: separations stay in fixed-point units (L/2^32) and the
 // per-particle sums are rescaled once.
-template <bool FUSED, bool CUBIC, int MINB>
+// PF (list staging): 0 - the next batch of indices is loaded while the
+// current one is computed; 1 - in addition, lane 0 asks L2 for the warp's
+// whole list tile at entry (one bulk prefetch, so the list stream does not
+// wait on DRAM batch by batch); 2 - as 1, and the position gathers of the
+// next batch are issued before the current batch is computed.
+template <int PF>
+__device__ __forceinline__ void lj_prefetch_tile(const PairArgs &a, long i, int cnt)
+{
+	if (PF == 0) return;
+	const int mx = __reduce_max_sync(0xffffffffu, cnt);
+	if ((threadIdx.x & 31) == 0 && mx > 0) {
+		const int *base = a.nl + nl_index(i, 0, a.maxnb);      // lane 0 starts the tile
+		const unsigned bytes = (unsigned)((mx + 3) >> 2) * 512u;   // groups of 4 entries x 32 lanes
+		asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(base), "r"(bytes) : "memory");
+	}
+}
+
+// The neighbour loop of k_lj.  OBS: accumulate energy, hit count and
+// virial (skipped on steps whose sepret nobody reads).
+template <bool OBS, bool CUBIC, int PF>
+__device__ __forceinline__ void lj_pairs(const PairArgs &a, long i, int cnt, const int4 &pi,
+					 float sx, float sy, float sz, float rc2, float sig2,
+					 float &fx, float &fy, float &fz, float &e, float &nin,
+					 float (&w)[6])
+{
+	const float eps48 = a.eps48, eps4 = a.eps4, awh = a.awh, aw = a.aw;
+	auto pair4 = [&](const int4 (&pj)[4], int rem) {
+#pragma unroll
+		for (int b = 0; b < 4; b++) {
+			const float dx = (float)(pi.x - pj[b].x) * sx;
+			const float dy = (float)(pi.y - pj[b].y) * sy;
+			const float dz = (float)(pi.z - pj[b].z) * sz;
+			const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+			const bool in = (b < rem) && (r2 < rc2);
+			// pairs outside the cut-off get s2 = 0, which zeroes their
+			// force and energy; the shift is added per hit at the end
+			const float s2 = in ? sig2 * fast_rcp(r2) : 0.f;
+			const float s6 = s2 * s2 * s2;
+			const float ft = eps48 * s6 * (s6 - awh) * s2;
+			// the force terms are rounded products (never contracted into
+			// the sums), so observed and unobserved steps give the same bits
+			const float gx = __fmul_rn(ft, dx), gy = __fmul_rn(ft, dy), gz = __fmul_rn(ft, dz);
+			fx += gx; fy += gy; fz += gz;
+			if (OBS) {
+				e = fmaf(eps4 * s6, s6 - aw, e);
+				nin += in ? 1.f : 0.f;
+				w[0] = fmaf(gx, dx, w[0]); w[1] = fmaf(gx, dy, w[1]); w[2] = fmaf(gx, dz, w[2]);
+				w[3] = fmaf(gy, dy, w[3]); w[4] = fmaf(gy, dz, w[4]); w[5] = fmaf(gz, dz, w[5]);
+			}
+		}
+	};
+	const int4 *lp = (const int4 *)(a.nl + nl_index(i, 0, a.maxnb));
+	const int nb = (cnt + 3) >> 2;
+	// indices past the count point at the particle itself (masked)
+	auto idx = [&](const int4 &jc, int rem, int (&j)[4]) {
+		j[0] = jc.x; j[1] = rem > 1 ? jc.y : (int)i;
+		j[2] = rem > 2 ? jc.z : (int)i; j[3] = rem > 3 ? jc.w : (int)i;
+	};
+	if (PF < 2) {
+		int4 jn = nb > 0 ? __ldg(lp) : make_int4(0, 0, 0, 0);
+		for (int s0 = 0; s0 < nb; s0++) {
+			const int4 jc = jn;
+			if (s0 + 1 < nb) jn = __ldg(lp + (s0 + 1) * 32);
+			const int rem = cnt - 4 * s0;
+			int j[4];
+			idx(jc, rem, j);
+			int4 pj[4];
+#pragma unroll
+			for (int b = 0; b < 4; b++) pj[b] = __ldg(&a.pos[j[b]]);
+			pair4(pj, rem);
+		}
+	} else if (nb > 0) {
+		int4 jn = nb > 1 ? __ldg(lp + 32) : make_int4(0, 0, 0, 0);
+		int4 pn[4];
+		{
+			int j[4];
+			idx(__ldg(lp), cnt, j);
+#pragma unroll
+			for (int b = 0; b < 4; b++) pn[b] = __ldg(&a.pos[j[b]]);
+		}
+		for (int s0 = 0; s0 < nb; s0++) {
+			int4 pc[4];
+#pragma unroll
+			for (int b = 0; b < 4; b++) pc[b] = pn[b];
+			if (s0 + 1 < nb) {
+				int j[4];
+				idx(jn, cnt - 4 * (s0 + 1), j);
+#pragma unroll
+				for (int b = 0; b < 4; b++) pn[b] = __ldg(&a.pos[j[b]]);
+				if (s0 + 2 < nb) jn = __ldg(lp + (s0 + 2) * 32);
+			}
+			pair4(pc, cnt - 4 * s0);
+		}
+	}
+}
+
+template <bool FUSED, bool CUBIC, int MINB, int PF>
 __global__ void __launch_bounds__(256, MINB) k_lj(long n, PairArgs a)
 {
 	if (FUSED) step_decide_entry(a.dec);
@@ -254,46 +350,18 @@ __global__ void __launch_bounds__(256, MINB) k_lj(long n, PairArgs a)
 	const float sx = CUBIC ? 1.f : a.fs[0], sy = CUBIC ? 1.f : a.fs[1], sz = CUBIC ? 1.f : a.fs[2];
 	const float rc2 = CUBIC ? a.rc2 / (u * u) : a.rc2;
 	const float sig2 = CUBIC ? a.sig2 / (u * u) : a.sig2;
-	const float eps48 = a.eps48, eps4 = a.eps4, awh = a.awh, aw = a.aw;
 	float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f, nin = 0.f;
-	float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f, w4 = 0.f, w5 = 0.f;
+	float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 	int4 pi = make_int4(0, 0, 0, 0);
+	const int cnt = act ? a.ncnt[i] : 0;
+	lj_prefetch_tile<PF>(a, i, cnt);
+	const bool obs = !FUSED || (!a.skip_obs && step_observed(a.dec));
 	if (act) {
 		pi = a.pos[i];
-		const int cnt = a.ncnt[i];
-		const int4 *lp = (const int4 *)(a.nl + nl_index(i, 0, a.maxnb));
-		const int nb = (cnt + 3) >> 2;
-		int4 jn = nb > 0 ? __ldg(lp) : make_int4(0, 0, 0, 0);
-		for (int s0 = 0; s0 < nb; s0++) {
-			const int4 jc = jn;
-			if (s0 + 1 < nb) jn = __ldg(lp + (s0 + 1) * 32);
-			const int rem = cnt - 4 * s0;
-			const int j[4] = {jc.x, rem > 1 ? jc.y : (int)i, rem > 2 ? jc.z : (int)i,
-					  rem > 3 ? jc.w : (int)i};
-			int4 pj[4];
-#pragma unroll
-			for (int b = 0; b < 4; b++) pj[b] = __ldg(&a.pos[j[b]]);
-#pragma unroll
-			for (int b = 0; b < 4; b++) {
-				const float dx = (float)(pi.x - pj[b].x) * sx;
-				const float dy = (float)(pi.y - pj[b].y) * sy;
-				const float dz = (float)(pi.z - pj[b].z) * sz;
-				const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-				const bool in = (b < rem) && (r2 < rc2);
-				// pairs outside the cut-off get s2 = 0, which zeroes their
-				// force and energy; the shift is added per hit at the end
-				const float s2 = in ? sig2 * fast_rcp(r2) : 0.f;
-				const float s6 = s2 * s2 * s2;
-				const float ft = eps48 * s6 * (s6 - awh) * s2;
-				e = fmaf(eps4 * s6, s6 - aw, e);
-				nin += in ? 1.f : 0.f;
-				const float gx = ft * dx, gy = ft * dy, gz = ft * dz;
-				fx += gx; fy += gy; fz += gz;
-				w0 = fmaf(gx, dx, w0); w1 = fmaf(gx, dy, w1); w2 = fmaf(gx, dz, w2);
-				w3 = fmaf(gy, dy, w3); w4 = fmaf(gy, dz, w4); w5 = fmaf(gz, dz, w5);
-			}
-		}
+		if (obs) lj_pairs<true, CUBIC, PF>(a, i, cnt, pi, sx, sy, sz, rc2, sig2, fx, fy, fz, e, nin, w);
+		else lj_pairs<false, CUBIC, PF>(a, i, cnt, pi, sx, sy, sz, rc2, sig2, fx, fy, fz, e, nin, w);
 	}
+	float w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3], w4 = w[4], w5 = w[5];
 	e = fmaf(nin, a.ushift, e);
 	if (CUBIC) {
 		fx *= u; fy *= u; fz *= u;
@@ -403,6 +471,7 @@ void sepdev_fill_args(sepdev *d, PairArgs &a, const sepdev_pairset *ps, double d
 	a.pslot = pslot;
 	a.lslot = lslot;
 	a.flags = NULL;
+	a.skip_obs = 0;
 	memset(&a.dec, 0, sizeof a.dec);
 }
 
@@ -423,11 +492,14 @@ static void launch_fused(sepdev *d, int var, const PairArgs &a, size_t shm)
 	const bool cubic = d->L[0] == d->L[1] && d->L[1] == d->L[2];
 	if (var == VAR_SINGLE && cubic) {
 		switch (d->lj_variant) {
-		case 1: k_lj<FUSED, true, 5><<<grid, B, 0, d->st>>>(d->n, a); break;
-		default: k_lj<FUSED, true, 4><<<grid, B, 0, d->st>>>(d->n, a); break;
+		case 1: k_lj<FUSED, true, 5, 0><<<grid, B, 0, d->st>>>(d->n, a); break;
+		case 2: k_lj<FUSED, true, 4, 1><<<grid, B, 0, d->st>>>(d->n, a); break;
+		case 3: k_lj<FUSED, true, 3, 2><<<grid, B, 0, d->st>>>(d->n, a); break;
+		case 4: k_lj<FUSED, true, 4, 2><<<grid, B, 0, d->st>>>(d->n, a); break;
+		default: k_lj<FUSED, true, 4, 0><<<grid, B, 0, d->st>>>(d->n, a); break;
 		}
 	} else if (var == VAR_SINGLE)
-		k_lj<FUSED, false, 4><<<grid, B, 0, d->st>>>(d->n, a);
+		k_lj<FUSED, false, 4, 0><<<grid, B, 0, d->st>>>(d->n, a);
 	else if (var == VAR_GENERAL)
 		k_pair<VAR_GENERAL, FUSED><<<grid, B, shm, d->st>>>(d->n, a);
 	else
@@ -454,8 +526,8 @@ extern "C" int sepdev_pair_forces(sepdev *d, const sepdev_pairset *ps, int accum
 	return sepdev_launch_pair(d, ps, a, false);
 }
 
-extern "C" int sepdev_step(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
-			   int nh, double alpha, int pair_slot, int lf_slot)
+extern "C" int sepdev_step_obs(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
+			       int nh, double alpha, int pair_slot, int lf_slot, int observe)
 {
 	if (!d->list_valid || pair_slot < 0 || pair_slot >= d->nslots || lf_slot < 0 ||
 	    lf_slot >= d->nslots)
@@ -464,9 +536,16 @@ extern "C" int sepdev_step(sepdev *d, const sepdev_pairset *ps, int accumulate, 
 	if ((rc = sepdev_upload_pairset(d, ps))) return rc;
 	PairArgs a;
 	sepdev_fill_args(d, a, ps, dt, nh, alpha, accumulate, pair_slot, lf_slot, d->cur);
+	a.skip_obs = !observe;
 	if ((rc = sepdev_launch_pair(d, ps, a, true))) return rc;
 	d->cur ^= 1;
 	return SEPDEV_OK;
+}
+
+extern "C" int sepdev_step(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
+			   int nh, double alpha, int pair_slot, int lf_slot)
+{
+	return sepdev_step_obs(d, ps, accumulate, dt, nh, alpha, pair_slot, lf_slot, 1);
 }
 
 extern "C" int sepdev_leapfrog(sepdev *d, double dt, int nh, double alpha, int slot)

@@ -31,6 +31,7 @@ struct PairArgs {
 	int pslot, lslot;
 	const unsigned *flags;
 	DecideArgs dec;            // graph loop: decision at the end of a fused step
+	int skip_obs;              // fused step whose energy and virial nobody reads
 };
 
 

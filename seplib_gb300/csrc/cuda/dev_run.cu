@@ -214,7 +214,7 @@ static bool graph_matches(const sepdev *d, const Runner *r, const sepdev_pairset
 
 // the state at the start of a call: alpha already advanced for the first step
 static int run_begin(sepdev *d, Runner *r, const sepdev_pairset *ps, const sepdev_runcfg *cfg,
-		     double alpha, double sumv2)
+		     double alpha, double sumv2, long nsteps)
 {
 	int rc = sepdev_upload_pairset(d, ps);
 	if (rc) return rc;
@@ -224,6 +224,7 @@ static int run_begin(sepdev *d, Runner *r, const sepdev_pairset *ps, const sepde
 	h->alpha = alpha;
 	h->alpha_last = alpha;
 	h->force_trig = cfg->force_trigger;
+	h->total = nsteps;
 	CK(cudaMemsetAsync(d->slots, 0, sizeof(long long) * SLOT_FIELDS, d->st));
 	CK(cudaMemsetAsync(d->flags, 0, sizeof(unsigned) * 2, d->st));
 	return SEPDEV_OK;
@@ -260,7 +261,7 @@ extern "C" int sepdev_run(sepdev *d, const sepdev_pairset *ps, const sepdev_runc
 	Runner *r;
 	int rc = runner_get(d, &r);
 	if (rc) return rc;
-	if ((rc = run_begin(d, r, ps, cfg, *alpha, *sumv2))) return rc;
+	if ((rc = run_begin(d, r, ps, cfg, *alpha, *sumv2, nsteps))) return rc;
 	RunState *h = r->h_rs;
 	int recoveries = 0;
 	while (h->done < nsteps) {
@@ -490,7 +491,7 @@ extern "C" int sepdev_run_timed(sepdev *d, const sepdev_pairset *ps, const sepde
 	Runner *r;
 	int rc = runner_get(d, &r);
 	if (rc) return rc;
-	if ((rc = run_begin(d, r, ps, cfg, *alpha, *sumv2))) return rc;
+	if ((rc = run_begin(d, r, ps, cfg, *alpha, *sumv2, nsteps))) return rc;
 	TimedEvents *ev = (TimedEvents *)calloc(1, sizeof(TimedEvents));
 	if (!ev) return SEPDEV_ENOMEM;
 	TimedGraph tg[2];

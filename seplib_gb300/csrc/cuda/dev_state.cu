@@ -98,6 +98,7 @@ extern "C" void sepdev_destroy(sepdev *d)
 	for (int k = 0; k < SEPDEV_MAXTAB; k++)
 		if (d->tab[k]) cudaFree(d->tab[k]);
 	if (d->h_slots) cudaFreeHost(d->h_slots);
+	if (d->stage) cudaFreeHost(d->stage);
 	if (d->h_flags) cudaFreeHost(d->h_flags);
 	for (int k = 0; k < SEPDEV_NEV; k++)
 		if (d->ev[k]) cudaEventDestroy(d->ev[k]);
@@ -125,12 +126,37 @@ static double from_fixed(unsigned hi, unsigned lo, double L)
 	return (ldexp((double)hi, -32) + ldexp((double)lo, -64)) * L;
 }
 
-template <class T>
-static int hpin(T **p, size_t count)
+// Pinned staging for uploads and downloads, kept by the context: pinning
+// tens of megabytes costs milliseconds, so it is done once, not per call.
+// Arrays are carved out of one block in 256-byte aligned pieces.
+struct Stage {
+	char *base;
+	size_t off;
+	template <class T> T *take(long n)
+	{
+		T *p = (T *)(base + off);
+		off += ((sizeof(T) * (size_t)n + 255) & ~(size_t)255);
+		return p;
+	}
+};
+
+static int stage_get(sepdev *d, size_t bytes, Stage *st)
 {
-	cudaError_t e = cudaMallocHost((void **)p, sizeof(T) * (count ? count : 1));
-	if (e != cudaSuccess) { sepdev_set_error("cudaMallocHost", e); return SEPDEV_ENOMEM; }
+	if (d->stage_bytes < bytes) {
+		if (d->stage) { cudaFreeHost(d->stage); d->stage = NULL; d->stage_bytes = 0; }
+		cudaError_t e = cudaMallocHost(&d->stage, bytes);
+		if (e != cudaSuccess) { sepdev_set_error("cudaMallocHost(staging)", e); return SEPDEV_ENOMEM; }
+		d->stage_bytes = bytes;
+	}
+	st->base = (char *)d->stage;
+	st->off = 0;
 	return SEPDEV_OK;
+}
+
+// upper bound of the staging bytes of one upload or download of n particles
+static size_t stage_need(long n)
+{
+	return 12 * (((size_t)n * 16 + 255) & ~(size_t)255);
 }
 
 extern "C" int sepdev_upload(sepdev *d, const double *x, const double *v, const double *f,
@@ -144,13 +170,13 @@ extern "C" int sepdev_upload(sepdev *d, const double *x, const double *v, const 
 		d->L[k] = L[k];
 		d->fscale[k] = (float)(L[k] / 4294967296.0);
 	}
-	int4 *hp = NULL; uint4 *hl = NULL; float4 *hvh = NULL, *hvl = NULL, *hf = NULL;
-	int4 *hc = NULL, *hb = NULL; int *hg = NULL, *hm = NULL; float *hq = NULL;
-	int rc = SEPDEV_OK;
-	if ((rc = hpin(&hp, n)) || (rc = hpin(&hl, n)) || (rc = hpin(&hvh, n)) ||
-	    (rc = hpin(&hvl, n)) || (rc = hpin(&hf, n)) || (rc = hpin(&hc, n)) ||
-	    (rc = hpin(&hb, n)) || (rc = hpin(&hg, n)) || (rc = hpin(&hm, n)) || (rc = hpin(&hq, n)))
-		goto done;
+	Stage sg;
+	int rc = stage_get(d, stage_need(n), &sg);
+	if (rc) return rc;
+	int4 *hp = sg.take<int4>(n); uint4 *hl = sg.take<uint4>(n);
+	float4 *hvh = sg.take<float4>(n), *hvl = sg.take<float4>(n), *hf = sg.take<float4>(n);
+	int4 *hc = sg.take<int4>(n), *hb = sg.take<int4>(n);
+	int *hg = sg.take<int>(n), *hm = sg.take<int>(n); float *hq = sg.take<float>(n);
 	d->has_charge = 0;
 	for (long i = 0; i < n; i++) {
 		unsigned h[3], l[3];
@@ -189,8 +215,6 @@ extern "C" int sepdev_upload(sepdev *d, const double *x, const double *v, const 
 	d->list_valid = 0;
 done:
 	if (rc == SEPDEV_ECUDA) sepdev_set_error("upload", cudaGetLastError());
-	cudaFreeHost(hp); cudaFreeHost(hl); cudaFreeHost(hvh); cudaFreeHost(hvl); cudaFreeHost(hf);
-	cudaFreeHost(hc); cudaFreeHost(hb); cudaFreeHost(hg); cudaFreeHost(hm); cudaFreeHost(hq);
 	return rc;
 }
 
@@ -198,13 +222,13 @@ extern "C" int sepdev_download(sepdev *d, double *x, double *v, double *f, int *
 			       int *cross_neighb, double *xn)
 {
 	const long n = d->n;
-	int4 *hp = NULL, *hc = NULL, *hb = NULL, *hx = NULL; uint4 *hl = NULL;
-	float4 *hvh = NULL, *hvl = NULL, *hf = NULL; int *hg = NULL;
-	int rc = SEPDEV_OK;
-	if ((rc = hpin(&hp, n)) || (rc = hpin(&hl, n)) || (rc = hpin(&hvh, n)) ||
-	    (rc = hpin(&hvl, n)) || (rc = hpin(&hf, n)) || (rc = hpin(&hc, n)) ||
-	    (rc = hpin(&hb, n)) || (rc = hpin(&hg, n)) || (rc = hpin(&hx, n)))
-		goto done;
+	Stage sg;
+	int rc = stage_get(d, stage_need(n), &sg);
+	if (rc) return rc;
+	int4 *hp = sg.take<int4>(n), *hc = sg.take<int4>(n), *hb = sg.take<int4>(n);
+	int4 *hx = sg.take<int4>(n); uint4 *hl = sg.take<uint4>(n);
+	float4 *hvh = sg.take<float4>(n), *hvl = sg.take<float4>(n), *hf = sg.take<float4>(n);
+	int *hg = sg.take<int>(n);
 #define DN(dst, src) if ((rc = (cudaMemcpyAsync(dst, src, sizeof(*(dst)) * n, cudaMemcpyDeviceToHost, d->st) == cudaSuccess) ? 0 : SEPDEV_ECUDA)) goto done
 	DN(hp, d->pos[d->cur]); DN(hl, d->xlo); DN(hvh, d->vhi); DN(hvl, d->vlo); DN(hf, d->frc);
 	DN(hc, d->cross); DN(hb, d->cbase); DN(hg, d->gid); DN(hx, d->xn);
@@ -230,8 +254,6 @@ extern "C" int sepdev_download(sepdev *d, double *x, double *v, double *f, int *
 	}
 done:
 	if (rc == SEPDEV_ECUDA) sepdev_set_error("download", cudaGetLastError());
-	cudaFreeHost(hp); cudaFreeHost(hl); cudaFreeHost(hvh); cudaFreeHost(hvl); cudaFreeHost(hf);
-	cudaFreeHost(hc); cudaFreeHost(hb); cudaFreeHost(hg); cudaFreeHost(hx);
 	return rc;
 }
 

@@ -196,6 +196,11 @@ int sep_gpu_run(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
 	return 0;
 }
 
+static double time_kernel_loop(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
+			       double (*fun)(double, char), const double *ljparam, double cf,
+			       unsigned opt, int nh, double T0, double *alpha, double tau,
+			       long nsteps, long flush);
+
 int sep_gpu_run_timed(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
 		      double (*fun)(double, char), const double *ljparam, double cf, unsigned opt,
 		      int nh, double T0, double *alpha, double tau, long nsteps, sep_gpu_timing *tm)
@@ -208,6 +213,18 @@ int sep_gpu_run_timed(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
 	if (nsteps <= 0) {
 		tm->ms_steps = tm->ms_kernel = 0.0;
 		tm->launches = tm->overflows = 0;
+		return 0;
+	}
+	if (tm->kernel_spans) {
+		/* stream events around host-launched steps: an event node inside
+		 * a graph costs several microseconds, a stream event much less */
+		double a0 = alpha ? *alpha : 0.0;
+		tm->ms_kernel = time_kernel_loop(ptr, sys, ret, types, fun, ljparam, cf, opt, nh, T0,
+						 &a0, tau, nsteps, tm->flush_bytes);
+		if (alpha && nh) *alpha = a0;
+		tm->ms_steps = 0.0;
+		tm->launches = nsteps;
+		tm->overflows = 0;
 		return 0;
 	}
 	sepdev_pairset ps;
@@ -253,13 +270,15 @@ int sep_gpu_flush_l2(seppart *ptr, long bytes)
 	return 0;
 }
 
-int sep_gpu_time_step_kernel(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
-			     double (*fun)(double, char), const double *ljparam, double cf,
-			     unsigned opt, int nh, double T0, double *alpha, double tau,
-			     long nsteps, double *ms_per_launch)
+/* the prgs loop one step at a time from the host, with events around each
+ * fused step kernel; list rebuilds and (flush > 0) an L2 flush before each
+ * step stay outside the events.  Returns the summed kernel time in ms. */
+static double time_kernel_loop(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
+			       double (*fun)(double, char), const double *ljparam, double cf,
+			       unsigned opt, int nh, double T0, double *alpha, double tau,
+			       long nsteps, long flush)
 {
 	double total = 0.0;
-	long timed = 0;
 	for (long s = 0; s < nsteps; s++) {
 		sepdev_pairset ps;
 		rt_ctx *c = loop_setup(ptr, sys, types, fun, ljparam, cf, opt, &ps);
@@ -269,13 +288,15 @@ int sep_gpu_time_step_kernel(seppart *ptr, sepsys *sys, sepret *ret, const char 
 			*alpha = *alpha + sys->dt / (tau * tau) * (temp / T0 - 1.0);
 		}
 		const int slot = rt_new_slot(c), lf = rt_new_slot(c);
+		if (flush > 0) rt_check(sepdev_flush_l2(c->dev, (size_t)flush, (unsigned)s), "L2 flush");
 		rt_check(sepdev_event_record(c->dev, 0), "event");
-		rt_check(sepdev_step(c->dev, &ps, 0, sys->dt, nh, nh ? *alpha : 0.0, slot, lf), "step");
+		/* as in the device loop, only the last step reports energy and virial */
+		rt_check(sepdev_step_obs(c->dev, &ps, 0, sys->dt, nh, nh ? *alpha : 0.0, slot, lf,
+					 s + 1 == nsteps), "step");
 		rt_check(sepdev_event_record(c->dev, 1), "event");
 		float ms = 0.f;
 		rt_check(sepdev_event_elapsed(c->dev, 0, 1, &ms), "event");
 		total += ms;
-		timed++;
 		sep_reset_retval(ret);
 		rt_add_op(c, ret, OP_PAIR_ASSIGN, slot, 0);
 		rt_add_op(c, ret, OP_VIRIAL, slot, 0);
@@ -293,6 +314,16 @@ int sep_gpu_time_step_kernel(seppart *ptr, sepsys *sys, sepret *ret, const char 
 		c->host_valid = 0;
 		c->forces_zero = 0;
 	}
-	if (ms_per_launch) *ms_per_launch = timed ? total / timed : 0.0;
+	return total;
+}
+
+int sep_gpu_time_step_kernel(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
+			     double (*fun)(double, char), const double *ljparam, double cf,
+			     unsigned opt, int nh, double T0, double *alpha, double tau,
+			     long nsteps, double *ms_per_launch)
+{
+	const double total = time_kernel_loop(ptr, sys, ret, types, fun, ljparam, cf, opt, nh, T0,
+					       alpha, tau, nsteps, 0);
+	if (ms_per_launch) *ms_per_launch = nsteps > 0 ? total / nsteps : 0.0;
 	return 0;
 }

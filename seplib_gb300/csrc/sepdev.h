@@ -143,6 +143,10 @@ int sepdev_leapfrog(sepdev *d, double dt, int nh, double alpha, int slot);
 /* Fused pair forces + optional Nose-Hoover friction + leap-frog in one kernel. */
 int sepdev_step(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
 		int nh, double alpha, int pair_slot, int lf_slot);
+/* the same with observe = 0: the pair slot receives no energy or virial (a
+ * step of a loop whose sepret only reports its last step) */
+int sepdev_step_obs(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
+		    int nh, double alpha, int pair_slot, int lf_slot, int observe);
 
 /* f -= alpha m v on the stored forces. */
 int sepdev_friction(sepdev *d, double alpha);
