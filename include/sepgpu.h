@@ -64,6 +64,8 @@ typedef struct {
 	int list_max;         /* largest neighbour count of the current list */
 	double list_mean;     /* mean neighbour count (full list) */
 	int tpp;
+	int direct_io;        /* 1: uploads/downloads read and write the seppart array from
+	                       * device code (GPU access to pageable host memory) */
 } sep_gpu_info;
 
 int sep_gpu_info_get(seppart *ptr, sep_gpu_info *info);

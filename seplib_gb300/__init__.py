@@ -21,7 +21,8 @@ _lib = None
 class GpuInfo(C.Structure):
     """``sep_gpu_info`` (include/sepgpu.h)."""
     _fields_ = [("launches", C.c_long), ("list_builds", C.c_long), ("list_capacity", C.c_int),
-                ("list_max", C.c_int), ("list_mean", C.c_double), ("tpp", C.c_int)]
+                ("list_max", C.c_int), ("list_mean", C.c_double), ("tpp", C.c_int),
+                ("direct_io", C.c_int)]
 
 
 class GpuTiming(C.Structure):

@@ -107,6 +107,12 @@ struct sepdev {
 	void *stage;
 	size_t stage_bytes;
 
+	// in-place transfers: the device reads and writes the seppart array
+	// itself (set when the GPU can address pageable host memory)
+	int hostio_direct;
+	void *hio_scr;
+	size_t hio_bytes;
+
 	// kernel variants chosen by the tuner (SEPLIB_LJ_VARIANT overrides)
 	int lj_variant;
 	int nsm;

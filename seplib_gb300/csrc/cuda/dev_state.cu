@@ -72,6 +72,15 @@ extern "C" int sepdev_create(sepdev **out, long n)
 	d->tpp = 1;
 	CK(cudaDeviceGetAttribute(&d->nsm, cudaDevAttrMultiProcessorCount, d->device));
 	{
+		// in-place transfers need device access to pageable host memory
+		// (GB300: coherent NVLink-C2C through the host page tables);
+		// SEPLIB_HOSTIO=staged selects the staged copies regardless
+		int pma = 0;
+		CK(cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, d->device));
+		const char *hio = getenv("SEPLIB_HOSTIO");
+		d->hostio_direct = pma == 1 && !(hio && strcmp(hio, "staged") == 0);
+	}
+	{
 		const char *v = getenv("SEPLIB_LJ_VARIANT");
 		d->lj_variant = v ? atoi(v) : 0;
 	}
@@ -92,7 +101,7 @@ extern "C" void sepdev_destroy(sepdev *d)
 			d->celloff, d->cellcount, d->cellstart, d->perm, d->nl, d->ncnt, d->exb_start,
 			d->exb_idx, d->exa_start, d->exa_idx, d->bonds, d->angles, d->diheds_abcd,
 			d->dihed_type, d->inc_start, d->inc_term, d->term_out, d->slots, d->flags,
-			d->d_ps, d->flush_buf};
+			d->d_ps, d->flush_buf, d->hio_scr};
 	for (size_t k = 0; k < sizeof bufs / sizeof bufs[0]; k++)
 		if (bufs[k]) cudaFree(bufs[k]);
 	for (int k = 0; k < SEPDEV_MAXTAB; k++)

@@ -65,6 +65,7 @@ int sep_gpu_info_get(seppart *ptr, sep_gpu_info *info)
 	info->list_mean = mean;
 	extern int sepdev_get_tpp(sepdev *d);
 	info->tpp = sepdev_get_tpp(c->dev);
+	info->direct_io = sepdev_direct_io(c->dev);
 	return 0;
 }
 

@@ -128,6 +128,22 @@ void rt_need_device(rt_ctx *c, const sepsys *sys)
 		if (c->tpp) sepdev_set_tpp(c->dev, c->tpp);
 	}
 	if (c->dev_valid && !c->topo_dirty) return;
+	if (!c->dev_valid && sepdev_direct_io(c->dev)) {
+		/* the device reads the seppart records itself */
+		double sv2 = 0.0, maxd2 = 0.0;
+		int nt = 0;
+		const int rc = sepdev_upload_parts(c->dev, c->ptr, sys->length, SEPDEV_MAXTYPES, c->tchar,
+						   &nt, &sv2, &maxd2);
+		if (rc == SEPDEV_EOVERFLOW)
+			sep_error("more than %d particle types are not supported on the GPU", SEPDEV_MAXTYPES);
+		rt_check(rc, "upload");
+		c->ntypes = nt;
+		c->dev_valid = 1;
+		c->list_stale = 1;
+		c->sumv2 = sv2;
+		c->sumv2_valid = 1;
+		c->pending_trigger = sqrt(maxd2) > 0.5 * sys->skin;
+	}
 	if (!c->dev_valid) {
 		const long n = c->n;
 		seppart *p = c->ptr;
@@ -175,10 +191,28 @@ void rt_need_device(rt_ctx *c, const sepsys *sys)
 	if (c->topo_dirty) upload_topology(c);
 }
 
+/* bond lengths, angles and dihedral angles of the last bonded calls */
+static void term_values_to_host(rt_ctx *c)
+{
+	if (c->has_topo && c->topo_sys && c->topo_sys->molptr) {
+		sepmolinfo *m = c->topo_sys->molptr;
+		if (m->flag_bonds && m->blengths) sepdev_term_values(c->dev, 0, m->blengths);
+		if (m->flag_angles && m->angles) sepdev_term_values(c->dev, 1, m->angles);
+		if (m->flag_dihedrals && m->dihedrals) sepdev_term_values(c->dev, 2, m->dihedrals);
+	}
+}
+
 void rt_need_host(rt_ctx *c)
 {
 	if (c->host_valid) return;
 	rt_flush(c);
+	if (sepdev_direct_io(c->dev)) {
+		/* the device writes the seppart records itself */
+		rt_check(sepdev_download_parts(c->dev, c->ptr, c->forces_zero), "download");
+		term_values_to_host(c);
+		c->host_valid = 1;
+		return;
+	}
 	const long n = c->n;
 	seppart *p = c->ptr;
 	double *x = malloc(sizeof(double) * 3 * n), *v = malloc(sizeof(double) * 3 * n);
@@ -197,12 +231,7 @@ void rt_need_host(rt_ctx *c)
 			p[i].xn[k] = xn[3 * i + k];
 		}
 	free(x); free(v); free(f); free(xn); free(cr); free(cn);
-	if (c->has_topo && c->topo_sys && c->topo_sys->molptr) {
-		sepmolinfo *m = c->topo_sys->molptr;
-		if (m->flag_bonds && m->blengths) sepdev_term_values(c->dev, 0, m->blengths);
-		if (m->flag_angles && m->angles) sepdev_term_values(c->dev, 1, m->angles);
-		if (m->flag_dihedrals && m->dihedrals) sepdev_term_values(c->dev, 2, m->dihedrals);
-	}
+	term_values_to_host(c);
 	c->host_valid = 1;
 }
 

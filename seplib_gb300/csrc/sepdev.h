@@ -99,6 +99,22 @@ int sepdev_upload(sepdev *d, const double *x, const double *v, const double *f,
 int sepdev_download(sepdev *d, double *x, double *v, double *f, int *crossings,
 		    int *cross_neighb, double *xn);
 
+/*
+ * In-place transfers: the device reads and writes the seppart array itself
+ * (parts = the program's seppart pointer, n records).  Available when the GPU
+ * can address pageable host memory (sepdev_direct_io != 0).  The upload also
+ * returns the type characters in order of first appearance (at most
+ * max_types, ids 0..*ntypes-1), sum m v^2 (FP64, fixed summation order) and
+ * the largest squared displacement from the records' xn; more than
+ * max_types characters give SEPDEV_EOVERFLOW.  The download
+ * writes x, v, f (zero when forces_zero), a = f/m, crossings, cross_neighb
+ * and xn.
+ */
+int sepdev_direct_io(const sepdev *d);
+int sepdev_upload_parts(sepdev *d, const void *parts, const double *L, int max_types,
+			char *tchar, int *ntypes, double *sumv2, double *maxd2);
+int sepdev_download_parts(sepdev *d, void *parts, int forces_zero);
+
 /* Sum of m v^2 over the current velocities (one reduction, synchronous). */
 int sepdev_sumv2(sepdev *d, double *out);
 
