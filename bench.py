@@ -58,6 +58,12 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=0, help="oracle steps for cpu_baseline (0: auto)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--tpp", type=int, default=0)
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched"],
+                    help="plain: one N=4 ncell^3 system (the headline); batched: 512 independent "
+                         "systems stepped together")
+    ap.add_argument("--nsys", type=int, default=512)
+    ap.add_argument("--single-steps", type=int, default=200,
+                    help="steps per system of the one-system-per-launch comparison (batched)")
     return ap.parse_args()
 
 
@@ -196,11 +202,84 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def run_batched(args, rank, world):
+    """512 independent LJ systems (N log-uniform in [108, 4000], rho* in
+    [0.70, 0.95], T* in [0.7, 1.5], Nose-Hoover) stepped together with the
+    sepb_* API, against the same systems run one at a time through
+    sep_gpu_run (one graph per system)."""
+    from seplib_gb300 import build, configs, load, sepapi as A
+    from seplib_gb300.batch import Batch
+    build.build()
+    lib = load()
+    systems, rhos, temps = configs.replica_sweep(nsys=args.nsys, seed=4 + rank)
+    ntot = int(sum(s.n for s in systems))
+    b = Batch(lib, systems, rc=RC, skin=SKIN, dt=DT, T0=temps, tau=TAU)
+    b.run(max(3, args.warmup))
+    clocks = Clocks()
+    clocks.start()
+    barrier(world)
+    ms = b.run_timed(args.steps, FLUSH_BYTES)
+    barrier(world)
+    clk = clocks.stop()
+    t_dev = allmax(world, ms / 1e3)
+    value = world * ntot * args.steps / t_dev
+    # the production loop (one graph, no flush), wall clock around the call
+    t0 = time.perf_counter()
+    b.run(args.steps)
+    t_graph = time.perf_counter() - t0
+    slots = b.slots()
+    b.close()
+    # one system per launch: each system through its own device loop
+    fun = A.fun_ptr(lib, "sep_lj_shift")
+    ks = args.single_steps
+    t_single = 0.0
+    for k, s in enumerate(systems):
+        atoms, sys_ = new_system(lib, s)
+        ret = A.SepRet()
+        alpha = C.c_double(0.0)
+        run = lambda n: lib.sep_gpu_run(atoms, C.byref(sys_), C.byref(ret), b"AA", fun, None, RC,
+                                        A.SEP_ALL, 1, temps[k], C.byref(alpha), TAU, n)
+        assert run(16) == 0
+        lib.sep_gpu_stream_sync(atoms)
+        t0 = time.perf_counter()
+        assert run(ks) == 0
+        t_single += time.perf_counter() - t0
+        lib.sep_close(atoms, s.n)
+    single_pss = ntot * ks / t_single
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 pair / fixed-point x / f64-exact sums",
+            "data": "synthetic (seeded fcc lattices with vacancies, Maxwell-Boltzmann velocities)",
+            "config": {"workload": "%d independent LJ NVT systems, N log-uniform in [108, 4000] "
+                                   "(total %d), rho* ~ U[0.70, 0.95], T* ~ U[0.7, 1.5], Nose-Hoover "
+                                   "Q=%.0f, shifted LJ rc=%.1f, skin %.1f, dt=%.3f"
+                                   % (args.nsys, ntot, TAU, RC, SKIN, DT),
+                       "n_systems": args.nsys, "n_particles": ntot, "device_slots": slots,
+                       "l2": "flushed: %d MiB before every timed step, outside the spans" % (FLUSH_BYTES >> 20),
+                       "graph_loop_no_flush": {"value": ntot * args.steps / t_graph,
+                                               "unit": "particle-steps/s",
+                                               "what": "sepb_run, wall clock around the call"},
+                       "one_system_per_launch": {"value": single_pss, "unit": "particle-steps/s",
+                                                 "steps_per_system": ks,
+                                                 "what": "each system through sep_gpu_run in turn, "
+                                                         "wall clock"},
+                       "speedup_vs_one_system_per_launch": value / single_pss},
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+
+
 def main():
     args = parse()
     rank, world = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "batched":
+        run_batched(args, rank, world)
         return
     from seplib_gb300 import build, configs, load, sepapi as A, GpuInfo, GpuTiming
     build.build()

@@ -31,6 +31,13 @@ class GpuTiming(C.Structure):
                 ("ms_kernel", C.c_double), ("launches", C.c_long), ("overflows", C.c_long)]
 
 
+class SepbResult(C.Structure):
+    """``sepb_result`` (include/sepbatch.h)."""
+    _fields_ = [("epot", C.c_double), ("ekin", C.c_double), ("pot_P", (C.c_double * 3) * 3),
+                ("kin_P", (C.c_double * 3) * 3), ("alpha", C.c_double), ("max_dist2", C.c_double),
+                ("sumv2", C.c_double), ("nupdate", C.c_uint)]
+
+
 _GPU_SIGNATURES = {
     "sep_gpu_available": (C.c_int, []),
     "sep_gpu_error": (C.c_char_p, []),
@@ -52,6 +59,16 @@ _GPU_SIGNATURES = {
                                    sepapi.D_P, C.c_double, C.c_uint, C.c_int, C.c_double, sepapi.D_P,
                                    C.c_double, C.c_long, C.POINTER(GpuTiming)]),
     "sep_gpu_flush_l2": (C.c_int, [sepapi.PART_P, C.c_long]),
+    "sepb_create": (C.c_void_p, [C.c_int, C.POINTER(C.c_int), sepapi.D_P, C.c_double, C.c_double,
+                                 C.c_double, sepapi.D_P]),
+    "sepb_set_state": (C.c_int, [C.c_void_p, C.c_int, sepapi.D_P, sepapi.D_P, sepapi.D_P]),
+    "sepb_set_thermostat": (C.c_int, [C.c_void_p, sepapi.D_P, C.c_double, sepapi.D_P]),
+    "sepb_run": (C.c_int, [C.c_void_p, C.c_long]),
+    "sepb_run_timed": (C.c_int, [C.c_void_p, C.c_long, C.c_long, sepapi.D_P]),
+    "sepb_get_state": (C.c_int, [C.c_void_p, C.c_int, sepapi.D_P, sepapi.D_P, sepapi.D_P]),
+    "sepb_get_results": (C.c_int, [C.c_void_p, C.POINTER(SepbResult)]),
+    "sepb_particles": (C.c_long, [C.c_void_p]),
+    "sepb_destroy": (None, [C.c_void_p]),
 }
 
 

@@ -1,0 +1,65 @@
+// dev_batch.cuh - shared declarations of the batched multi-system path.
+//
+// Many independent LJ systems share one set of device arrays.  System s
+// owns the slots [off, off + npad) (npad = n rounded up to a warp, so every
+// warp belongs to one system; slots past n are inert padding) and the cell
+// entries [coff, coff + ncell + 2): its real cells, one cell that holds its
+// padding, and the end of the last range.  Per-warp and per-cell tables give
+// the owning system.
+#pragma once
+#include "dev_common.cuh"
+#include "dev_decide.cuh"
+#include "dev_pair.cuh"
+
+struct BatchSys {
+	int off, n, npad;      // slots and real particles
+	int coff, ncell;       // cell offset, real cells
+	int nc[3];             // cells per side
+	float fs;              // L / 2^32 (cubic box)
+	float shi, slo;        // dt * 2^64 / L as a float pair
+	double L;
+	double T0;             // thermostat target
+};
+
+// per-system loop state
+struct BatchState {
+	double alpha;          // alpha for the next step
+	double alpha_last;     // alpha used by the last completed step
+	double sumv2;
+	long long ntrig;       // skin-triggered updates (the reference's nupdate_neighb)
+	int force_trig;        // report an update after the next step
+	int last_trig;
+	double last[SLOT_FIELDS];
+};
+
+// loop state shared by all systems
+struct BatchRun {
+	long long remaining;   // loop iterations left
+	long long done;        // steps completed
+	long long total;       // steps in this call (the last one reports observables)
+	unsigned arrive;       // systems decided in the current step
+	unsigned any;          // some system asked for a rebuild in the current step
+	unsigned last_any;     // ... in the last completed step
+	int abort;
+};
+
+struct BatchDecide {
+	const BatchSys *sys;
+	BatchState *bs;
+	BatchRun *run;
+	long long *slots;      // SLOT_FIELDS per system
+	unsigned *flag;        // per system: rebuild before the next step
+	const unsigned *oflow; // list overflow word
+	int nsys;
+	float thr2;
+	double dt_tau2;
+	int nh;
+	int pair_end, use_handles, reset_while;
+	cudaGraphConditionalHandle h_next, h_while;
+};
+
+// launchers implemented next to the single-system kernels they share code with
+int sepdev_batch_step(sepdev *d, const PairArgs &a, const BatchSys *sys, const int *wsys, int nwarps,
+		      const BatchState *bs, const BatchRun *run, long long *slots, const BatchDecide &dec);
+int sepdev_batch_build(sepdev *d, int parity, const int *cellstart, const BatchSys *sys,
+		       const int *wsys, int nwarps, const unsigned *flag, float rl2);

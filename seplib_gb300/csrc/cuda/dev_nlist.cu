@@ -22,6 +22,8 @@
 #include <string.h>
 #include <math.h>
 #include "dev_common.cuh"
+#include "dev_batch.cuh"
+#include "dev_cellsort.cuh"
 
 __global__ void k_bin(long n, const int4 *__restrict__ pos, int ncx, int ncy, int ncz,
 		      int *__restrict__ cellof, int *__restrict__ celloff, int *__restrict__ count)
@@ -205,15 +207,12 @@ __device__ __forceinline__ float warp_max_f(float v, unsigned mask)
 	return v;
 }
 
-__global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles(long n, BuildArgs a)
+// One warp builds the lists of the tile of 32 particles starting at i0 (n:
+// end of the particles to build); sp and ring are the warp's shared staging.
+__device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, float4 *sp, int *ring)
 {
-	__shared__ float4 sp_all[BT_WARPS][BT_CAP];
-	__shared__ int ring_all[BT_WARPS][BT_RING * 32];
 	const unsigned FULL = 0xffffffffu;
-	const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	float4 *sp = sp_all[w];
-	int *ring = ring_all[w];
-	const long i0 = ((long)blockIdx.x * BT_WARPS + w) * 32;
+	const int lane = threadIdx.x & 31;
 	if (i0 >= n) return;
 	const long i = i0 + lane;
 	const bool act = i < n;
@@ -267,6 +266,20 @@ __global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles(long n, BuildArgs
 					const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 					const int j = __float_as_int(q.w);
 					const bool hit = (r2 < a.rl2) & (j != (int)i);
+					ring[(cnt & (BT_RING - 1)) * 32 + lane] = j;
+					cnt += hit ? 1 : 0;
+				}
+			} else if (a.excl == SEPDEV_EXCL_NONE) {
+				// minimum-image separations per candidate, appended in
+				// candidate order without branches (as the local form)
+#pragma unroll 4
+				for (int c = 0; c < fill; c++) {
+					const float4 q = sp[c];
+					const float dx = sep_hi(pi.x, __float_as_int(q.x), a.fs[0]);
+					const float dy = sep_hi(pi.y, __float_as_int(q.y), a.fs[1]);
+					const float dz = sep_hi(pi.z, __float_as_int(q.z), a.fs[2]);
+					const int j = __float_as_int(q.w);
+					const bool hit = (dx * dx + dy * dy + dz * dz < a.rl2) & (j != (int)i);
 					ring[(cnt & (BT_RING - 1)) * 32 + lane] = j;
 					cnt += hit ? 1 : 0;
 				}
@@ -370,31 +383,45 @@ __global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles(long n, BuildArgs
 	if (lane == 0) atomicMax(&a.flags[1], mxc);
 }
 
-// Deterministic order inside each cell: one warp per cell ranks its members
-// by user index with shuffles (cells of more than 32 fall back to a serial
-// insertion sort in lane 0).
-__global__ void k_cellsort_w(long m, const int *__restrict__ start, const int *__restrict__ gid,
-			     int *__restrict__ perm)
+__global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles(long n, BuildArgs a)
 {
+	__shared__ float4 sp_all[BT_WARPS][BT_CAP];
+	__shared__ int ring_all[BT_WARPS][BT_RING * 32];
+	const int w = threadIdx.x >> 5;
+	build_tile(n, a, ((long)blockIdx.x * BT_WARPS + w) * 32, sp_all[w], ring_all[w]);
+}
+
+// Batched systems: each warp builds its tile with its own system's cell grid
+// and box, and only for systems whose rebuild flag is set.
+__global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles_batch(BuildArgs a, const BatchSys *sys,
+								    const int *wsys, int nwarps,
+								    const unsigned *flag)
+{
+	__shared__ float4 sp_all[BT_WARPS][BT_CAP];
+	__shared__ int ring_all[BT_WARPS][BT_RING * 32];
+	const int w = threadIdx.x >> 5;
+	const long wg = (long)blockIdx.x * BT_WARPS + w;
+	if (wg >= nwarps) return;
+	const int s = wsys[wg];
+	if (!flag[s]) return;
+	const BatchSys S = sys[s];
+	BuildArgs b = a;
+	b.cellstart = a.cellstart + S.coff;
+	for (int k = 0; k < 3; k++) { b.nc[k] = S.nc[k]; b.fs[k] = S.fs; }
+	build_tile(S.off + S.n, b, wg * 32, sp_all[w], ring_all[w]);
+}
+
+// Deterministic order inside each cell: one warp per cell ranks its members
+// by user index (dev_cellsort.cuh).  Launched with 256 threads.
+__global__ void __launch_bounds__(256) k_cellsort_w(long m, const int *__restrict__ start,
+						    const int *__restrict__ gid, int *__restrict__ perm)
+{
+	__shared__ int sk[8][CS_MAX], sv[8][CS_MAX];
 	const long c = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
-	const int lane = threadIdx.x & 31;
 	if (c >= m) return;
-	const int lo = start[c], cnt = start[c + 1] - lo;
-	if (cnt <= 1) return;
-	if (cnt <= 32) {
-		const int v = lane < cnt ? perm[lo + lane] : 0;
-		const int key = lane < cnt ? gid[v] : 0x7fffffff;
-		int rank = 0;
-		for (int l = 0; l < cnt; l++) rank += (__shfl_sync(0xffffffffu, key, l) < key);
-		__syncwarp();
-		if (lane < cnt) perm[lo + rank] = v;
-	} else if (lane == 0) {
-		for (int x = lo + 1; x < lo + cnt; x++) {
-			int v = perm[x], key = gid[v], b = x - 1;
-			while (b >= lo && gid[perm[b]] > key) { perm[b + 1] = perm[b]; b--; }
-			perm[b + 1] = v;
-		}
-	}
+	const int w = threadIdx.x >> 5;
+	const int lo = start[c];
+	cell_sort_warp(lo, start[c + 1] - lo, gid, perm, sk[w], sv[w]);
 }
 
 // Copy the gathered arrays back into the primary buffers, so buffer
@@ -532,6 +559,12 @@ static int list_capacity(sepdev *d, int maxnb)
 	return SEPDEV_OK;
 }
 
+// capacity for at least maxnb neighbours per particle (existing lists are lost)
+int sepdev_grow_list_to(sepdev *d, int maxnb)
+{
+	return list_capacity(d, maxnb);
+}
+
 int sepdev_build_args(sepdev *d, BuildArgs *a, int parity)
 {
 	a->pos = d->pos[parity];
@@ -547,6 +580,26 @@ int sepdev_build_args(sepdev *d, BuildArgs *a, int parity)
 	a->mol = d->mol;
 	a->exs = d->excl == SEPDEV_EXCL_BONDS ? d->exb_start : d->exa_start;
 	a->exi = d->excl == SEPDEV_EXCL_BONDS ? d->exb_idx : d->exa_idx;
+	return SEPDEV_OK;
+}
+
+int sepdev_batch_build(sepdev *d, int parity, const int *cellstart, const BatchSys *sys,
+		       const int *wsys, int nwarps, const unsigned *flag, float rl2)
+{
+	BuildArgs a;
+	memset(&a, 0, sizeof a);
+	a.pos = d->pos[parity];
+	a.cellstart = cellstart;
+	a.rl2 = rl2;
+	a.maxnb = d->maxnb;
+	a.nl = d->nl;
+	a.ncnt = d->ncnt;
+	a.flags = d->flags;
+	a.excl = SEPDEV_EXCL_NONE;
+	a.gid = d->gid;
+	a.mol = d->mol;
+	k_build_tiles_batch<<<grid_for(nwarps, BT_WARPS), BT_WARPS * 32, 0, d->st>>>(a, sys, wsys, nwarps, flag);
+	CKL(d);
 	return SEPDEV_OK;
 }
 

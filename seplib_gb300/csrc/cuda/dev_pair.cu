@@ -25,6 +25,7 @@
 #include "dev_common.cuh"
 
 #include "dev_pair.cuh"
+#include "dev_batch.cuh"
 
 enum { VAR_SINGLE = 0, VAR_GENERAL = 1, VAR_GENERAL_COUL = 2 };
 
@@ -50,10 +51,12 @@ __device__ __forceinline__ void tab_eval(const float2 *__restrict__ t, int nt, f
 }
 
 // Integrate particle i (leap-frog, optional friction) and return its kinetic
-// contributions; F is the total force before friction.
-__device__ __forceinline__ void integrate(long i, float fx, float fy, float fz, float ei,
-					  const int4 pi, const PairArgs &a, float alpha, int4 *pos_out,
-					  float &ek, float (&kp)[6], float &sv2, float &d2)
+// contributions; F is the total force before friction.  fs, shi, slo: the
+// box-dependent scales (L/2^32 and dt*2^64/L split in two floats).
+__device__ __forceinline__ void integrate_s(long i, float fx, float fy, float fz, float ei,
+					    const int4 pi, const PairArgs &a, const float (&fs)[3],
+					    const float (&shi)[3], const float (&slo)[3], float alpha,
+					    int4 *pos_out, float &ek, float (&kp)[6], float &sv2, float &d2)
 {
 	float4 vh = a.vhi[i], vl = a.vlo[i];
 	const uint4 lo = a.xlo[i];
@@ -76,9 +79,9 @@ __device__ __forceinline__ void integrate(long i, float fx, float fy, float fz, 
 	kp[0] = m * tx * tx; kp[1] = m * tx * ty; kp[2] = m * tx * tz;
 	kp[3] = m * ty * ty; kp[4] = m * ty * tz; kp[5] = m * tz * tz;
 	sv2 = m * (vh.x * vh.x + vh.y * vh.y + vh.z * vh.z);
-	const long long ix = ff_mul_fix(vh.x, vl.x, a.shi[0], a.slo[0]);
-	const long long iy = ff_mul_fix(vh.y, vl.y, a.shi[1], a.slo[1]);
-	const long long iz = ff_mul_fix(vh.z, vl.z, a.shi[2], a.slo[2]);
+	const long long ix = ff_mul_fix(vh.x, vl.x, shi[0], slo[0]);
+	const long long iy = ff_mul_fix(vh.y, vl.y, shi[1], slo[1]);
+	const long long iz = ff_mul_fix(vh.z, vl.z, shi[2], slo[2]);
 	const unsigned long long X0 = ((unsigned long long)(unsigned)pi.x << 32) | lo.x;
 	const unsigned long long Y0 = ((unsigned long long)(unsigned)pi.y << 32) | lo.y;
 	const unsigned long long Z0 = ((unsigned long long)(unsigned)pi.z << 32) | lo.z;
@@ -100,10 +103,17 @@ __device__ __forceinline__ void integrate(long i, float fx, float fy, float fz, 
 	a.vhi[i] = vh;
 	a.vlo[i] = vl;
 	const int4 xn = a.xn[i];
-	const float dx = sep_hi(po.x, xn.x, a.fs[0]);
-	const float dy = sep_hi(po.y, xn.y, a.fs[1]);
-	const float dz = sep_hi(po.z, xn.z, a.fs[2]);
+	const float dx = sep_hi(po.x, xn.x, fs[0]);
+	const float dy = sep_hi(po.y, xn.y, fs[1]);
+	const float dz = sep_hi(po.z, xn.z, fs[2]);
 	d2 = dx * dx + dy * dy + dz * dz;
+}
+
+__device__ __forceinline__ void integrate(long i, float fx, float fy, float fz, float ei,
+					  const int4 pi, const PairArgs &a, float alpha, int4 *pos_out,
+					  float &ek, float (&kp)[6], float &sv2, float &d2)
+{
+	integrate_s(i, fx, fy, fz, ei, pi, a, a.fs, a.shi, a.slo, alpha, pos_out, ek, kp, sv2, d2);
 }
 
 template <int VAR, bool FUSED>
@@ -473,6 +483,74 @@ void sepdev_fill_args(sepdev *d, PairArgs &a, const sepdev_pairset *ps, double d
 	a.flags = NULL;
 	a.skip_obs = 0;
 	memset(&a.dec, 0, sizeof a.dec);
+}
+
+// Batched systems: one fused step (LJ forces, Nose-Hoover friction,
+// leap-frog) over every system at once.  A warp belongs to one system and
+// takes that system's box scales and thermostat; the arithmetic per particle
+// is the single-system k_lj's (cubic form), and each warp adds its sums to
+// its system's accumulator slot with the same fixed-point conversion as the
+// block reduction there, so a system's results do not depend on the batch.
+__global__ void __launch_bounds__(256, 4) k_lj_batch(PairArgs a, const BatchSys *sys, const int *wsys,
+						    int nwarps, const BatchState *bs, const BatchRun *run,
+						    long long *slots, BatchDecide dec)
+{
+	const unsigned FULL = 0xffffffffu;
+	if (dec.reset_while && blockIdx.x == 0 && threadIdx.x == 0)
+		cudaGraphSetConditional(dec.h_while, 0);
+	if (a.flags && (a.flags[0] & 1u)) return;      // list overflow: the decision stops the loop
+	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	const long wg = i >> 5;
+	if (wg >= nwarps) return;                      // whole warps
+	const int s = wsys[wg];
+	const BatchSys S = sys[s];
+	const bool act = i - S.off < S.n;
+	const float u = S.fs;
+	const float rc2 = a.rc2 / (u * u);
+	const float sig2 = a.sig2 / (u * u);
+	float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f, nin = 0.f;
+	float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+	int4 pi = make_int4(0, 0, 0, 0);
+	const int cnt = act ? a.ncnt[i] : 0;
+	const bool obs = run->done + 1 >= run->total;
+	if (act) {
+		pi = a.pos[i];
+		if (obs) lj_pairs<true, true, 0>(a, i, cnt, pi, 1.f, 1.f, 1.f, rc2, sig2, fx, fy, fz, e, nin, w);
+		else lj_pairs<false, true, 0>(a, i, cnt, pi, 1.f, 1.f, 1.f, rc2, sig2, fx, fy, fz, e, nin, w);
+	}
+	e = fmaf(nin, a.ushift, e);
+	fx *= u; fy *= u; fz *= u;
+	const float u2 = u * u;
+	for (int k = 0; k < 6; k++) w[k] *= u2;
+	float ek = 0.f, kp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, sv2 = 0.f, d2 = 0.f;
+	if (act) {
+		const float fsv[3] = {S.fs, S.fs, S.fs}, shv[3] = {S.shi, S.shi, S.shi}, slv[3] = {S.slo, S.slo, S.slo};
+		const float alpha = (float)bs[s].alpha;
+		integrate_s(i, fx, fy, fz, 0.5f * e, pi, a, fsv, shv, slv, alpha, a.pos_out, ek, kp, sv2, d2);
+	}
+	float v[15] = {0.5f * e, 0.5f * w[0], 0.5f * w[1], 0.5f * w[2], 0.5f * w[3], 0.5f * w[4], 0.5f * w[5],
+		       ek, kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], sv2};
+	const int fld[15] = {SLOT_EPOT0, SLOT_POTP, SLOT_POTP + 1, SLOT_POTP + 2, SLOT_POTP + 3,
+			     SLOT_POTP + 4, SLOT_POTP + 5, SLOT_EKIN, SLOT_KINP, SLOT_KINP + 1,
+			     SLOT_KINP + 2, SLOT_KINP + 3, SLOT_KINP + 4, SLOT_KINP + 5, SLOT_SUMV2};
+	warp_sum<15>(v);
+	const unsigned mx = __reduce_max_sync(FULL, __float_as_uint(d2));
+	if ((threadIdx.x & 31) == 0) {
+		long long *sl = slots + (long)s * SLOT_FIELDS;
+		for (int k = 0; k < 15; k++) {
+			const long long q = __float2ll_rn(v[k] * FX_SCALE);
+			if (q != 0) atomicAdd((unsigned long long *)&sl[fld[k]], (unsigned long long)q);
+		}
+		if (mx) atomicMax((unsigned long long *)&sl[SLOT_MAXD2], (unsigned long long)mx);
+	}
+}
+
+int sepdev_batch_step(sepdev *d, const PairArgs &a, const BatchSys *sys, const int *wsys, int nwarps,
+		      const BatchState *bs, const BatchRun *run, long long *slots, const BatchDecide &dec)
+{
+	k_lj_batch<<<grid_for((long)nwarps * 32, 256), 256, 0, d->st>>>(a, sys, wsys, nwarps, bs, run, slots, dec);
+	CKL(d);
+	return SEPDEV_OK;
 }
 
 int sepdev_upload_pairset(sepdev *d, const sepdev_pairset *ps)
