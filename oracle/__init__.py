@@ -224,3 +224,25 @@ def run_lj(x, v, m, types_arr, L, kind, param, cf, skin, dt, nsteps, nh=False, T
 
 def nsubbox(cf, delta, L):
     return lib().ora_nsubbox(cf, delta, L)
+
+
+def lj_loss(x, v, m, L, param, dt, nsteps):
+    """FP64 loss of the NVE loop: (1/K) sum_n (epot_n + p_n), brute-force pairs."""
+    x = _f64(x); v = _f64(v); m = _f64(m); L = _f64(L); p = _f64(param)
+    f = lib().ora_lj_loss
+    f.restype = C.c_double
+    return f(len(x), _p(x, C.c_double), _p(v, C.c_double), _p(m, C.c_double), _p(L, C.c_double),
+             _p(p, C.c_double), C.c_double(dt), C.c_long(nsteps))
+
+
+def lj_adjoint(x, v, m, L, param, dt, nsteps):
+    """FP64 gradient of lj_loss: (dL/deps, dL/dsigma, dL/dx0)."""
+    x = _f64(x); v = _f64(v); m = _f64(m); L = _f64(L); p = _f64(param)
+    de, ds = C.c_double(), C.c_double()
+    gx = np.zeros_like(x)
+    rc = lib().ora_lj_adjoint(len(x), _p(x, C.c_double), _p(v, C.c_double), _p(m, C.c_double),
+                              _p(L, C.c_double), _p(p, C.c_double), C.c_double(dt), C.c_long(nsteps),
+                              C.byref(de), C.byref(ds), _p(gx, C.c_double))
+    if rc != 0:
+        raise MemoryError("ora_lj_adjoint")
+    return de.value, ds.value, gx

@@ -576,3 +576,160 @@ int ora_run_lj(long n, double *x, double *v, const double *m, const char *type,
 	free(f); free(a); free(xn); free(cn); free(cr); free(start); free(nb);
 	return 0;
 }
+
+/* ---- gradients of an MD loss (the adjoint's oracle) -------------------------
+ *
+ * The loss of the NVE prgs loop with sep_force_lj (param = {cf, eps, sigma,
+ * aw}) and sep_leapfrog (source/sepprfrc.c:743-1000, source/sepintgr.c:42-88):
+ *     L = (1/K) sum_{n<K} ( epot_n + (tr kin_P_n + tr pot_P_n) / 3V )
+ * in FP64, serial, brute-force pairs (small systems only).  ora_lj_adjoint
+ * returns its gradient by the reverse sweep over stored states; the FD test
+ * pins it against ora_lj_loss. */
+
+/* per-pair functions of s = r^2 for the reference's LJ force scalar phi
+ * (F_i += phi d), energy u, virial w = phi s, their s-derivatives, and their
+ * eps- and sigma-derivatives */
+typedef struct { double phi, u, phis, us, ws, phie, ue, phisg, usg; } ora_pairfn;
+
+static void ora_lj_pairfn(const double *p, double s, ora_pairfn *o)
+{
+	const double cf = p[0], eps = p[1], sig = p[2], aw = p[3], awh = 0.5 * aw;
+	const double sr = sig / cf, sr6 = pow(sr, 6.0);
+	const double shift = -4.0 * eps * (sr6 * sr6 - aw * sr6);
+	const double dshift_sig = -24.0 * eps / sig * (2.0 * sr6 * sr6 - aw * sr6);
+	const double q = sig * sig / s, s6 = q * q * q;
+	o->phi = 48.0 * eps * q * s6 * (s6 - awh);
+	o->u = 4.0 * eps * s6 * (s6 - aw) + shift;
+	o->phis = -48.0 * eps * q * s6 * (7.0 * s6 - 4.0 * awh) / s;
+	o->us = -12.0 * eps * s6 * (2.0 * s6 - aw) / s;
+	o->ws = -144.0 * eps * q * s6 * (2.0 * s6 - awh);
+	o->phie = o->phi / eps;
+	o->ue = o->u / eps;
+	o->phisg = 96.0 * eps * q * s6 * (7.0 * s6 - 4.0 * awh) / sig;
+	o->usg = 24.0 * eps / sig * s6 * (2.0 * s6 - aw) + dshift_sig;
+}
+
+/* one force evaluation: F (3n), epot, tr pot_P */
+static void ora_lj_forces_brute(long n, const double *x, const double L[3], const double *p,
+				double *F, double *epot, double *trw)
+{
+	const double cf2 = p[0] * p[0];
+	memset(F, 0, sizeof(double) * 3 * n);
+	double e = 0.0, w = 0.0;
+	for (long i = 0; i < n; i++)
+		for (long j = i + 1; j < n; j++) {
+			double d[3];
+			const double s = ora_sep(x, i, j, L, d);
+			if (s >= cf2) continue;
+			ora_pairfn f;
+			ora_lj_pairfn(p, s, &f);
+			for (int k = 0; k < 3; k++) {
+				F[3 * i + k] += f.phi * d[k];
+				F[3 * j + k] -= f.phi * d[k];
+			}
+			e += f.u;
+			w += f.phi * s;
+		}
+	*epot = e;
+	*trw = w;
+}
+
+static void ora_wrap_all(double *x, const double L[3], long n)
+{
+	for (long i = 0; i < n; i++)
+		for (int k = 0; k < 3; k++) {
+			x[3 * i + k] -= L[k] * floor(x[3 * i + k] / L[k]);
+			if (x[3 * i + k] >= L[k]) x[3 * i + k] -= L[k];
+		}
+}
+
+double ora_lj_loss(long n, const double *x0, const double *v0, const double *m, const double L[3],
+		   const double *p, double dt, long nsteps)
+{
+	double *x = malloc(sizeof(double) * 3 * n), *u = malloc(sizeof(double) * 3 * n);
+	double *F = malloc(sizeof(double) * 3 * n);
+	if (!x || !u || !F) return NAN;
+	memcpy(x, x0, sizeof(double) * 3 * n);
+	memcpy(u, v0, sizeof(double) * 3 * n);
+	const double V = L[0] * L[1] * L[2];
+	double loss = 0.0;
+	for (long step = 0; step < nsteps; step++) {
+		double ep, trw, trk = 0.0;
+		ora_lj_forces_brute(n, x, L, p, F, &ep, &trw);
+		for (long i = 0; i < n; i++)
+			for (int k = 0; k < 3; k++) {
+				const double a = F[3 * i + k] / m[i];
+				u[3 * i + k] += a * dt;
+				x[3 * i + k] += u[3 * i + k] * dt;
+				const double vt = u[3 * i + k] - 0.5 * a * dt;
+				trk += m[i] * vt * vt;
+			}
+		ora_wrap_all(x, L, n);
+		loss += ep + (trk + trw) / (3.0 * V);
+	}
+	free(x); free(u); free(F);
+	return loss / nsteps;
+}
+
+int ora_lj_adjoint(long n, const double *x0, const double *v0, const double *m, const double L[3],
+		   const double *p, double dt, long nsteps, double *dL_deps, double *dL_dsig,
+		   double *dL_dx0)
+{
+	const long K = nsteps;
+	double *X = malloc(sizeof(double) * 3 * n * (K + 1)), *U = malloc(sizeof(double) * 3 * n * (K + 1));
+	double *F = malloc(sizeof(double) * 3 * n), *lx = calloc(3 * n, sizeof(double));
+	double *lu = calloc(3 * n, sizeof(double)), *h = malloc(sizeof(double) * 3 * n);
+	if (!X || !U || !F || !lx || !lu || !h) return -1;
+	memcpy(X, x0, sizeof(double) * 3 * n);
+	memcpy(U, v0, sizeof(double) * 3 * n);
+	for (long s = 0; s < K; s++) {
+		double *x = X + 3 * n * s, *u = U + 3 * n * s, *x1 = X + 3 * n * (s + 1), *u1 = U + 3 * n * (s + 1);
+		double ep, trw;
+		ora_lj_forces_brute(n, x, L, p, F, &ep, &trw);
+		for (long q = 0; q < 3 * n; q++) {
+			u1[q] = u[q] + F[q] / m[q / 3] * dt;
+			x1[q] = x[q] + u1[q] * dt;
+		}
+		ora_wrap_all(x1, L, n);
+	}
+	const double V = L[0] * L[1] * L[2], cK = 1.0 / K, cf2 = p[0] * p[0];
+	double ge = 0.0, gs = 0.0;
+	for (long s = K - 1; s >= 0; s--) {
+		const double *x = X + 3 * n * s, *u = U + 3 * n * s, *u1 = U + 3 * n * (s + 1);
+		for (long q = 0; q < 3 * n; q++) {
+			const double mi = m[q / 3];
+			const double kin = cK * mi * 0.5 * (u[q] + u1[q]) / (3.0 * V);
+			const double g = lu[q] + dt * lx[q] + kin;
+			lu[q] = g + kin;
+			h[q] = dt / mi * g;
+		}
+		for (long i = 0; i < n; i++)
+			for (long j = i + 1; j < n; j++) {
+				double d[3];
+				const double sq = ora_sep(x, i, j, L, d);
+				if (sq >= cf2) continue;
+				ora_pairfn f;
+				ora_lj_pairfn(p, sq, &f);
+				double dh[3], ddh = 0.0, dhi = 0.0, dhj = 0.0;
+				for (int k = 0; k < 3; k++) {
+					dh[k] = h[3 * i + k] - h[3 * j + k];
+					ddh += d[k] * dh[k];
+					dhi += d[k] * h[3 * i + k];
+					dhj += d[k] * h[3 * j + k];
+				}
+				const double c2 = 2.0 * f.phis * ddh + 2.0 * cK * (f.us + f.ws / (3.0 * V));
+				for (int k = 0; k < 3; k++) {
+					const double t = f.phi * dh[k] + c2 * d[k];
+					lx[3 * i + k] += t;
+					lx[3 * j + k] -= t;
+				}
+				ge += f.phie * (dhi - dhj) + cK * (f.ue + f.phie * sq / (3.0 * V));
+				gs += f.phisg * (dhi - dhj) + cK * (f.usg + f.phisg * sq / (3.0 * V));
+			}
+	}
+	*dL_deps = ge;
+	*dL_dsig = gs;
+	memcpy(dL_dx0, lx, sizeof(double) * 3 * n);
+	free(X); free(U); free(F); free(lx); free(lu); free(h);
+	return 0;
+}

@@ -1,0 +1,604 @@
+// dev_adj.cu - reverse-mode gradients through the LJ force and leap-frog
+// (sepadj_* API), on the batched layout of dev_batch.cu.
+//
+// Forward (per replica, NVE): u_{n+1} = u_n + dt/m F(x_n), x_{n+1} = x_n +
+// dt u_{n+1}, loss L = (1/K) sum_n l_n with l_n = U(x_n) + (sum m vt^2 +
+// W(x_n)) / 3V, vt = (u_n + u_{n+1}) / 2, W = sum_pairs f.d.  Backward, with
+// lx = dL/dx, lu = dL/du (zero after the last step), for n = K-1 .. 0:
+//     g   = lu + dt lx + (1/K) m vt / 3V          (dL/du_{n+1} in total)
+//     h   = dt/m g
+//     lx += sum_j [ phi (h_i - h_j) + 2 phi' d (d.(h_i - h_j))
+//                   + (2/K)(u' + w'/3V) d ]        (pair terms at x_n)
+//     lu  = g + (1/K) m vt / 3V
+// with per-pair functions of s = r^2: the force scalar phi (F_i = sum phi d,
+// the reference's 48 eps s6 (s6 - aw/2) sigma^2/s), the energy u and the
+// virial phi s; primes are d/ds.  The parameter gradients add, per pair and
+// side, phi_theta d.h_i + (1/2K)(u_theta + phi_theta s / 3V).
+//
+// Slot order never changes after the initial sort: list rebuilds use a
+// per-particle scan of index-only cell lists, so no permutation has to be
+// undone in reverse.  Checkpoints every C steps hold the full replica state
+// and list; the backward pass recomputes a segment from its checkpoint,
+// keeping the states and the lists of every rebuilt replica, and sweeps it.
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <vector>
+#include "dev_common.cuh"
+#include "dev_batch.cuh"
+#include "sepadj.h"
+#include "sepbatch.h"
+
+// ---- list rebuild without moving particles ----------------------------------
+
+// one thread per particle of a flagged system: scan the (deduplicated) 27
+// neighbouring cells of the index-only cell list, append every j with
+// r^2 < rl2 in cell order (members ordered by user index)
+__global__ void ka_build(const BatchSys *sys, const int *wsys, int nwarps, const unsigned *flag,
+			 const int4 *pos, const int *cellstart, const int *perm, int *nl, int *ncnt,
+			 int maxnb, float rl2, unsigned *oflow)
+{
+	const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	const long wg = t >> 5;
+	if (wg >= nwarps) return;
+	const int s = wsys[wg];
+	if (!flag[s]) return;
+	const BatchSys S = sys[s];
+	if (t - S.off >= S.n) return;
+	const int4 pi = pos[t];
+	const int nc0 = S.nc[0], nc1 = S.nc[1], nc2 = S.nc[2];
+	const int cx = (int)__umulhi((unsigned)pi.x, (unsigned)nc0);
+	const int cy = (int)__umulhi((unsigned)pi.y, (unsigned)nc1);
+	const int cz = (int)__umulhi((unsigned)pi.z, (unsigned)nc2);
+	const int lx = nc0 >= 3 ? -1 : 0, hx = nc0 >= 2 ? 1 : 0;
+	const int ly = nc1 >= 3 ? -1 : 0, hy = nc1 >= 2 ? 1 : 0;
+	const int lz = nc2 >= 3 ? -1 : 0, hz = nc2 >= 2 ? 1 : 0;
+	int cnt = 0;
+	for (int oz = lz; oz <= hz; oz++) {
+		const int zz = (cz + oz + nc2) % nc2;
+		for (int oy = ly; oy <= hy; oy++) {
+			const int yy = (cy + oy + nc1) % nc1;
+			for (int ox = lx; ox <= hx; ox++) {
+				const int xx = (cx + ox + nc0) % nc0;
+				const int c = S.coff + xx + nc0 * (yy + nc1 * zz);
+				for (int k = cellstart[c], ke = cellstart[c + 1]; k < ke; k++) {
+					const int j = perm[k];
+					if (j == (int)t) continue;
+					const int4 pj = pos[j];
+					const float dx = sep_hi(pi.x, pj.x, S.fs);
+					const float dy = sep_hi(pi.y, pj.y, S.fs);
+					const float dz = sep_hi(pi.z, pj.z, S.fs);
+					if (dx * dx + dy * dy + dz * dz < rl2) {
+						if (cnt < maxnb) nl[nl_index(t, cnt, maxnb)] = j;
+						cnt++;
+					}
+				}
+			}
+		}
+	}
+	ncnt[t] = cnt < maxnb ? cnt : maxnb;
+	if (cnt > maxnb) atomicOr(oflow, 1u);
+}
+
+// a rebuilt system measures displacements from here on (skin test)
+__global__ void ka_xn(const int *wsys, int nwarps, const unsigned *flag, const int4 *pos, int4 *xn,
+		      const int4 *cross, int4 *cbase)
+{
+	const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	const long wg = t >> 5;
+	if (wg >= nwarps || !flag[wsys[wg]]) return;
+	xn[t] = pos[t];
+	cbase[t] = cross[t];
+}
+
+// ---- the backward step --------------------------------------------------------
+
+struct AdjState {        // one stored step: positions and velocities per slot
+	int4 *pos;
+	uint4 *xlo;
+	float4 *vhi, *vlo;
+};
+
+__device__ __forceinline__ double3 ff3(const float4 h, const float4 l)
+{
+	return make_double3((double)h.x + (double)l.x, (double)h.y + (double)l.y, (double)h.z + (double)l.z);
+}
+
+// g = lu + dt lx + kin, h = dt/m g, lu = g + kin  (kin = (1/K) m vt / 3V)
+__global__ void ka_h(const BatchSys *sys, const int *wsys, int nwarps, AdjState un, AdjState un1,
+		     double *lx, double *lu, float4 *h, double dt, double cK)
+{
+	const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	const long wg = t >> 5;
+	if (wg >= nwarps) return;
+	const BatchSys S = sys[wsys[wg]];
+	if (t - S.off >= S.n) {
+		h[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+		return;
+	}
+	const float4 a0 = un.vhi[t], b0 = un.vlo[t], a1 = un1.vhi[t], b1 = un1.vlo[t];
+	const double3 u0 = ff3(a0, b0), u1 = ff3(a1, b1);
+	const double m = (double)a0.w;
+	const double c = cK * m / (3.0 * S.L * S.L * S.L);
+	const double vt[3] = {0.5 * (u0.x + u1.x), 0.5 * (u0.y + u1.y), 0.5 * (u0.z + u1.z)};
+	double g[3];
+	for (int k = 0; k < 3; k++) {
+		const double kin = c * vt[k];
+		g[k] = lu[3 * t + k] + dt * lx[3 * t + k] + kin;
+		lu[3 * t + k] = g[k] + kin;
+	}
+	const double w = dt / m;
+	h[t] = make_float4((float)(w * g[0]), (float)(w * g[1]), (float)(w * g[2]), 0.f);
+}
+
+struct AdjPair {
+	const BatchSys *sys;
+	const int *wsys;
+	int nwarps;
+	const int4 *pos;         // x_n (high words)
+	const int *pool;         // stored lists
+	const long *lbase;       // per system: offset of its list at this step (ints)
+	int maxnb;
+	const float4 *h;
+	double *lx;
+	long long *gslots;       // per system: d/deps, d/dsigma (fixed point)
+	float rc2, sig2, eps48, eps4, aw, awh, ushift;
+	float inv_eps, inv_sig, dsh_sig;   // 1/eps, 1/sigma, d ushift / d sigma
+	float cK;
+};
+
+__global__ void __launch_bounds__(256) ka_pair(AdjPair a)
+{
+	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	const long wg = i >> 5;
+	if (wg >= a.nwarps) return;                   // whole warps
+	const int sidx = a.wsys[wg];
+	const BatchSys S = a.sys[sidx];
+	const bool act = i - S.off < S.n;
+	float lxx = 0.f, lxy = 0.f, lxz = 0.f, ge = 0.f, gs = 0.f;
+	if (act) {
+		const float fs = S.fs;
+		const float inv3V = (float)(1.0 / (3.0 * S.L * S.L * S.L));
+		const int *lp = a.pool + a.lbase[sidx];
+		const long li = i - S.off;                // index inside the system's list segment
+		const int cnt = lp[(long)S.npad * a.maxnb + li];
+		const int4 pi = a.pos[i];
+		const float4 hi = a.h[i];
+		for (int k = 0; k < cnt; k++) {
+			const int j = lp[nl_index(li, k, a.maxnb)];
+			const int4 pj = a.pos[j];
+			const float dx = sep_hi(pi.x, pj.x, fs), dy = sep_hi(pi.y, pj.y, fs), dz = sep_hi(pi.z, pj.z, fs);
+			const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+			if (s >= a.rc2) continue;
+			const float is = 1.0f / s;
+			const float q = a.sig2 * is;
+			const float s6 = q * q * q;
+			const float phi = a.eps48 * q * s6 * (s6 - a.awh);
+			const float phis = -a.eps48 * q * s6 * (7.f * s6 - 4.f * a.awh) * is;
+			const float us = -0.25f * a.eps48 * s6 * (2.f * s6 - a.aw) * is;
+			const float ws = -3.f * a.eps48 * q * s6 * (2.f * s6 - a.awh);
+			const float u = a.eps4 * s6 * (s6 - a.aw) + a.ushift;
+			const float4 hj = a.h[j];
+			const float dhx = hi.x - hj.x, dhy = hi.y - hj.y, dhz = hi.z - hj.z;
+			const float ddh = dx * dhx + dy * dhy + dz * dhz;
+			const float c2 = 2.f * phis * ddh + 2.f * a.cK * (us + ws * inv3V);
+			lxx += phi * dhx + c2 * dx;
+			lxy += phi * dhy + c2 * dy;
+			lxz += phi * dhz + c2 * dz;
+			const float dhi = dx * hi.x + dy * hi.y + dz * hi.z;
+			const float phie = phi * a.inv_eps, ue = u * a.inv_eps;
+			const float phisg = 2.f * a.eps48 * q * s6 * (7.f * s6 - 4.f * a.awh) * a.inv_sig;
+			const float usg = 0.5f * a.eps48 * a.inv_sig * s6 * (2.f * s6 - a.aw) + a.dsh_sig;
+			ge += phie * dhi + 0.5f * a.cK * (ue + phie * s * inv3V);
+			gs += phisg * dhi + 0.5f * a.cK * (usg + phisg * s * inv3V);
+		}
+		a.lx[3 * i] += (double)lxx;
+		a.lx[3 * i + 1] += (double)lxy;
+		a.lx[3 * i + 2] += (double)lxz;
+	}
+	float v[2] = {ge, gs};
+	warp_sum<2>(v);
+	if ((threadIdx.x & 31) == 0) {
+		long long *g = a.gslots + 2 * (long)sidx;
+		for (int k = 0; k < 2; k++) {
+			const long long q = __float2ll_rn(v[k] * FX_SCALE);
+			if (q != 0) atomicAdd((unsigned long long *)&g[k], (unsigned long long)q);
+		}
+	}
+}
+
+// ---- host side ------------------------------------------------------------------
+
+struct Ckpt {
+	char *dev;                       // pos | xlo | vhi | vlo | xn | cross | cbase | ncnt | nl
+	std::vector<BatchState> bs;
+	std::vector<unsigned> flag;
+	unsigned last_any;
+	int cur;
+};
+
+struct sepadj {
+	sepb *b;
+	int C;
+	long K;
+	double eps, sigma, aw, cf;
+	std::vector<Ckpt> ck;
+	size_t ck_bytes;
+	char *seg;                       // (C + 1) stored steps
+	size_t seg_step_bytes;
+	int *pool;
+	long pool_cap, pool_used;
+	std::vector<long> lbase;         // (C + 1) x nsys
+	long *d_lbase;
+	double *lx, *lu;
+	float4 *h;
+	long long *gslots;
+	unsigned *h_flag;                // pinned
+	std::vector<double> loss;
+	int have_forward;
+};
+
+static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static void ck_layout(sepadj *A, size_t off[10])
+{
+	const long n = A->b->ntot;
+	const int maxnb = A->b->d->maxnb;
+	const size_t sz[9] = {16 * (size_t)n, 16 * (size_t)n, 16 * (size_t)n, 16 * (size_t)n,
+			      16 * (size_t)n, 16 * (size_t)n, 16 * (size_t)n, 4 * (size_t)n,
+			      4 * (size_t)n * maxnb};
+	off[0] = 0;
+	for (int k = 0; k < 9; k++) off[k + 1] = off[k] + al256(sz[k]);
+}
+
+static AdjState seg_state(sepadj *A, int k)
+{
+	const long n = A->b->ntot;
+	char *p = A->seg + (size_t)k * A->seg_step_bytes;
+	AdjState s;
+	s.pos = (int4 *)p;
+	s.xlo = (uint4 *)(p + al256(16 * (size_t)n));
+	s.vhi = (float4 *)(p + 2 * al256(16 * (size_t)n));
+	s.vlo = (float4 *)(p + 3 * al256(16 * (size_t)n));
+	return s;
+}
+
+extern "C" void sepadj_destroy(sepadj *A)
+{
+	if (!A) return;
+	if (A->b && A->b->d) cudaStreamSynchronize(A->b->d->st);
+	for (auto &c : A->ck)
+		if (c.dev) cudaFree(c.dev);
+	void *dv[] = {A->seg, A->pool, A->d_lbase, A->lx, A->lu, A->h, A->gslots};
+	for (size_t k = 0; k < sizeof dv / sizeof dv[0]; k++)
+		if (dv[k]) cudaFree(dv[k]);
+	if (A->h_flag) cudaFreeHost(A->h_flag);
+	if (A->b) sepb_destroy(A->b);
+	delete A;
+}
+
+extern "C" sepadj *sepadj_create(int nrep, const int *npart, const double *L, double rc, double skin,
+				 double dt, const double *ljparam, int ckpt_every)
+{
+	if (!ljparam || ckpt_every < 1) {
+		batch_fail("sepadj_create: ljparam and ckpt_every >= 1 are required", SEPDEV_EINVAL);
+		return NULL;
+	}
+	sepb *b = sepb_create(nrep, npart, L, rc, skin, dt, ljparam);
+	if (!b) return NULL;
+	sepadj *A = new sepadj();
+	A->b = b;
+	A->C = ckpt_every;
+	A->cf = ljparam[0]; A->eps = ljparam[1]; A->sigma = ljparam[2]; A->aw = ljparam[3];
+	const long n = b->ntot;
+	cudaError_t e = cudaMalloc((void **)&A->lx, sizeof(double) * 3 * n);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&A->lu, sizeof(double) * 3 * n);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&A->h, sizeof(float4) * n);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&A->gslots, sizeof(long long) * 2 * nrep);
+	if (e == cudaSuccess) e = cudaMallocHost((void **)&A->h_flag, sizeof(unsigned) * nrep);
+	if (e != cudaSuccess) {
+		sepdev_set_error("sepadj_create", e);
+		sepadj_destroy(A);
+		return NULL;
+	}
+	A->loss.assign(nrep, 0.0);
+	return A;
+}
+
+extern "C" int sepadj_set_state(sepadj *A, int r, const double *x, const double *v, const double *m)
+{
+	if (!A) return batch_fail("sepadj_set_state: no adjoint", SEPDEV_EINVAL);
+	A->have_forward = 0;
+	for (auto &c : A->ck) { if (c.dev) cudaFree(c.dev); c.dev = NULL; }
+	A->ck.clear();
+	return sepb_set_state(A->b, r, x, v, m);
+}
+
+// sort-free list rebuild of the flagged systems from buffer `parity`
+static int adj_rebuild(sepadj *A, int parity)
+{
+	sepb *b = A->b;
+	sepdev *d = b->d;
+	int rc = batch_cells_launch(b, parity);
+	if (rc) return rc;
+	CK(cudaMemsetAsync(d->flags, 0, sizeof(unsigned) * 2, d->st));
+	const float rl = (float)(b->rc + b->skin);
+	ka_build<<<grid_for(b->ntot, 256), 256, 0, d->st>>>(b->sys, b->wsys, b->nwarps, b->flag, d->pos[parity],
+							   b->cellstart, d->perm, d->nl, d->ncnt, d->maxnb,
+							   rl * rl, d->flags);
+	ka_xn<<<grid_for(b->ntot, 256), 256, 0, d->st>>>(b->wsys, b->nwarps, b->flag, d->pos[parity], d->xn,
+							d->cross, d->cbase);
+	CKL(d);
+	return SEPDEV_OK;
+}
+
+static int ck_save(sepadj *A, Ckpt &c)
+{
+	sepb *b = A->b;
+	sepdev *d = b->d;
+	const long n = b->ntot;
+	size_t off[10];
+	ck_layout(A, off);
+	if (!c.dev) CK(cudaMalloc((void **)&c.dev, off[9]));
+	char *p = c.dev;
+	CK(cudaMemcpyAsync(p + off[0], d->pos[d->cur], 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(p + off[1], d->xlo, 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(p + off[2], d->vhi, 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(p + off[3], d->vlo, 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(p + off[4], d->xn, 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(p + off[5], d->cross, 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(p + off[6], d->cbase, 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(p + off[7], d->ncnt, 4 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(p + off[8], d->nl, 4 * (size_t)n * d->maxnb, cudaMemcpyDeviceToDevice, d->st));
+	c.bs.resize(b->nsys);
+	c.flag.resize(b->nsys);
+	CK(cudaMemcpyAsync(c.bs.data(), b->bs, sizeof(BatchState) * b->nsys, cudaMemcpyDeviceToHost, d->st));
+	CK(cudaMemcpyAsync(c.flag.data(), b->flag, sizeof(unsigned) * b->nsys, cudaMemcpyDeviceToHost, d->st));
+	CK(cudaStreamSynchronize(d->st));
+	c.last_any = b->h_run->last_any;
+	c.cur = d->cur;
+	return SEPDEV_OK;
+}
+
+static int ck_restore(sepadj *A, const Ckpt &c)
+{
+	sepb *b = A->b;
+	sepdev *d = b->d;
+	const long n = b->ntot;
+	size_t off[10];
+	ck_layout(A, off);
+	d->cur = c.cur;
+	const char *p = c.dev;
+	CK(cudaMemcpyAsync(d->pos[d->cur], p + off[0], 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(d->xlo, p + off[1], 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(d->vhi, p + off[2], 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(d->vlo, p + off[3], 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(d->xn, p + off[4], 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(d->cross, p + off[5], 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(d->cbase, p + off[6], 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(d->ncnt, p + off[7], 4 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(d->nl, p + off[8], 4 * (size_t)n * d->maxnb, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(b->bs, c.bs.data(), sizeof(BatchState) * b->nsys, cudaMemcpyHostToDevice, d->st));
+	CK(cudaMemcpyAsync(b->flag, c.flag.data(), sizeof(unsigned) * b->nsys, cudaMemcpyHostToDevice, d->st));
+	b->h_run->last_any = c.last_any;
+	CK(cudaStreamSynchronize(d->st));
+	return SEPDEV_OK;
+}
+
+// one NVE step of every replica from the host (fused step, decision); the
+// caller rebuilds first when the last decision asked for it.  Leaves the
+// flags of the new decision in h_flag.
+static int adj_step(sepadj *A, double loss_scale)
+{
+	sepb *b = A->b;
+	sepdev *d = b->d;
+	BatchRun *h = b->h_run;
+	int rc;
+	BatchDecide dec = batch_decide_args(b);
+	dec.loss_scale = loss_scale;
+	const long done0 = h->done;
+	if ((rc = batch_step_launch(b, d->cur, dec))) return rc;
+	CK(cudaMemcpyAsync(h, b->run, sizeof *h, cudaMemcpyDeviceToHost, d->st));
+	CK(cudaMemcpyAsync(A->h_flag, b->flag, sizeof(unsigned) * b->nsys, cudaMemcpyDeviceToHost, d->st));
+	CK(cudaStreamSynchronize(d->st));
+	if ((h->done - done0) & 1) d->cur ^= 1;
+	if (h->abort) return batch_fail("sepadj: neighbour list overflow", SEPDEV_EOVERFLOW);
+	return SEPDEV_OK;
+}
+
+static int run_reset(sepadj *A)
+{
+	sepb *b = A->b;
+	sepdev *d = b->d;
+	BatchRun &r = *b->h_run;
+	const unsigned la = r.last_any;
+	memset(&r, 0, sizeof r);
+	r.total = 0;                     // every step reports its observables
+	r.last_any = la;
+	CK(cudaMemcpyAsync(b->run, &r, sizeof r, cudaMemcpyHostToDevice, d->st));
+	CK(cudaMemsetAsync(b->slots, 0, sizeof(long long) * SLOT_FIELDS * b->nsys, d->st));
+	CK(cudaMemsetAsync(d->flags, 0, sizeof(unsigned) * 2, d->st));
+	return SEPDEV_OK;
+}
+
+extern "C" int sepadj_forward(sepadj *A, long nsteps, double *loss)
+{
+	if (!A || nsteps < 1) return batch_fail("sepadj_forward: invalid arguments", SEPDEV_EINVAL);
+	sepb *b = A->b;
+	int rc;
+	for (int s = 0; s < b->nsys; s++)
+		if (!b->have[s]) return batch_fail("sepadj_forward: a replica has no state", SEPDEV_EINVAL);
+	const long nseg = (nsteps + A->C - 1) / A->C;
+	if (A->ck.empty()) {
+		// the initial lists (sorted once) and the initial state
+		if ((rc = batch_initial_lists(b))) return rc;
+		b->h_run->last_any = 0;
+		CK(cudaMemcpy(b->bs, b->h_bs, sizeof(BatchState) * b->nsys, cudaMemcpyHostToDevice));
+		A->ck.resize(1);
+		if ((rc = ck_save(A, A->ck[0]))) return rc;
+	} else if ((rc = ck_restore(A, A->ck[0]))) {
+		return rc;
+	}
+	if ((long)A->ck.size() < nseg) A->ck.resize(nseg);
+	// loss accumulators start at zero
+	std::vector<BatchState> bs(b->nsys);
+	CK(cudaMemcpy(bs.data(), b->bs, sizeof(BatchState) * b->nsys, cudaMemcpyDeviceToHost));
+	for (auto &x : bs) x.loss = 0.0;
+	CK(cudaMemcpy(b->bs, bs.data(), sizeof(BatchState) * b->nsys, cudaMemcpyHostToDevice));
+	if ((rc = run_reset(A))) return rc;
+	const double cK = 1.0 / (double)nsteps;
+	for (long n = 0; n < nsteps; n++) {
+		if (n % A->C == 0 && n > 0 && (rc = ck_save(A, A->ck[n / A->C]))) return rc;
+		if (b->h_run->last_any && (rc = adj_rebuild(A, b->d->cur))) return rc;
+		if ((rc = adj_step(A, cK))) return rc;
+	}
+	CK(cudaMemcpy(bs.data(), b->bs, sizeof(BatchState) * b->nsys, cudaMemcpyDeviceToHost));
+	for (int s = 0; s < b->nsys; s++) {
+		A->loss[s] = bs[s].loss;
+		if (loss) loss[s] = bs[s].loss;
+	}
+	A->K = nsteps;
+	A->have_forward = 1;
+	return SEPDEV_OK;
+}
+
+static int seg_alloc(sepadj *A)
+{
+	sepb *b = A->b;
+	const long n = b->ntot;
+	const int maxnb = b->d->maxnb;
+	A->seg_step_bytes = 4 * al256(16 * (size_t)n);
+	if (!A->seg) CK(cudaMalloc((void **)&A->seg, A->seg_step_bytes * (A->C + 1)));
+	// every system may be rebuilt at every step of a segment
+	const long per_step = (long)n * maxnb + n;
+	if (!A->pool) {
+		A->pool_cap = per_step * (A->C + 2);
+		CK(cudaMalloc((void **)&A->pool, sizeof(int) * A->pool_cap));
+	}
+	if (!A->d_lbase) CK(cudaMalloc((void **)&A->d_lbase, sizeof(long) * b->nsys * (A->C + 1)));
+	A->lbase.assign((size_t)b->nsys * (A->C + 1), 0);
+	return SEPDEV_OK;
+}
+
+// copy system s's current list (and counts) into the pool; returns its offset
+static int snap(sepadj *A, int s, long *where)
+{
+	sepb *b = A->b;
+	sepdev *d = b->d;
+	const BatchSys &S = b->hsys[s];
+	const long len = (long)S.npad * d->maxnb;
+	if (A->pool_used + len + S.npad > A->pool_cap) return batch_fail("sepadj: list pool full", SEPDEV_ENOMEM);
+	*where = A->pool_used;
+	CK(cudaMemcpyAsync(A->pool + A->pool_used, d->nl + (long)S.off * d->maxnb, sizeof(int) * len,
+			   cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(A->pool + A->pool_used + len, d->ncnt + S.off, sizeof(int) * S.npad,
+			   cudaMemcpyDeviceToDevice, d->st));
+	A->pool_used += len + S.npad;
+	return SEPDEV_OK;
+}
+
+static int seg_store(sepadj *A, int k)
+{
+	sepdev *d = A->b->d;
+	const long n = A->b->ntot;
+	AdjState s = seg_state(A, k);
+	CK(cudaMemcpyAsync(s.pos, d->pos[d->cur], 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(s.xlo, d->xlo, 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(s.vhi, d->vhi, 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	CK(cudaMemcpyAsync(s.vlo, d->vlo, 16 * (size_t)n, cudaMemcpyDeviceToDevice, d->st));
+	return SEPDEV_OK;
+}
+
+extern "C" int sepadj_backward(sepadj *A, double *dloss_deps, double *dloss_dsigma, double *dloss_dx0)
+{
+	if (!A || !A->have_forward) return batch_fail("sepadj_backward: no forward pass", SEPDEV_EINVAL);
+	sepb *b = A->b;
+	sepdev *d = b->d;
+	const long n = b->ntot;
+	const int nsys = b->nsys;
+	int rc;
+	if ((rc = seg_alloc(A))) return rc;
+	CK(cudaMemsetAsync(A->lx, 0, sizeof(double) * 3 * n, d->st));
+	CK(cudaMemsetAsync(A->lu, 0, sizeof(double) * 3 * n, d->st));
+	CK(cudaMemsetAsync(A->gslots, 0, sizeof(long long) * 2 * nsys, d->st));
+	const double cK = 1.0 / (double)A->K;
+	AdjPair P;
+	memset(&P, 0, sizeof P);
+	P.sys = b->sys; P.wsys = b->wsys; P.nwarps = b->nwarps; P.pool = A->pool;
+	P.maxnb = d->maxnb; P.h = A->h; P.lx = A->lx; P.gslots = A->gslots;
+	P.rc2 = (float)(A->cf * A->cf);
+	P.sig2 = (float)(A->sigma * A->sigma);
+	P.eps48 = (float)(48.0 * A->eps);
+	P.eps4 = (float)(4.0 * A->eps);
+	P.aw = (float)A->aw;
+	P.awh = (float)(0.5 * A->aw);
+	P.ushift = (float)b->ushift;
+	P.inv_eps = (float)(1.0 / A->eps);
+	P.inv_sig = (float)(1.0 / A->sigma);
+	const double sr = A->sigma / A->cf, sr6 = pow(sr, 6.0);
+	P.dsh_sig = (float)(-24.0 * A->eps / A->sigma * (2.0 * sr6 * sr6 - A->aw * sr6));
+	P.cK = (float)cK;
+	const long nseg = (A->K + A->C - 1) / A->C;
+	for (long sg = nseg - 1; sg >= 0; sg--) {
+		const long c0 = sg * A->C, c1 = c0 + A->C < A->K ? c0 + A->C : A->K;
+		const int m = (int)(c1 - c0);
+		// recompute the segment from its checkpoint, keeping states and lists
+		if ((rc = ck_restore(A, A->ck[sg]))) return rc;
+		if ((rc = run_reset(A))) return rc;
+		A->pool_used = 0;
+		for (int s = 0; s < nsys; s++)
+			if ((rc = snap(A, s, &A->lbase[s]))) return rc;
+		memcpy(A->h_flag, A->ck[sg].flag.data(), sizeof(unsigned) * nsys);
+		for (int k = 0; k < m; k++) {
+			if ((rc = seg_store(A, k))) return rc;
+			long *lb = &A->lbase[(size_t)k * nsys];
+			if (k > 0) memcpy(lb, lb - nsys, sizeof(long) * nsys);
+			const bool rebuild = b->h_run->last_any != 0;
+			std::vector<unsigned> fl(A->h_flag, A->h_flag + nsys);
+			if (rebuild && (rc = adj_rebuild(A, d->cur))) return rc;
+			if (rebuild)
+				for (int s = 0; s < nsys; s++)
+					if (fl[s] && (rc = snap(A, s, &lb[s]))) return rc;
+			if ((rc = adj_step(A, 0.0))) return rc;
+		}
+		if ((rc = seg_store(A, m))) return rc;
+		CK(cudaMemcpyAsync(A->d_lbase, A->lbase.data(), sizeof(long) * nsys * m, cudaMemcpyHostToDevice,
+				   d->st));
+		// the backward sweep of the segment
+		for (int k = m - 1; k >= 0; k--) {
+			ka_h<<<grid_for(n, 256), 256, 0, d->st>>>(b->sys, b->wsys, b->nwarps, seg_state(A, k),
+								 seg_state(A, k + 1), A->lx, A->lu, A->h, b->dt, cK);
+			P.pos = seg_state(A, k).pos;
+			P.lbase = A->d_lbase + (size_t)k * nsys;
+			ka_pair<<<grid_for(n, 256), 256, 0, d->st>>>(P);
+			CKL(d);
+		}
+	}
+	// gradients out
+	std::vector<long long> g(2 * nsys);
+	CK(cudaMemcpyAsync(g.data(), A->gslots, sizeof(long long) * 2 * nsys, cudaMemcpyDeviceToHost, d->st));
+	std::vector<double> lx;
+	std::vector<int> gid;
+	if (dloss_dx0) {
+		lx.resize(3 * n);
+		gid.resize(n);
+		CK(cudaMemcpyAsync(lx.data(), A->lx, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, d->st));
+		CK(cudaMemcpyAsync(gid.data(), d->gid, sizeof(int) * n, cudaMemcpyDeviceToHost, d->st));
+	}
+	CK(cudaStreamSynchronize(d->st));
+	long out = 0;
+	for (int s = 0; s < nsys; s++) {
+		if (dloss_deps) dloss_deps[s] = (double)g[2 * s] * FX_ISCALE;
+		if (dloss_dsigma) dloss_dsigma[s] = (double)g[2 * s + 1] * FX_ISCALE;
+		if (dloss_dx0) {
+			const BatchSys &S = b->hsys[s];
+			for (int t = 0; t < S.n; t++) {
+				const int u = gid[S.off + t];
+				if (u < 0 || u >= S.n) return batch_fail("sepadj_backward: slot map corrupt", SEPDEV_EINVAL);
+				for (int k = 0; k < 3; k++) dloss_dx0[3 * (out + u) + k] = lx[3 * (size_t)(S.off + t) + k];
+			}
+			out += S.n;
+		}
+	}
+	return SEPDEV_OK;
+}

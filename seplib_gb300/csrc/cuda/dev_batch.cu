@@ -211,7 +211,18 @@ __global__ void kb_decide(BatchDecide a)
 		slot[lane] = 0;
 		const double sumv2 = __shfl_sync(FULL, val, SLOT_SUMV2);
 		const double maxd2 = __shfl_sync(FULL, val, SLOT_MAXD2);
+		// loss term of this step: epot + p, p = tr(kin_P + pot_P) / 3V
+		const double ep = __shfl_sync(FULL, val, SLOT_EPOT0);
+		double tr = 0.0;
+		for (int k = 0; k < 3; k++) {
+			const int dk = k == 0 ? 0 : (k == 1 ? 3 : 5);
+			tr += __shfl_sync(FULL, val, SLOT_KINP + dk) + __shfl_sync(FULL, val, SLOT_POTP + dk);
+		}
 		if (lane == 0) {
+			if (a.loss_scale != 0.0) {
+				const double V = a.sys[s].L * a.sys[s].L * a.sys[s].L;
+				st->loss += a.loss_scale * (ep + tr / (3.0 * V));
+			}
 			st->sumv2 = sumv2;
 			st->alpha_last = st->alpha;
 			if (a.nh) {
@@ -261,42 +272,8 @@ __global__ void kb_flush(uint4 *buf, long n16, unsigned tag)
 
 // ---- host side ---------------------------------------------------------------
 
-struct sepb {
-	sepdev *d;                 // the shared per-slot arrays, list, stream
-	int nsys;
-	long ntot;                 // slots (sum of npad)
-	int nwarps;
-	long ncells;               // cell entries (sum of ncell + 2)
-	double rc, skin, dt, tau;
-	int nh;
-	double cf, eps, sigma, aw, ushift;
-	std::vector<BatchSys> hsys;
-	BatchSys *sys;             // device
-	int *wsys, *csys;
-	unsigned *flag;
-	int *cellcount, *cellstart;
-	long long *slots;
-	BatchState *bs;            // device
-	BatchRun *run;
-	BatchState *h_bs;          // pinned
-	BatchRun *h_run;
-	int state_set;             // systems whose state has been set
-	std::vector<char> have;
-	std::vector<unsigned> nupd;    // list updates since set-up (the reference's nupdate_neighb)
-	std::vector<double> alpha0;    // initial thermostat states
-	int list_ok;
-	// graph of the loop
-	cudaGraph_t graph;
-	cudaGraphExec_t exec;
-	int graph_parity;
-	const int *graph_nl;       // list the graph was captured with
-	int graph_maxnb;
-	// timing
-	void *flush_buf;
-	size_t flush_bytes;
-};
 
-static void fixed_from_double(double x, double L, unsigned *hi, unsigned *lo)
+void batch_to_fixed(double x, double L, unsigned *hi, unsigned *lo)
 {
 	double fr = x / L;
 	fr -= floor(fr);
@@ -308,12 +285,12 @@ static void fixed_from_double(double x, double L, unsigned *hi, unsigned *lo)
 	*lo = (unsigned)floor(r);
 }
 
-static double double_from_fixed(unsigned hi, unsigned lo, double L)
+double batch_from_fixed(unsigned hi, unsigned lo, double L)
 {
 	return (ldexp((double)hi, -32) + ldexp((double)lo, -64)) * L;
 }
 
-static int fail(const char *what, int rc)
+int batch_fail(const char *what, int rc)
 {
 	sepdev_set_error(what, cudaErrorInvalidValue);
 	return rc;
@@ -342,7 +319,7 @@ extern "C" sepb *sepb_create(int nsys, const int *npart, const double *L, double
 			     double dt, const double *ljparam)
 {
 	if (nsys <= 0 || !npart || !L || !(rc > 0) || !(skin >= 0) || !(dt > 0)) {
-		fail("sepb_create: invalid arguments", SEPDEV_EINVAL);
+		batch_fail("sepb_create: invalid arguments", SEPDEV_EINVAL);
 		return NULL;
 	}
 	sepb *b = new sepb();          // value-initialised: pointers and counters start at zero
@@ -350,7 +327,7 @@ extern "C" sepb *sepb_create(int nsys, const int *npart, const double *L, double
 	b->rc = rc; b->skin = skin; b->dt = dt;
 	b->tau = 10.0;
 	if (ljparam) {
-		if (ljparam[0] > rc) { fail("sepb_create: LJ cut-off larger than rc", SEPDEV_EINVAL); delete b; return NULL; }
+		if (ljparam[0] > rc) { batch_fail("sepb_create: LJ cut-off larger than rc", SEPDEV_EINVAL); delete b; return NULL; }
 		b->cf = ljparam[0]; b->eps = ljparam[1]; b->sigma = ljparam[2]; b->aw = ljparam[3];
 		b->ushift = -4.0 * b->eps * (pow(b->sigma / b->cf, 12.) - b->aw * pow(b->sigma / b->cf, 6.));
 	} else {
@@ -366,7 +343,7 @@ extern "C" sepb *sepb_create(int nsys, const int *npart, const double *L, double
 	std::vector<int> hw, hc;
 	for (int s = 0; s < nsys; s++) {
 		BatchSys &S = b->hsys[s];
-		if (npart[s] <= 0 || !(L[s] > 0)) { fail("sepb_create: empty system or box", SEPDEV_EINVAL); delete b; return NULL; }
+		if (npart[s] <= 0 || !(L[s] > 0)) { batch_fail("sepb_create: empty system or box", SEPDEV_EINVAL); delete b; return NULL; }
 		S.n = npart[s];
 		S.npad = (S.n + 31) & ~31;
 		S.off = (int)off;
@@ -393,7 +370,7 @@ extern "C" sepb *sepb_create(int nsys, const int *npart, const double *L, double
 		hc.push_back(-1);                       // the end entry
 		off += S.npad;
 		coff += S.ncell + 2;
-		if (off > (1L << 30)) { fail("sepb_create: too many particles", SEPDEV_EINVAL); delete b; return NULL; }
+		if (off > (1L << 30)) { batch_fail("sepb_create: too many particles", SEPDEV_EINVAL); delete b; return NULL; }
 	}
 	b->ntot = off;
 	b->nwarps = (int)(off / 32);
@@ -435,7 +412,7 @@ extern "C" sepb *sepb_create(int nsys, const int *npart, const double *L, double
 
 extern "C" int sepb_set_state(sepb *b, int s, const double *x, const double *v, const double *m)
 {
-	if (!b || s < 0 || s >= b->nsys || !x || !v) return fail("sepb_set_state: invalid arguments", SEPDEV_EINVAL);
+	if (!b || s < 0 || s >= b->nsys || !x || !v) return batch_fail("sepb_set_state: invalid arguments", SEPDEV_EINVAL);
 	const BatchSys &S = b->hsys[s];
 	sepdev *d = b->d;
 	const int n = S.n, np = S.npad;
@@ -448,7 +425,7 @@ extern "C" int sepb_set_state(sepb *b, int s, const double *x, const double *v, 
 	for (int i = 0; i < np; i++) {
 		if (i < n) {
 			unsigned h[3], l[3];
-			for (int k = 0; k < 3; k++) fixed_from_double(x[3 * i + k], S.L, &h[k], &l[k]);
+			for (int k = 0; k < 3; k++) batch_to_fixed(x[3 * i + k], S.L, &h[k], &l[k]);
 			hp[i] = make_int4((int)h[0], (int)h[1], (int)h[2], 0);
 			hl[i] = make_uint4(l[0], l[1], l[2], 0u);
 			float vh[3], vl[3];
@@ -492,9 +469,9 @@ extern "C" int sepb_set_state(sepb *b, int s, const double *x, const double *v, 
 
 extern "C" int sepb_set_thermostat(sepb *b, const double *T0, double tau, const double *alpha)
 {
-	if (!b) return fail("sepb_set_thermostat: no batch", SEPDEV_EINVAL);
+	if (!b) return batch_fail("sepb_set_thermostat: no batch", SEPDEV_EINVAL);
 	if (!T0) { b->nh = 0; return SEPDEV_OK; }
-	if (!(tau > 0)) return fail("sepb_set_thermostat: tau must be positive", SEPDEV_EINVAL);
+	if (!(tau > 0)) return batch_fail("sepb_set_thermostat: tau must be positive", SEPDEV_EINVAL);
 	b->nh = 1;
 	b->tau = tau;
 	for (int s = 0; s < b->nsys; s++) {
@@ -506,7 +483,7 @@ extern "C" int sepb_set_thermostat(sepb *b, const double *T0, double tau, const 
 	return SEPDEV_OK;
 }
 
-static PairArgs pair_args(sepb *b, int parity)
+PairArgs batch_pair_args(sepb *b, int parity)
 {
 	sepdev_pairset ps;
 	memset(&ps, 0, sizeof ps);
@@ -526,7 +503,7 @@ static PairArgs pair_args(sepb *b, int parity)
 	return a;
 }
 
-static BatchDecide decide_args(sepb *b)
+BatchDecide batch_decide_args(sepb *b)
 {
 	BatchDecide a;
 	memset(&a, 0, sizeof a);
@@ -562,7 +539,26 @@ static BGather gather_args(sepb *b, int parity)
 }
 
 // sort + list build of the flagged systems from buffer `parity`; capturable
-static int rebuild_launch(sepb *b, int parity)
+// cell lists of the flagged systems without moving particles: bin, scan,
+// scatter of slot indices, deterministic order inside cells; capturable
+int batch_cells_launch(sepb *b, int parity)
+{
+	sepdev *d = b->d;
+	const int B = 256;
+	const long nt = b->ntot;
+	CK(cudaMemsetAsync(b->cellcount, 0, sizeof(int) * b->ncells, d->st));
+	kb_bin<<<grid_for(nt, B), B, 0, d->st>>>(b->sys, b->wsys, b->nwarps, b->flag, d->pos[parity],
+						d->cellof, d->celloff, b->cellcount);
+	kb_scan<<<b->nsys, 256, 0, d->st>>>(b->sys, b->flag, b->cellcount, b->cellstart);
+	kb_scatter<<<grid_for(nt, B), B, 0, d->st>>>(b->wsys, b->nwarps, b->flag, d->cellof, d->celloff,
+						    b->cellstart, d->perm);
+	kb_cellsort<<<grid_for(b->ncells * 32, B), B, 0, d->st>>>(b->ncells, b->csys, b->flag, b->cellstart,
+								 d->gid, d->perm);
+	CKL(d);
+	return SEPDEV_OK;
+}
+
+int batch_rebuild_launch(sepb *b, int parity)
 {
 	sepdev *d = b->d;
 	const int B = 256;
@@ -584,9 +580,9 @@ static int rebuild_launch(sepb *b, int parity)
 				  (float)((b->rc + b->skin) * (b->rc + b->skin)));
 }
 
-static int step_launch(sepb *b, int parity, const BatchDecide &dec)
+int batch_step_launch(sepb *b, int parity, const BatchDecide &dec)
 {
-	PairArgs a = pair_args(b, parity);
+	PairArgs a = batch_pair_args(b, parity);
 	CK(cudaGetLastError());
 	int rc = sepdev_batch_step(b->d, a, b->sys, b->wsys, b->nwarps, b->bs, b->run, b->slots, dec);
 	if (rc) return rc;
@@ -634,19 +630,19 @@ static int build_graph(sepb *b, int parity)
 		CK(cudaGraphAddNode(&nif, body, k ? &tail : NULL, NULL, k ? 1 : 0, &ip));
 		CK(cudaStreamBeginCaptureToGraph(d->st, ip.conditional.phGraph_out[0], NULL, NULL, 0,
 						 cudaStreamCaptureModeRelaxed));
-		int rc = rebuild_launch(b, p);
+		int rc = batch_rebuild_launch(b, p);
 		cudaGraph_t tmp;
 		cudaError_t e = cudaStreamEndCapture(d->st, &tmp);
 		if (rc) return rc;
 		if (e != cudaSuccess) { sepdev_set_error("capture(batch rebuild)", e); return SEPDEV_ECUDA; }
-		BatchDecide dec = decide_args(b);
+		BatchDecide dec = batch_decide_args(b);
 		dec.use_handles = 1;
 		dec.h_next = hif[(k + 1) % RUN_UNROLL_B];
 		dec.h_while = hw;
 		dec.reset_while = (k == 0);
 		dec.pair_end = (k == RUN_UNROLL_B - 1);
 		CK(cudaStreamBeginCaptureToGraph(d->st, body, &nif, NULL, 1, cudaStreamCaptureModeRelaxed));
-		rc = step_launch(b, p, dec);
+		rc = batch_step_launch(b, p, dec);
 		if (!rc) rc = capture_tail(d, &tail);
 		e = cudaStreamEndCapture(d->st, &tmp);
 		if (rc) return rc;
@@ -690,12 +686,12 @@ static int run_begin(sepb *b, long nsteps)
 	return SEPDEV_OK;
 }
 
-static int initial_lists(sepb *b)
+int batch_initial_lists(sepb *b)
 {
 	sepdev *d = b->d;
 	std::vector<unsigned> ones(b->nsys, 1u);
 	CK(cudaMemcpyAsync(b->flag, ones.data(), sizeof(unsigned) * b->nsys, cudaMemcpyHostToDevice, d->st));
-	int rc = rebuild_launch(b, d->cur);
+	int rc = batch_rebuild_launch(b, d->cur);
 	if (rc) return rc;
 	unsigned fl[2];
 	CK(cudaMemcpyAsync(fl, d->flags, sizeof fl, cudaMemcpyDeviceToHost, d->st));
@@ -705,11 +701,11 @@ static int initial_lists(sepb *b)
 		// the first lists set the capacity: grow once to their largest count
 		if ((rc = sepdev_grow_list_to(d, (int)(fl[1] + fl[1] / 2 + 32)))) return rc;
 		CK(cudaMemcpyAsync(b->flag, ones.data(), sizeof(unsigned) * b->nsys, cudaMemcpyHostToDevice, d->st));
-		if ((rc = rebuild_launch(b, d->cur))) return rc;
+		if ((rc = batch_rebuild_launch(b, d->cur))) return rc;
 		CK(cudaMemcpyAsync(fl, d->flags, sizeof fl, cudaMemcpyDeviceToHost, d->st));
 		CK(cudaMemsetAsync(b->flag, 0, sizeof(unsigned) * b->nsys, d->st));
 		CK(cudaStreamSynchronize(d->st));
-		if (fl[0] & 1u) return fail("sepb: neighbour list overflow at set-up", SEPDEV_EOVERFLOW);
+		if (fl[0] & 1u) return batch_fail("sepb: neighbour list overflow at set-up", SEPDEV_EOVERFLOW);
 	}
 	b->list_ok = 1;
 	b->h_run->last_any = 0;
@@ -718,12 +714,12 @@ static int initial_lists(sepb *b)
 
 static int run_steps(sepb *b, long nsteps, int timed, long flush, double *ms)
 {
-	if (!b || nsteps < 0) return fail("sepb_run: invalid arguments", SEPDEV_EINVAL);
+	if (!b || nsteps < 0) return batch_fail("sepb_run: invalid arguments", SEPDEV_EINVAL);
 	for (int s = 0; s < b->nsys; s++)
-		if (!b->have[s]) return fail("sepb_run: a system has no state (sepb_set_state)", SEPDEV_EINVAL);
+		if (!b->have[s]) return batch_fail("sepb_run: a system has no state (sepb_set_state)", SEPDEV_EINVAL);
 	sepdev *d = b->d;
 	int rc;
-	if (!b->list_ok && (rc = initial_lists(b))) return rc;
+	if (!b->list_ok && (rc = batch_initial_lists(b))) return rc;
 	if (nsteps == 0) return SEPDEV_OK;
 	const unsigned pending = b->h_run->last_any;
 	if ((rc = run_begin(b, nsteps))) return rc;
@@ -748,11 +744,11 @@ static int run_steps(sepb *b, long nsteps, int timed, long flush, double *ms)
 				kb_flush<<<d->nsm * 4, 512, 0, d->st>>>((uint4 *)b->flush_buf, flush / 16, (unsigned)done0);
 			}
 			CK(cudaEventRecord(e0, d->st));
-			if (h->last_any && (rc = rebuild_launch(b, d->cur))) return rc;
-			if ((rc = step_launch(b, d->cur, decide_args(b)))) return rc;
+			if (h->last_any && (rc = batch_rebuild_launch(b, d->cur))) return rc;
+			if ((rc = batch_step_launch(b, d->cur, batch_decide_args(b)))) return rc;
 			CK(cudaEventRecord(e1, d->st));
 		} else if (todo >= RUN_UNROLL_B) {
-			if (h->last_any && (rc = rebuild_launch(b, d->cur))) return rc;
+			if (h->last_any && (rc = batch_rebuild_launch(b, d->cur))) return rc;
 			h->remaining = todo / RUN_UNROLL_B;
 			CK(cudaMemcpyAsync(b->run, h, sizeof *h, cudaMemcpyHostToDevice, d->st));
 			const bool stale = !b->exec || b->graph_parity != d->cur || b->graph_nl != d->nl ||
@@ -760,8 +756,8 @@ static int run_steps(sepb *b, long nsteps, int timed, long flush, double *ms)
 			if (stale && (rc = build_graph(b, d->cur))) return rc;
 			CK(cudaGraphLaunch(b->exec, d->st));
 		} else {
-			if (h->last_any && (rc = rebuild_launch(b, d->cur))) return rc;
-			if ((rc = step_launch(b, d->cur, decide_args(b)))) return rc;
+			if (h->last_any && (rc = batch_rebuild_launch(b, d->cur))) return rc;
+			if ((rc = batch_step_launch(b, d->cur, batch_decide_args(b)))) return rc;
 		}
 		CK(cudaMemcpyAsync(h, b->run, sizeof *h, cudaMemcpyDeviceToHost, d->st));
 		CK(cudaStreamSynchronize(d->st));
@@ -771,7 +767,7 @@ static int run_steps(sepb *b, long nsteps, int timed, long flush, double *ms)
 			total_ms += x;
 		}
 		if ((h->done - done0) & 1) d->cur ^= 1;
-		if (h->abort) return fail("sepb_run: neighbour list overflow", SEPDEV_EOVERFLOW);
+		if (h->abort) return batch_fail("sepb_run: neighbour list overflow", SEPDEV_EOVERFLOW);
 	}
 	CK(cudaMemcpy(b->h_bs, b->bs, sizeof(BatchState) * b->nsys, cudaMemcpyDeviceToHost));
 	for (int s = 0; s < b->nsys; s++) b->nupd[s] += (unsigned)b->h_bs[s].ntrig;
@@ -791,7 +787,7 @@ extern "C" int sepb_run_timed(sepb *b, long nsteps, long flush_bytes, double *ms
 
 extern "C" int sepb_get_state(sepb *b, int s, double *x, double *v, double *f)
 {
-	if (!b || s < 0 || s >= b->nsys) return fail("sepb_get_state: invalid arguments", SEPDEV_EINVAL);
+	if (!b || s < 0 || s >= b->nsys) return batch_fail("sepb_get_state: invalid arguments", SEPDEV_EINVAL);
 	const BatchSys &S = b->hsys[s];
 	sepdev *d = b->d;
 	const int n = S.n;
@@ -811,13 +807,13 @@ extern "C" int sepb_get_state(sepb *b, int s, double *x, double *v, double *f)
 	// slots hold exactly its particles
 	for (int t = 0; t < n; t++) {
 		const int u = hg[t];
-		if (u < 0 || u >= n) return fail("sepb_get_state: slot map corrupt", SEPDEV_EINVAL);
+		if (u < 0 || u >= n) return batch_fail("sepb_get_state: slot map corrupt", SEPDEV_EINVAL);
 		const unsigned hi[3] = {(unsigned)hp[t].x, (unsigned)hp[t].y, (unsigned)hp[t].z};
 		const unsigned lo[3] = {hl[t].x, hl[t].y, hl[t].z};
 		const float vh[3] = {hvh[t].x, hvh[t].y, hvh[t].z}, vl[3] = {hvl[t].x, hvl[t].y, hvl[t].z};
 		const float ff[3] = {hf[t].x, hf[t].y, hf[t].z};
 		for (int k = 0; k < 3; k++) {
-			if (x) x[3 * u + k] = double_from_fixed(hi[k], lo[k], S.L);
+			if (x) x[3 * u + k] = batch_from_fixed(hi[k], lo[k], S.L);
 			if (v) v[3 * u + k] = (double)vh[k] + (double)vl[k];
 			if (f) f[3 * u + k] = (double)ff[k];
 		}
@@ -827,7 +823,7 @@ extern "C" int sepb_get_state(sepb *b, int s, double *x, double *v, double *f)
 
 extern "C" int sepb_get_results(sepb *b, sepb_result *out)
 {
-	if (!b || !out) return fail("sepb_get_results: invalid arguments", SEPDEV_EINVAL);
+	if (!b || !out) return batch_fail("sepb_get_results: invalid arguments", SEPDEV_EINVAL);
 	const int map[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
 	for (int s = 0; s < b->nsys; s++) {
 		const BatchState &st = b->h_bs[s];

@@ -7,6 +7,7 @@
 // padding, and the end of the last range.  Per-warp and per-cell tables give
 // the owning system.
 #pragma once
+#include <vector>
 #include "dev_common.cuh"
 #include "dev_decide.cuh"
 #include "dev_pair.cuh"
@@ -29,6 +30,7 @@ struct BatchState {
 	long long ntrig;       // skin-triggered updates (the reference's nupdate_neighb)
 	int force_trig;        // report an update after the next step
 	int last_trig;
+	double loss;           // sum of loss_scale * (epot + p) over the steps (adjoint runs)
 	double last[SLOT_FIELDS];
 };
 
@@ -55,6 +57,7 @@ struct BatchDecide {
 	double dt_tau2;
 	int nh;
 	int pair_end, use_handles, reset_while;
+	double loss_scale;     // != 0: accumulate the loss term of every step
 	cudaGraphConditionalHandle h_next, h_while;
 };
 
@@ -63,3 +66,49 @@ int sepdev_batch_step(sepdev *d, const PairArgs &a, const BatchSys *sys, const i
 		      const BatchState *bs, const BatchRun *run, long long *slots, const BatchDecide &dec);
 int sepdev_batch_build(sepdev *d, int parity, const int *cellstart, const BatchSys *sys,
 		       const int *wsys, int nwarps, const unsigned *flag, float rl2);
+
+// host-side batch (dev_batch.cu); the adjoint (dev_adj.cu) builds on it
+struct sepb {
+	sepdev *d;                 // the shared per-slot arrays, list, stream
+	int nsys;
+	long ntot;                 // slots (sum of npad)
+	int nwarps;
+	long ncells;               // cell entries (sum of ncell + 2)
+	double rc, skin, dt, tau;
+	int nh;
+	double cf, eps, sigma, aw, ushift;
+	std::vector<BatchSys> hsys;
+	BatchSys *sys;             // device
+	int *wsys, *csys;
+	unsigned *flag;
+	int *cellcount, *cellstart;
+	long long *slots;
+	BatchState *bs;            // device
+	BatchRun *run;
+	BatchState *h_bs;          // pinned
+	BatchRun *h_run;
+	int state_set;             // systems whose state has been set
+	std::vector<char> have;
+	std::vector<unsigned> nupd;    // list updates since set-up (the reference's nupdate_neighb)
+	std::vector<double> alpha0;    // initial thermostat states
+	int list_ok;
+	// graph of the loop
+	cudaGraph_t graph;
+	cudaGraphExec_t exec;
+	int graph_parity;
+	const int *graph_nl;       // list the graph was captured with
+	int graph_maxnb;
+	// timing
+	void *flush_buf;
+	size_t flush_bytes;
+};
+
+PairArgs batch_pair_args(sepb *b, int parity);
+BatchDecide batch_decide_args(sepb *b);
+int batch_cells_launch(sepb *b, int parity);
+int batch_rebuild_launch(sepb *b, int parity);
+int batch_step_launch(sepb *b, int parity, const BatchDecide &dec);
+int batch_initial_lists(sepb *b);
+int batch_fail(const char *what, int rc);
+void batch_to_fixed(double x, double L, unsigned *hi, unsigned *lo);
+double batch_from_fixed(unsigned hi, unsigned lo, double L);
