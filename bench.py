@@ -58,9 +58,10 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=0, help="oracle steps for cpu_baseline (0: auto)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--tpp", type=int, default=0)
-    ap.add_argument("--workload", default="plain", choices=["plain", "batched"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "adjoint"],
                     help="plain: one N=4 ncell^3 system (the headline); batched: 512 independent "
-                         "systems stepped together")
+                         "systems stepped together; adjoint: gradients of 64 replicas x 4000")
+    ap.add_argument("--ckpt", type=int, default=20, help="adjoint checkpoint interval")
     ap.add_argument("--nsys", type=int, default=512)
     ap.add_argument("--single-steps", type=int, default=200,
                     help="steps per system of the one-system-per-launch comparison (batched)")
@@ -272,6 +273,51 @@ def run_batched(args, rank, world):
         print(json.dumps(line))
 
 
+def run_adjoint(args, rank, world):
+    """64 NVE replicas of N=4000 (fcc 10^3 cells at rho*=0.8442, T*=1.0,
+    seeded), 200 steps, loss (1/K) sum_n (epot_n + p_n), gradients wrt eps,
+    sigma and x0, checkpoints every 20 steps: wall time of the forward pass,
+    of the backward pass (segment recompute + reverse sweep), their ratio."""
+    from seplib_gb300 import build, configs, load
+    from seplib_gb300.adjoint import Adjoint
+    build.build()
+    lib = load()
+    nrep, steps = 64, args.steps
+    systems = [configs.plain_lj_large(10, seed=100 + 64 * rank + k, temp=1.0) for k in range(nrep)]
+    param = (RC, 1.0, 1.0, 1.0)
+    a = Adjoint(lib, systems, param, rc=RC, skin=SKIN, dt=DT, ckpt=args.ckpt)
+    a.forward(min(steps, 20))                       # warm-up (allocation, first lists)
+    a.backward()
+    barrier(world)
+    t0 = time.perf_counter()
+    loss = a.forward(steps)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    de, ds, gx = a.backward()
+    t_bwd = time.perf_counter() - t0
+    a.close()
+    t_fwd, t_bwd = allmax(world, t_fwd), allmax(world, t_bwd)
+    ntot = sum(s.n for s in systems)
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s", "value": world * ntot * steps / (t_fwd + t_bwd),
+            "unit": "particle-steps/s", "n_gpus": world, "steps": steps, "warmup": 1,
+            "ms_per_step": 1e3 * (t_fwd + t_bwd) / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 pair / f64 adjoint state", "data": "synthetic (seeded fcc, Maxwell-Boltzmann)",
+            "config": {"workload": "adjoint: %d NVE replicas x N=4000 (fcc 10^3, rho*=0.8442, T*=1.0), "
+                                   "%d steps, dt=%.3f, LJ {2.5, 1, 1, 1}, loss (1/K) sum (epot + p), "
+                                   "gradients wrt eps, sigma, x0; checkpoint every %d steps"
+                                   % (nrep, steps, DT, args.ckpt),
+                       "forward_s": t_fwd, "backward_s": t_bwd,
+                       "backward_over_forward": t_bwd / t_fwd,
+                       "forward_particle_steps_per_s": ntot * steps / t_fwd,
+                       "mean_loss": float(np.mean(loss)), "mean_dloss_deps": float(np.mean(de)),
+                       "mean_dloss_dsigma": float(np.mean(ds))},
+        }
+        print(json.dumps(line))
+
+
 def main():
     args = parse()
     rank, world = dist_setup(args)
@@ -280,6 +326,9 @@ def main():
         return
     if args.workload == "batched":
         run_batched(args, rank, world)
+        return
+    if args.workload == "adjoint":
+        run_adjoint(args, rank, world)
         return
     from seplib_gb300 import build, configs, load, sepapi as A, GpuInfo, GpuTiming
     build.build()
