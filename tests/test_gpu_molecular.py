@@ -206,3 +206,35 @@ def test_butane_nvt_trajectory(gpu_lib, ora, tmp_path):
     assert np.abs(h.view["v"] - st.v).max() < 2e-3
     assert abs(h.alpha.value - alpha) < 1e-5 * max(1e-3, abs(alpha))
     h.close()
+
+
+def test_butane_full_size_forces(gpu_lib, ora, tmp_path):
+    """the molecular workload at full size: 8000 butane chains (32000 beads)
+    at rho* = 0.6, one force evaluation (LJ with intramolecular exclusions,
+    bonds, angles, Ryckaert-Bellemans torsions) against the FP64 oracle"""
+    s = cfg.butane(nmol=8000, rho=0.6, seed=3)
+    s.x = np.mod(s.x + np.random.default_rng(17).normal(0, 0.02, s.x.shape), s.L)
+    top = tmp_path / "b8000.top"
+    cfg.write_top(str(top), s)
+    h = Handle(gpu_lib, s, update=A.SEP_LLIST_NEIGHBLIST, dt=0.002)
+    lib = gpu_lib
+    lib.sep_read_topology_file(h.atoms, str(top).encode(), C.byref(h.sys), b"q")
+    mol = h.view["molindex"].copy()
+    lib.sep_reset_retval(C.byref(h.ret))
+    lib.sep_reset_force(h.atoms, C.byref(h.sys))
+    lib.sep_force_pairs(h.atoms, b"CC", 2.5, h.fun(), C.byref(h.sys), C.byref(h.ret), A.SEP_EXCL_SAME_MOL)
+    lib.sep_stretch_harmonic(h.atoms, 0, 0.4, 33615.0, C.byref(h.sys), C.byref(h.ret))
+    lib.sep_angle_harmonic(h.atoms, 0, 1.9, 866.0, C.byref(h.sys), C.byref(h.ret))
+    lib.sep_torsion_Ryckaert(h.atoms, 0, (C.c_double * 6)(*RB), C.byref(h.sys), C.byref(h.ret))
+    h.sync()
+    nsub = [ora.nsubbox(2.5, 0.25, s.L[k]) for k in range(3)]
+    cs, cn = ora.llist(s.x, s.L, nsub, 2.5, 0.25, ora.EXCL_SAMEMOL, mol)
+    f, e, _ = ora.pair_forces(s.x, s.types, s.L, "CC", ora.POT_LJSHIFT, None, 2.5, cs, cn)
+    fb, eb = ora.stretch_harmonic(np.asarray(s.bonds)[:, 1:].reshape(-1), 0, 0.4, 33615.0, s.x, s.L)[:2]
+    fa, ea = ora.angles(np.asarray(s.angles)[:, 1:].reshape(-1), 0, 1.9, 866.0, False, s.x, s.L)[:2]
+    ft, et = ora.torsion_rb(np.asarray(s.dihedrals)[:, 1:].reshape(-1), 0, RB, s.x, s.L)[:2]
+    fref = f + fb + fa + ft
+    assert rel_l2(h.view["f"], fref) < 1e-5
+    eref = e + eb + ea + et
+    assert abs(h.ret.epot - eref) < 1e-5 * (abs(e) + abs(eb) + abs(ea) + abs(et))
+    h.close()
