@@ -13,6 +13,7 @@
 #include "sepmisc.h"
 #include "sepret.h"
 #include "sepcoulomb.h"
+#include "sepsampler.h"
 #include "sepgpu.h"
 
 #endif

@@ -1,0 +1,87 @@
+/*
+ * sepsampler.h - time-correlation samplers (GB300 implementation).
+ *
+ * The API and the sampler structure follow the reference's
+ * include/sepsampler.h:214-299; programs keep a sepsampler by value and pass
+ * its address, so the member list and order are the reference's (the
+ * per-sampler structures behind the pointers are this library's own and
+ * opaque to programs).  Supported samplers: "sacf" (stress autocorrelation),
+ * "vacf" (velocity autocorrelation), "msd" (mean square displacement,
+ * non-Gaussian parameter, self-intermediate scattering function).  They
+ * write the reference's files (sacf.dat, vacf.dat, msd.dat,
+ * msd-gaussparam.dat, msd-incoherent.dat, msd-k.dat) in the same formats.
+ * The particle data a sample needs stays on the GPU: vacf keeps its window
+ * of velocities in device memory and msd reduces on the device, so sampling
+ * costs no download of the particle arrays.  Any other sampler name ends
+ * the program with sep_error.
+ */
+#ifndef SEP_GB300_SEPSAMPLER_H
+#define SEP_GB300_SEPSAMPLER_H
+
+#include "sepstrct.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sepsacf sepsacf;
+typedef struct sepvacf sepvacf;
+typedef struct sepgh sepgh;
+typedef struct sepprofs sepprofs;
+typedef struct sepradial sepradial;
+typedef struct sepmsd sepmsd;
+typedef struct sepscatt sepscatt;
+typedef struct sepmsacf sepmsacf;
+typedef struct sepmcacf sepmcacf;
+typedef struct sepmgh sepmgh;
+typedef struct sepmprofs sepmprofs;
+typedef struct sepmvacf sepmvacf;
+typedef struct sepmavacf sepmavacf;
+typedef struct sepmmsd sepmmsd;
+
+/* Reference include/sepsampler.h:214-239. */
+typedef struct {
+	sepmol *molptr;
+
+	/* atomic samplers */
+	int flag_sacf; sepsacf *sacf;
+	int flag_vacf; sepvacf *vacf;
+	int flag_gh; sepgh *gh;
+	int flag_profs; sepprofs *profs;
+	int flag_radial; sepradial *radial;
+	int flag_msd; sepmsd *msd;
+	int flag_scatt; sepscatt **scatt;
+
+	/* molecular samplers */
+	int flag_msacf; sepmsacf *msacf;
+	int flag_mcacf; sepmcacf *mcacf;
+	int flag_mgh; sepmgh *mgh;
+	int flag_mprofs; sepmprofs *mprofs;
+	int flag_mvacf; sepmvacf *mvacf;
+	int flag_mavacf; sepmavacf *mavacf;
+	int flag_mmsd; sepmmsd *mmsd;
+
+	long unsigned msd_counter;
+} sepsampler;
+
+/* Reference include/sepsampler.h:247. */
+sepsampler sep_init_sampler(void);
+
+/* Reference include/sepsampler.h:275: "sacf", "vacf": lvec samples over a
+ * time span (double); "msd": lvec samples (0: log-spaced) over a time span
+ * (double), number of wave vectors (int), particle type (char). */
+void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec, ...);
+
+/* Reference include/sepsampler.h:281. */
+void sep_close_sampler(sepsampler *ptr);
+
+/* Reference include/sepsampler.h:291: call once per step n. */
+void sep_sample(seppart *pptr, sepsampler *sptr, sepret *ret, sepsys sys, unsigned n);
+
+/* Reference include/sepsampler.h:299 (molecular samplers are not provided). */
+void sep_add_mol_sampler(sepsampler *sptr, sepmol *mols);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

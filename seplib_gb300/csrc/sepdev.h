@@ -233,6 +233,24 @@ int sepdev_run_timed(sepdev *d, const sepdev_pairset *ps, const sepdev_runcfg *c
 /* queue a write of `bytes` (rounded down to 16) to a context-owned buffer */
 int sepdev_flush_l2(sepdev *d, size_t bytes, unsigned tag);
 
+/* ---- samplers (dev_sampler.cu) ----
+ * vacf: a device ring of lvec rows of x-velocities by user index; _store
+ * fills row index from the current state, _block returns C[k] = sum_i sum_kk
+ * v[kk][i] v[k+kk][i] for k < lvec (host array).  msd: _base keeps the
+ * current unwrapped positions and crossing counts; _sample returns (host,
+ * 2 + nk) sum |dr|^2, sum |dr|^4 and sum cos(k_j dr_x) over particles of
+ * type id type_id.  FP64, fixed summation order. */
+typedef struct sepdev_vacf sepdev_vacf;
+typedef struct sepdev_msd sepdev_msd;
+int sepdev_vacf_create(sepdev *d, int lvec, sepdev_vacf **out);
+void sepdev_vacf_destroy(sepdev_vacf *v);
+int sepdev_vacf_store(sepdev *d, sepdev_vacf *v, int index);
+int sepdev_vacf_block(sepdev *d, sepdev_vacf *v, double *out);
+int sepdev_msd_create(sepdev *d, int nk, const double *k, sepdev_msd **out);
+void sepdev_msd_destroy(sepdev_msd *m);
+int sepdev_msd_base(sepdev *d, sepdev_msd *m);
+int sepdev_msd_sample(sepdev *d, sepdev_msd *m, int type_id, double *out);
+
 /* lanes per particle in the pair kernels (1, 2, 4); invalidates the list */
 int sepdev_set_tpp(sepdev *d, int tpp);
 int sepdev_get_tpp(sepdev *d);

@@ -90,6 +90,14 @@ PART_DTYPE = np.dtype({
 
 POTFUN = C.CFUNCTYPE(C.c_double, C.c_double, C.c_char)
 
+class SepSampler(C.Structure):
+    """sepsampler (include/sepsampler.h): pointers and flags only."""
+    _fields_ = [("molptr", C.c_void_p)] + [x for name in (
+        "sacf", "vacf", "gh", "profs", "radial", "msd", "scatt",
+        "msacf", "mcacf", "mgh", "mprofs", "mvacf", "mavacf", "mmsd")
+        for x in (("flag_" + name, C.c_int), (name, C.c_void_p))] + [("msd_counter", C.c_ulong)]
+
+
 PART_P = C.POINTER(SepPart)
 SYS_P = C.POINTER(SepSys)
 RET_P = C.POINTER(SepRet)
