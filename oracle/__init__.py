@@ -246,3 +246,107 @@ def lj_adjoint(x, v, m, L, param, dt, nsteps):
     if rc != 0:
         raise MemoryError("ora_lj_adjoint")
     return de.value, ds.value, gx
+
+
+# ---- stochastic dynamics -------------------------------------------------------
+
+def philox(ctr, key):
+    """Philox4x32-10 of a 4-word counter and a 2-word key -> 4 words."""
+    c = (C.c_uint32 * 4)(*[int(v) & 0xffffffff for v in ctr])
+    lib().ora_philox.restype = None
+    lib().ora_philox(c, C.c_uint32(int(key[0]) & 0xffffffff), C.c_uint32(int(key[1]) & 0xffffffff))
+    return [int(v) for v in c]
+
+
+def dpd_uniform(seed, gi, gj, call):
+    """the GPU library's DPD pair uniform in [0, 1)"""
+    f = lib().ora_dpd_uniform
+    f.restype = C.c_double
+    f.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_uint32]
+    return f(seed, gi, gj, call)
+
+
+STREAM_DPD, STREAM_FP, STREAM_GJF = 1, 2, 3
+
+
+def gauss3(seed, gids, call, stream):
+    """the GPU library's standard normals, (len(gids), 3)"""
+    f = lib().ora_gauss3
+    f.restype = None
+    f.argtypes = [C.c_uint64, C.c_int, C.c_uint32, C.c_int, C.POINTER(C.c_double)]
+    out = np.zeros((len(gids), 3))
+    for r, g in enumerate(gids):
+        f(seed, int(g), call, stream, _p(out[r], C.c_double))
+    return out
+
+
+def dpd_forces(x, pv, type_chars, L, types, cf, aij, temp, sigma, dt, pairs, uni, per_pair, f=None):
+    """DPD pair forces over `pairs` (visit order); returns (f, epot)."""
+    x = _f64(x); pv = _f64(pv); L = _f64(L)
+    n = len(x)
+    f = np.zeros((n, 3)) if f is None else _f64(f).copy()
+    pr = _i32(pairs).reshape(-1, 2)
+    u = _f64(uni)
+    ty = np.ascontiguousarray(np.asarray(type_chars, dtype="S1"))
+    e = C.c_double()
+    g = lib().ora_dpd_forces
+    g.restype = None
+    g(C.c_long(n), _p(x, C.c_double), _p(pv, C.c_double), ty.ctypes.data_as(C.c_char_p),
+      _p(L, C.c_double), C.c_char_p(types), C.c_double(cf), C.c_double(aij), C.c_double(temp),
+      C.c_double(sigma), C.c_double(dt), C.c_long(len(pr)), _p(pr, C.c_int), _p(u, C.c_double),
+      C.c_int(per_pair), _p(f, C.c_double), C.byref(e))
+    return f, e.value
+
+
+class StochState(LeapState):
+    """LeapState plus the DPD / Langevin per-particle fields."""
+
+    def __init__(self, x, v, m, pv=None, pa=None, prevf=None, randn=None, ldiff=None):
+        super().__init__(x, v, m)
+        n = len(x)
+        z = lambda a, shape: np.zeros(shape) if a is None else _f64(a).copy()  # noqa: E731
+        self.pv = z(pv, (n, 3)); self.pa = z(pa, (n, 3))
+        self.prevf = z(prevf, (n, 3)); self.randn = z(randn, (n, 3))
+        self.ldiff = np.ones(n) if ldiff is None else _f64(ldiff).copy()
+
+
+def _common_tail(st, L, dt, skin, md, ek, kP):
+    return [_p(st.cn, C.c_int), _p(st.cr, C.c_int), _p(st.xn, C.c_double), _p(L, C.c_double),
+            C.c_double(dt), C.c_double(skin), C.byref(md), C.byref(ek), _p(kP, C.c_double)]
+
+
+def verlet_dpd(st, f, L, dt, skin, lam, stepnow, max_dist2=0.0):
+    """Groot-Warren step on StochState; returns (flag, max_dist2, ekin, kinP)."""
+    md = C.c_double(max_dist2); ek = C.c_double(0.0); kP = np.zeros(9)
+    f = _f64(f); L = _f64(L)
+    g = lib().ora_verlet_dpd
+    g.restype = C.c_int
+    flag = g(C.c_long(len(st.x)), _p(st.x, C.c_double), _p(st.v, C.c_double), _p(f, C.c_double),
+             _p(st.a, C.c_double), _p(st.m, C.c_double), _p(st.pv, C.c_double), _p(st.pa, C.c_double),
+             C.c_double(lam), C.c_int(stepnow), *_common_tail(st, L, dt, skin, md, ek, kP))
+    return flag, md.value, ek.value, kP.reshape(3, 3)
+
+
+def fp_step(st, f, gauss, temp, L, dt, skin, max_dist2=0.0):
+    """Fokker-Planck step on StochState; returns (flag, max_dist2, ekin, kinP)."""
+    md = C.c_double(max_dist2); ek = C.c_double(0.0); kP = np.zeros(9)
+    f = _f64(f); L = _f64(L); gs = _f64(gauss)
+    g = lib().ora_fp
+    g.restype = C.c_int
+    flag = g(C.c_long(len(st.x)), _p(st.x, C.c_double), _p(st.v, C.c_double), _p(f, C.c_double),
+             _p(st.m, C.c_double), _p(st.ldiff, C.c_double), _p(gs, C.c_double), C.c_double(temp),
+             *_common_tail(st, L, dt, skin, md, ek, kP))
+    return flag, md.value, ek.value, kP.reshape(3, 3)
+
+
+def langevin_gjf(st, f, gauss, temp, alpha, L, dt, skin, max_dist2=0.0):
+    """GJF Langevin step on StochState; returns (flag, max_dist2, ekin, kinP)."""
+    md = C.c_double(max_dist2); ek = C.c_double(0.0); kP = np.zeros(9)
+    f = _f64(f); L = _f64(L); gs = _f64(gauss)
+    g = lib().ora_langevin_gjf
+    g.restype = C.c_int
+    flag = g(C.c_long(len(st.x)), _p(st.x, C.c_double), _p(st.v, C.c_double), _p(f, C.c_double),
+             _p(st.a, C.c_double), _p(st.m, C.c_double), _p(st.prevf, C.c_double),
+             _p(st.randn, C.c_double), _p(gs, C.c_double), C.c_double(temp), C.c_double(alpha),
+             *_common_tail(st, L, dt, skin, md, ek, kP))
+    return flag, md.value, ek.value, kP.reshape(3, 3)

@@ -733,3 +733,249 @@ int ora_lj_adjoint(long n, const double *x0, const double *v0, const double *m, 
 	free(X); free(U); free(F); free(lx); free(lu); free(h);
 	return 0;
 }
+
+/* ======================================================================
+ * Stochastic dynamics: DPD pair force, Groot-Warren integrator,
+ * Fokker-Planck and Langevin (GJF) integrators.
+ *
+ * The reference draws its random numbers from the C library's rand() in
+ * the order its loops visit pairs and particles.  The restatements below
+ * take the random numbers as inputs, so they can be driven either by that
+ * stream (to pin them against the reference) or by the GPU library's
+ * counter-based streams (ora_dpd_uniform, ora_gauss3) to check the GPU.
+ * ====================================================================== */
+
+#include <stdint.h>
+
+/* Philox4x32-10 (J. K. Salmon, M. A. Moraes, R. O. Dror, D. E. Shaw,
+ * "Parallel random numbers: as easy as 1, 2, 3", SC'11): ten rounds of two
+ * 32x32->64 multiplications with the Weyl key schedule. */
+void ora_philox(uint32_t c[4], uint32_t k0, uint32_t k1)
+{
+	for (int r = 0; r < 10; r++) {
+		if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+		const uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+		const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+		c[1] = (uint32_t)p1;
+		c[3] = (uint32_t)p0;
+		c[0] = n0;
+		c[2] = n2;
+	}
+}
+
+/* stream ids of the GPU library's counters (fourth counter word) */
+enum { ORA_STREAM_DPD = 1, ORA_STREAM_FP = 2, ORA_STREAM_GJF = 3 };
+
+/* DPD pair uniform in [0, 1) of the GPU library: counter (min gid, max gid,
+ * call, DPD), key = seed; 24 bits of the first output word */
+double ora_dpd_uniform(uint64_t seed, int gi, int gj, uint32_t call)
+{
+	uint32_t c[4] = {(uint32_t)(gi < gj ? gi : gj), (uint32_t)(gi < gj ? gj : gi), call, ORA_STREAM_DPD};
+	ora_philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+	return (double)(c[0] >> 8) * (1.0 / 16777216.0);
+}
+
+/* three standard normal numbers of particle gid for one call of a stream:
+ * counter (gid, 0, call, stream); Box-Muller on the output pairs
+ * (w0, w1) and (w2, w3), u1 in (0, 1], u2 in [0, 1) */
+void ora_gauss3(uint64_t seed, int gid, uint32_t call, int stream, double g[3])
+{
+	uint32_t c[4] = {(uint32_t)gid, 0u, call, (uint32_t)stream};
+	ora_philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+	const double two_pi = 6.283185307179586;
+	for (int h = 0; h < 2; h++) {
+		const double u1 = (double)((c[2 * h] >> 8) + 1u) * (1.0 / 16777216.0);
+		const double u2 = (double)(c[2 * h + 1] >> 8) * (1.0 / 16777216.0);
+		const double r = sqrt(-2.0 * log(u1));
+		g[2 * h] = r * cos(two_pi * u2);
+		if (h == 0) g[1] = r * sin(two_pi * u2);
+	}
+}
+
+/*
+ * DPD pair force of Groot and Warren (source/sepprfrc.c:1007-1104).  Pairs are
+ * visited in the order given (i, j) = pairs[2p], pairs[2p+1]; a pair is used
+ * when the first particle's type is one of types[0..1], the two types match
+ * the pair in either order, and r^2 < cf^2.  With w = 1 - r, rhat = r/|r|,
+ * vij = pv_i - pv_j (predicted velocities), gamma = sigma^2 / (2 T):
+ *   fC = aij w rhat, fD = -gamma w^2 (rhat . vij) rhat,
+ *   fR = sigma w rhat dt^(-1/2) (u - 0.5) 2 sqrt(3),
+ * added to i and subtracted from j; epot = sum aij w^2 / 2 (assigned).
+ * u: per_pair = 0 consumes uni[] in order, one per used pair (the
+ * reference's rand() stream); per_pair = 1 takes uni[p] of the pair's index.
+ * The sums go to a separate array that is added to f at the end, as the
+ * reference does.
+ */
+void ora_dpd_forces(long n, const double *x, const double *pv, const char *type, const double L[3],
+		    const char *types, double cf, double aij, double temp, double sigma, double dt,
+		    long npairs, const int *pairs, const double *uni, int per_pair, double *f, double *epot)
+{
+	const double cf2 = cf * cf, isqrtdt = 1.0 / sqrt(dt), facchk = 2.0 * sqrt(3.0);
+	const double gamma = sigma * sigma / (2.0 * temp);
+	double *fa = calloc(3 * (size_t)n, sizeof(double));
+	double e = 0.0;
+	long used = 0;
+	for (long p = 0; p < npairs; p++) {
+		const int i1 = pairs[2 * p], i2 = pairs[2 * p + 1];
+		if (type[i1] != types[0] && type[i1] != types[1]) continue;
+		if (!((type[i1] == types[0] && type[i2] == types[1]) || (type[i1] == types[1] && type[i2] == types[0])))
+			continue;
+		double r[3], r2 = 0.0;
+		for (int k = 0; k < 3; k++) {
+			r[k] = ora_wrap(x[3 * i1 + k] - x[3 * i2 + k], L[k]);
+			r2 += r[k] * r[k];
+		}
+		if (!(r2 < cf2)) continue;
+		const double dij = sqrt(r2), w = 1.0 - dij;
+		double rhat[3], dotrv = 0.0;
+		for (int k = 0; k < 3; k++) {
+			rhat[k] = r[k] / dij;
+			dotrv += rhat[k] * (pv[3 * i1 + k] - pv[3 * i2 + k]);
+		}
+		const double u = per_pair ? uni[p] : uni[used];
+		used++;
+		const double rn = (u - 0.5) * facchk;
+		for (int k = 0; k < 3; k++) {
+			const double fC = aij * w * rhat[k];
+			const double fD = -gamma * w * w * dotrv * rhat[k];
+			const double fR = sigma * w * rhat[k] * isqrtdt * rn;
+			fa[3 * i1 + k] += fC + fD + fR;
+			fa[3 * i2 + k] -= fC + fD + fR;
+		}
+		e += 0.5 * aij * w * w;
+	}
+	for (long q = 0; q < 3 * n; q++) f[q] += fa[q];
+	free(fa);
+	*epot = e;
+}
+
+/* reference sep_periodic (source/sepintgr.c:17-37): wrap one coordinate
+ * set, count crossings, return |x + cross_neighb L - xn|^2 */
+static double ora_periodic(long i, double *x, int *cross_neighb, int *crossings, const double *xn,
+			   const double L[3])
+{
+	double d2 = 0.0;
+	for (int k = 0; k < 3; k++) {
+		const long q = 3 * i + k;
+		if (x[q] > L[k]) { x[q] -= L[k]; cross_neighb[q]++; crossings[q]++; }
+		else if (x[q] < 0.0) { x[q] += L[k]; cross_neighb[q]--; crossings[q]--; }
+		const double ri = (x[q] + cross_neighb[q] * L[k]) - xn[q];
+		d2 += ri * ri;
+	}
+	return d2;
+}
+
+/* the skin test shared by the integrators: xn = x, cross_neighb = 0 */
+static int ora_skin(long n, const double *x, int *cross_neighb, double *xn, double skin, double max_dist2)
+{
+	if (!(sqrt(max_dist2) > 0.5 * skin)) return 0;
+	memcpy(xn, x, sizeof(double) * 3 * n);
+	memset(cross_neighb, 0, sizeof(int) * 3 * n);
+	return 1;
+}
+
+/*
+ * Groot-Warren velocity Verlet (source/sepintgr.c:296-345): a = f/m;
+ * v += dt (a + pa)/2 unless stepnow == 0; x += v dt + a dt^2/2;
+ * pv = v + lambda dt a; pa = a; ekin += sum m v^2 / 2 and kin_P += m v v^T
+ * with the updated v.  Returns 1 when the skin test fired (the reference
+ * raises neighb_flag there but does not count the update).
+ */
+int ora_verlet_dpd(long n, double *x, double *v, const double *f, double *a, const double *m,
+		   double *pv, double *pa, double lambda, int stepnow, int *cross_neighb, int *crossings,
+		   double *xn, const double L[3], double dt, double skin, double *max_dist2,
+		   double *ekin, double *kinP)
+{
+	double sum = 0.0;
+	for (long i = 0; i < n; i++) {
+		for (int k = 0; k < 3; k++) {
+			const long q = 3 * i + k;
+			a[q] = f[q] / m[i];
+			if (stepnow > 0) v[q] += 0.5 * dt * (a[q] + pa[q]);
+			x[q] += v[q] * dt + 0.5 * dt * dt * a[q];
+			pv[q] = v[q] + lambda * dt * a[q];
+			pa[q] = a[q];
+			sum += v[q] * v[q] * m[i];
+		}
+		const double d2 = ora_periodic(i, x, cross_neighb, crossings, xn, L);
+		if (d2 > *max_dist2) *max_dist2 = d2;
+		for (int k = 0; k < 3; k++)
+			for (int kk = 0; kk < 3; kk++) kinP[3 * k + kk] += v[3 * i + k] * v[3 * i + kk] * m[i];
+	}
+	*ekin += 0.5 * sum;
+	return ora_skin(n, x, cross_neighb, xn, skin, *max_dist2);
+}
+
+/*
+ * Fokker-Planck (Brownian) integrator (source/sepintgr.c:235-293): per
+ * coordinate a = g sqrt(1/12) sqrt(24 T fric/dt) with g standard normal
+ * (gauss[3 i + k]) and fric = T / ldiff; x += dt v (old v);
+ * v += dt/m (f - fric v + a); wrap; ekin, kin_P from the new v.  Returns 1
+ * when the skin test fired (the reference counts that update).
+ */
+int ora_fp(long n, double *x, double *v, const double *f, const double *m, const double *ldiff,
+	   const double *gauss, double temp, int *cross_neighb, int *crossings, double *xn,
+	   const double L[3], double dt, double skin, double *max_dist2, double *ekin, double *kinP)
+{
+	const double fac = sqrt(1.0 / 12.0);
+	double sum = 0.0;
+	for (long i = 0; i < n; i++) {
+		const double im = 1.0 / m[i], fric = temp / ldiff[i];
+		const double gaussfac = sqrt(24 * temp * fric / dt);
+		double d2 = 0.0;
+		for (int k = 0; k < 3; k++) {
+			const long q = 3 * i + k;
+			const double ak = gauss[q] * fac * gaussfac;
+			x[q] += dt * v[q];
+			v[q] += im * dt * (f[q] - fric * v[q] + ak);
+			if (x[q] > L[k]) { x[q] -= L[k]; cross_neighb[q]++; crossings[q]++; }
+			else if (x[q] < 0.0) { x[q] += L[k]; cross_neighb[q]--; crossings[q]--; }
+			sum += v[q] * v[q] * m[i];
+			const double ri = (x[q] + cross_neighb[q] * L[k]) - xn[q];
+			d2 += ri * ri;
+		}
+		if (d2 > *max_dist2) *max_dist2 = d2;
+		for (int k = 0; k < 3; k++)
+			for (int kk = 0; kk < 3; kk++) kinP[3 * k + kk] += v[3 * i + k] * v[3 * i + kk] * m[i];
+	}
+	*ekin += 0.5 * sum;
+	return ora_skin(n, x, cross_neighb, xn, skin, *max_dist2);
+}
+
+/*
+ * Langevin integrator of Gronbech-Jensen and Farago
+ * (source/sepintgr.c:91-146): cc = exp(-alpha dt), fac = sqrt(T (1 - cc^2)),
+ * c = alpha dt / (2 m), a' = (1 - c)/(1 + c), b = 1/(1 + c);
+ * v = a' v + dt/(2m) (a' prevf + f) + b randn / m; prevf = f;
+ * randn = fac g (new draw, gauss[3 i + k]);
+ * x += b dt v + b dt^2/(2m) f + b dt/(2m) randn; wrap; ekin and kin_P from
+ * the new v.  Returns 1 when the skin test fired (counted).
+ */
+int ora_langevin_gjf(long n, double *x, double *v, const double *f, double *a, const double *m,
+		     double *prevf, double *randn, const double *gauss, double temp, double alpha,
+		     int *cross_neighb, int *crossings, double *xn, const double L[3], double dt,
+		     double skin, double *max_dist2, double *ekin, double *kinP)
+{
+	const double cc = exp(-alpha * dt);
+	double sum = 0.0;
+	for (long i = 0; i < n; i++) {
+		const double mass = m[i], imass = 1.0 / mass, imass2 = 0.5 * imass;
+		const double fac = sqrt(temp * (1.0 - cc * cc));
+		const double c = alpha * dt * imass2, ap = (1.0 - c) / (1.0 + c), b = 1.0 / (1.0 + c);
+		for (int k = 0; k < 3; k++) {
+			const long q = 3 * i + k;
+			v[q] = ap * v[q] + dt * imass2 * (ap * prevf[q] + f[q]) + b * imass * randn[q];
+			a[q] = f[q] * imass;
+			prevf[q] = f[q];
+			sum += v[q] * v[q] * mass;
+			randn[q] = fac * gauss[q];
+			x[q] += b * dt * v[q] + b * dt * dt * imass2 * f[q] + b * dt * imass2 * randn[q];
+		}
+		const double d2 = ora_periodic(i, x, cross_neighb, crossings, xn, L);
+		if (d2 > *max_dist2) *max_dist2 = d2;
+		for (int k = 0; k < 3; k++)
+			for (int kk = 0; kk < 3; kk++) kinP[3 * k + kk] += v[3 * i + k] * v[3 * i + kk] * mass;
+	}
+	*ekin += 0.5 * sum;
+	return ora_skin(n, x, cross_neighb, xn, skin, *max_dist2);
+}

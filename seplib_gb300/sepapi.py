@@ -81,10 +81,12 @@ assert C.sizeof(SepPart) == 568 and C.sizeof(SepSys) == 168 and C.sizeof(SepRet)
 # numpy view of a seppart array (same offsets as SepPart)
 PART_DTYPE = np.dtype({
     "names": ["x", "v", "f", "a", "m", "type", "z", "cross_neighb", "crossings",
-              "molindex", "bond", "angle", "dihed", "xn"],
+              "molindex", "bond", "angle", "dihed", "ldiff", "xn", "pv", "pa", "randn", "prevf"],
     "formats": [("f8", 3), ("f8", 3), ("f8", 3), ("f8", 3), "f8", "S1", "f8",
-                ("i4", 3), ("i4", 3), "i4", ("i4", 10), ("i4", 10), ("i4", 20), ("f8", 3)],
-    "offsets": [0, 24, 48, 72, 96, 104, 112, 128, 140, 152, 156, 196, 236, 400],
+                ("i4", 3), ("i4", 3), "i4", ("i4", 10), ("i4", 10), ("i4", 20), "f8", ("f8", 3),
+                ("f8", 3), ("f8", 3), ("f8", 3), ("f8", 3)],
+    "offsets": [0, 24, 48, 72, 96, 104, 112, 128, 140, 152, 156, 196, 236, 344, 400,
+                472, 496, 520, 544],
     "itemsize": 568,
 })
 
@@ -140,6 +142,12 @@ SIGNATURES = {
     "sep_set_xn": (None, [PART_P, C.c_int]),
     "sep_count_type": (C.c_int, [PART_P, C.c_char, C.c_int]),
     "sep_nsubbox": (C.c_int, [D, D, D]),
+    "sep_force_dpd": (None, [PART_P, C.c_char_p, D, D, D, D, SYS_P, RET_P, C.c_uint]),
+    "sep_verlet_dpd": (None, [PART_P, D, C.c_int, SYS_P, RET_P]),
+    "sep_fp": (None, [PART_P, D, SYS_P, RET_P]),
+    "sep_langevinGJF": (None, [PART_P, D, D, SYS_P, RET_P]),
+    "sep_set_ldiff": (None, [PART_P, C.c_char, D, SepSys]),
+    "sep_randn": (D, []),
 }
 
 

@@ -144,13 +144,110 @@ def host_api(lib):
     return d
 
 
-def main():
+def visit_pairs(h_atoms, n):
+    """the reference's neighbour list in the order its force loops visit it"""
+    out = []
+    for i in range(n):
+        arr = np.ctypeslib.as_array(h_atoms[i].neighb, shape=(A.SEP_NEIGHB,))
+        k = int(np.argmax(arr == -1))
+        out += [(i, int(j)) for j in arr[:k]]
+    return np.array(out, dtype=np.int32)
+
+
+def stochastic(lib):
+    """DPD force, Groot-Warren, Fokker-Planck and GJF Langevin steps.
+
+    The reference draws from the C library's rand(); each call is preceded
+    by srand(seed), and the same stream is re-drawn afterwards (uniforms from
+    rand(), normals from the reference's own sep_randn) so the restatement
+    can consume it.  n is even: every call draws 3n normals, so sep_randn's
+    cached second value is unused between calls."""
+    libc = C.CDLL(None)
+    rng = np.random.default_rng(11)
+    n, rho = 256, 3.0
+    L = (n / rho) ** (1 / 3)
+    atoms = lib.sep_init(n, A.SEP_NEIGHB)
+    v = A.parts_view(atoms, n)
+    v["x"] = rng.uniform(0, L, (n, 3))
+    v["v"] = rng.normal(0, 1, (n, 3))
+    v["pv"] = v["v"] + rng.normal(0, 0.1, (n, 3))
+    v["pa"] = rng.normal(0, 5, (n, 3))
+    v["type"] = np.where(rng.uniform(size=n) < 0.7, b"A", b"B")
+    v["m"] = np.where(v["type"] == b"A", 1.0, 2.0)
+    v["xn"] = v["x"]
+    sys_ = lib.sep_sys_setup(L, L, L, 1.0, 0.02, n, A.SEP_LLIST_NEIGHBLIST)
+    ret = A.SepRet()
+    d = dict(L=np.array([L] * 3), dt=0.02, skin=sys_.skin, types=v["type"].copy(),
+             m=v["m"].copy(), x0=v["x"].copy(), v0=v["v"].copy(), pv0=v["pv"].copy(),
+             pa0=v["pa"].copy())
+    lib.sep_reset_retval(C.byref(ret))
+    lib.sep_reset_force(atoms, C.byref(sys_))
+    # DPD: "AA" then "AB" (forces accumulate, the energy is assigned)
+    for tag, types, seed in (("aa", b"AA", 101), ("ab", b"AB", 202)):
+        libc.srand(seed)
+        lib.sep_force_dpd(atoms, types, 1.0, 25.0, 1.0, 3.0, C.byref(sys_), C.byref(ret), A.SEP_ALL)
+        pairs = visit_pairs(atoms, n)
+        libc.srand(seed)
+        d["dpd_%s_uni" % tag] = np.array([libc.rand() / 2147483648.0 for _ in range(len(pairs))])
+        d["dpd_%s_f" % tag] = v["f"].copy()
+        d["dpd_%s_epot" % tag] = ret.epot
+    d["dpd_pairs"] = pairs
+    # Groot-Warren, stepnow = 1 then 0
+    for tag, stepnow in (("vd1", 1), ("vd0", 0)):
+        d[tag + "_in"] = dict_state(v)
+        lib.sep_reset_retval(C.byref(ret))
+        sys_.max_dist2 = 0.0
+        lib.sep_verlet_dpd(atoms, 0.5, stepnow, C.byref(sys_), C.byref(ret))
+        d[tag + "_out"] = dict_state(v)
+        d[tag + "_ret"] = np.array([ret.ekin, sys_.max_dist2, sys_.neighb_flag] + list(np.ravel(ret.kin_P)))
+    # Fokker-Planck with two diffusion coefficients, then GJF Langevin
+    lib.sep_set_ldiff(atoms, b"B", 0.5, sys_)
+    d["ldiff"] = v["ldiff"].copy()
+    v["f"] = rng.normal(0, 3, (n, 3))
+    v["prevf"] = rng.normal(0, 3, (n, 3))
+    v["randn"] = rng.normal(0, 1, (n, 3))
+    for tag, call, seed in (("fp", lambda: lib.sep_fp(atoms, 1.2, C.byref(sys_), C.byref(ret)), 303),
+                            ("gjf", lambda: lib.sep_langevinGJF(atoms, 1.2, 0.7, C.byref(sys_),
+                                                                C.byref(ret)), 404)):
+        d[tag + "_in"] = dict_state(v)
+        lib.sep_reset_retval(C.byref(ret))
+        sys_.max_dist2 = 0.0
+        nup = sys_.nupdate_neighb
+        libc.srand(seed)
+        call()
+        d[tag + "_out"] = dict_state(v)
+        d[tag + "_ret"] = np.array([ret.ekin, sys_.max_dist2, sys_.nupdate_neighb - nup] +
+                                   list(np.ravel(ret.kin_P)))
+        libc.srand(seed)
+        d[tag + "_gauss"] = np.array([lib.sep_randn() for _ in range(3 * n)]).reshape(n, 3)
+    lib.sep_close(atoms, n)
+    # flatten the nested state dicts for npz
+    out = {}
+    for k, val in d.items():
+        if isinstance(val, dict):
+            for kk, vv in val.items():
+                out[k + "_" + kk] = vv
+        else:
+            out[k] = val
+    return out
+
+
+def dict_state(v):
+    return {k: v[k].copy() for k in ("x", "v", "f", "pv", "pa", "prevf", "randn",
+                                      "cross_neighb", "crossings", "xn")}
+
+
+def main(only=()):
+    """write every fixture, or only the ones named on the command line"""
     lib = ref_lib()
     with tempfile.TemporaryDirectory() as tmp:
         for name, fn in (("lj_small", lambda: lj_small(lib)),
                          ("butane_small", lambda: butane_small(lib, tmp)),
                          ("water_small", lambda: water_small(lib, tmp)),
-                         ("host_api", lambda: host_api(lib))):
+                         ("host_api", lambda: host_api(lib)),
+                         ("stoch_small", lambda: stochastic(lib))):
+            if only and name not in only:
+                continue
             d = fn()
             path = os.path.join(HERE, name + ".npz")
             np.savez_compressed(path, **d)
@@ -158,4 +255,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))
