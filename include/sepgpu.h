@@ -35,6 +35,12 @@ int sep_gpu_sync(seppart *ptr);
  * next device call. */
 int sep_gpu_invalidate(seppart *ptr);
 
+/* Key of the counter-based random streams of sep_force_dpd, sep_fp and
+ * sep_langevinGJF (Philox4x32-10; a draw depends on the seed, the user
+ * indices it is for and the number of earlier calls of the same function).
+ * Setting the seed also restarts those call counts.  0 on success. */
+int sep_gpu_set_seed(seppart *ptr, unsigned long long seed);
+
 /*
  * Device-resident MD loop: nsteps repetitions of
  *     sep_reset_retval; sep_reset_force;

@@ -67,6 +67,9 @@ void sep_set_skin(sepsys *sys, double value);
 /* Sets mass or charge of every particle of a type (reference :320-330). */
 void sep_set_charge(seppart *ptr, char type, double z, sepsys sys);
 void sep_set_mass(seppart *ptr, char type, double m, sepsys sys);
+/* Sets the Langevin diffusion coefficient of every particle of a type
+ * (reference :449, source/sepmisc.c:1162-1170). */
+void sep_set_ldiff(seppart *ptr, char type, double ldiff, sepsys sys);
 
 /* Removes the centre-of-mass momentum of one type (reference :338). */
 void sep_reset_momentum(seppart *ptr, const char type, sepsys *sys);

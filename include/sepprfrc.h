@@ -30,6 +30,28 @@ int sep_force_pairs(seppart *ptr, const char *types, double cf,
 void sep_force_lj(seppart *ptr, const char *types, const double *param,
 		  sepsys *sys, sepret *retval, const unsigned opt);
 
+/*
+ * DPD pair force of Groot and Warren between the types of `types` within cf:
+ * with w = 1 - r, conservative aij w, dissipative -gamma w^2 (rhat . vij)
+ * on the predicted velocities pv, gamma = sigma^2/(2 T), and random
+ * sigma w dt^(-1/2) theta with theta uniform of unit variance, all along
+ * rhat.  On the neighbour list the energy sum aij w^2/2 is ASSIGNED to
+ * ret->epot; under SEP_BRUTE it is added, with the conservative virial added
+ * to pot_P and the three parts to pot_P_conservative, pot_P_random and
+ * pot_P_dissipative (reference :89-101, :172-176,
+ * source/sepprfrc.c:278-301, :1007-1235).  The random numbers are this
+ * library's counter-based streams (sep_gpu_set_seed), not rand().
+ */
+void sep_force_dpd(seppart *ptr, const char *types, const double cf, const double aij,
+		   const double temp_desired, const double sigma, sepsys *sys, sepret *retval,
+		   const unsigned opt);
+void sep_dpdforce_neighb(seppart *ptr, const char *types, const double cf, const double aij,
+			 const double temp_desired, const double sigma, sepsys *sys,
+			 sepret *retval, const unsigned opt);
+void sep_dpdforce_brute(seppart *ptr, const char *types, const double cf, const double aij,
+			const double temp_desired, const double sigma, sepsys *sys,
+			sepret *retval);
+
 /* Exclusion predicates on the per-particle partner arrays
  * (reference :120-123, source/sepprfrc.c:703-740). */
 unsigned int sep_bond_share(seppart *ptr, int j1, int j2);

@@ -280,8 +280,10 @@ def gauss3(seed, gids, call, stream):
     return out
 
 
-def dpd_forces(x, pv, type_chars, L, types, cf, aij, temp, sigma, dt, pairs, uni, per_pair, f=None):
-    """DPD pair forces over `pairs` (visit order); returns (f, epot)."""
+def dpd_forces(x, pv, type_chars, L, types, cf, aij, temp, sigma, dt, pairs, uni, per_pair, f=None,
+               virial=False):
+    """DPD pair forces over `pairs` (visit order); returns (f, epot), plus
+    the (conservative, random, dissipative) virials when `virial`."""
     x = _f64(x); pv = _f64(pv); L = _f64(L)
     n = len(x)
     f = np.zeros((n, 3)) if f is None else _f64(f).copy()
@@ -289,12 +291,15 @@ def dpd_forces(x, pv, type_chars, L, types, cf, aij, temp, sigma, dt, pairs, uni
     u = _f64(uni)
     ty = np.ascontiguousarray(np.asarray(type_chars, dtype="S1"))
     e = C.c_double()
+    vir = np.zeros(27) if virial else None
     g = lib().ora_dpd_forces
     g.restype = None
     g(C.c_long(n), _p(x, C.c_double), _p(pv, C.c_double), ty.ctypes.data_as(C.c_char_p),
       _p(L, C.c_double), C.c_char_p(types), C.c_double(cf), C.c_double(aij), C.c_double(temp),
       C.c_double(sigma), C.c_double(dt), C.c_long(len(pr)), _p(pr, C.c_int), _p(u, C.c_double),
-      C.c_int(per_pair), _p(f, C.c_double), C.byref(e))
+      C.c_int(per_pair), _p(f, C.c_double), C.byref(e), _p(vir, C.c_double))
+    if virial:
+        return f, e.value, vir.reshape(3, 3, 3)
     return f, e.value
 
 

@@ -804,11 +804,14 @@ void ora_gauss3(uint64_t seed, int gid, uint32_t call, int stream, double g[3])
  * u: per_pair = 0 consumes uni[] in order, one per used pair (the
  * reference's rand() stream); per_pair = 1 takes uni[p] of the pair's index.
  * The sums go to a separate array that is added to f at the end, as the
- * reference does.
+ * reference's list form does.  vir (27 doubles, may be NULL) accumulates the
+ * virials of the O(N^2) form (source/sepprfrc.c:1196-1206): fC_k r_kk,
+ * fR_k r_kk, fD_k r_kk, row-major 3x3 each.
  */
 void ora_dpd_forces(long n, const double *x, const double *pv, const char *type, const double L[3],
 		    const char *types, double cf, double aij, double temp, double sigma, double dt,
-		    long npairs, const int *pairs, const double *uni, int per_pair, double *f, double *epot)
+		    long npairs, const int *pairs, const double *uni, int per_pair, double *f, double *epot,
+		    double *vir)
 {
 	const double cf2 = cf * cf, isqrtdt = 1.0 / sqrt(dt), facchk = 2.0 * sqrt(3.0);
 	const double gamma = sigma * sigma / (2.0 * temp);
@@ -841,6 +844,12 @@ void ora_dpd_forces(long n, const double *x, const double *pv, const char *type,
 			const double fR = sigma * w * rhat[k] * isqrtdt * rn;
 			fa[3 * i1 + k] += fC + fD + fR;
 			fa[3 * i2 + k] -= fC + fD + fR;
+			if (vir)
+				for (int kk = 0; kk < 3; kk++) {
+					vir[3 * k + kk] += fC * r[kk];
+					vir[9 + 3 * k + kk] += fR * r[kk];
+					vir[18 + 3 * k + kk] += fD * r[kk];
+				}
 		}
 		e += 0.5 * aij * w * w;
 	}

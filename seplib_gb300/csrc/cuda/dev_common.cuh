@@ -47,6 +47,12 @@ struct sepdev {
 	int *mol, *mol_b;
 	int has_charge;
 
+	// stochastic-dynamics fields, allocated on first use (NULL otherwise):
+	// [SEPDEV_EXT_PV] predicted velocity, .w = Langevin diffusion
+	// coefficient; [SEPDEV_EXT_PA] previous acceleration; [SEPDEV_EXT_PREVF]
+	// previous force; [SEPDEV_EXT_RANDN] the last Gaussian draws (GJF)
+	float4 *ext[SEPDEV_NEXT], *ext_b[SEPDEV_NEXT];
+
 	// cell list
 	int ncell[3];
 	long ncells, cap_cells;

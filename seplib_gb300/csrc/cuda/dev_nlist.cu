@@ -123,6 +123,7 @@ struct GatherArgs {
 	const int *gid; int *gid_o;
 	const float *chg; float *chg_o;
 	const int *mol; int *mol_o;
+	const float4 *ext[SEPDEV_NEXT]; float4 *ext_o[SEPDEV_NEXT];
 	int4 *xn; int *inv;
 	int trigger;
 };
@@ -147,6 +148,9 @@ __global__ void k_gather(long n, GatherArgs a)
 	a.inv[g] = (int)t;
 	a.chg_o[t] = a.chg[o];
 	a.mol_o[t] = a.mol[o];
+#pragma unroll
+	for (int k = 0; k < SEPDEV_NEXT; k++)
+		if (a.ext[k]) a.ext_o[k][t] = a.ext[k][o];
 }
 
 __device__ __forceinline__ bool in_csr(const int *__restrict__ st, const int *__restrict__ idx,
@@ -437,6 +441,7 @@ struct CopyArgs {
 	const int *gid_s; int *gid_d;
 	const float *chg_s; float *chg_d;
 	const int *mol_s; int *mol_d;
+	const float4 *ext_s[SEPDEV_NEXT]; float4 *ext_d[SEPDEV_NEXT];
 };
 
 __global__ void k_copyback(long n, CopyArgs a)
@@ -453,6 +458,9 @@ __global__ void k_copyback(long n, CopyArgs a)
 	a.gid_d[t] = a.gid_s[t];
 	a.chg_d[t] = a.chg_s[t];
 	a.mol_d[t] = a.mol_s[t];
+#pragma unroll
+	for (int k = 0; k < SEPDEV_NEXT; k++)
+		if (a.ext_s[k]) a.ext_d[k][t] = a.ext_s[k][t];
 }
 
 static int grow(sepdev *d, void **p, size_t bytes, size_t *cap)
@@ -528,6 +536,7 @@ int sepdev_sort_async(sepdev *d, int parity, int trigger)
 	g.gid = d->gid; g.gid_o = d->gid_b;
 	g.chg = d->charge; g.chg_o = d->charge_b;
 	g.mol = d->mol; g.mol_o = d->mol_b;
+	for (int k = 0; k < SEPDEV_NEXT; k++) { g.ext[k] = d->ext[k]; g.ext_o[k] = d->ext_b[k]; }
 	g.xn = d->xn; g.inv = d->inv;
 	g.trigger = trigger;
 	k_gather<<<grid_for(n, B), B, 0, d->st>>>(n, g);
@@ -543,6 +552,7 @@ int sepdev_sort_async(sepdev *d, int parity, int trigger)
 	c.gid_s = d->gid_b; c.gid_d = d->gid;
 	c.chg_s = d->charge_b; c.chg_d = d->charge;
 	c.mol_s = d->mol_b; c.mol_d = d->mol;
+	for (int k = 0; k < SEPDEV_NEXT; k++) { c.ext_s[k] = d->ext_b[k]; c.ext_d[k] = d->ext[k]; }
 	k_copyback<<<grid_for(n, B), B, 0, d->st>>>(n, c);
 	CKL(d);
 	return SEPDEV_OK;

@@ -106,6 +106,10 @@ extern "C" void sepdev_destroy(sepdev *d)
 		if (bufs[k]) cudaFree(bufs[k]);
 	for (int k = 0; k < SEPDEV_MAXTAB; k++)
 		if (d->tab[k]) cudaFree(d->tab[k]);
+	for (int k = 0; k < SEPDEV_NEXT; k++) {
+		if (d->ext[k]) cudaFree(d->ext[k]);
+		if (d->ext_b[k]) cudaFree(d->ext_b[k]);
+	}
 	if (d->h_slots) cudaFreeHost(d->h_slots);
 	if (d->stage) cudaFreeHost(d->stage);
 	if (d->h_flags) cudaFreeHost(d->h_flags);

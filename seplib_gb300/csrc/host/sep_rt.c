@@ -53,6 +53,7 @@ rt_ctx *rt_register(seppart *ptr, long n)
 			c->list_stale = 1;
 			c->pass_slot = -1;
 			c->forces_zero = 0;
+			c->seed = RT_SEED_DEFAULT;
 			g_ctx[k] = c;
 			return c;
 		}
@@ -80,6 +81,61 @@ static int type_id(rt_ctx *c, char t)
 		sep_error("more than %d particle types are not supported on the GPU", SEPDEV_MAXTYPES);
 	c->tchar[c->ntypes] = t;
 	return c->ntypes++;
+}
+
+int rt_type_id(rt_ctx *c, char t)
+{
+	for (int k = 0; k < c->ntypes; k++)
+		if (c->tchar[k] == t) return k;
+	return -1;
+}
+
+/* pv, pa, prevf, randn and ldiff of the seppart records to the device */
+static void ext_upload(rt_ctx *c)
+{
+	const long n = c->n;
+	const seppart *p = c->ptr;
+	double *buf = malloc(sizeof(double) * 13 * n);
+	if (!buf) sep_error("couldn't allocate memory");
+	double *pv = buf, *pa = buf + 3 * n, *pf = buf + 6 * n, *rn = buf + 9 * n, *ld = buf + 12 * n;
+	for (long i = 0; i < n; i++) {
+		for (int k = 0; k < 3; k++) {
+			pv[3 * i + k] = p[i].pv[k];
+			pa[3 * i + k] = p[i].pa[k];
+			pf[3 * i + k] = p[i].prevf[k];
+			rn[3 * i + k] = p[i].randn[k];
+		}
+		ld[i] = p[i].ldiff;
+	}
+	rt_check(sepdev_ext_enable(c->dev), "stochastic fields");
+	rt_check(sepdev_ext_upload(c->dev, pv, pa, pf, rn, ld), "stochastic upload");
+	free(buf);
+}
+
+static void ext_download(rt_ctx *c)
+{
+	const long n = c->n;
+	seppart *p = c->ptr;
+	double *buf = malloc(sizeof(double) * 12 * n);
+	if (!buf) sep_error("couldn't allocate memory");
+	double *pv = buf, *pa = buf + 3 * n, *pf = buf + 6 * n, *rn = buf + 9 * n;
+	rt_check(sepdev_ext_download(c->dev, pv, pa, pf, rn), "stochastic download");
+	for (long i = 0; i < n; i++)
+		for (int k = 0; k < 3; k++) {
+			p[i].pv[k] = pv[3 * i + k];
+			p[i].pa[k] = pa[3 * i + k];
+			p[i].prevf[k] = pf[3 * i + k];
+			p[i].randn[k] = rn[3 * i + k];
+		}
+	free(buf);
+}
+
+void rt_need_ext(rt_ctx *c, const sepsys *sys)
+{
+	rt_need_device(c, sys);
+	if (c->ext_on) return;
+	c->ext_on = 1;
+	ext_upload(c);
 }
 
 static void upload_topology(rt_ctx *c)
@@ -128,6 +184,7 @@ void rt_need_device(rt_ctx *c, const sepsys *sys)
 		if (c->tpp) sepdev_set_tpp(c->dev, c->tpp);
 	}
 	if (c->dev_valid && !c->topo_dirty) return;
+	const int uploading = !c->dev_valid;
 	if (!c->dev_valid && sepdev_direct_io(c->dev)) {
 		/* the device reads the seppart records itself */
 		double sv2 = 0.0, maxd2 = 0.0;
@@ -188,6 +245,7 @@ void rt_need_device(rt_ctx *c, const sepsys *sys)
 		 * reference's next leap-frog reports an update, so ours does too. */
 		c->pending_trigger = sqrt(maxd2) > 0.5 * sys->skin;
 	}
+	if (uploading && c->ext_on) ext_upload(c);
 	if (c->topo_dirty) upload_topology(c);
 }
 
@@ -210,6 +268,7 @@ void rt_need_host(rt_ctx *c)
 		/* the device writes the seppart records itself */
 		rt_check(sepdev_download_parts(c->dev, c->ptr, c->forces_zero), "download");
 		term_values_to_host(c);
+		if (c->ext_on) ext_download(c);
 		c->host_valid = 1;
 		return;
 	}
@@ -232,6 +291,7 @@ void rt_need_host(rt_ctx *c)
 		}
 	free(x); free(v); free(f); free(xn); free(cr); free(cn);
 	term_values_to_host(c);
+	if (c->ext_on) ext_download(c);
 	c->host_valid = 1;
 }
 
@@ -359,6 +419,12 @@ void rt_read_slots(rt_ctx *c, sepsys *sys, int lf_slot)
 			add_sym(r->pot_P_bond, s + SLOT_POTPB, 1.0);
 			break;
 		case OP_EADD: r->epot += s[SLOT_EPOT0]; break;
+		case OP_DPD_VIR:
+			add_sym(r->pot_P, s + SLOT_POTP, 1.0);
+			add_sym(r->pot_P_conservative, s + SLOT_POTP, 1.0);
+			add_sym(r->pot_P_random, s + SLOT_POTPB, 1.0);
+			add_sym(r->pot_P_dissipative, vals + o->chan * SLOT_FIELDS + SLOT_POTP, 1.0);
+			break;
 		case OP_KIN:
 			r->ekin += 0.5 * s[SLOT_EKIN];
 			add_sym(r->kin_P, s + SLOT_KINP, 1.0);

@@ -44,7 +44,9 @@ enum {
 	OP_COUL,             /* epot += Ec, ecoul += Ec                 (sep_coulomb_sf) */
 	OP_BOND,             /* epot += E0, pot_P += P, pot_P_bond += P (stretch) */
 	OP_EADD,             /* epot += E0                              (angles, torsions) */
-	OP_KIN               /* ekin += Ek/2, kin_P += K                (leap-frog) */
+	OP_KIN,              /* ekin += Ek/2, kin_P += K                (leap-frog) */
+	OP_DPD_VIR           /* pot_P, pot_P_conservative += C; pot_P_random += R;
+	                      * pot_P_dissipative += D (chan: slot of D) (O(N^2) DPD) */
 };
 
 typedef struct {
@@ -108,10 +110,20 @@ typedef struct rt_ctx {
 	double tab_rc[4];
 	int ntab;
 
+	/* stochastic dynamics: the device holds pv, pa, prevf, randn and ldiff
+	 * once ext_on is set; seed keys the random streams, ncall counts the
+	 * calls of each stream (DPD, Fokker-Planck, GJF) */
+	int ext_on;
+	unsigned long long seed;
+	unsigned ncall[4];
+
 	/* statistics */
 	long nbuild;
 	int tpp;
 } rt_ctx;
+
+#define RT_SEED_DEFAULT 0x5eb15eedULL
+enum { RT_STREAM_DPD = 1, RT_STREAM_FP = 2, RT_STREAM_GJF = 3 };
 
 rt_ctx *rt_find(const seppart *ptr);
 rt_ctx *rt_get(seppart *ptr, const char *caller);   /* exits with sep_error if unknown */
@@ -136,6 +148,8 @@ void rt_flush(rt_ctx *c);                /* everything pending, then read slots 
 void rt_prepare_list(rt_ctx *c, sepsys *sys, unsigned opt, int brute_excl_bonds);
 
 void rt_check(int rc, const char *what);
+void rt_need_ext(rt_ctx *c, const sepsys *sys);    /* stochastic fields on the device */
+int rt_type_id(rt_ctx *c, char t);                 /* -1 when no particle has type t */
 void rt_pairset(rt_ctx *c, sepdev_pairset *ps);   /* pending terms -> device table */   /* sep_error on a device failure */
 
 extern char rt_errbuf[512];

@@ -34,6 +34,10 @@ typedef struct sepdev sepdev;
 #define SEPDEV_ENODEV       -5   /* no CUDA device */
 
 #define SEPDEV_MAXTYPES 16
+
+/* stochastic-dynamics per-particle fields (sepdev_ext_*) */
+enum { SEPDEV_EXT_PV = 0, SEPDEV_EXT_PA = 1, SEPDEV_EXT_PREVF = 2, SEPDEV_EXT_RANDN = 3,
+       SEPDEV_NEXT = 4 };
 #define SEPDEV_MAXCHAN   4
 
 /* fields of one accumulator slot (int64, value * 2^32) */
@@ -250,6 +254,36 @@ int sepdev_msd_create(sepdev *d, int nk, const double *k, sepdev_msd **out);
 void sepdev_msd_destroy(sepdev_msd *m);
 int sepdev_msd_base(sepdev *d, sepdev_msd *m);
 int sepdev_msd_sample(sepdev *d, sepdev_msd *m, int type_id, double *out);
+
+/* ---- stochastic dynamics (dev_stoch.cu) ----
+ * _ext_enable allocates the SEPDEV_EXT_* fields (zero); _ext_upload and
+ * _ext_download move them in user order (3 n doubles each, ldiff n
+ * doubles; any pointer may be NULL to skip a field).  Random numbers come
+ * from Philox4x32-10 keyed by `seed`: a DPD pair draws from the counter
+ * (min gid, max gid, call, 1), a particle of sep_fp / GJF from
+ * (gid, 0, call, 2 / 3).  Each integrator writes its kinetic sums (m v^2,
+ * m v v^T of the updated velocities), sum m v^2 and the displacement
+ * maximum into `slot`. */
+typedef struct {
+	int tA, tB;              /* type ids of the pair (-1: absent) */
+	double cf, aij, gamma, sigma, dt;
+	unsigned long long seed;
+	unsigned call;
+	int virial;              /* 1: pot_P (conservative) to slot, random and
+	                          * dissipative parts to slot2 (the O(N^2) form) */
+} sepdev_dpd;
+int sepdev_ext_enable(sepdev *d);
+int sepdev_ext_enabled(const sepdev *d);
+int sepdev_ext_upload(sepdev *d, const double *pv, const double *pa, const double *prevf,
+		      const double *randn, const double *ldiff);
+int sepdev_ext_download(sepdev *d, double *pv, double *pa, double *prevf, double *randn);
+/* DPD pair forces added to (accumulate) or stored into the forces; the
+ * energy sum aij w^2 / 2 into slot's channel 0 */
+int sepdev_dpd_forces(sepdev *d, const sepdev_dpd *p, int accumulate, int slot, int slot2);
+int sepdev_verlet_dpd(sepdev *d, double dt, double lambda, int stepnow, int slot);
+int sepdev_fp(sepdev *d, double dt, double temp, unsigned long long seed, unsigned call, int slot);
+int sepdev_gjf(sepdev *d, double dt, double temp, double alpha, unsigned long long seed,
+	       unsigned call, int slot);
 
 /* lanes per particle in the pair kernels (1, 2, 4); invalidates the list */
 int sepdev_set_tpp(sepdev *d, int tpp);

@@ -148,6 +148,8 @@ SIGNATURES = {
     "sep_langevinGJF": (None, [PART_P, D, D, SYS_P, RET_P]),
     "sep_set_ldiff": (None, [PART_P, C.c_char, D, SepSys]),
     "sep_randn": (D, []),
+    "sep_dpdforce_brute": (None, [PART_P, C.c_char_p, D, D, D, D, SYS_P, RET_P]),
+    "sep_gpu_set_seed": (C.c_int, [PART_P, C.c_ulonglong]),
 }
 
 

@@ -221,6 +221,27 @@ def stochastic(lib):
         libc.srand(seed)
         d[tag + "_gauss"] = np.array([lib.sep_randn() for _ in range(3 * n)]).reshape(n, 3)
     lib.sep_close(atoms, n)
+    # the O(N^2) form: all pairs i < j in order, energy added, virials
+    nb = 128
+    Lb = (nb / rho) ** (1 / 3)
+    atoms = lib.sep_init(nb, A.SEP_NEIGHB)
+    v = A.parts_view(atoms, nb)
+    v["x"] = rng.uniform(0, Lb, (nb, 3))
+    v["pv"] = rng.normal(0, 1, (nb, 3))
+    v["type"] = np.where(rng.uniform(size=nb) < 0.6, b"A", b"B")
+    sys_ = lib.sep_sys_setup(Lb, Lb, Lb, 1.0, 0.02, nb, A.SEP_BRUTE)
+    ret = A.SepRet()
+    lib.sep_reset_retval(C.byref(ret))
+    lib.sep_reset_force(atoms, C.byref(sys_))
+    libc.srand(505)
+    lib.sep_force_dpd(atoms, b"AB", 1.0, 25.0, 1.0, 3.0, C.byref(sys_), C.byref(ret), A.SEP_ALL)
+    ii, jj = np.triu_indices(nb, 1)
+    libc.srand(505)
+    d.update(br_L=np.array([Lb] * 3), br_x=v["x"].copy(), br_pv=v["pv"].copy(), br_types=v["type"].copy(),
+             br_f=v["f"].copy(), br_epot=ret.epot,
+             br_vir=np.array([ret.pot_P, ret.pot_P_conservative, ret.pot_P_random, ret.pot_P_dissipative]),
+             br_uni=np.array([libc.rand() / 2147483648.0 for _ in range(len(ii))]))
+    lib.sep_close(atoms, nb)
     # flatten the nested state dicts for npz
     out = {}
     for k, val in d.items():

@@ -104,3 +104,20 @@ def test_langevin_gjf_matches_reference(ora, g):
                          float(g["skin"]))
     check_out(s, g, "gjf", (("x", "x"), ("v", "v"), ("prevf", "prevf"), ("randn", "randn")))
     check_ret(r, g["gjf_ret"])
+
+
+def test_dpd_brute_matches_reference(ora, g):
+    """The O(N^2) form visits i < j in order, adds the energy and fills the
+    conservative, random and dissipative virials."""
+    nb = len(g["br_x"])
+    ii, jj = np.triu_indices(nb, 1)
+    pairs = np.stack([ii, jj], 1)
+    f, e, vir = ora.dpd_forces(g["br_x"], g["br_pv"], g["br_types"], g["br_L"], b"AB", 1.0, 25.0, 1.0,
+                               3.0, 0.02, pairs, g["br_uni"], 0, virial=True)
+    assert rel(f, g["br_f"]) < 1e-13
+    assert e == pytest.approx(float(g["br_epot"]), rel=1e-13)
+    ref = g["br_vir"]
+    np.testing.assert_allclose(vir[0], ref[0], rtol=1e-12, atol=1e-12)     # pot_P
+    np.testing.assert_allclose(vir[0], ref[1], rtol=1e-12, atol=1e-12)     # conservative
+    np.testing.assert_allclose(vir[1], ref[2], rtol=1e-12, atol=1e-12)     # random
+    np.testing.assert_allclose(vir[2], ref[3], rtol=1e-12, atol=1e-12)     # dissipative
