@@ -50,12 +50,13 @@ def test_struct_layout(tmp_path):
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_PRGS), reason="reference programs not present")
-@pytest.mark.parametrize("prg", ["prg0.c", "prg1.c", "prg4.c"])
+@pytest.mark.parametrize("prg", ["prg0.c", "prg1.c", "prg4.c", "prg6.c", "prg9.c"])
 @pytest.mark.parametrize("headers", ["ours", "reference"])
 def test_reference_programs_link_unchanged(lib, tmp_path, prg, headers):
-    """prgs/prg0.c, prg1.c (with the vacf, sacf and msd samplers) and prg4.c
-    compile against these headers (or the reference's own) and link against
-    libsep.so without a source change."""
+    """prgs/prg0.c, prg1.c (with the vacf, sacf and msd samplers), prg4.c,
+    prg6.c (DPD) and prg9.c (Brownian dynamics) compile against these
+    headers (or the reference's own) and link against libsep.so without a
+    source change."""
     inc = INC if headers == "ours" else REF_INC
     exe = tmp_path / prg.replace(".c", "")
     cmd = ["gcc", "-std=c99", "-fgnu89-inline", "-DCOMPLEX", "-w", "-I", inc,
