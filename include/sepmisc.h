@@ -67,6 +67,22 @@ void sep_set_skin(sepsys *sys, double value);
 /* Sets mass or charge of every particle of a type (reference :320-330). */
 void sep_set_charge(seppart *ptr, char type, double z, sepsys sys);
 void sep_set_mass(seppart *ptr, char type, double m, sepsys sys);
+/*
+ * Box changes.  sep_compress_box scales every edge and coordinate by xi
+ * (1/xi when the density is above rhoD; nothing within 1e-6 of it);
+ * sep_compress_box_dir (density below rhoD) and sep_compress_box_dir_length
+ * (edge above length) scale one edge by xi and its coordinates by xi^(1/3);
+ * the Berendsen barostat takes xi = 1 - beta dt (Pd - p) from the current
+ * pressure and scales L_z (sep_berendsen) or every edge (sep_berendsen_iso)
+ * by xi and the same coordinates by xi^(1/3).  The volume and the sub-box
+ * grid follow (reference :181-216, :373-401, source/sepmisc.c:892-1084).
+ */
+void sep_compress_box(sepatom *ptr, double rhoD, double xi, sepsys *sys);
+void sep_compress_box_dir(sepatom *ptr, double rhoD, double xi, int dir, sepsys *sys);
+void sep_compress_box_dir_length(sepatom *ptr, double length, double xi, int dir, sepsys *sys);
+void sep_berendsen(sepatom *ptr, double Pd, double beta, sepret *ret, sepsys *sys);
+void sep_berendsen_iso(sepatom *ptr, double Pd, double beta, sepret *ret, sepsys *sys);
+
 /* Sets the Langevin diffusion coefficient of every particle of a type
  * (reference :449, source/sepmisc.c:1162-1170). */
 void sep_set_ldiff(seppart *ptr, char type, double ldiff, sepsys sys);

@@ -355,3 +355,42 @@ def langevin_gjf(st, f, gauss, temp, alpha, L, dt, skin, max_dist2=0.0):
              _p(st.randn, C.c_double), _p(gs, C.c_double), C.c_double(temp), C.c_double(alpha),
              *_common_tail(st, L, dt, skin, md, ek, kP))
     return flag, md.value, ek.value, kP.reshape(3, 3)
+
+
+# ---- box changes --------------------------------------------------------------
+
+class Box:
+    """positions and the box fields a box change updates"""
+
+    def __init__(self, x, L, nsub, lsub, cf, skin, update):
+        self.x = _f64(x).copy(); self.L = _f64(L).copy()
+        self.volume = C.c_double(float(np.prod(self.L)))
+        self.nsub = _i32(nsub).copy(); self.lsub = _f64(lsub).copy()
+        self.cf, self.skin, self.update = float(cf), float(skin), int(update)
+
+    def _head(self):
+        return [C.c_long(len(self.x)), _p(self.x, C.c_double), _p(self.L, C.c_double),
+                C.byref(self.volume), _p(self.nsub, C.c_int), _p(self.lsub, C.c_double),
+                C.c_double(self.cf)]
+
+    def compress(self, rhoD, xi):
+        g = lib().ora_compress_box
+        g.restype = C.c_int
+        return g(*self._head(), C.c_double(self.skin), C.c_int(self.update), C.c_double(rhoD),
+                 C.c_double(xi))
+
+    def compress_dir(self, rhoD, xi, d):
+        g = lib().ora_compress_box_dir
+        g.restype = C.c_int
+        return g(*self._head(), C.c_int(self.update), C.c_double(rhoD), C.c_double(xi), C.c_int(d))
+
+    def compress_dir_length(self, length, xi, d):
+        g = lib().ora_compress_box_dir_length
+        g.restype = C.c_int
+        return g(*self._head(), C.c_int(self.update), C.c_double(length), C.c_double(xi), C.c_int(d))
+
+    def berendsen(self, p, Pd, beta, dt, iso):
+        g = lib().ora_berendsen
+        g.restype = None
+        g(*self._head(), C.c_int(self.update), C.c_double(p), C.c_double(Pd), C.c_double(beta),
+          C.c_double(dt), C.c_int(iso))

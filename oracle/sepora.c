@@ -988,3 +988,78 @@ int ora_langevin_gjf(long n, double *x, double *v, const double *f, double *a, c
 	*ekin += 0.5 * sum;
 	return ora_skin(n, x, cross_neighb, xn, skin, *max_dist2);
 }
+
+/* ======================================================================
+ * Box changes: compression and the Berendsen barostat
+ * (source/sepmisc.c:892-1084).  L, volume and the reference's sub-box grid
+ * (nsub, lsub) change with the box; positions are scaled in place and are
+ * not wrapped (the next integrator step does that).  update = the system's
+ * neighb_update (0: SEP_BRUTE keeps the grid).
+ * ====================================================================== */
+
+static void ora_subbox(int k, double cf, double delta, const double L[3], int update, int nsub[3],
+		       double lsub[3])
+{
+	if (update == 0) return;
+	nsub[k] = ora_nsubbox(cf, delta, L[k]);
+	lsub[k] = L[k] / nsub[k];
+}
+
+/* sep_compress_box (:989-1024): returns 0 when the density is within 1e-6
+ * of rhoD (nothing changes) */
+int ora_compress_box(long n, double *x, double L[3], double *volume, int nsub[3], double lsub[3],
+		     double cf, double skin, int update, double rhoD, double xi)
+{
+	const double density = n / *volume;
+	if (fabs(density - rhoD) < 1e-6) return 0;
+	if (density > rhoD) xi = 1.0 / xi;
+	for (int k = 0; k < 3; k++) L[k] *= xi;
+	for (long i = 0; i < 3 * n; i++) x[i] *= xi;
+	for (int k = 0; k < 3; k++) ora_subbox(k, cf, skin, L, update, nsub, lsub);
+	*volume = L[0] * L[1] * L[2];
+	return 1;
+}
+
+/* sep_compress_box_dir (:1029-1054) and sep_compress_box_dir_length
+ * (:1057-1082): one axis, positions scaled by xi^(1/3) */
+static void ora_compress_axis(long n, double *x, double L[3], double *volume, int nsub[3],
+			      double lsub[3], double cf, int update, double xi, int dir)
+{
+	L[dir] *= xi;
+	const double scale = pow(xi, 1.0 / 3.0);
+	for (long i = 0; i < n; i++) x[3 * i + dir] *= scale;
+	ora_subbox(dir, cf, 0.0, L, update, nsub, lsub);
+	*volume = L[0] * L[1] * L[2];
+}
+
+int ora_compress_box_dir(long n, double *x, double L[3], double *volume, int nsub[3], double lsub[3],
+			 double cf, int update, double rhoD, double xi, int dir)
+{
+	if (!(n / *volume < rhoD)) return 0;
+	ora_compress_axis(n, x, L, volume, nsub, lsub, cf, update, xi, dir);
+	return 1;
+}
+
+int ora_compress_box_dir_length(long n, double *x, double L[3], double *volume, int nsub[3],
+				double lsub[3], double cf, int update, double length, double xi, int dir)
+{
+	if (!(L[dir] > length)) return 0;
+	ora_compress_axis(n, x, L, volume, nsub, lsub, cf, update, xi, dir);
+	return 1;
+}
+
+/* sep_berendsen (:892-916) and sep_berendsen_iso (:920-946):
+ * xi = 1 - beta dt (Pd - p); iso = 0 scales L_z by xi, iso = 1 all three
+ * edges; positions are scaled by xi^(1/3) on the same axes */
+void ora_berendsen(long n, double *x, double L[3], double *volume, int nsub[3], double lsub[3],
+		   double cf, int update, double p, double Pd, double beta, double dt, int iso)
+{
+	const double xi = 1 - beta * dt * (Pd - p);
+	const int k0 = iso ? 0 : 2;
+	for (int k = k0; k < 3; k++) L[k] *= xi;
+	const double scale = pow(xi, 1.0 / 3.0);
+	for (long i = 0; i < n; i++)
+		for (int k = k0; k < 3; k++) x[3 * i + k] *= scale;
+	*volume = L[0] * L[1] * L[2];
+	for (int k = k0; k < 3; k++) ora_subbox(k, cf, 0.0, L, update, nsub, lsub);
+}

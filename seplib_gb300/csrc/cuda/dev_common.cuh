@@ -268,6 +268,24 @@ __device__ __forceinline__ void block_to_slot(float (&v)[NV], const int (&fld)[N
 	}
 }
 
+// host to_fixed (dev_state.cu) with the same operations and roundings
+__device__ __forceinline__ void to_fixed_dev(double x, double L, unsigned &hi, unsigned &lo)
+{
+	double fr = __ddiv_rn(x, L);
+	fr = __dsub_rn(fr, floor(fr));
+	if (fr >= 1.0) fr = 0.0;
+	const double t = ldexp(fr, 32);
+	const double h = floor(t);
+	const double r = ldexp(__dsub_rn(t, h), 32);
+	hi = (unsigned)h;
+	lo = (unsigned)floor(r);
+}
+
+__device__ __forceinline__ double from_fixed_dev(unsigned hi, unsigned lo, double L)
+{
+	return __dmul_rn(__dadd_rn(ldexp((double)hi, -32), ldexp((double)lo, -64)), L);
+}
+
 // Neighbour-list layout (one lane per particle): particle i is lane
 // p = i % 32 of tile t = i / 32; its entry k lives at
 //     nl[t*maxnb*32 + (k/4)*128 + p*4 + (k%4)]

@@ -1,0 +1,109 @@
+/*
+ * sep_api_box.c - box changes of the sep C API: compression
+ * (sep_compress_box, sep_compress_box_dir, sep_compress_box_dir_length) and
+ * the Berendsen barostat (sep_berendsen, sep_berendsen_iso), reference
+ * source/sepmisc.c:892-1084.  The box arithmetic and the sub-box grid
+ * bookkeeping run on the host as in the reference; the positions are
+ * rescaled on the device when it holds them.
+ */
+#include <math.h>
+#include <stdio.h>
+#include "sep_rt.h"
+
+/* new edges L1, positions x_k *= sx[k] */
+static void apply(seppart *ptr, sepsys *sys, const double L1[3], const double sx[3])
+{
+	rt_ctx *c = rt_find(ptr);
+	if (c && c->dev && c->dev_valid) {
+		/* pending pair terms belong to the old box */
+		rt_materialize_forces(c);
+		rt_check(sepdev_rescale_box(c->dev, L1, sx), "box change");
+		c->host_valid = 0;
+	} else {
+		for (long n = 0; n < sys->npart; n++)
+			for (int k = 0; k < 3; k++)
+				if (sx[k] != 1.0) ptr[n].x[k] *= sx[k];
+	}
+	for (int k = 0; k < 3; k++) sys->length[k] = L1[k];
+}
+
+static void subbox(sepsys *sys, int k, double delta, const char *caller)
+{
+	if (sys->neighb_update == 0) return;
+	sys->nsubbox[k] = sep_nsubbox(sys->cf, delta, sys->length[k]);
+	if (sys->nsubbox[k] < 3)
+		sep_warning("%s: Number of subboxes in x direction are less than three", caller);
+	sys->lsubbox[k] = sys->length[k] / sys->nsubbox[k];
+}
+
+/* source/sepmisc.c:989-1024 */
+void sep_compress_box(sepatom *ptr, double rhoD, double xi, sepsys *sys)
+{
+	const double density = sys->npart / sys->volume;
+	if (fabs(density - rhoD) < 1e-6) return;
+	if (density > rhoD) xi = 1.0 / xi;
+	double L1[3], sx[3];
+	for (int k = 0; k < 3; k++) {
+		L1[k] = sys->length[k] * xi;
+		sx[k] = xi;
+		if (L1[k] < sys->cf * 2.0)
+			sep_warning("%s: Box length too small compared to the maximum cut-off", __func__);
+	}
+	apply(ptr, sys, L1, sx);
+	for (int k = 0; k < 3; k++) subbox(sys, k, sys->skin, __func__);
+	sys->volume = sys->length[0] * sys->length[1] * sys->length[2];
+}
+
+/* one axis: edge times xi, positions times xi^(1/3) */
+static void compress_axis(sepatom *ptr, double xi, int dir, sepsys *sys, const char *caller)
+{
+	double L1[3] = {sys->length[0], sys->length[1], sys->length[2]}, sx[3] = {1.0, 1.0, 1.0};
+	L1[dir] *= xi;
+	if (L1[dir] < sys->cf * 2.0)
+		sep_warning("%s: Box length too small compared to the maximum cut-off", caller);
+	sx[dir] = pow(xi, 1.0 / 3.0);
+	apply(ptr, sys, L1, sx);
+	subbox(sys, dir, 0.0, caller);
+	sys->volume = sys->length[0] * sys->length[1] * sys->length[2];
+}
+
+/* source/sepmisc.c:1029-1054 */
+void sep_compress_box_dir(sepatom *ptr, double rhoD, double xi, int dir, sepsys *sys)
+{
+	if (sys->npart / sys->volume < rhoD) compress_axis(ptr, xi, dir, sys, __func__);
+}
+
+/* source/sepmisc.c:1057-1082 */
+void sep_compress_box_dir_length(sepatom *ptr, double length, double xi, int dir, sepsys *sys)
+{
+	if (sys->length[dir] > length) compress_axis(ptr, xi, dir, sys, __func__);
+}
+
+/* source/sepmisc.c:892-946: xi = 1 - beta dt (Pd - p) from the current
+ * pressure; iso = 0 changes L_z only, iso = 1 all edges; positions are
+ * scaled by xi^(1/3) on the same axes */
+static void berendsen(sepatom *ptr, double Pd, double beta, sepret *ret, sepsys *sys, int iso)
+{
+	sep_pressure_tensor(ret, sys);
+	const double xi = 1 - beta * sys->dt * (Pd - ret->p);
+	const int k0 = iso ? 0 : 2;
+	double L1[3] = {sys->length[0], sys->length[1], sys->length[2]}, sx[3] = {1.0, 1.0, 1.0};
+	const double scale = pow(xi, 1.0 / 3.0);
+	for (int k = k0; k < 3; k++) {
+		L1[k] *= xi;
+		sx[k] = scale;
+	}
+	apply(ptr, sys, L1, sx);
+	sys->volume = sys->length[0] * sys->length[1] * sys->length[2];
+	for (int k = k0; k < 3; k++) subbox(sys, k, 0.0, iso ? "sep_berendsen_iso" : "sep_berendsen");
+}
+
+void sep_berendsen(sepatom *ptr, double Pd, double beta, sepret *ret, sepsys *sys)
+{
+	berendsen(ptr, Pd, beta, ret, sys, 0);
+}
+
+void sep_berendsen_iso(sepatom *ptr, double Pd, double beta, sepret *ret, sepsys *sys)
+{
+	berendsen(ptr, Pd, beta, ret, sys, 1);
+}

@@ -285,6 +285,12 @@ int sepdev_fp(sepdev *d, double dt, double temp, unsigned long long seed, unsign
 int sepdev_gjf(sepdev *d, double dt, double temp, double alpha, unsigned long long seed,
 	       unsigned call, int slot);
 
+/* ---- box changes (dev_box.cu) ----
+ * New box edges L1; every position coordinate k is multiplied by sx[k]
+ * (in FP64) and re-expressed in the new box, wrapped with its crossing
+ * counted; the last-update positions keep their absolute values. */
+int sepdev_rescale_box(sepdev *d, const double *L1, const double *sx);
+
 /* lanes per particle in the pair kernels (1, 2, 4); invalidates the list */
 int sepdev_set_tpp(sepdev *d, int tpp);
 int sepdev_get_tpp(sepdev *d);

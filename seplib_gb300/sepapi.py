@@ -150,6 +150,11 @@ SIGNATURES = {
     "sep_randn": (D, []),
     "sep_dpdforce_brute": (None, [PART_P, C.c_char_p, D, D, D, D, SYS_P, RET_P]),
     "sep_gpu_set_seed": (C.c_int, [PART_P, C.c_ulonglong]),
+    "sep_compress_box": (None, [PART_P, D, D, SYS_P]),
+    "sep_compress_box_dir": (None, [PART_P, D, D, C.c_int, SYS_P]),
+    "sep_compress_box_dir_length": (None, [PART_P, D, D, C.c_int, SYS_P]),
+    "sep_berendsen": (None, [PART_P, D, D, RET_P, SYS_P]),
+    "sep_berendsen_iso": (None, [PART_P, D, D, RET_P, SYS_P]),
 }
 
 

@@ -253,6 +253,106 @@ def stochastic(lib):
     return out
 
 
+def box_ops(lib):
+    """sep_compress_box / _dir / _dir_length and sep_berendsen / _iso one at
+    a time, then a Berendsen run (prgs/prg7.c) and a compression run
+    (prgs/prg3.c's schedule on an LJ liquid) with per-step traces."""
+    rng = np.random.default_rng(13)
+    d = {}
+    # single operations
+    n = 1000
+    L = (n / 0.8) ** (1 / 3)
+    atoms = lib.sep_init(n, A.SEP_NEIGHB)
+    v = A.parts_view(atoms, n)
+    sys_ = lib.sep_sys_setup(L, L, L, 2.5, 0.005, n, A.SEP_LLIST_NEIGHBLIST)
+    lib.sep_set_lattice(atoms, sys_)
+    v["x"] = np.mod(v["x"] + rng.normal(0, 0.05, (n, 3)), L)
+    ret = A.SepRet()
+    kin = np.array([[820.0, 3.0, -2.0], [3.0, 790.0, 1.5], [-2.0, 1.5, 805.0]])
+    pot = np.array([[5200.0, -12.0, 4.0], [-12.0, 5350.0, 7.0], [4.0, 7.0, 5100.0]])
+
+    def berendsen(fn):
+        def run():
+            for a in range(3):
+                for b in range(3):
+                    ret.kin_P[a][b] = kin[a][b]
+                    ret.pot_P[a][b] = pot[a][b]
+            fn(atoms, 5.91, 0.1, C.byref(ret), C.byref(sys_))
+        return run
+
+    ops = (("c1", lambda: lib.sep_compress_box(atoms, 0.9, 0.995, C.byref(sys_))),
+           ("c2", lambda: lib.sep_compress_box(atoms, 0.5, 0.995, C.byref(sys_))),
+           ("cd", lambda: lib.sep_compress_box_dir(atoms, 2.0, 0.99, 2, C.byref(sys_))),
+           ("cl", lambda: lib.sep_compress_box_dir_length(atoms, 1.0, 0.99, 0, C.byref(sys_))),
+           ("b", berendsen(lib.sep_berendsen)),
+           ("bi", berendsen(lib.sep_berendsen_iso)))
+    for tag, fn in ops:
+        d[tag + "_x0"] = v["x"].copy()
+        d[tag + "_L0"] = np.array(sys_.length)
+        d[tag + "_nsub0"] = np.array(sys_.nsubbox)
+        d[tag + "_lsub0"] = np.array(sys_.lsubbox)
+        fn()
+        d[tag + "_x1"] = v["x"].copy()
+        d[tag + "_L1"] = np.array(sys_.length)
+        d[tag + "_vol1"] = sys_.volume
+        d[tag + "_nsub1"] = np.array(sys_.nsubbox)
+        d[tag + "_lsub1"] = np.array(sys_.lsubbox)
+        d[tag + "_p"] = ret.p
+    d["ops_kin"], d["ops_pot"], d["ops_skin"] = kin, pot, sys_.skin
+    lib.sep_close(atoms, n)
+
+    # prgs/prg7.c: NH (T 0.5, Q 0.1) + Berendsen (Pd 5.91, beta 0.1), SEP_BRUTE
+    n = 216
+    L = (n / 0.844) ** (1 / 3)
+    atoms = lib.sep_init(n, A.SEP_NEIGHB)
+    v = A.parts_view(atoms, n)
+    sys_ = lib.sep_sys_setup(L, L, L, 2.5, 0.005, n, A.SEP_BRUTE)
+    lib.sep_set_lattice(atoms, sys_)
+    v["v"] = rng.normal(0, 0.85, (n, 3))
+    v["v"] -= v["v"].mean(0)
+    d["b7_x0"], d["b7_v0"], d["b7_L0"] = v["x"].copy(), v["v"].copy(), L
+    alpha = C.c_double(0.1)
+    tr = []
+    for step in range(60):
+        lib.sep_reset_retval(C.byref(ret))
+        lib.sep_reset_force(atoms, C.byref(sys_))
+        lib.sep_force_pairs(atoms, b"AA", 2.5, A.fun_ptr(lib, "sep_lj_shift"), C.byref(sys_),
+                            C.byref(ret), A.SEP_ALL)
+        lib.sep_nosehoover(atoms, 0.5, C.byref(alpha), 0.1, C.byref(sys_))
+        lib.sep_leapfrog(atoms, C.byref(sys_), C.byref(ret))
+        lib.sep_berendsen(atoms, 5.91, 0.1, C.byref(ret), C.byref(sys_))
+        tr.append([ret.epot, ret.ekin, ret.p, sys_.volume, sys_.length[2]])
+    d["b7_trace"], d["b7_x"] = np.array(tr), v["x"].copy()
+    lib.sep_close(atoms, n)
+
+    # compression every 5 steps towards rho 0.86 (prgs/prg3.c's schedule), NVT LJ
+    n = 1000
+    L = (n / 0.8) ** (1 / 3)
+    atoms = lib.sep_init(n, A.SEP_NEIGHB)
+    v = A.parts_view(atoms, n)
+    sys_ = lib.sep_sys_setup(L, L, L, 2.5, 0.005, n, A.SEP_LLIST_NEIGHBLIST)
+    lib.sep_set_lattice(atoms, sys_)
+    v["v"] = rng.normal(0, 1.0, (n, 3))
+    v["v"] -= v["v"].mean(0)
+    v["xn"] = 0.0
+    d["c3_x0"], d["c3_v0"], d["c3_L0"] = v["x"].copy(), v["v"].copy(), L
+    alpha = C.c_double(0.0)
+    tr = []
+    for step in range(60):
+        lib.sep_reset_retval(C.byref(ret))
+        lib.sep_reset_force(atoms, C.byref(sys_))
+        lib.sep_force_pairs(atoms, b"AA", 2.5, A.fun_ptr(lib, "sep_lj_shift"), C.byref(sys_),
+                            C.byref(ret), A.SEP_ALL)
+        lib.sep_nosehoover(atoms, 1.0, C.byref(alpha), 0.1, C.byref(sys_))
+        lib.sep_leapfrog(atoms, C.byref(sys_), C.byref(ret))
+        if step % 5 == 0 and n / sys_.volume < 0.86:
+            lib.sep_compress_box(atoms, 0.86, 0.995, C.byref(sys_))
+        tr.append([ret.epot, ret.ekin, sys_.volume, sys_.nupdate_neighb])
+    d["c3_trace"], d["c3_x"] = np.array(tr), v["x"].copy()
+    lib.sep_close(atoms, n)
+    return d
+
+
 def dict_state(v):
     return {k: v[k].copy() for k in ("x", "v", "f", "pv", "pa", "prevf", "randn",
                                       "cross_neighb", "crossings", "xn")}
@@ -266,7 +366,8 @@ def main(only=()):
                          ("butane_small", lambda: butane_small(lib, tmp)),
                          ("water_small", lambda: water_small(lib, tmp)),
                          ("host_api", lambda: host_api(lib)),
-                         ("stoch_small", lambda: stochastic(lib))):
+                         ("stoch_small", lambda: stochastic(lib)),
+                         ("box_small", lambda: box_ops(lib))):
             if only and name not in only:
                 continue
             d = fn()
