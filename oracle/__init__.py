@@ -394,3 +394,70 @@ class Box:
         g.restype = None
         g(*self._head(), C.c_int(self.update), C.c_double(p), C.c_double(Pd), C.c_double(beta),
           C.c_double(dt), C.c_int(iso))
+
+
+# ---- molecular pressure tensor --------------------------------------------------
+
+def mol_tables(molindex, nmol):
+    """(first, nuau, start, atoms): the first atom and atom count of each
+    molecule, and its atom list as CSR in index order"""
+    mi = np.asarray(molindex)
+    first = np.zeros(nmol, np.int32); nuau = np.zeros(nmol, np.int32)
+    atoms = np.nonzero(mi >= 0)[0]
+    order = np.argsort(mi[atoms], kind="stable")
+    atoms = atoms[order].astype(np.int32)
+    counts = np.bincount(mi[atoms], minlength=nmol)
+    start = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+    for i in range(nmol):
+        first[i] = atoms[start[i]] if counts[i] else 0
+        nuau[i] = counts[i]
+    return first, nuau, start, atoms
+
+
+def mol_fij(x, type_chars, L, molindex, nmol, terms, pairs):
+    """dense F[i][j] (nmol, nmol, 3) from pair terms over an unordered pair list;
+    terms: ("pair", types, kind, param, cf) or ("coul", z, cf)"""
+    x = _f64(x); L = _f64(L); mi = _i32(molindex)
+    st, nb = csr_from_pairs(len(x), pairs)
+    st = _as_long(st)
+    F = np.zeros(nmol * nmol * 3)
+    ty = np.ascontiguousarray(np.asarray(type_chars, dtype="S1"))
+    for t in terms:
+        if t[0] == "pair":
+            _, types, kind, param, cf = t
+            p = _f64(param if param is not None else np.zeros(4))
+            g = lib().ora_pair_fij
+            g.restype = None
+            g(C.c_long(len(x)), _p(x, C.c_double), ty.ctypes.data_as(C.c_char_p), _p(L, C.c_double),
+              C.c_char_p(types.encode() if isinstance(types, str) else types), C.c_int(kind),
+              _p(p, C.c_double), C.c_double(cf), _p(st, C.c_long), _p(nb, C.c_int), _p(mi, C.c_int),
+              C.c_int(nmol), _p(F, C.c_double))
+        else:
+            _, z, cf = t
+            z = _f64(z)
+            g = lib().ora_coulomb_fij
+            g.restype = None
+            g(C.c_long(len(x)), _p(x, C.c_double), _p(z, C.c_double), _p(L, C.c_double), C.c_double(cf),
+              _p(st, C.c_long), _p(nb, C.c_int), _p(mi, C.c_int), C.c_int(nmol), _p(F, C.c_double))
+    return F.reshape(nmol, nmol, 3)
+
+
+def mol_pressure(F, x, v, m, L, molindex, nmol):
+    """(kin_P_mol, pot_P_mol, cm, vcm) at positions x, velocities v"""
+    first, nuau, start, atoms = mol_tables(molindex, nmol)
+    x = _f64(x); v = _f64(v); m = _f64(m); L = _f64(L); F = _f64(F)
+    mmol = np.zeros(nmol)
+    np.add.at(mmol, np.asarray(molindex)[atoms], m[atoms])
+    cm = np.zeros((nmol, 3)); vcm = np.zeros((nmol, 3))
+    lb = lib()
+    lb.ora_mol_cm.restype = None
+    lb.ora_mol_cm(C.c_int(nmol), _p(first, C.c_int), _p(nuau, C.c_int), _p(mmol, C.c_double),
+                  _p(x, C.c_double), _p(m, C.c_double), _p(L, C.c_double), _p(cm, C.c_double))
+    lb.ora_mol_velcm.restype = None
+    lb.ora_mol_velcm(C.c_int(nmol), _p(start, C.c_int), _p(atoms, C.c_int), _p(mmol, C.c_double),
+                     _p(v, C.c_double), _p(m, C.c_double), _p(vcm, C.c_double))
+    kin = np.zeros(9); pot = np.zeros(9)
+    lb.ora_mol_pressure.restype = None
+    lb.ora_mol_pressure(C.c_int(nmol), _p(F, C.c_double), _p(cm, C.c_double), _p(vcm, C.c_double),
+                        _p(mmol, C.c_double), _p(L, C.c_double), _p(kin, C.c_double), _p(pot, C.c_double))
+    return kin.reshape(3, 3), pot.reshape(3, 3), cm, vcm

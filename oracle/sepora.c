@@ -1063,3 +1063,116 @@ void ora_berendsen(long n, double *x, double L[3], double *volume, int nsub[3], 
 	*volume = L[0] * L[1] * L[2];
 	for (int k = k0; k < 3; k++) ora_subbox(k, cf, 0.0, L, update, nsub, lsub);
 }
+
+/* ======================================================================
+ * Molecular pressure tensor (source/sepmol.c:683-748 centres of mass,
+ * :913-959 sep_eval_mol_pressure_tensor; source/sepret.c:85-102).
+ * The reference accumulates the intermolecular force matrix F[i][j] (the
+ * force molecule j exerts on molecule i) during the pair-force calls and
+ * forms the tensor later from the centres of mass at that later time.
+ * F is dense nmol x nmol x 3 here (test sizes only).
+ * ====================================================================== */
+
+/* F[mi][mj] += f, F[mj][mi] -= f for each pair force f on i from j with both
+ * molecule indices set (source/sepprfrc.c:199-204 and :905-910) */
+static void ora_fij_add(double *F, int nmol, int mi, int mj, const double f[3])
+{
+	if (mi < 0 || mj < 0) return;
+	for (int k = 0; k < 3; k++) {
+		F[((long)mi * nmol + mj) * 3 + k] += f[k];
+		F[((long)mj * nmol + mi) * 3 + k] -= f[k];
+	}
+}
+
+void ora_pair_fij(long n, const double *x, const char *type, const double L[3], const char *types,
+		  int kind, const double *p, double cf, const long *start, const int *nb,
+		  const int *molindex, int nmol, double *F)
+{
+	const double cf2 = cf * cf;
+	for (long i = 0; i < n; i++) {
+		if (type[i] != types[0] && type[i] != types[1]) continue;
+		for (long s = start[i]; s < start[i + 1]; s++) {
+			const long j = nb[s];
+			if (!ora_typematch(type[i], type[j], types)) continue;
+			double d[3], r2 = ora_sep(x, i, j, L, d), ft, u;
+			if (r2 >= cf2) continue;
+			ora_pot(kind, p, r2, &ft, &u);
+			const double f[3] = {ft * d[0], ft * d[1], ft * d[2]};
+			ora_fij_add(F, nmol, molindex[i], molindex[j], f);
+		}
+	}
+}
+
+/* the shifted-force Coulomb contribution (source/sepcoulomb.c:140-145) */
+void ora_coulomb_fij(long n, const double *x, const double *z, const double L[3], double cf,
+		     const long *start, const int *nb, const int *molindex, int nmol, double *F)
+{
+	const double cf2 = cf * cf, icf2 = 1.0 / cf2;
+	for (long i = 0; i < n; i++) {
+		if (fabs(z[i]) < 2.220446049250313e-16) continue;
+		for (long s = start[i]; s < start[i + 1]; s++) {
+			const long j = nb[s];
+			double d[3], r2 = ora_sep(x, i, j, L, d);
+			if (r2 >= cf2) continue;
+			const double r = sqrt(r2), ft = z[i] * z[j] * (1.0 / r2 - icf2) / r;
+			const double f[3] = {ft * d[0], ft * d[1], ft * d[2]};
+			ora_fij_add(F, nmol, molindex[i], molindex[j], f);
+		}
+	}
+}
+
+/* centre of mass (source/sepmol.c:683-729): the chain of atoms first,
+ * first+1, ... first+nuau-1 unwrapped bond by bond from the first atom,
+ * mass-weighted (masses of those atoms, divided by the molecule mass),
+ * wrapped into the box; centre-of-mass velocity (:731-748) over the
+ * molecule's atom list (CSR start/atoms) */
+void ora_mol_cm(int nmol, const int *first, const int *nuau, const double *mmol, const double *x,
+		const double *m, const double L[3], double *cm)
+{
+	for (int i = 0; i < nmol; i++) {
+		const int a0 = first[i];
+		double prev[3] = {x[3 * a0], x[3 * a0 + 1], x[3 * a0 + 2]}, c[3] = {0.0, 0.0, 0.0};
+		for (int q = 0; q < nuau[i]; q++) {
+			const int a = a0 + q;
+			if (q > 0)
+				for (int k = 0; k < 3; k++) prev[k] += ora_wrap(x[3 * a + k] - x[3 * (a - 1) + k], L[k]);
+			for (int k = 0; k < 3; k++) c[k] += m[a] * prev[k];
+		}
+		for (int k = 0; k < 3; k++) {
+			double v = c[k] / mmol[i];
+			if (v > L[k]) v -= L[k];
+			else if (v < 0.0) v += L[k];
+			cm[3 * i + k] = v;
+		}
+	}
+}
+
+void ora_mol_velcm(int nmol, const int *start, const int *atoms, const double *mmol, const double *v,
+		   const double *m, double *vcm)
+{
+	for (int i = 0; i < nmol; i++) {
+		double s[3] = {0.0, 0.0, 0.0};
+		for (int q = start[i]; q < start[i + 1]; q++)
+			for (int k = 0; k < 3; k++) s[k] += v[3 * atoms[q] + k] * m[atoms[q]];
+		for (int k = 0; k < 3; k++) vcm[3 * i + k] = s[k] / mmol[i];
+	}
+}
+
+/* kin_P_mol = sum M v v^T; pot_P_mol = sum_{i<j} F[i][j] (x) R_ij with R_ij
+ * the minimum image of cm_i - cm_j (row-major 3x3 each) */
+void ora_mol_pressure(int nmol, const double *F, const double *cm, const double *vcm,
+		      const double *mmol, const double L[3], double *kinP, double *potP)
+{
+	for (int q = 0; q < 9; q++) kinP[q] = potP[q] = 0.0;
+	for (int i = 0; i < nmol; i++)
+		for (int k = 0; k < 3; k++)
+			for (int kk = 0; kk < 3; kk++) kinP[3 * k + kk] += mmol[i] * vcm[3 * i + k] * vcm[3 * i + kk];
+	for (int i = 0; i < nmol - 1; i++)
+		for (int j = i + 1; j < nmol; j++) {
+			double r[3];
+			for (int k = 0; k < 3; k++) r[k] = ora_wrap(cm[3 * i + k] - cm[3 * j + k], L[k]);
+			const double *f = F + ((long)i * nmol + j) * 3;
+			for (int k = 0; k < 3; k++)
+				for (int kk = 0; kk < 3; kk++) potP[3 * k + kk] += f[k] * r[kk];
+		}
+}

@@ -100,6 +100,18 @@ class SepSampler(C.Structure):
         for x in (("flag_" + name, C.c_int), (name, C.c_void_p))] + [("msd_counter", C.c_ulong)]
 
 
+class SepMol(C.Structure):
+    """``sepmol`` (include/sepstrct.h)"""
+    _fields_ = [
+        ("m", C.c_double), ("x", C.c_double * 3), ("xtrue", C.c_double * 3), ("v", C.c_double * 3),
+        ("nuau", C.c_uint), ("index", C.POINTER(C.c_int)), ("ete", C.c_double * 3), ("re2", C.c_double),
+        ("rg", C.c_double), ("S", C.c_double * 3), ("s", C.c_double * 3),
+        ("inertia", C.c_double * 3 * 3), ("w", C.c_double * 3), ("method_w", C.c_int),
+        ("pel", C.c_double * 3), ("type", C.c_char), ("nbonds", C.c_uint),
+        ("blength", C.POINTER(C.c_double)), ("shake_flag", C.c_int),
+    ]
+
+
 PART_P = C.POINTER(SepPart)
 SYS_P = C.POINTER(SepSys)
 RET_P = C.POINTER(SepRet)
@@ -127,8 +139,11 @@ SIGNATURES = {
     "sep_leapfrog": (None, [PART_P, SYS_P, RET_P]),
     "sep_nosehoover": (None, [PART_P, D, D_P, D, SYS_P]),
     "sep_read_topology_file": (None, [PART_P, C.c_char_p, SYS_P, C.c_char]),
-    "sep_init_mol": (C.c_void_p, [PART_P, SYS_P]),
-    "sep_free_mol": (None, [C.c_void_p, SYS_P]),
+    "sep_init_mol": (C.POINTER(SepMol), [PART_P, SYS_P]),
+    "sep_free_mol": (None, [C.POINTER(SepMol), SYS_P]),
+    "sep_mol_pressure_tensor": (None, [PART_P, C.POINTER(SepMol), RET_P, SYS_P]),
+    "sep_mol_cm": (None, [PART_P, C.POINTER(SepMol), SYS_P]),
+    "sep_mol_velcm": (None, [PART_P, C.POINTER(SepMol), SYS_P]),
     "sep_reset_force_mol": (None, [SYS_P]),
     "sep_stretch_harmonic": (None, [PART_P, C.c_int, D, D, SYS_P, RET_P]),
     "sep_angle_harmonic": (None, [PART_P, C.c_int, D, D, SYS_P, RET_P]),

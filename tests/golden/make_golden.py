@@ -253,6 +253,46 @@ def stochastic(lib):
     return out
 
 
+def molp_small(lib, tmp):
+    """sep_mol_pressure_tensor after a prgs/prg3.c step (LJ on O, SF Coulomb,
+    bonds, cos^2 angles, Nose-Hoover, leap-frog), once without and once
+    with a sep_compress_box between the step and the call."""
+    s = cfg.water_like(nmol=216, rho=0.09, seed=5)
+    top = os.path.join(tmp, "w.top")
+    cfg.write_top(top, s)
+    d = dict(x=s.x, v=s.v, L=s.L, z=s.z, m=s.m, types=s.types.astype("S1"), bonds=s.bonds,
+             angles=s.angles)
+    for tag, compress in (("a", False), ("c", True)):
+        h = Handle(lib, s, cf=3.0, update=A.SEP_LLIST_NEIGHBLIST, dt=0.0005)
+        lib.sep_read_topology_file(h.atoms, top.encode(), C.byref(h.sys), b"q")
+        mols = lib.sep_init_mol(h.atoms, C.byref(h.sys))
+        d["molindex"] = h.view["molindex"].copy()
+        d["nmol"] = h.sys.molptr.contents.num_mols
+        lib.sep_reset_retval(C.byref(h.ret))
+        lib.sep_reset_force(h.atoms, C.byref(h.sys))
+        lib.sep_reset_force_mol(C.byref(h.sys))
+        lib.sep_force_pairs(h.atoms, b"OO", 2.5, h.fun(), C.byref(h.sys), C.byref(h.ret),
+                            A.SEP_EXCL_SAME_MOL)
+        lib.sep_stretch_harmonic(h.atoms, 0, 0.316, 68421.0, C.byref(h.sys), C.byref(h.ret))
+        lib.sep_angle_cossq(h.atoms, 0, 1.97, 490.0, C.byref(h.sys), C.byref(h.ret))
+        lib.sep_coulomb_sf(h.atoms, 3.0, C.byref(h.sys), C.byref(h.ret), A.SEP_EXCL_SAME_MOL)
+        lib.sep_nosehoover(h.atoms, 3.0, C.byref(h.alpha), 0.01, C.byref(h.sys))
+        lib.sep_leapfrog(h.atoms, C.byref(h.sys), C.byref(h.ret))
+        if compress:
+            lib.sep_compress_box(h.atoms, 0.12, 0.995, C.byref(h.sys))
+        lib.sep_mol_pressure_tensor(h.atoms, mols, C.byref(h.ret), C.byref(h.sys))
+        nm = d["nmol"]
+        d.update({tag + "_x1": h.view["x"].copy(), tag + "_v1": h.view["v"].copy(),
+                  tag + "_L1": np.array(h.sys.length), tag + "_kin": np.array(h.ret.kin_P_mol),
+                  tag + "_pot": np.array(h.ret.pot_P_mol), tag + "_P": np.array(h.ret.P_mol),
+                  tag + "_p": h.ret.p_mol,
+                  tag + "_cm": np.array([list(mols[i].x) for i in range(nm)]),
+                  tag + "_vcm": np.array([list(mols[i].v) for i in range(nm)])})
+        lib.sep_free_mol(mols, C.byref(h.sys))
+        h.close()
+    return d
+
+
 def box_ops(lib):
     """sep_compress_box / _dir / _dir_length and sep_berendsen / _iso one at
     a time, then a Berendsen run (prgs/prg7.c) and a compression run
@@ -367,7 +407,8 @@ def main(only=()):
                          ("water_small", lambda: water_small(lib, tmp)),
                          ("host_api", lambda: host_api(lib)),
                          ("stoch_small", lambda: stochastic(lib)),
-                         ("box_small", lambda: box_ops(lib))):
+                         ("box_small", lambda: box_ops(lib)),
+                         ("molp_small", lambda: molp_small(lib, tmp))):
             if only and name not in only:
                 continue
             d = fn()
