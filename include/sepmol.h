@@ -34,6 +34,12 @@ void sep_torsion_Ryckaert(sepatom *ptr, int type, const double g[6],
 sepmol *sep_init_mol(sepatom *atom, sepsys *sys);
 void sep_free_mol(sepmol *ptr, sepsys *sys);
 
+/* Centre of mass of every molecule into mol[i].x (the chain of consecutive
+ * atoms from its first one, bonds unwrapped, wrapped into the box) and
+ * centre-of-mass velocity into mol[i].v (source/sepmol.c:683-748). */
+void sep_mol_cm(seppart *ptr, sepmol *mol, sepsys *sys);
+void sep_mol_velcm(seppart *atom, sepmol *mol, sepsys *sys);
+
 /* Section readers and list release (reference :212-219). */
 void sep_read_bonds_top(sepatom *aptr, sepmolinfo *ptr, const char *file, int npart, char opt);
 void sep_read_angles_top(sepatom *aptr, sepmolinfo *ptr, const char *file, int npart, char opt);

@@ -53,6 +53,18 @@ struct sepdev {
 	// previous force; [SEPDEV_EXT_RANDN] the last Gaussian draws (GJF)
 	float4 *ext[SEPDEV_NEXT], *ext_b[SEPDEV_NEXT];
 
+	// molecular pressure tensor (sepdev_molvir_enable): molecule tables in
+	// user indices, centres of mass of the last pair pass and its box, the
+	// per-atom intermolecular force since the last reset (user order)
+	int molvir_on, nmolv;
+	int *mv_first, *mv_nuau, *mv_start, *mv_atoms;
+	double *mv_mass;
+	int4 *mv_cm;
+	float4 *mv_finter;
+	double *mv_out;
+	double mv_L[3];
+	int mv_slot;            // slot the next pair pass writes its molecular sums to
+
 	// cell list
 	int ncell[3];
 	long ncells, cap_cells;

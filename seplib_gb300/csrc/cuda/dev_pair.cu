@@ -116,7 +116,14 @@ __device__ __forceinline__ void integrate(long i, float fx, float fy, float fz, 
 	integrate_s(i, fx, fy, fz, ei, pi, a, a.fs, a.shi, a.slo, alpha, pos_out, ek, kp, sv2, d2);
 }
 
-template <int VAR, bool FUSED>
+// MOLV: also the molecular virial of the pass.  For each pair of atoms in
+// different molecules (both molecule indices set) the pair force f adds
+// f (x) R_ij, R_ij the minimum image of the two molecules' centres of mass
+// at this pass, and f (x) n_ij, n_ij the periodic image (-1, 0, 1 per axis)
+// that minimum image takes; both nine components, halved for the full list,
+// into fields 0-8 and 9-17 of slot a.mslot.  f is also added to the atom's
+// intermolecular force.
+template <int VAR, bool FUSED, bool MOLV = false>
 __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 {
 	constexpr int NCH = VAR == VAR_SINGLE ? 1 : 4;
@@ -140,9 +147,19 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 	for (int c = 0; c < NCH; c++) e[c] = 0.f;
 	float ec = 0.f;
 	float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f, w4 = 0.f, w5 = 0.f;
+	float wm[18];
+#pragma unroll
+	for (int k = 0; k < 18; k++) wm[k] = 0.f;
+	float gix = 0.f, giy = 0.f, giz = 0.f;
+	int mi = -1;
+	int4 ci = make_int4(0, 0, 0, 0);
 	int4 pi = make_int4(0, 0, 0, 0);
 	if (act) {
 		pi = a.pos[i];
+		if (MOLV) {
+			mi = a.mol[i];
+			if (mi >= 0) ci = a.mcm[mi];
+		}
 		const int cnt = a.ncnt[i];
 		const int *base = a.nl + nl_index(i, 0, a.maxnb);
 		float qi = 0.f;
@@ -190,6 +207,35 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 			fx += gx; fy += gy; fz += gz;
 			w0 += gx * dx; w1 += gx * dy; w2 += gx * dz;
 			w3 += gy * dy; w4 += gy * dz; w5 += gz * dz;
+			if (MOLV && mi >= 0) {
+				const int mj = __ldg(&a.mol[j]);
+				if (mj >= 0 && mj != mi) {
+					const int4 cj = __ldg(&a.mcm[mj]);
+					const unsigned hi[3] = {(unsigned)ci.x, (unsigned)ci.y, (unsigned)ci.z};
+					const unsigned hj[3] = {(unsigned)cj.x, (unsigned)cj.y, (unsigned)cj.z};
+					const float sc[3] = {sx, sy, sz}, g3[3] = {gx, gy, gz};
+					float R[3], nim[3];
+#pragma unroll
+					for (int q = 0; q < 3; q++) {
+						const int dI = (int)(hi[q] - hj[q]);
+						R[q] = (float)dI * sc[q];
+						nim[q] = (float)((((long long)hi[q] - (long long)hj[q]) - dI) >> 32);
+					}
+#pragma unroll
+					for (int p = 0; p < 3; p++)
+#pragma unroll
+						for (int q = 0; q < 3; q++) {
+							wm[3 * p + q] += g3[p] * R[q];
+							wm[9 + 3 * p + q] += g3[p] * nim[q];
+						}
+					gix += gx; giy += gy; giz += gz;
+				}
+			}
+		}
+		if (MOLV && mi >= 0) {
+			float4 fo = a.finter[a.gid[i]];
+			fo.x += gix; fo.y += giy; fo.z += giz;
+			a.finter[a.gid[i]] = fo;
 		}
 	}
 	float etot = ec;
@@ -210,9 +256,11 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 	}
 	// reductions: pair terms (halved for the full list) into pslot, kinetic into lslot
 	long long *ps = a.slots + (long)a.pslot * SLOT_FIELDS;
+	constexpr int NM = MOLV ? 18 : 0;
+	const int moff = (a.mslot - a.pslot) * SLOT_FIELDS;
 	if (!FUSED) {
-		float v[NCH + 7];
-		int fld[NCH + 7];
+		float v[NCH + 7 + NM];
+		int fld[NCH + 7 + NM];
 #pragma unroll
 		for (int c = 0; c < NCH; c++) { v[c] = 0.5f * e[c]; fld[c] = SLOT_EPOT0 + c; }
 		v[NCH] = 0.5f * ec; fld[NCH] = SLOT_ECOUL;
@@ -220,12 +268,14 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 		v[NCH + 4] = 0.5f * w3; v[NCH + 5] = 0.5f * w4; v[NCH + 6] = 0.5f * w5;
 #pragma unroll
 		for (int k = 0; k < 6; k++) fld[NCH + 1 + k] = SLOT_POTP + k;
-		block_to_slot<NCH + 7>(v, fld, ps, 0.f, -1);
+#pragma unroll
+		for (int k = 0; k < NM; k++) { v[NCH + 7 + k] = 0.5f * wm[k]; fld[NCH + 7 + k] = moff + k; }
+		block_to_slot<NCH + 7 + NM>(v, fld, ps, 0.f, -1);
 	} else {
 		long long *ls = a.slots + (long)a.lslot * SLOT_FIELDS;
 		const long long off = ls - ps;
-		float v[NCH + 15];
-		int fld[NCH + 15];
+		float v[NCH + 15 + NM];
+		int fld[NCH + 15 + NM];
 #pragma unroll
 		for (int c = 0; c < NCH; c++) { v[c] = 0.5f * e[c]; fld[c] = SLOT_EPOT0 + c; }
 		v[NCH] = 0.5f * ec; fld[NCH] = SLOT_ECOUL;
@@ -237,7 +287,9 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 #pragma unroll
 		for (int k = 0; k < 6; k++) { v[NCH + 8 + k] = kp[k]; fld[NCH + 8 + k] = (int)off + SLOT_KINP + k; }
 		v[NCH + 14] = sv2; fld[NCH + 14] = (int)off + SLOT_SUMV2;
-		block_to_slot<NCH + 15>(v, fld, ps, d2, (int)off + SLOT_MAXD2);
+#pragma unroll
+		for (int k = 0; k < NM; k++) { v[NCH + 15 + k] = 0.5f * wm[k]; fld[NCH + 15 + k] = moff + k; }
+		block_to_slot<NCH + 15 + NM>(v, fld, ps, d2, (int)off + SLOT_MAXD2);
 		step_decide_exit(a.dec);
 	}
 }
@@ -563,12 +615,17 @@ int sepdev_upload_pairset(sepdev *d, const sepdev_pairset *ps)
 }
 
 template <bool FUSED>
-static void launch_fused(sepdev *d, int var, const PairArgs &a, size_t shm)
+static void launch_fused(sepdev *d, int var, const PairArgs &a, size_t shm, bool molv)
 {
 	const int B = 256;
 	const int grid = grid_for(d->n, B);
 	const bool cubic = d->L[0] == d->L[1] && d->L[1] == d->L[2];
-	if (var == VAR_SINGLE && cubic) {
+	if (molv) {
+		if (var == VAR_GENERAL_COUL)
+			k_pair<VAR_GENERAL_COUL, FUSED, true><<<grid, B, shm, d->st>>>(d->n, a);
+		else
+			k_pair<VAR_GENERAL, FUSED, true><<<grid, B, shm, d->st>>>(d->n, a);
+	} else if (var == VAR_SINGLE && cubic) {
 		switch (d->lj_variant) {
 		case 1: k_lj<FUSED, true, 5, 0><<<grid, B, 0, d->st>>>(d->n, a); break;
 		case 2: k_lj<FUSED, true, 4, 1><<<grid, B, 0, d->st>>>(d->n, a); break;
@@ -588,8 +645,19 @@ int sepdev_launch_pair(sepdev *d, const sepdev_pairset *ps, PairArgs &a, bool fu
 {
 	const int var = single_variant(ps) ? VAR_SINGLE : (ps->coulomb ? VAR_GENERAL_COUL : VAR_GENERAL);
 	const size_t shm = sizeof(sepdev_pot) * ps->ntypes * ps->ntypes;
-	if (fused) launch_fused<true>(d, var, a, shm);
-	else launch_fused<false>(d, var, a, shm);
+	// the molecular sums of a pass go to the slot named for it (consumed
+	// here, so a launch nobody named a slot for carries none)
+	const bool molv = d->molvir_on && d->mv_slot >= 0 && d->mv_slot < d->nslots;
+	if (molv) {
+		// centres of mass at the positions of this pass
+		int rc = sepdev_molvir_cm(d, a.pos);
+		if (rc) return rc;
+		a.mol = d->mol; a.gid = d->gid; a.mcm = d->mv_cm; a.finter = d->mv_finter;
+		a.mslot = d->mv_slot;
+	}
+	d->mv_slot = -1;
+	if (fused) launch_fused<true>(d, var, a, shm, molv);
+	else launch_fused<false>(d, var, a, shm, molv);
 	CKL(d);
 	return SEPDEV_OK;
 }

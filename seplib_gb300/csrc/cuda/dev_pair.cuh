@@ -32,9 +32,18 @@ struct PairArgs {
 	const unsigned *flags;
 	DecideArgs dec;            // graph loop: decision at the end of a fused step
 	int skip_obs;              // fused step whose energy and virial nobody reads
+	// molecular virial (k_pair<..., MOLV>): molecule of each slot, centres of
+	// mass of this pass, per-atom intermolecular force (user order)
+	const int *mol;
+	const int *gid;
+	const int4 *mcm;
+	float4 *finter;
+	int mslot;
 };
 
 
 void sepdev_fill_args(sepdev *d, PairArgs &a, const sepdev_pairset *ps, double dt, int nh,
 		      double alpha, int accumulate, int pslot, int lslot, int parity);
 int sepdev_launch_pair(sepdev *d, const sepdev_pairset *ps, PairArgs &a, bool fused);
+// centres of mass of the molecules at positions pos (dev_molp.cu)
+int sepdev_molvir_cm(sepdev *d, const int4 *pos);

@@ -253,9 +253,9 @@ static void run_end(const RunState *h, double *alpha, double *sumv2, double *las
 	if (last_trig) *last_trig = h->last_trig;
 }
 
-extern "C" int sepdev_run(sepdev *d, const sepdev_pairset *ps, const sepdev_runcfg *cfg,
-			  long nsteps, double *alpha, double *sumv2, double *last, long *ntrig,
-			  int *last_trig)
+static int run_loop(sepdev *d, const sepdev_pairset *ps, const sepdev_runcfg *cfg,
+		    long nsteps, double *alpha, double *sumv2, double *last, long *ntrig,
+		    int *last_trig)
 {
 	if (!d->list_valid || nsteps < 0) return SEPDEV_EINVAL;
 	Runner *r;
@@ -292,6 +292,19 @@ extern "C" int sepdev_run(sepdev *d, const sepdev_pairset *ps, const sepdev_runc
 	}
 	run_end(h, alpha, sumv2, last, ntrig, last_trig);
 	return SEPDEV_OK;
+}
+
+// The loop graphs carry no molecular-tensor sums: those are kept off while
+// they are captured and launched.
+extern "C" int sepdev_run(sepdev *d, const sepdev_pairset *ps, const sepdev_runcfg *cfg,
+			  long nsteps, double *alpha, double *sumv2, double *last, long *ntrig,
+			  int *last_trig)
+{
+	const int mv = d->molvir_on;
+	d->molvir_on = 0;
+	const int rc = run_loop(d, ps, cfg, nsteps, alpha, sumv2, last, ntrig, last_trig);
+	d->molvir_on = mv;
+	return rc;
 }
 
 // ---- timed loop: L2 flushed between steps, events around every step -------
@@ -480,9 +493,24 @@ static int run_timed_inner(sepdev *d, Runner *r, const sepdev_pairset *ps, const
 	return SEPDEV_OK;
 }
 
+static int run_timed_loop(sepdev *d, const sepdev_pairset *ps, const sepdev_runcfg *cfg,
+			  long nsteps, double *alpha, double *sumv2, double *last, long *ntrig,
+			  int *last_trig, sepdev_timing *tm);
+
 extern "C" int sepdev_run_timed(sepdev *d, const sepdev_pairset *ps, const sepdev_runcfg *cfg,
 				long nsteps, double *alpha, double *sumv2, double *last, long *ntrig,
 				int *last_trig, sepdev_timing *tm)
+{
+	const int mv = d->molvir_on;
+	d->molvir_on = 0;
+	const int rc = run_timed_loop(d, ps, cfg, nsteps, alpha, sumv2, last, ntrig, last_trig, tm);
+	d->molvir_on = mv;
+	return rc;
+}
+
+static int run_timed_loop(sepdev *d, const sepdev_pairset *ps, const sepdev_runcfg *cfg,
+			  long nsteps, double *alpha, double *sumv2, double *last, long *ntrig,
+			  int *last_trig, sepdev_timing *tm)
 {
 	if (!d->list_valid || nsteps < 0 || !tm) return SEPDEV_EINVAL;
 	tm->ms_steps = tm->ms_kernel = 0.0;

@@ -110,6 +110,12 @@ extern "C" void sepdev_destroy(sepdev *d)
 		if (d->ext[k]) cudaFree(d->ext[k]);
 		if (d->ext_b[k]) cudaFree(d->ext_b[k]);
 	}
+	{
+		void *mv[] = {d->mv_first, d->mv_nuau, d->mv_start, d->mv_atoms, d->mv_mass, d->mv_cm,
+			      d->mv_finter, d->mv_out};
+		for (size_t k = 0; k < sizeof mv / sizeof mv[0]; k++)
+			if (mv[k]) cudaFree(mv[k]);
+	}
 	if (d->h_slots) cudaFreeHost(d->h_slots);
 	if (d->stage) cudaFreeHost(d->stage);
 	if (d->h_flags) cudaFreeHost(d->h_flags);

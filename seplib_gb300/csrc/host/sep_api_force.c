@@ -136,10 +136,7 @@ static void add_term(rt_ctx *c, rt_term *T, const char *types, sepret *ret, int 
 	T->t0 = types[0];
 	T->t1 = types[1];
 	if (c->pass_slot >= 0 && (c->nterms == RT_MAXTERMS || term_overlaps(c, T))) rt_launch_pass(c);
-	if (c->pass_slot < 0) {
-		c->pass_slot = rt_new_slot(c);
-		rt_add_op(c, ret, OP_VIRIAL, c->pass_slot, 0);
-	}
+	if (c->pass_slot < 0) rt_open_pass(c, ret);
 	c->terms[c->nterms] = *T;
 	rt_add_op(c, ret, opkind, c->pass_slot, c->nterms);
 	c->nterms++;
@@ -201,10 +198,7 @@ void sep_coulomb_sf(seppart *ptr, double cf, sepsys *sys, sepret *retval, const 
 		sys->neighb_flag = flag;
 	}
 	if (c->pass_slot >= 0 && c->coul_on) rt_launch_pass(c);
-	if (c->pass_slot < 0) {
-		c->pass_slot = rt_new_slot(c);
-		rt_add_op(c, retval, OP_VIRIAL, c->pass_slot, 0);
-	}
+	if (c->pass_slot < 0) rt_open_pass(c, retval);
 	c->coul_on = 1;
 	c->coul_cf = cf;
 	rt_add_op(c, retval, OP_COUL, c->pass_slot, 0);
@@ -439,8 +433,10 @@ void sep_free_dihedrals(sepmolinfo *m)
 	if (m && m->flag_dihedrals == 1) { free(m->dlist); free(m->dihedrals); m->flag_dihedrals = 0; }
 }
 
-/* molecule table (source/sepmol.c:590-658).  The molecular force matrix Fij is
- * not evaluated on the GPU, so flag_Fij stays 0 and no nmol^2 array is held. */
+/* molecule table (source/sepmol.c:590-658).  With at most SEP_MAX_NUM_MOL
+ * molecules flag_Fij is set, as in the reference, and the molecular virial
+ * is accumulated on the device (dev_molp.cu); the nmol^2 force matrix
+ * itself is never formed, so molptr->Fij stays NULL. */
 sepmol *sep_init_mol(sepatom *atom, sepsys *sys)
 {
 	rt_ctx *c = rt_get(atom, __func__);
@@ -469,12 +465,52 @@ sepmol *sep_init_mol(sepatom *atom, sepsys *sys)
 	}
 	free(cnt);
 	sys->molptr->flag_Fij = 0;
+	int ok = nm >= 1 && nm <= SEP_MAX_NUM_MOL;
+	for (unsigned k = 0; k < nm && ok; k++)
+		if (mol[k].nuau < 1 || mol[k].index[0] + (long)mol[k].nuau > sys->npart) ok = 0;
+	if (!ok) {
+		sep_warning("Molecular force/torque evaluation disabled");
+		return mol;
+	}
+	rt_mv_drop(c);
+	c->mv_nmol = (int)nm;
+	c->mv_first = malloc(sizeof(int) * nm);
+	c->mv_nuau = malloc(sizeof(int) * nm);
+	c->mv_start = malloc(sizeof(int) * (nm + 1));
+	c->mv_mass = malloc(sizeof(double) * nm);
+	long tot = 0;
+	for (unsigned k = 0; k < nm; k++) tot += mol[k].nuau;
+	c->mv_atoms = malloc(sizeof(int) * (tot > 0 ? tot : 1));
+	if (!c->mv_first || !c->mv_nuau || !c->mv_start || !c->mv_mass || !c->mv_atoms)
+		sep_error("%s: Couldn't allocate memory", __func__);
+	c->mv_start[0] = 0;
+	for (unsigned k = 0; k < nm; k++) {
+		c->mv_first[k] = mol[k].index[0];
+		c->mv_nuau[k] = (int)mol[k].nuau;
+		c->mv_mass[k] = mol[k].m;
+		for (unsigned q = 0; q < mol[k].nuau; q++) c->mv_atoms[c->mv_start[k] + q] = mol[k].index[q];
+		c->mv_start[k + 1] = c->mv_start[k] + (int)mol[k].nuau;
+	}
+	for (int q = 0; q < 9; q++) c->molW[q] = c->molN[q] = 0.0;
+	c->mv_info = sys->molptr;
+	c->mv_on = 1;
+	c->mv_uploaded = 0;
+	if (c->dev) {
+		rt_flush(c);
+		rt_check(sepdev_molvir_enable(c->dev, c->mv_nmol, c->mv_first, c->mv_nuau, c->mv_start,
+					      c->mv_atoms, c->mv_mass), "molecular tables");
+		c->mv_uploaded = 1;
+	}
+	sys->molptr->flag_Fij = 1;
 	return mol;
 }
 
 void sep_free_mol(sepmol *mol, sepsys *sys)
 {
 	if (!mol) return;
+	rt_ctx *c = rt_find_molinfo(sys->molptr);
+	if (c) rt_mv_drop(c);
+	sys->molptr->flag_Fij = 0;
 	for (unsigned k = 0; k < sys->molptr->num_mols; k++) {
 		free(mol[k].index);
 		if (mol[k].shake_flag == 1) free(mol[k].blength);

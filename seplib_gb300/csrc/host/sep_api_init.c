@@ -381,15 +381,22 @@ void sep_reset_force(seppart *ptr, sepsys *sys)
 	}
 }
 
+/* source/sepmisc.c:403-425: zero the molecular forces; the reference
+ * exits when sep_init_mol did not enable them.  Here the molecular virial
+ * of the passes so far and the per-atom intermolecular forces are zeroed
+ * (pending passes run first, so they count in the window they belong to). */
 void sep_reset_force_mol(sepsys *sys)
 {
 	sys->fun_cstate = 0;
-	/* sep_init_mol here keeps flag_Fij at 0 (no molecular force matrix on
-	 * the GPU path), so the reset has nothing to clear */
-	if (sys->molptr->flag_Fij == 0 || !sys->molptr->Fij) return;
-	for (unsigned i = 0; i < sys->molptr->num_mols; i++)
-		for (unsigned j = 0; j < sys->molptr->num_mols; j++)
-			for (int k = 0; k < 3; k++) sys->molptr->Fij[i][j][k] = 0.0f;
+	if (sys->molptr->flag_Fij == 0)
+		sep_error("%s: Tried to reset mol force, but flag is zero", __func__);
+	rt_ctx *c = rt_find_molinfo(sys->molptr);
+	if (!c) return;
+	if (c->dev) {
+		rt_flush(c);
+		if (c->mv_uploaded) rt_check(sepdev_molvir_reset(c->dev), "molecular force reset");
+	}
+	for (int q = 0; q < 9; q++) c->molW[q] = c->molN[q] = 0.0;
 }
 
 /* ---- pressure (source/sepret.c:50-82) -------------------------------------------------- */

@@ -52,6 +52,7 @@ void sep_leapfrog(seppart *ptr, sepsys *sys, sepret *retval)
 		sepdev_pairset ps;
 		extern void rt_pairset(rt_ctx *c, sepdev_pairset *ps);
 		rt_pairset(c, &ps);
+		rt_pass_mol_slot(c);
 		lf = rt_new_slot(c);
 		rt_check(sepdev_step(c->dev, &ps, !c->forces_zero, sys->dt, c->friction,
 				     c->friction_alpha, c->pass_slot, lf), "fused step");

@@ -65,6 +65,7 @@ void rt_unregister(seppart *ptr)
 {
 	for (int k = 0; k < RT_MAXCTX; k++)
 		if (g_ctx[k] && g_ctx[k]->ptr == ptr) {
+			rt_mv_drop(g_ctx[k]);
 			if (g_ctx[k]->dev) sepdev_destroy(g_ctx[k]->dev);
 			free(g_ctx[k]);
 			g_ctx[k] = NULL;
@@ -246,7 +247,29 @@ void rt_need_device(rt_ctx *c, const sepsys *sys)
 		c->pending_trigger = sqrt(maxd2) > 0.5 * sys->skin;
 	}
 	if (uploading && c->ext_on) ext_upload(c);
+	if (c->mv_on && !c->mv_uploaded) {
+		rt_check(sepdev_molvir_enable(c->dev, c->mv_nmol, c->mv_first, c->mv_nuau, c->mv_start,
+					      c->mv_atoms, c->mv_mass), "molecular tables");
+		c->mv_uploaded = 1;
+	}
 	if (c->topo_dirty) upload_topology(c);
+}
+
+rt_ctx *rt_find_molinfo(const sepmolinfo *m)
+{
+	for (int k = 0; k < RT_MAXCTX; k++)
+		if (g_ctx[k] && g_ctx[k]->mv_on && g_ctx[k]->mv_info == m) return g_ctx[k];
+	return NULL;
+}
+
+void rt_mv_drop(rt_ctx *c)
+{
+	free(c->mv_first); free(c->mv_nuau); free(c->mv_start); free(c->mv_atoms); free(c->mv_mass);
+	c->mv_first = c->mv_nuau = c->mv_start = c->mv_atoms = NULL;
+	c->mv_mass = NULL;
+	c->mv_on = c->mv_uploaded = 0;
+	c->mv_info = NULL;
+	if (c->dev) sepdev_molvir_disable(c->dev);
 }
 
 /* bond lengths, angles and dihedral angles of the last bonded calls */
@@ -374,11 +397,32 @@ static void clear_pass(rt_ctx *c)
 	c->pass_slot = -1;
 }
 
+void rt_open_pass(rt_ctx *c, sepret *ret)
+{
+	/* both slots of a pass come from one flush window */
+	if (c->nslots >= 14) rt_flush(c);
+	c->pass_slot = rt_new_slot(c);
+	rt_add_op(c, ret, OP_VIRIAL, c->pass_slot, 0);
+	c->mv_slot = -1;
+	if (c->mv_on) {
+		c->mv_slot = rt_new_slot(c);
+		rt_add_op(c, NULL, OP_MOLVIR, c->mv_slot, 0);
+	}
+}
+
+/* the device writes the next pass's molecular sums to the pass's own slot */
+void rt_pass_mol_slot(rt_ctx *c)
+{
+	if (c->mv_on && c->mv_uploaded)
+		rt_check(sepdev_molvir_slot(c->dev, c->mv_slot), "molecular slot");
+}
+
 void rt_launch_pass(rt_ctx *c)
 {
 	if (!pass_pending(c)) return;
 	sepdev_pairset ps;
 	rt_pairset(c, &ps);
+	rt_pass_mol_slot(c);
 	rt_check(sepdev_pair_forces(c->dev, &ps, !c->forces_zero, c->pass_slot), "pair forces");
 	c->forces_zero = 0;
 	clear_pass(c);
@@ -419,6 +463,12 @@ void rt_read_slots(rt_ctx *c, sepsys *sys, int lf_slot)
 			add_sym(r->pot_P_bond, s + SLOT_POTPB, 1.0);
 			break;
 		case OP_EADD: r->epot += s[SLOT_EPOT0]; break;
+		case OP_MOLVIR:
+			for (int q = 0; q < 9; q++) {
+				c->molW[q] += s[q];
+				c->molN[q] += s[9 + q];
+			}
+			break;
 		case OP_DPD_VIR:
 			add_sym(r->pot_P, s + SLOT_POTP, 1.0);
 			add_sym(r->pot_P_conservative, s + SLOT_POTP, 1.0);

@@ -45,8 +45,9 @@ enum {
 	OP_BOND,             /* epot += E0, pot_P += P, pot_P_bond += P (stretch) */
 	OP_EADD,             /* epot += E0                              (angles, torsions) */
 	OP_KIN,              /* ekin += Ek/2, kin_P += K                (leap-frog) */
-	OP_DPD_VIR           /* pot_P, pot_P_conservative += C; pot_P_random += R;
+	OP_DPD_VIR,          /* pot_P, pot_P_conservative += C; pot_P_random += R;
 	                      * pot_P_dissipative += D (chan: slot of D) (O(N^2) DPD) */
+	OP_MOLVIR            /* context molW += W, molN += N (molecular sums of a pass) */
 };
 
 typedef struct {
@@ -87,6 +88,7 @@ typedef struct rt_ctx {
 	int coul_on;
 	double coul_cf;
 	int pass_slot;          /* slot of the pending pair pass, -1 if none */
+	int mv_slot;            /* its molecular sums' slot (molecular tensor on) */
 	int forces_zero;        /* stored forces are logically zero */
 	int friction;           /* Nose-Hoover friction pending */
 	double friction_alpha;
@@ -117,6 +119,15 @@ typedef struct rt_ctx {
 	unsigned long long seed;
 	unsigned ncall[4];
 
+	/* molecular pressure tensor: sep_init_mol's tables (first atom, chain
+	 * length, atom lists as CSR, masses) for the device, the molecular
+	 * virial of the pair passes since the last sep_reset_force_mol */
+	int mv_on, mv_uploaded, mv_nmol;
+	sepmolinfo *mv_info;
+	int *mv_first, *mv_nuau, *mv_start, *mv_atoms;
+	double *mv_mass;
+	double molW[9], molN[9];
+
 	/* statistics */
 	long nbuild;
 	int tpp;
@@ -139,6 +150,8 @@ void rt_host_modified(rt_ctx *c);                    /* host data changed: devic
 int rt_new_slot(rt_ctx *c);
 void rt_add_op(rt_ctx *c, sepret *ret, int kind, int slot, int chan);
 void rt_launch_pass(rt_ctx *c);          /* launch the pending pair pass (force only) */
+void rt_open_pass(rt_ctx *c, sepret *ret); /* new pending pass: slots and their operations */
+void rt_pass_mol_slot(rt_ctx *c);          /* before launching the pending pass */
 void rt_materialize_forces(rt_ctx *c);   /* pending pass + friction + zeroing into stored forces */
 void rt_read_slots(rt_ctx *c, sepsys *sys, int leapfrog_slot);   /* sync, apply ops */
 int rt_ret_pending(rt_ctx *c, const sepret *ret);
@@ -150,6 +163,8 @@ void rt_prepare_list(rt_ctx *c, sepsys *sys, unsigned opt, int brute_excl_bonds)
 void rt_check(int rc, const char *what);
 void rt_need_ext(rt_ctx *c, const sepsys *sys);    /* stochastic fields on the device */
 int rt_type_id(rt_ctx *c, char t);                 /* -1 when no particle has type t */
+rt_ctx *rt_find_molinfo(const sepmolinfo *m);      /* context of sep_init_mol's system */
+void rt_mv_drop(rt_ctx *c);                        /* forget the molecule tables */
 void rt_pairset(rt_ctx *c, sepdev_pairset *ps);   /* pending terms -> device table */   /* sep_error on a device failure */
 
 extern char rt_errbuf[512];

@@ -291,6 +291,27 @@ int sepdev_gjf(sepdev *d, double dt, double temp, double alpha, unsigned long lo
  * counted; the last-update positions keep their absolute values. */
 int sepdev_rescale_box(sepdev *d, const double *L1, const double *sx);
 
+/* ---- molecular pressure tensor (dev_molp.cu) ----
+ * _enable: nmol molecules; first/nuau: the chain of consecutive user indices
+ * the centre of mass is taken over; start/atoms: each molecule's atoms
+ * (CSR, user indices); mass: molecule masses.  While enabled every pair pass
+ * computes the centres of mass of its positions and accumulates the
+ * molecular virial and the per-atom intermolecular force; _slot names the
+ * slot that receives the pass's molecular sums (fields 0-8: sum f (x) R_ij;
+ * 9-17: sum f (x) n_ij, n_ij the periodic image of R_ij).  _reset zeroes the
+ * per-atom forces.  _state returns kin (9: sum M v v^T), corr (9:
+ * sum_i F_i (x) dR_i, dR_i = L1 f1_i - L0 f0_i the change of the centre of
+ * mass since the last pass in the box of each time), and each molecule's
+ * centre of mass (3 nmol, wrapped) and velocity (3 nmol); the current and
+ * the pass's box are returned in L1 and L0 (3 each, may be NULL). */
+int sepdev_molvir_enable(sepdev *d, int nmol, const int *first, const int *nuau, const int *start,
+			 const int *atoms, const double *mass);
+int sepdev_molvir_reset(sepdev *d);
+int sepdev_molvir_slot(sepdev *d, int slot);
+void sepdev_molvir_disable(sepdev *d);
+int sepdev_mol_state(sepdev *d, double *kin, double *corr, double *cm, double *vcm, double *L0,
+		     double *L1);
+
 /* lanes per particle in the pair kernels (1, 2, 4); invalidates the list */
 int sepdev_set_tpp(sepdev *d, int tpp);
 int sepdev_get_tpp(sepdev *d);

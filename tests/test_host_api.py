@@ -145,3 +145,16 @@ def test_potential_callbacks_match_reference_formulas(lib):
         assert abs(lib.sep_lj(r2, b"f") - 48 * ri3 * (ri3 - 0.5) * ri) < 1e-12
         assert abs(lib.sep_lj_shift(r2, b"u") - (4 * ri3 * (ri3 - 1) + A.SEP_LJCF2)) < 1e-12
         assert abs(lib.sep_wca(r2, b"u") - (4 * ri3 * (ri3 - 1) + 1.0)) < 1e-12
+
+
+def test_reset_force_mol_without_init_exits(lib):
+    """As in the reference, resetting molecular forces that sep_init_mol did
+    not enable ends the program with sep_error."""
+    code = ("import ctypes as C\n"
+            "from seplib_gb300 import load, sepapi as A\n"
+            "lib = load()\n"
+            "sys_ = lib.sep_sys_setup(10.0, 10.0, 10.0, 2.5, 0.005, 10, A.SEP_BRUTE)\n"
+            "lib.sep_reset_force_mol(C.byref(sys_))\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                       cwd=os.path.dirname(HERE))
+    assert r.returncode != 0 and "flag is zero" in (r.stdout + r.stderr)
