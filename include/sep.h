@@ -14,6 +14,7 @@
 #include "sepret.h"
 #include "sepcoulomb.h"
 #include "sepsampler.h"
+#include "separray.h"
 #include "sepgpu.h"
 
 #endif
