@@ -12,9 +12,11 @@ Printed JSON line (rank 0):
           library's stream, max over ranks;
   e2e     the same metric through the reference-facing C API, prgs-style
           loop (sep_reset_retval, sep_reset_force, sep_force_pairs,
-          sep_nosehoover, sep_leapfrog) starting from host seppart arrays:
-          the host->device upload, every per-step copy and the final
-          device->host download are inside the timed region;
+          sep_nosehoover, sep_leapfrog) run by a C program as a seplib
+          program runs it (seplib_gb300/csrc/driver/e2e_loop.c), starting
+          from host seppart arrays: the host->device upload, every per-step
+          copy and the final device->host download are inside the timed
+          region;
   roofline  the fused step kernel: algorithmic bytes per launch
           N*(4*nbar_f + 128), nbar_f = 4/3 pi (rc+skin)^3 rho, divided by its
           mean launch duration (events around each launch);
@@ -30,8 +32,10 @@ import ctypes as C
 import json
 import math
 import os
+import struct
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -477,35 +481,28 @@ def main():
     achieved_step = n * (4 * nbar + 128 + (4 * nbar + 64) * rebuilds / args.steps) * args.steps / t_dev / 1e9
 
     # ---- end to end through the sep C API with host buffers ----
-    atoms, sys_ = new_system(lib, s)
-    ret = A.SepRet()
-    alpha = C.c_double(0.0)
-    nh_alpha = C.byref(alpha)
-
-    def api_steps(k):
-        for _ in range(k):
-            lib.sep_reset_retval(C.byref(ret))
-            lib.sep_reset_force(atoms, C.byref(sys_))
-            lib.sep_force_pairs(atoms, b"AA", RC, fun, C.byref(sys_), C.byref(ret), A.SEP_ALL)
-            lib.sep_nosehoover(atoms, T0, nh_alpha, TAU, C.byref(sys_))
-            lib.sep_leapfrog(atoms, C.byref(sys_), C.byref(ret))
-
-    api_steps(max(3, args.warmup // 10))      # warm the path (context, list, caches)
-    lib.sep_gpu_sync(atoms)
-    lib.sep_gpu_invalidate(atoms)             # next call uploads the host arrays again
+    # The prgs-style loop runs in C (seplib_gb300/csrc/driver/e2e_loop.c, built
+    # with the library), as a seplib program calls the API; the same initial
+    # state goes to it through a file.  Per timed step: the five API calls,
+    # each step's sepret read-back; the first step uploads the host arrays,
+    # the final sep_gpu_sync (timed) downloads them.
     e_steps = args.steps
-    barrier(world)
-    t_e2e = 0.0
-    for _ in range(e_steps):
-        lib.sep_gpu_flush_l2(atoms, FLUSH_BYTES)   # untimed; the step's readback is synchronous
-        t0 = time.perf_counter()
-        api_steps(1)
-        t_e2e += time.perf_counter() - t0
-    t0 = time.perf_counter()
-    lib.sep_gpu_sync(atoms)                   # device -> host download of x, v, f, ...
-    t_e2e += time.perf_counter() - t0
-    t_e2e = allmax(world, t_e2e)
-    lib.sep_close(atoms, n)
+    e2e_warm = max(3, args.warmup // 10)
+    with tempfile.TemporaryDirectory() as tmp:
+        state = os.path.join(tmp, "state.bin")
+        with open(state, "wb") as fh:
+            fh.write(struct.pack("<q", n))
+            fh.write(np.asarray(s.L, "<f8").tobytes())
+            fh.write(np.ascontiguousarray(s.x, "<f8").tobytes())
+            fh.write(np.ascontiguousarray(s.v, "<f8").tobytes())
+        from seplib_gb300 import build as sbuild
+        barrier(world)
+        r = subprocess.run([sbuild.E2E, state, str(e_steps), str(e2e_warm), str(FLUSH_BYTES), repr(RC),
+                            repr(DT), repr(SKIN), repr(T0), repr(TAU)], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise SystemExit("e2e driver failed: %s" % (r.stderr or r.stdout))
+        e2e_run = json.loads(r.stdout.strip().splitlines()[-1])
+    t_e2e = allmax(world, e2e_run["seconds"])
     state_bytes = n * (16 + 16 + 16 + 16 + 16 + 4 + 4 + 16 + 16)   # what upload/download move
     h2d = (state_bytes + 8 * 4 * n) / e_steps + 16
     d2h = (state_bytes + 4 * n) / e_steps + 2 * 8 * 32 + 16
@@ -542,8 +539,13 @@ def main():
             "data": "synthetic (seeded fcc lattice, Maxwell-Boltzmann velocities)",
             "config": cfgd,
             "e2e": {"value": e2e_val, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "steps": e_steps,
-                    "path": "sep C API prgs-style loop, host seppart arrays, upload+download timed"},
+                    "d2h_bytes_per_step": d2h, "steps": e_steps, "list_rebuilds": e2e_run["rebuilds"],
+                    "first_step_ms": 1e3 * e2e_run["first_step_s"],
+                    "final_download_ms": 1e3 * e2e_run["final_download_s"],
+                    "path": "prgs-style C loop through the sep C API (seplib_gb300/csrc/driver/"
+                            "e2e_loop.c): host seppart arrays, first-step upload, per-step sepret "
+                            "read-back and the final download timed; L2 flushed between steps, "
+                            "untimed"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": K_LJ_TRAFFIC.get(args.ncell),
                          "traffic_unit": "bytes per launch", "peak_source": peak_kind,

@@ -20,6 +20,7 @@ INC = os.path.join(ROOT, "include")
 LIBDIR = os.path.join(PKG, "lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libsep.so")
+E2E = os.path.join(LIBDIR, "sep_e2e_loop")
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 CC = os.environ.get("CC", "gcc")
@@ -78,6 +79,14 @@ def build(verbose=False, jobs=None):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed\n%s\n%s" % (r.stdout, r.stderr))
+    # the prgs-style loop driver that times the C API end to end
+    src = os.path.join(CSRC, "driver", "e2e_loop.c")
+    if not os.path.exists(E2E) or os.path.getmtime(E2E) < max(os.path.getmtime(LIB), os.path.getmtime(src)):
+        cmd = [CC, "-std=c99", "-O2", "-Wall", "-I", INC, src, "-o", E2E, "-L", LIBDIR,
+               "-Wl,-rpath," + LIBDIR, "-lsep", "-lm"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("driver build failed\n%s\n%s" % (r.stdout, r.stderr))
     return LIB
 
 

@@ -23,11 +23,51 @@
 //     pending-update test), and whether any charge is non-zero.
 #include <math.h>
 #include <stdlib.h>
+#include <stddef.h>
 #include <string.h>
 #include "dev_common.cuh"
 #include "sepstrct.h"
 
-#define HIO_B 256
+#define HIO_B 128
+
+// The fields a transfer touches, as 8-byte words of the 568-byte record:
+// the head (x, v, f, a, m, type, z, neighb, cross_neighb, crossings,
+// molindex: bytes 0-159) and xn.  A block moves the words of its HIO_B
+// consecutive records through shared memory, so every warp-wide access to
+// host memory covers one or two contiguous runs of a record instead of 32
+// records 568 bytes apart.
+#define HW_HEAD 20
+#define HW_XN 3
+#define HW (HW_HEAD + HW_XN)
+static_assert(sizeof(seppart) % 8 == 0, "seppart is a whole number of 8-byte words");
+static_assert(offsetof(seppart, molindex) + sizeof(int) <= 8 * HW_HEAD, "head words");
+static_assert(offsetof(seppart, xn) % 8 == 0, "xn word-aligned");
+#define RW (sizeof(seppart) / 8)
+#define XN_W (offsetof(seppart, xn) / 8)
+
+// word q of the record block: record q / HW, head word or xn word
+__device__ __forceinline__ long rec_word(long r0, int q, int *r, int *w)
+{
+	*r = q / HW;
+	*w = q - *r * HW;
+	return (r0 + *r) * (long)RW + (*w < HW_HEAD ? *w : XN_W + *w - HW_HEAD);
+}
+
+// the block's records [r0, r0 + cnt) into sm[HIO_B][HW]
+__device__ __forceinline__ void rec_load(const seppart *p, long r0, int cnt, unsigned long long (*sm)[HW])
+{
+	const unsigned long long *g = (const unsigned long long *)p;
+	for (int q = threadIdx.x; q < cnt * HW; q += HIO_B) {
+		int r, w;
+		const long gi = rec_word(r0, q, &r, &w);
+		sm[r][w] = g[gi];
+	}
+}
+
+// typed views of a staged record
+#define SM_D(rec, field, k) (((const double *)(rec))[offsetof(seppart, field) / 8 + (k)])
+#define SM_I(rec, field, k) (((const int *)(rec))[offsetof(seppart, field) / 4 + (k)])
+#define SM_XN(rec, k) (((const double *)(rec))[HW_HEAD + (k)])
 
 struct HioUp {
 	const seppart *p;
@@ -47,43 +87,50 @@ struct HioUp {
 
 __global__ void __launch_bounds__(HIO_B) k_upload_parts(HioUp a)
 {
+	__shared__ unsigned long long sm[HIO_B][HW];
 	__shared__ double red[HIO_B];
-	const long i = blockIdx.x * (long)HIO_B + threadIdx.x;
+	const long r0 = blockIdx.x * (long)HIO_B;
+	const int cnt = (int)min((long)HIO_B, a.n - r0);
+	rec_load(a.p, r0, cnt, sm);
+	__syncthreads();
+	const long i = r0 + threadIdx.x;
 	double q = 0.0;
 	if (i < a.n) {
-		const seppart &p = a.p[i];
+		const unsigned long long *rec = sm[threadIdx.x];
 		unsigned h[3], l[3];
 		double d2 = 0.0;
 		float vh[3], vl[3];
+		const double m = SM_D(rec, m, 0);
 		for (int k = 0; k < 3; k++) {
-			to_fixed_dev(p.x[k], a.L[k], h[k], l[k]);
-			const double v = p.v[k];
+			const double x = SM_D(rec, x, k), v = SM_D(rec, v, k);
+			to_fixed_dev(x, a.L[k], h[k], l[k]);
 			vh[k] = (float)v;
 			vl[k] = (float)__dsub_rn(v, (double)vh[k]);
-			q = __dadd_rn(q, __dmul_rn(__dmul_rn(v, v), p.m));
-			double r = __dsub_rn(p.x[k], p.xn[k]);
+			q = __dadd_rn(q, __dmul_rn(__dmul_rn(v, v), m));
+			double r = __dsub_rn(x, SM_XN(rec, k));
 			if (r > 0.5 * a.L[k]) r = __dsub_rn(r, a.L[k]);
 			else if (r < -0.5 * a.L[k]) r = __dadd_rn(r, a.L[k]);
 			d2 = __dadd_rn(d2, __dmul_rn(r, r));
 		}
-		const unsigned char tc = (unsigned char)p.type;
+		const unsigned char tc = ((const unsigned char *)rec)[offsetof(seppart, type)];
 		atomicMin(&a.first[tc], (int)i);
 		const int4 ph = make_int4((int)h[0], (int)h[1], (int)h[2], (int)tc);   // .w remapped later
 		a.pos[i] = ph;
 		a.xn[i] = ph;
 		a.xlo[i] = make_uint4(l[0], l[1], l[2], 0u);
-		const double m = p.m;
 		a.vhi[i] = make_float4(vh[0], vh[1], vh[2], (float)m);
 		a.vlo[i] = make_float4(vl[0], vl[1], vl[2], (float)__ddiv_rn(1.0, m));
-		a.frc[i] = make_float4((float)p.f[0], (float)p.f[1], (float)p.f[2], 0.f);
-		const int c0 = p.crossings[0], c1 = p.crossings[1], c2 = p.crossings[2];
+		a.frc[i] = make_float4((float)SM_D(rec, f, 0), (float)SM_D(rec, f, 1), (float)SM_D(rec, f, 2), 0.f);
+		const int c0 = SM_I(rec, crossings, 0), c1 = SM_I(rec, crossings, 1), c2 = SM_I(rec, crossings, 2);
 		a.cross[i] = make_int4(c0, c1, c2, 0);
-		a.cbase[i] = make_int4(c0 - p.cross_neighb[0], c1 - p.cross_neighb[1], c2 - p.cross_neighb[2], 0);
+		a.cbase[i] = make_int4(c0 - SM_I(rec, cross_neighb, 0), c1 - SM_I(rec, cross_neighb, 1),
+				       c2 - SM_I(rec, cross_neighb, 2), 0);
 		a.gid[i] = (int)i;
 		a.inv[i] = (int)i;
-		a.mol[i] = p.molindex;
-		a.charge[i] = (float)p.z;
-		if (fabs(p.z) >= 2.220446049250313e-16) atomicOr(a.has_charge, 1u);
+		a.mol[i] = SM_I(rec, molindex, 0);
+		const double z = SM_D(rec, z, 0);
+		a.charge[i] = (float)z;
+		if (fabs(z) >= 2.220446049250313e-16) atomicOr(a.has_charge, 1u);
 		atomicMax(a.maxd2, (unsigned long long)__double_as_longlong(d2));
 	}
 	// sum of q over the block, fixed tree order
@@ -216,37 +263,65 @@ struct HioDown {
 	const int4 *pos, *cross, *cbase, *xn;
 	const uint4 *xlo;
 	const float4 *vhi, *vlo, *frc;
-	const int *gid;
+	const int *inv;
 	int forces_zero;
 	unsigned *bad;
 };
 
+// Words written back: x, v, f, a (head words 0-11), cross_neighb and
+// crossings (the 24 bytes at their offset), xn.  One thread per record
+// (user index order) fills its words in shared memory from the device arrays
+// at its slot; the block then stores them as contiguous runs.
+#define DW_XVFA 12
+#define DW_CROSS 3
+#define DW (DW_XVFA + DW_CROSS + HW_XN)
+static_assert(offsetof(seppart, a) / 8 + 3 == DW_XVFA, "x v f a are words 0-11");
+static_assert(offsetof(seppart, cross_neighb) % 8 == 0 &&
+	      offsetof(seppart, crossings) == offsetof(seppart, cross_neighb) + 12, "crossing words");
+#define CROSS_W (offsetof(seppart, cross_neighb) / 8)
+
 __global__ void __launch_bounds__(HIO_B) k_download_parts(HioDown a)
 {
-	const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
-	if (s >= a.n) return;
-	const long u = a.gid[s];
-	if (u < 0 || u >= a.n) { atomicOr(a.bad, 1u); return; }
-	seppart &p = a.p[u];
-	const int4 ph = a.pos[s];
-	const uint4 pl = a.xlo[s];
-	const float4 vh = a.vhi[s], vl = a.vlo[s], f = a.frc[s];
-	const int4 c = a.cross[s], cb = a.cbase[s], xh = a.xn[s];
-	const unsigned hi[3] = {(unsigned)ph.x, (unsigned)ph.y, (unsigned)ph.z};
-	const unsigned lo[3] = {pl.x, pl.y, pl.z};
-	const float vhk[3] = {vh.x, vh.y, vh.z}, vlk[3] = {vl.x, vl.y, vl.z}, fk[3] = {f.x, f.y, f.z};
-	const int ck[3] = {c.x, c.y, c.z}, cbk[3] = {cb.x, cb.y, cb.z};
-	const unsigned xnk[3] = {(unsigned)xh.x, (unsigned)xh.y, (unsigned)xh.z};
-	const double m = p.m;
-	for (int k = 0; k < 3; k++) {
-		p.x[k] = from_fixed_dev(hi[k], lo[k], a.L[k]);
-		p.v[k] = __dadd_rn((double)vhk[k], (double)vlk[k]);
-		const double fd = a.forces_zero ? 0.0 : (double)fk[k];
-		p.f[k] = fd;
-		p.a[k] = __ddiv_rn(fd, m);
-		p.crossings[k] = ck[k];
-		p.cross_neighb[k] = ck[k] - cbk[k];
-		p.xn[k] = from_fixed_dev(xnk[k], 0u, a.L[k]);
+	__shared__ unsigned long long sm[HIO_B][DW];
+	const long r0 = blockIdx.x * (long)HIO_B;
+	const int cnt = (int)min((long)HIO_B, a.n - r0);
+	const long u = r0 + threadIdx.x;
+	if (u < a.n) {
+		const long s = a.inv[u];
+		if (s < 0 || s >= a.n) atomicOr(a.bad, 1u);
+		const long ss = (s < 0 || s >= a.n) ? 0 : s;
+		const double m = a.p[u].m;
+		const int4 ph = a.pos[ss];
+		const uint4 pl = a.xlo[ss];
+		const float4 vh = a.vhi[ss], vl = a.vlo[ss], f = a.frc[ss];
+		const int4 c = a.cross[ss], cb = a.cbase[ss], xh = a.xn[ss];
+		const unsigned hi[3] = {(unsigned)ph.x, (unsigned)ph.y, (unsigned)ph.z};
+		const unsigned lo[3] = {pl.x, pl.y, pl.z};
+		const float vhk[3] = {vh.x, vh.y, vh.z}, vlk[3] = {vl.x, vl.y, vl.z}, fk[3] = {f.x, f.y, f.z};
+		const int ck[3] = {c.x, c.y, c.z}, cbk[3] = {cb.x, cb.y, cb.z};
+		const unsigned xnk[3] = {(unsigned)xh.x, (unsigned)xh.y, (unsigned)xh.z};
+		double *w = (double *)sm[threadIdx.x];
+		int *wi = (int *)&sm[threadIdx.x][DW_XVFA];
+		for (int k = 0; k < 3; k++) {
+			w[k] = from_fixed_dev(hi[k], lo[k], a.L[k]);
+			w[3 + k] = __dadd_rn((double)vhk[k], (double)vlk[k]);
+			const double fd = a.forces_zero ? 0.0 : (double)fk[k];
+			w[6 + k] = fd;
+			w[9 + k] = __ddiv_rn(fd, m);
+			wi[k] = ck[k] - cbk[k];          // cross_neighb
+			wi[3 + k] = ck[k];               // crossings
+			w[DW_XVFA + DW_CROSS + k] = from_fixed_dev(xnk[k], 0u, a.L[k]);
+		}
+	}
+	__syncthreads();
+	unsigned long long *g = (unsigned long long *)a.p;
+	for (int q = threadIdx.x; q < cnt * DW; q += HIO_B) {
+		const int r = q / DW, wq = q - r * DW;
+		const long base = (r0 + r) * (long)RW;
+		const long gi = wq < DW_XVFA ? base + wq
+			      : (wq < DW_XVFA + DW_CROSS ? base + CROSS_W + wq - DW_XVFA
+							  : base + XN_W + wq - DW_XVFA - DW_CROSS);
+		g[gi] = sm[r][wq];
 	}
 }
 
@@ -263,7 +338,7 @@ extern "C" int sepdev_download_parts(sepdev *d, void *parts, int forces_zero)
 	a.n = n;
 	for (int k = 0; k < 3; k++) a.L[k] = d->L[k];
 	a.pos = d->pos[d->cur]; a.xlo = d->xlo; a.vhi = d->vhi; a.vlo = d->vlo; a.frc = d->frc;
-	a.cross = d->cross; a.cbase = d->cbase; a.xn = d->xn; a.gid = d->gid;
+	a.cross = d->cross; a.cbase = d->cbase; a.xn = d->xn; a.inv = d->inv;
 	a.forces_zero = forces_zero;
 	a.bad = bad;
 	unsigned hbad = 0;
