@@ -50,58 +50,70 @@ __global__ void k_bin(long n, const int4 *__restrict__ pos, int ncx, int ncy, in
 	}
 }
 
-// exclusive scan of count[0..m) into start[0..m], one block of 1024 threads.
-// The counts are taken in tiles of 1024 (one per thread, coalesced); up to
-// SCAN_REG tiles are loaded together so their latencies overlap, then each
-// tile is scanned with warp shuffles plus one pass over the 32 warp totals,
-// carrying the running sum from tile to tile.
+// exclusive scan of count[0..m) into start[0..m] (start[m] = total), one
+// block of 1024 threads.  The counts are taken in tiles of 1024 * SCAN_REG:
+// each thread owns SCAN_REG consecutive counts (16-byte loads and stores),
+// sums them serially, and one block-wide scan of the thread sums (warp
+// shuffles plus a pass over the 32 warp totals) gives every thread its
+// offset; the running total carries from tile to tile.
 #define SCAN_REG 16
 __global__ void __launch_bounds__(1024) k_scan(long m, const int *__restrict__ count, int *__restrict__ start)
 {
 	__shared__ int wsum[32];
-	__shared__ int carry_s;
 	const unsigned FULL = 0xffffffffu;
 	const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-	if (t == 0) carry_s = 0;
+	int carry = 0;
 	for (long base = 0; base < m; base += 1024L * SCAN_REG) {
+		const long k0 = base + (long)t * SCAN_REG;
 		int v[SCAN_REG];
+		if (k0 + SCAN_REG <= m) {
+			const int4 *src = (const int4 *)(count + k0);
 #pragma unroll
-		for (int r = 0; r < SCAN_REG; r++) {
-			const long k = base + (long)r * 1024 + t;
-			v[r] = k < m ? __ldg(count + k) : 0;
+			for (int q = 0; q < SCAN_REG / 4; q++) {
+				const int4 c = __ldg(src + q);
+				v[4 * q] = c.x; v[4 * q + 1] = c.y; v[4 * q + 2] = c.z; v[4 * q + 3] = c.w;
+			}
+		} else {
+#pragma unroll
+			for (int r = 0; r < SCAN_REG; r++) v[r] = k0 + r < m ? __ldg(count + k0 + r) : 0;
 		}
+		int sum = 0;
 #pragma unroll
-		for (int r = 0; r < SCAN_REG; r++) {
-			if (base + (long)r * 1024 >= m) continue;       // uniform over the block
-			int x = v[r];
+		for (int r = 0; r < SCAN_REG; r++) { const int c = v[r]; v[r] = sum; sum += c; }
+		int x = sum;
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1) {
+			const int y = __shfl_up_sync(FULL, x, o);
+			if (lane >= o) x += y;
+		}
+		if (lane == 31) wsum[w] = x;
+		__syncthreads();
+		if (w == 0) {
+			int ws = wsum[lane];
 #pragma unroll
 			for (int o = 1; o < 32; o <<= 1) {
-				const int y = __shfl_up_sync(FULL, x, o);
-				if (lane >= o) x += y;
+				const int y = __shfl_up_sync(FULL, ws, o);
+				if (lane >= o) ws += y;
 			}
-			__syncthreads();                                // wsum / carry_s of the last tile are consumed
-			if (lane == 31) wsum[w] = x;
-			__syncthreads();
-			if (w == 0) {
-				int ws = wsum[lane];
-#pragma unroll
-				for (int o = 1; o < 32; o <<= 1) {
-					const int y = __shfl_up_sync(FULL, ws, o);
-					if (lane >= o) ws += y;
-				}
-				wsum[lane] = ws;                        // inclusive over warps
-			}
-			__syncthreads();
-			const int carry = carry_s;
-			const int excl = carry + (w ? wsum[w - 1] : 0) + x - v[r];
-			const long k = base + (long)r * 1024 + t;
-			if (k < m) start[k] = excl;
-			__syncthreads();
-			if (t == 1023) carry_s = carry + wsum[31];
+			wsum[lane] = ws;                            // inclusive over warps
 		}
+		__syncthreads();
+		const int off = carry + (w ? wsum[w - 1] : 0) + x - sum;
+		const int total = wsum[31];
+		if (k0 + SCAN_REG <= m) {
+			int4 *dst = (int4 *)(start + k0);
+#pragma unroll
+			for (int q = 0; q < SCAN_REG / 4; q++)
+				dst[q] = make_int4(off + v[4 * q], off + v[4 * q + 1], off + v[4 * q + 2], off + v[4 * q + 3]);
+		} else {
+#pragma unroll
+			for (int r = 0; r < SCAN_REG; r++)
+				if (k0 + r < m) start[k0 + r] = off + v[r];
+		}
+		carry += total;
+		__syncthreads();                                    // wsum is reused by the next tile
 	}
-	__syncthreads();
-	if (t == 0) start[m] = carry_s;
+	if (t == 0) start[m] = carry;
 }
 
 __global__ void k_scatter(long n, const int *__restrict__ cellof, const int *__restrict__ celloff,
