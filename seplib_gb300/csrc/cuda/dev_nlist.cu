@@ -225,6 +225,10 @@ __device__ __forceinline__ float warp_max_f(float v, unsigned mask)
 
 // One warp builds the lists of the tile of 32 particles starting at i0 (n:
 // end of the particles to build); sp and ring are the warp's shared staging.
+// WRAPFAST: runs whose region wraps around the box (small boxes: the batched
+// systems) also get the branch-free test loop; without it they take the
+// general loop, which keeps the common in-box loop's code tight.
+template <bool WRAPFAST>
 __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, float4 *sp, int *ring)
 {
 	const unsigned FULL = 0xffffffffu;
@@ -285,7 +289,7 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 					ring[(cnt & (BT_RING - 1)) * 32 + lane] = j;
 					cnt += hit ? 1 : 0;
 				}
-			} else if (a.excl == SEPDEV_EXCL_NONE) {
+			} else if (WRAPFAST && a.excl == SEPDEV_EXCL_NONE) {
 				// minimum-image separations per candidate, appended in
 				// candidate order without branches (as the local form)
 #pragma unroll 4
@@ -404,7 +408,7 @@ __global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles(long n, BuildArgs
 	__shared__ float4 sp_all[BT_WARPS][BT_CAP];
 	__shared__ int ring_all[BT_WARPS][BT_RING * 32];
 	const int w = threadIdx.x >> 5;
-	build_tile(n, a, ((long)blockIdx.x * BT_WARPS + w) * 32, sp_all[w], ring_all[w]);
+	build_tile<false>(n, a, ((long)blockIdx.x * BT_WARPS + w) * 32, sp_all[w], ring_all[w]);
 }
 
 // Batched systems: each warp builds its tile with its own system's cell grid
@@ -424,7 +428,7 @@ __global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles_batch(BuildArgs a
 	BuildArgs b = a;
 	b.cellstart = a.cellstart + S.coff;
 	for (int k = 0; k < 3; k++) { b.nc[k] = S.nc[k]; b.fs[k] = S.fs; }
-	build_tile(S.off + S.n, b, wg * 32, sp_all[w], ring_all[w]);
+	build_tile<true>(S.off + S.n, b, wg * 32, sp_all[w], ring_all[w]);
 }
 
 // Deterministic order inside each cell: one warp per cell ranks its members
