@@ -175,6 +175,28 @@ def new_system(lib, s):
     return atoms, sys_
 
 
+def write_state(path, s):
+    """the C loop driver's input: n, box, positions, velocities, masses, types"""
+    with open(path, "wb") as fh:
+        fh.write(struct.pack("<q", s.n))
+        fh.write(np.asarray(s.L, "<f8").tobytes())
+        fh.write(np.ascontiguousarray(s.x, "<f8").tobytes())
+        fh.write(np.ascontiguousarray(s.v, "<f8").tobytes())
+        fh.write(np.ascontiguousarray(s.m, "<f8").tobytes())
+        fh.write(np.ascontiguousarray(s.types, "S1").tobytes())
+
+
+def run_driver(state, steps, warmup, rc, dt, skin, t0, tau, top=None):
+    """time the prgs-style loop in C (seplib_gb300/csrc/driver/e2e_loop.c)"""
+    from seplib_gb300 import build as sbuild
+    cmd = [sbuild.E2E, state, str(steps), str(warmup), str(FLUSH_BYTES), repr(rc), repr(dt), repr(skin),
+           repr(t0), repr(tau)] + ([top] if top else [])
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise SystemExit("loop driver failed: %s" % (r.stderr or r.stdout))
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
 def cpu_leg(s, steps, threads):
     """time the oracle's threaded LJ loop on a sample of the workload"""
     import oracle
@@ -326,56 +348,26 @@ def run_butane(args, rank, world):
     """8000 united-atom butane chains (32000 beads) at rho*=0.6, T*=4.0,
     dt=0.002: the prgs/prg2.c step (LJ with intramolecular exclusions, bonds,
     angles, Ryckaert-Bellemans torsions, Nose-Hoover, leap-frog) through the
-    sep C API from host seppart arrays.  The L2 is flushed before every step,
-    outside the per-step wall-clock spans (each step ends in a synchronous
-    read-back of its sepret)."""
-    import tempfile
-    from seplib_gb300 import build, configs, load, sepapi as A
+    sep C API from host seppart arrays, run by the C loop driver.  The L2 is
+    flushed before every step, outside the per-step wall-clock spans (each
+    step ends in a synchronous read-back of its sepret)."""
+    from seplib_gb300 import build, configs
     build.build()
-    lib = load()
     s = configs.butane(nmol=8000, rho=0.6, temp=4.0, seed=3 + rank)
     n = s.n
-    atoms = lib.sep_init(n, A.SEP_NEIGHB)
-    v = A.parts_view(atoms, n)
-    v["x"], v["v"], v["m"], v["type"] = s.x, s.v, s.m, s.types
-    sys_ = lib.sep_sys_setup(s.L[0], s.L[1], s.L[2], RC, 0.002, n, A.SEP_LLIST_NEIGHBLIST)
+    clocks = Clocks()
     with tempfile.TemporaryDirectory() as tmp:
         top = os.path.join(tmp, "b.top")
         configs.write_top(top, s)
-        lib.sep_read_topology_file(atoms, top.encode(), C.byref(sys_), b"q")
-    ret = A.SepRet()
-    alpha = C.c_double(0.0)
-    fun = A.fun_ptr(lib, "sep_lj_shift")
-    rb = (C.c_double * 6)(15.5, 20.3, -21.9, -5.1, 43.8, -52.6)
-
-    def step():
-        lib.sep_reset_retval(C.byref(ret))
-        lib.sep_reset_force(atoms, C.byref(sys_))
-        lib.sep_force_pairs(atoms, b"CC", RC, fun, C.byref(sys_), C.byref(ret), A.SEP_EXCL_SAME_MOL)
-        lib.sep_stretch_harmonic(atoms, 0, 0.4, 33615.0, C.byref(sys_), C.byref(ret))
-        lib.sep_angle_harmonic(atoms, 0, 1.9, 866.0, C.byref(sys_), C.byref(ret))
-        lib.sep_torsion_Ryckaert(atoms, 0, rb, C.byref(sys_), C.byref(ret))
-        lib.sep_nosehoover(atoms, 4.0, C.byref(alpha), 0.1, C.byref(sys_))
-        lib.sep_leapfrog(atoms, C.byref(sys_), C.byref(ret))
-
-    for _ in range(max(3, args.warmup)):
-        step()
-    lib.sep_gpu_sync(atoms)
-    upd0 = sys_.nupdate_neighb
-    clocks = Clocks()
-    clocks.start()
-    barrier(world)
-    t = 0.0
-    for _ in range(args.steps):
-        lib.sep_gpu_flush_l2(atoms, FLUSH_BYTES)
-        t0 = time.perf_counter()
-        step()
-        t += time.perf_counter() - t0
-    barrier(world)
-    clk = clocks.stop()
-    t = allmax(world, t)
-    temp = 2.0 * ret.ekin / (3.0 * n)
-    lib.sep_close(atoms, n)
+        state = os.path.join(tmp, "state.bin")
+        write_state(state, s)
+        clocks.start()
+        barrier(world)
+        run = run_driver(state, args.steps, max(3, args.warmup), RC, 0.002, 0.25, 4.0, 0.1, top)
+        barrier(world)
+        clk = clocks.stop()
+    t = allmax(world, run["seconds"])
+    temp = 2.0 * run["ekin"] / (3.0 * n)
     if rank == 0:
         line = {
             "metric": "particle-steps/s", "value": world * n * args.steps / t, "unit": "particle-steps/s",
@@ -386,9 +378,11 @@ def run_butane(args, rank, world):
             "config": {"workload": "butane: 8000 chains, 32000 beads, rho*=0.6, T*=4.0 (Nose-Hoover "
                                    "tau 0.1), dt=0.002, LJ rc=2.5 with intramolecular exclusions, "
                                    "bonds k=33615 l0=0.4, angles k=866 theta0=1.9, RB torsions",
-                       "path": "sep C API prgs/prg2.c step from host seppart arrays, "
-                               "wall clock per step, L2 flushed between steps (untimed)",
-                       "list_updates": sys_.nupdate_neighb - upd0, "final_temperature": temp},
+                       "path": "prgs/prg2.c step through the sep C API, run in C "
+                               "(seplib_gb300/csrc/driver/e2e_loop.c) from host seppart arrays: "
+                               "first-step upload and final download timed, L2 flushed between "
+                               "steps (untimed)",
+                       "list_updates": run["rebuilds"], "final_temperature": temp},
             "clocks": clk,
         }
         print(json.dumps(line))
@@ -490,18 +484,9 @@ def main():
     e2e_warm = max(3, args.warmup // 10)
     with tempfile.TemporaryDirectory() as tmp:
         state = os.path.join(tmp, "state.bin")
-        with open(state, "wb") as fh:
-            fh.write(struct.pack("<q", n))
-            fh.write(np.asarray(s.L, "<f8").tobytes())
-            fh.write(np.ascontiguousarray(s.x, "<f8").tobytes())
-            fh.write(np.ascontiguousarray(s.v, "<f8").tobytes())
-        from seplib_gb300 import build as sbuild
+        write_state(state, s)
         barrier(world)
-        r = subprocess.run([sbuild.E2E, state, str(e_steps), str(e2e_warm), str(FLUSH_BYTES), repr(RC),
-                            repr(DT), repr(SKIN), repr(T0), repr(TAU)], capture_output=True, text=True)
-        if r.returncode != 0:
-            raise SystemExit("e2e driver failed: %s" % (r.stderr or r.stdout))
-        e2e_run = json.loads(r.stdout.strip().splitlines()[-1])
+        e2e_run = run_driver(state, e_steps, e2e_warm, RC, DT, SKIN, T0, TAU)
     t_e2e = allmax(world, e2e_run["seconds"])
     state_bytes = n * (16 + 16 + 16 + 16 + 16 + 4 + 4 + 16 + 16)   # what upload/download move
     h2d = (state_bytes + 8 * 4 * n) / e_steps + 16

@@ -1,21 +1,27 @@
 /*
  * e2e_loop.c - the prgs-style MD step loop through the sep C API, timed by
- * wall clock the way a seplib program runs it (prgs/prg0.c's loop with a
- * Nose-Hoover thermostat):
+ * wall clock the way a seplib program runs it: prgs/prg0.c's loop with a
+ * Nose-Hoover thermostat,
  *
  *     sep_reset_retval; sep_reset_force; sep_force_pairs(lj_shift);
  *     sep_nosehoover; sep_leapfrog
+ *
+ * or, with a topology, the molecular step of prgs/prg2.c (LJ between
+ * different molecules, harmonic bonds and angles, Ryckaert-Bellemans
+ * torsions, Nose-Hoover, leap-frog) with the united-atom butane force field
+ * (bonds k = 33615, l0 = 0.4; angles k = 866, theta0 = 1.9; torsion
+ * coefficients 15.5, 20.3, -21.9, -5.1, 43.8, -52.6).
  *
  * The particle arrays live in host memory.  The first timed step uploads
  * them (the state is marked host-modified before it); every step reads its
  * sepret values back; the final sep_gpu_sync (timed) downloads x, v and f.
  *
- *   sep_e2e_loop STATE STEPS WARMUP FLUSH_BYTES RC DT SKIN T0 TAU
+ *   sep_e2e_loop STATE STEPS WARMUP FLUSH_BYTES RC DT SKIN T0 TAU [TOPOLOGY]
  *
- * STATE is a binary file: int64 n, double L[3], double x[3n], double v[3n]
- * (mass 1, type 'A').  Before every timed step FLUSH_BYTES are written on
- * the device (untimed) so no step finds the previous one's data in L2.
- * Prints one JSON line.
+ * STATE is a binary file: int64 n, double L[3], double x[3n], double v[3n],
+ * double m[n], char type[n].  Before every timed step FLUSH_BYTES are
+ * written on the device (untimed) so no step finds the previous one's data
+ * in L2.  Prints one JSON line.
  */
 #define _POSIX_C_SOURCE 199309L
 #include <stdint.h>
@@ -33,10 +39,11 @@ static double now(void)
 
 int main(int argc, char **argv)
 {
-	if (argc != 10) {
-		fprintf(stderr, "usage: %s STATE STEPS WARMUP FLUSH_BYTES RC DT SKIN T0 TAU\n", argv[0]);
+	if (argc != 10 && argc != 11) {
+		fprintf(stderr, "usage: %s STATE STEPS WARMUP FLUSH_BYTES RC DT SKIN T0 TAU [TOPOLOGY]\n", argv[0]);
 		return 2;
 	}
+	const char *top = argc == 11 ? argv[10] : NULL;
 	const long steps = atol(argv[2]), warmup = atol(argv[3]), flush = atol(argv[4]);
 	const double rc = atof(argv[5]), dt = atof(argv[6]), skin = atof(argv[7]);
 	const double temp = atof(argv[8]), tau = atof(argv[9]);
@@ -46,29 +53,49 @@ int main(int argc, char **argv)
 	double L[3];
 	if (fread(&n64, sizeof n64, 1, fp) != 1 || fread(L, sizeof(double), 3, fp) != 3) return 2;
 	const long n = (long)n64;
-	double *xv = malloc(sizeof(double) * 6 * n);
-	if (!xv || fread(xv, sizeof(double), 6 * n, fp) != (size_t)(6 * n)) return 2;
+	double *xv = malloc(sizeof(double) * 7 * n);
+	char *ty = malloc(n);
+	if (!xv || !ty || fread(xv, sizeof(double), 7 * n, fp) != (size_t)(7 * n) ||
+	    fread(ty, 1, n, fp) != (size_t)n)
+		return 2;
 	fclose(fp);
 
 	seppart *atoms = sep_init(n, SEP_NEIGHB);
-	for (long i = 0; i < n; i++)
+	for (long i = 0; i < n; i++) {
 		for (int k = 0; k < 3; k++) {
 			atoms[i].x[k] = xv[3 * i + k];
 			atoms[i].v[k] = xv[3 * n + 3 * i + k];
 		}
+		atoms[i].m = xv[6 * n + i];
+		atoms[i].type = ty[i];
+	}
 	free(xv);
+	const char types[3] = {ty[0], ty[0], 0};
+	free(ty);
 	sepsys sys = sep_sys_setup(L[0], L[1], L[2], rc, dt, n, SEP_LLIST_NEIGHBLIST);
 	sep_set_skin(&sys, skin);
+	if (top) sep_read_topology_file(atoms, top, &sys, 'q');
+	double rb[6] = {15.5, 20.3, -21.9, -5.1, 43.8, -52.6};
 	sepret ret;
 	double alpha = 0.0;
 
-	for (long s = 0; s < warmup; s++) {
-		sep_reset_retval(&ret);
-		sep_reset_force(atoms, &sys);
-		sep_force_pairs(atoms, "AA", rc, sep_lj_shift, &sys, &ret, SEP_ALL);
-		sep_nosehoover(atoms, temp, &alpha, tau, &sys);
-		sep_leapfrog(atoms, &sys, &ret);
-	}
+#define STEP()                                                                              \
+	do {                                                                                \
+		sep_reset_retval(&ret);                                                     \
+		sep_reset_force(atoms, &sys);                                               \
+		if (top) {                                                                  \
+			sep_force_pairs(atoms, types, rc, sep_lj_shift, &sys, &ret, SEP_EXCL_SAME_MOL); \
+			sep_stretch_harmonic(atoms, 0, 0.4, 33615.0, &sys, &ret);          \
+			sep_angle_harmonic(atoms, 0, 1.9, 866.0, &sys, &ret);              \
+			sep_torsion_Ryckaert(atoms, 0, rb, &sys, &ret);                     \
+		} else {                                                                    \
+			sep_force_pairs(atoms, types, rc, sep_lj_shift, &sys, &ret, SEP_ALL);      \
+		}                                                                           \
+		sep_nosehoover(atoms, temp, &alpha, tau, &sys);                             \
+		sep_leapfrog(atoms, &sys, &ret);                                            \
+	} while (0)
+
+	for (long s = 0; s < warmup; s++) STEP();
 	sep_gpu_sync(atoms);
 	sep_gpu_invalidate(atoms);          /* the first timed step uploads the host arrays */
 
@@ -77,11 +104,7 @@ int main(int argc, char **argv)
 	for (long s = 0; s < steps; s++) {
 		sep_gpu_flush_l2(atoms, flush);
 		const double t0 = now();
-		sep_reset_retval(&ret);
-		sep_reset_force(atoms, &sys);
-		sep_force_pairs(atoms, "AA", rc, sep_lj_shift, &sys, &ret, SEP_ALL);
-		sep_nosehoover(atoms, temp, &alpha, tau, &sys);
-		sep_leapfrog(atoms, &sys, &ret);
+		STEP();
 		const double dtw = now() - t0;
 		t += dtw;
 		if (s == 0) t_first = dtw;
