@@ -6,7 +6,9 @@
 // The reference loops over terms and scatters into both/all atoms.  Here
 // every atom gathers: one thread per particle walks the terms it belongs to
 // (an incidence CSR built once from the topology) and computes its own share
-// of each term, so the force array sees no atomics.  Each term is evaluated
+// of each term, so the force array sees no atomics.  The bonded calls of a
+// step are deferred and evaluated together, one pending term per kind, in
+// one launch.  Each term is evaluated
 // by every member atom from bit-identical inputs, so the shares cancel
 // exactly; energy, virial and the per-term observable are taken from the
 // role-0 atom only.  Separations come from the full 64-bit fixed-point
@@ -21,6 +23,8 @@
 #define TERM_DIHED 2
 #define ENC(kind, role, idx) (((unsigned)(kind) << 30) | ((unsigned)(role) << 27) | (unsigned)(idx))
 
+// One launch evaluates up to one pending term of each kind (bond, angle,
+// torsion) with its own parameters and accumulator slot.
 struct BondArgs {
 	const int4 *pos;
 	const uint4 *xlo;
@@ -32,11 +36,14 @@ struct BondArgs {
 	float *term_out;
 	long term_off[3];
 	float fs[3];
-	int type;
-	float p0, p1;         // bonds: l0, k; angles: theta0 (or cos(pi - theta0)), k
+	int has[3], type[3];
+	float bl0, bk;        // bonds: l0, k
+	float ap0, ak;        // angles: theta0 (or cos(pi - theta0)), k
 	int cossq;
-	float g[6];
-	long long *slot;
+	float g[6];           // torsions
+	int fld0[3];          // first accumulator field of each kind's slot
+	int accumulate;       // add to the stored forces (else store)
+	long long *slots;
 };
 
 // minimum-image separation x_a - x_b from the full fixed-point words
@@ -61,51 +68,53 @@ __device__ __forceinline__ float3 sep64(const BondArgs &a, int sa, int sb)
 
 __device__ __forceinline__ float dot3(float3 u, float3 w) { return u.x * w.x + u.y * w.y + u.z * w.z; }
 
-template <int KIND>
+// Each thread walks the incidence list of its particle once; every incident
+// term of a kind that is pending adds this atom's share.
 __global__ void __launch_bounds__(256) k_bonded(long n, BondArgs a)
 {
 	const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
-	float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
+	float fx = 0.f, fy = 0.f, fz = 0.f, eb = 0.f, ea = 0.f, ed = 0.f;
 	float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 	if (s < n) {
 		const int u = a.gid[s];
 		for (int t = a.inc_start[u], te = a.inc_start[u + 1]; t < te; t++) {
 			const unsigned code = (unsigned)a.inc_term[t];
-			if ((int)(code >> 30) != KIND) continue;
+			const int kind = (int)(code >> 30);
+			if (!a.has[kind]) continue;
 			const int role = (code >> 27) & 7;
 			const int idx = code & ((1u << 27) - 1u);
-			if (KIND == TERM_BOND) {
+			if (kind == TERM_BOND) {
 				const uint4 b = a.bonds[idx];
-				if ((int)b.z != a.type) continue;
+				if ((int)b.z != a.type[0]) continue;
 				const int sa = a.inv[b.x], sb = a.inv[b.y];
 				const float3 r = sep64(a, sa, sb);
 				const float r2 = dot3(r, r), dist = sqrtf(r2);
-				const float ft = -a.p1 * (dist - a.p0) / dist;
+				const float ft = -a.bk * (dist - a.bl0) / dist;
 				const float sg = role == 0 ? 1.f : -1.f;
 				fx += sg * ft * r.x; fy += sg * ft * r.y; fz += sg * ft * r.z;
 				if (role == 0) {
-					e += 0.5f * a.p1 * (dist - a.p0) * (dist - a.p0);
+					eb += 0.5f * a.bk * (dist - a.bl0) * (dist - a.bl0);
 					const float gx = ft * r.x, gy = ft * r.y, gz = ft * r.z;
 					w[0] += gx * r.x; w[1] += gx * r.y; w[2] += gx * r.z;
 					w[3] += gy * r.y; w[4] += gy * r.z; w[5] += gz * r.z;
 					a.term_out[a.term_off[0] + idx] = dist;
 				}
-			} else if (KIND == TERM_ANGLE) {
+			} else if (kind == TERM_ANGLE) {
 				const uint4 g = a.angles[idx];
-				if ((int)g.w != a.type) continue;
+				if ((int)g.w != a.type[1]) continue;
 				const int sa = a.inv[g.x], sb = a.inv[g.y], sc = a.inv[g.z];
 				const float3 d1 = sep64(a, sb, sa), d2 = sep64(a, sc, sb);
 				const float c11 = dot3(d1, d1), c12 = dot3(d1, d2), c22 = dot3(d2, d2);
 				const float cD = sqrtf(c11 * c22), cc = c12 / cD;
 				float pref, th;
 				if (a.cossq) {
-					pref = -a.p1 * (cc - a.p0);
+					pref = -a.ak * (cc - a.ap0);
 					th = 3.14159265358979f - acosf(fminf(fmaxf(cc, -1.f), 1.f));
-					if (role == 0) e += 0.5f * a.p1 * (cc - a.p0) * (cc - a.p0);
+					if (role == 0) ea += 0.5f * a.ak * (cc - a.ap0) * (cc - a.ap0);
 				} else {
 					th = 3.14159265358979f - acosf(fminf(fmaxf(cc, -1.f), 1.f));
-					pref = -a.p1 * (th - a.p0);
-					if (role == 0) e += 0.5f * a.p1 * (th - a.p0) * (th - a.p0);
+					pref = -a.ak * (th - a.ap0);
+					if (role == 0) ea += 0.5f * a.ak * (th - a.ap0) * (th - a.ap0);
 				}
 				const float q11 = c12 / c11, q22 = c12 / c22;
 				const float3 f1 = make_float3(pref * (q11 * d1.x - d2.x) / cD, pref * (q11 * d1.y - d2.y) / cD,
@@ -117,7 +126,7 @@ __global__ void __launch_bounds__(256) k_bonded(long n, BondArgs a)
 				else { fx += f2.x; fy += f2.y; fz += f2.z; }
 			} else {
 				const uint4 q = a.diheds[idx];
-				if (a.dtype[idx] != a.type) continue;
+				if (a.dtype[idx] != a.type[2]) continue;
 				const int sa = a.inv[q.x], sb = a.inv[q.y], sc = a.inv[q.z], sd = a.inv[q.w];
 				const float3 r1 = sep64(a, sb, sa), r2 = sep64(a, sc, sb), r3 = sep64(a, sd, sc);
 				const float c11 = dot3(r1, r1), c12 = dot3(r1, r2), c13 = dot3(r1, r3);
@@ -139,7 +148,7 @@ __global__ void __launch_bounds__(256) k_bonded(long n, BondArgs a)
 							      k2 * (t4 * r1.z + t5 * r2.z + t6 * r3.z));
 				if (role == 0) {
 					fx += f1.x; fy += f1.y; fz += f1.z;
-					e += gg[0] + (gg[1] + (gg[2] + (gg[3] + (gg[4] + gg[5] * cc) * cc) * cc) * cc) * cc;
+					ed += gg[0] + (gg[1] + (gg[2] + (gg[3] + (gg[4] + gg[5] * cc) * cc) * cc) * cc) * cc;
 					a.term_out[a.term_off[2] + idx] = 3.14159265358979f - acosf(fminf(fmaxf(cc, -1.f), 1.f));
 				} else if (role == 1) {
 					fx += -(1.f + cR1) * f1.x + cR2 * f2.x;
@@ -154,17 +163,29 @@ __global__ void __launch_bounds__(256) k_bonded(long n, BondArgs a)
 				}
 			}
 		}
-		if (fx != 0.f || fy != 0.f || fz != 0.f) {
-			float4 f = a.frc[s];
-			f.x += fx; f.y += fy; f.z += fz;
-			a.frc[s] = f;
+		if (a.accumulate) {
+			if (fx != 0.f || fy != 0.f || fz != 0.f) {
+				float4 f = a.frc[s];
+				f.x += fx; f.y += fy; f.z += fz;
+				a.frc[s] = f;
+			}
+		} else {
+			a.frc[s] = make_float4(fx, fy, fz, 0.f);
 		}
 	}
-	float v[13] = {e, w[0], w[1], w[2], w[3], w[4], w[5], w[0], w[1], w[2], w[3], w[4], w[5]};
-	const int fld[13] = {SLOT_EPOT0, SLOT_POTP, SLOT_POTP + 1, SLOT_POTP + 2, SLOT_POTP + 3,
-			     SLOT_POTP + 4, SLOT_POTP + 5, SLOT_POTPB, SLOT_POTPB + 1, SLOT_POTPB + 2,
-			     SLOT_POTPB + 3, SLOT_POTPB + 4, SLOT_POTPB + 5};
-	block_to_slot<13>(v, fld, a.slot, 0.f, -1);
+	// the bond slot takes energy, pot_P and pot_P_bond; angles and torsions
+	// their energy (kinds not pending add zero to field 0 of slot 0)
+	float v[15] = {eb, w[0], w[1], w[2], w[3], w[4], w[5], w[0], w[1], w[2], w[3], w[4], w[5], ea, ed};
+	int fld[15];
+	fld[0] = a.fld0[0] + SLOT_EPOT0;
+#pragma unroll
+	for (int k = 0; k < 6; k++) {
+		fld[1 + k] = a.fld0[0] + SLOT_POTP + k;
+		fld[7 + k] = a.fld0[0] + SLOT_POTPB + k;
+	}
+	fld[13] = a.fld0[1] + SLOT_EPOT0;
+	fld[14] = a.fld0[2] + SLOT_EPOT0;
+	block_to_slot<15>(v, fld, a.slots, 0.f, -1);
 }
 
 template <class T>
@@ -245,8 +266,10 @@ out:
 	return rc;
 }
 
-static void bond_args(sepdev *d, BondArgs &a, int type, int slot)
+extern "C" int sepdev_bonded(sepdev *d, const sepdev_bterm *t, int nt, int accumulate)
 {
+	if (!d->inc_start || nt < 1 || nt > 3) return SEPDEV_EINVAL;
+	BondArgs a;
 	memset(&a, 0, sizeof a);
 	a.pos = d->pos[d->cur]; a.xlo = d->xlo; a.frc = d->frc;
 	a.gid = d->gid; a.inv = d->inv;
@@ -255,41 +278,25 @@ static void bond_args(sepdev *d, BondArgs &a, int type, int slot)
 	a.term_out = d->term_out;
 	a.term_off[0] = 0; a.term_off[1] = d->nbond; a.term_off[2] = (long)d->nbond + d->nangle;
 	for (int k = 0; k < 3; k++) a.fs[k] = d->fscale[k];
-	a.type = type;
-	a.slot = d->slots + (long)slot * SLOT_FIELDS;
-}
-
-extern "C" int sepdev_bonds(sepdev *d, int type, double l0, double k, int slot)
-{
-	if (!d->inc_start || slot < 0 || slot >= d->nslots) return SEPDEV_EINVAL;
-	BondArgs a;
-	bond_args(d, a, type, slot);
-	a.p0 = (float)l0; a.p1 = (float)k;
-	k_bonded<TERM_BOND><<<grid_for(d->n, 256), 256, 0, d->st>>>(d->n, a);
-	CKL(d);
-	return SEPDEV_OK;
-}
-
-extern "C" int sepdev_angles(sepdev *d, int type, double theta0, double k, int cossq, int slot)
-{
-	if (!d->inc_start || slot < 0 || slot >= d->nslots) return SEPDEV_EINVAL;
-	BondArgs a;
-	bond_args(d, a, type, slot);
-	a.cossq = cossq;
-	a.p0 = cossq ? (float)cos(3.14159265358979 - theta0) : (float)theta0;
-	a.p1 = (float)k;
-	k_bonded<TERM_ANGLE><<<grid_for(d->n, 256), 256, 0, d->st>>>(d->n, a);
-	CKL(d);
-	return SEPDEV_OK;
-}
-
-extern "C" int sepdev_torsions(sepdev *d, int type, const double g[6], int slot)
-{
-	if (!d->inc_start || slot < 0 || slot >= d->nslots) return SEPDEV_EINVAL;
-	BondArgs a;
-	bond_args(d, a, type, slot);
-	for (int k = 0; k < 6; k++) a.g[k] = (float)g[k];
-	k_bonded<TERM_DIHED><<<grid_for(d->n, 256), 256, 0, d->st>>>(d->n, a);
+	for (int q = 0; q < nt; q++) {
+		const int k = t[q].kind;
+		if (k < 0 || k > 2 || a.has[k] || t[q].slot < 0 || t[q].slot >= d->nslots) return SEPDEV_EINVAL;
+		a.has[k] = 1;
+		a.type[k] = t[q].type;
+		a.fld0[k] = t[q].slot * SLOT_FIELDS;
+		if (k == TERM_BOND) {
+			a.bl0 = (float)t[q].p0; a.bk = (float)t[q].p1;
+		} else if (k == TERM_ANGLE) {
+			a.cossq = t[q].cossq;
+			a.ap0 = t[q].cossq ? (float)cos(3.14159265358979 - t[q].p0) : (float)t[q].p0;
+			a.ak = (float)t[q].p1;
+		} else {
+			for (int g = 0; g < 6; g++) a.g[g] = (float)t[q].g[g];
+		}
+	}
+	a.accumulate = accumulate;
+	a.slots = d->slots;
+	k_bonded<<<grid_for(d->n, 256), 256, 0, d->st>>>(d->n, a);
 	CKL(d);
 	return SEPDEV_OK;
 }

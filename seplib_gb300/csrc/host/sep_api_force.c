@@ -207,53 +207,58 @@ void sep_coulomb_sf(seppart *ptr, double cf, sepsys *sys, sepret *retval, const 
 
 /* ---- bonded terms (source/sepmol.c:372-587) ---------------------------------------- */
 
-static rt_ctx *bonded_prep(seppart *ptr, sepsys *sys, const char *who)
+/* The bonded calls are deferred: each takes its accumulator slot now and is
+ * evaluated with the other pending bonded terms in one launch when the
+ * forces are next needed (normally just before the leap-frog). */
+static void bonded(seppart *ptr, sepsys *sys, const char *who, sepret *ret, int op,
+		   sepdev_bterm *t)
 {
 	rt_ctx *c = rt_get(ptr, who);
 	if (!c->topo_sys) c->topo_sys = sys;
 	rt_need_device(c, sys);
-	rt_materialize_forces(c);
 	c->host_valid = 0;
-	return c;
+	t->slot = rt_new_slot(c);
+	rt_queue_bonded(c, t);
+	rt_add_op(c, ret, op, t->slot, 0);
 }
 
 void sep_stretch_harmonic(sepatom *aptr, int type, const double lbond, const double ks,
 			  sepsys *sys, sepret *ret)
 {
 	if (!sys->molptr->flag_bonds) return;
-	rt_ctx *c = bonded_prep(aptr, sys, __func__);
-	const int slot = rt_new_slot(c);
-	rt_check(sepdev_bonds(c->dev, type, lbond, ks, slot), "stretch");
-	rt_add_op(c, ret, OP_BOND, slot, 0);
+	sepdev_bterm t = {0};
+	t.kind = 0; t.type = type; t.p0 = lbond; t.p1 = ks;
+	bonded(aptr, sys, __func__, ret, OP_BOND, &t);
+}
+
+static void angles(seppart *ptr, int type, double angle0, double k, int cossq, sepsys *sys,
+		   sepret *ret, const char *who)
+{
+	if (!sys->molptr->flag_angles) return;
+	sepdev_bterm t = {0};
+	t.kind = 1; t.type = type; t.p0 = angle0; t.p1 = k; t.cossq = cossq;
+	bonded(ptr, sys, who, ret, OP_EADD, &t);
 }
 
 void sep_angle_harmonic(sepatom *ptr, int type, const double angle0, const double k,
 			sepsys *sys, sepret *ret)
 {
-	if (!sys->molptr->flag_angles) return;
-	rt_ctx *c = bonded_prep(ptr, sys, __func__);
-	const int slot = rt_new_slot(c);
-	rt_check(sepdev_angles(c->dev, type, angle0, k, 0, slot), "angle");
-	rt_add_op(c, ret, OP_EADD, slot, 0);
+	angles(ptr, type, angle0, k, 0, sys, ret, __func__);
 }
 
 void sep_angle_cossq(sepatom *ptr, int type, const double angle0, const double k,
 		     sepsys *sys, sepret *ret)
 {
-	if (!sys->molptr->flag_angles) return;
-	rt_ctx *c = bonded_prep(ptr, sys, __func__);
-	const int slot = rt_new_slot(c);
-	rt_check(sepdev_angles(c->dev, type, angle0, k, 1, slot), "angle");
-	rt_add_op(c, ret, OP_EADD, slot, 0);
+	angles(ptr, type, angle0, k, 1, sys, ret, __func__);
 }
 
 void sep_torsion_Ryckaert(sepatom *ptr, int type, const double g[6], sepsys *sys, sepret *ret)
 {
 	if (!sys->molptr->flag_dihedrals) return;
-	rt_ctx *c = bonded_prep(ptr, sys, __func__);
-	const int slot = rt_new_slot(c);
-	rt_check(sepdev_torsions(c->dev, type, g, slot), "torsion");
-	rt_add_op(c, ret, OP_EADD, slot, 0);
+	sepdev_bterm t = {0};
+	t.kind = 2; t.type = type;
+	for (int k = 0; k < 6; k++) t.g[k] = g[k];
+	bonded(ptr, sys, __func__, ret, OP_EADD, &t);
 }
 
 /* ---- topology reader (source/sepmol.c:5-369) ----------------------------------------

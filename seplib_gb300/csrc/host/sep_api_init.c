@@ -371,6 +371,7 @@ void sep_reset_force(seppart *ptr, sepsys *sys)
 	if (c->dev && c->dev_valid) {
 		/* stored device forces become logically zero; pending friction dies with them */
 		if (c->pass_slot >= 0) rt_launch_pass(c);
+		rt_launch_bonded(c);
 		c->forces_zero = 1;
 		c->friction = 0;
 		c->friction_alpha = 0.0;

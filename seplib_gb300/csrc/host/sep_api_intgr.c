@@ -48,6 +48,8 @@ void sep_leapfrog(seppart *ptr, sepsys *sys, sepret *retval)
 	rt_ctx *c = rt_get(ptr, __func__);
 	rt_need_device(c, sys);
 	int lf;
+	/* pending bonded terms go first; the step adds the pair forces to them */
+	rt_launch_bonded(c);
 	if (c->pass_slot >= 0) {
 		sepdev_pairset ps;
 		extern void rt_pairset(rt_ctx *c, sepdev_pairset *ps);

@@ -47,7 +47,7 @@ static void dpd(const char *caller, seppart *ptr, const char *types, double cf, 
 	/* the forces the DPD pass adds to must exist first; a reset that is
 	 * still pending is folded into the pass */
 	int accumulate = 1;
-	if (c->forces_zero && c->pass_slot < 0 && !c->friction) {
+	if (c->forces_zero && c->pass_slot < 0 && c->nbq == 0 && !c->friction) {
 		accumulate = 0;
 		c->forces_zero = 0;
 	} else {

@@ -428,9 +428,31 @@ void rt_launch_pass(rt_ctx *c)
 	clear_pass(c);
 }
 
+/* Bonded calls are evaluated together: the terms of one kind each that are
+ * pending go to one launch when the forces are next needed.  A second term
+ * of a kind already pending launches the batch first. */
+void rt_queue_bonded(rt_ctx *c, const sepdev_bterm *t)
+{
+	for (int k = 0; k < c->nbq; k++)
+		if (c->bq[k].kind == t->kind) {
+			rt_launch_bonded(c);
+			break;
+		}
+	c->bq[c->nbq++] = *t;
+}
+
+void rt_launch_bonded(rt_ctx *c)
+{
+	if (c->nbq == 0) return;
+	rt_check(sepdev_bonded(c->dev, c->bq, c->nbq, !c->forces_zero), "bonded forces");
+	c->forces_zero = 0;
+	c->nbq = 0;
+}
+
 void rt_materialize_forces(rt_ctx *c)
 {
 	if (pass_pending(c)) rt_launch_pass(c);
+	rt_launch_bonded(c);
 	if (c->forces_zero) {
 		rt_check(sepdev_zero_forces(c->dev), "force reset");
 		c->forces_zero = 0;
@@ -539,6 +561,7 @@ void rt_prepare_list(rt_ctx *c, sepsys *sys, unsigned opt, int brute_excl_bonds)
 	if (!c->list_stale) return;
 	/* the pending pass was meant for the old list */
 	if (pass_pending(c)) rt_launch_pass(c);
+	rt_launch_bonded(c);
 	if (want_excl != SEPDEV_EXCL_NONE && want_excl != SEPDEV_EXCL_SAMEMOL && c->topo_dirty)
 		rt_need_device(c, sys);
 	rt_check(sepdev_build_list(c->dev, rlist, want_excl, c->trigger_next), "neighbour-list build");

@@ -90,6 +90,8 @@ typedef struct rt_ctx {
 	int pass_slot;          /* slot of the pending pair pass, -1 if none */
 	int mv_slot;            /* its molecular sums' slot (molecular tensor on) */
 	int forces_zero;        /* stored forces are logically zero */
+	sepdev_bterm bq[3];     /* pending bonded terms, at most one per kind */
+	int nbq;
 	int friction;           /* Nose-Hoover friction pending */
 	double friction_alpha;
 
@@ -152,6 +154,8 @@ void rt_add_op(rt_ctx *c, sepret *ret, int kind, int slot, int chan);
 void rt_launch_pass(rt_ctx *c);          /* launch the pending pair pass (force only) */
 void rt_open_pass(rt_ctx *c, sepret *ret); /* new pending pass: slots and their operations */
 void rt_pass_mol_slot(rt_ctx *c);          /* before launching the pending pass */
+void rt_queue_bonded(rt_ctx *c, const sepdev_bterm *t); /* defer a bonded term */
+void rt_launch_bonded(rt_ctx *c);        /* launch the pending bonded terms (one kernel) */
 void rt_materialize_forces(rt_ctx *c);   /* pending pass + friction + zeroing into stored forces */
 void rt_read_slots(rt_ctx *c, sepsys *sys, int leapfrog_slot);   /* sync, apply ops */
 int rt_ret_pending(rt_ctx *c, const sepret *ret);

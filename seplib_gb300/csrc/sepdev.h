@@ -179,9 +179,19 @@ int sepdev_zero_forces(sepdev *d);
  * nd dihedrals (a,b,c,d,type). */
 int sepdev_set_topology(sepdev *d, int nb, const unsigned *blist, int na,
 			const unsigned *alist, int nd, const unsigned *dlist);
-int sepdev_bonds(sepdev *d, int type, double l0, double k, int slot);
-int sepdev_angles(sepdev *d, int type, double theta0, double k, int cossq, int slot);
-int sepdev_torsions(sepdev *d, int type, const double g[6], int slot);
+/* Bonded terms, up to one of each kind per launch: kind 0 bonds (p0 = l0,
+ * p1 = k; energy, pot_P and pot_P_bond to the term's slot), 1 angles
+ * (p0 = theta0, p1 = k, cossq: the cos^2 form; energy), 2 Ryckaert-Bellemans
+ * torsions (g; energy).  The forces are added to the stored ones
+ * (accumulate) or stored. */
+typedef struct {
+	int kind, type;
+	double p0, p1;
+	int cossq;
+	double g[6];
+	int slot;
+} sepdev_bterm;
+int sepdev_bonded(sepdev *d, const sepdev_bterm *t, int nt, int accumulate);
 /* per-term observables of the last call of each kind (0 bond lengths,
  * 1 angles, 2 dihedral angles), in topology order */
 int sepdev_term_values(sepdev *d, int kind, double *out);
