@@ -7,13 +7,19 @@
  * per-sampler structures behind the pointers are this library's own and
  * opaque to programs).  Supported samplers: "sacf" (stress autocorrelation),
  * "vacf" (velocity autocorrelation), "msd" (mean square displacement,
- * non-Gaussian parameter, self-intermediate scattering function).  They
- * write the reference's files (sacf.dat, vacf.dat, msd.dat,
- * msd-gaussparam.dat, msd-incoherent.dat, msd-k.dat) in the same formats.
- * The particle data a sample needs stays on the GPU: vacf keeps its window
- * of velocities in device memory and msd reduces on the device, so sampling
- * costs no download of the particle arrays.  Any other sampler name ends
- * the program with sep_error.
+ * non-Gaussian parameter, self-intermediate scattering function), and the
+ * molecular "msacf" (molecular stress autocorrelation), "mvacf" (centre-of-
+ * mass velocity autocorrelation) and "mgh" (molecular generalised
+ * hydrodynamics: momentum, density, energy, spin and dipole correlations
+ * per wavevector along y).  They write the reference's files (sacf.dat,
+ * vacf.dat, msd.dat, msd-gaussparam.dat, msd-incoherent.dat, msd-k.dat,
+ * msacf.dat, mvacf.dat, mgh-*.dat) in the same formats.  The particle data
+ * a sample needs stays on the GPU: vacf and mvacf keep their window of
+ * velocities in device memory, msd and mgh reduce on the device, so sampling
+ * costs no download of the particle arrays.  Unlike the reference, mgh does
+ * not write the centres of mass, spins and dipoles it evaluates back into
+ * the program's molecule array.  Any other sampler name ends the program
+ * with sep_error.
  */
 #ifndef SEP_GB300_SEPSAMPLER_H
 #define SEP_GB300_SEPSAMPLER_H
@@ -67,9 +73,12 @@ typedef struct {
 /* Reference include/sepsampler.h:247. */
 sepsampler sep_init_sampler(void);
 
-/* Reference include/sepsampler.h:275: "sacf", "vacf": lvec samples over a
- * time span (double); "msd": lvec samples (0: log-spaced) over a time span
- * (double), number of wave vectors (int), particle type (char). */
+/* Reference include/sepsampler.h:275: "sacf", "vacf", "msacf", "mvacf":
+ * lvec samples over a time span (double); "msd": lvec samples (0:
+ * log-spaced) over a time span (double), number of wave vectors (int),
+ * particle type (char); "mgh": lvec samples over a time span (double),
+ * number of wave vectors (int), safe (int; 0 also evaluates the angular
+ * velocities).  The molecular samplers need sep_add_mol_sampler first. */
 void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec, ...);
 
 /* Reference include/sepsampler.h:281. */
@@ -78,7 +87,7 @@ void sep_close_sampler(sepsampler *ptr);
 /* Reference include/sepsampler.h:291: call once per step n. */
 void sep_sample(seppart *pptr, sepsampler *sptr, sepret *ret, sepsys sys, unsigned n);
 
-/* Reference include/sepsampler.h:299 (molecular samplers are not provided). */
+/* Reference include/sepsampler.h:299: the molecules of msacf, mvacf and mgh. */
 void sep_add_mol_sampler(sepsampler *sptr, sepmol *mols);
 
 #ifdef __cplusplus

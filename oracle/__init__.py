@@ -461,3 +461,162 @@ def mol_pressure(F, x, v, m, L, molindex, nmol):
     lb.ora_mol_pressure(C.c_int(nmol), _p(F, C.c_double), _p(cm, C.c_double), _p(vcm, C.c_double),
                         _p(mmol, C.c_double), _p(L, C.c_double), _p(kin, C.c_double), _p(pot, C.c_double))
     return kin.reshape(3, 3), pot.reshape(3, 3), cm, vcm
+
+
+# ---- molecular samplers (msacf, mvacf, mgh) ---------------------------------------
+
+
+def _wrap(d, L):
+    """sep_Wrap (reference include/sepmisc.h:81-85), elementwise"""
+    d = np.array(d, dtype=float)
+    return np.where(d > 0.5 * L, d - L, np.where(d < -0.5 * L, d + L, d))
+
+
+def mol_props(x, v, m, z, first, nuau, start, atoms, L, pel, unsafe):
+    """Per-molecule quantities of the mgh sampler in FP64, one molecule at a
+    time as the reference does: centre of mass from the chain of consecutive
+    indices from the first atom, bonds unwrapped, wrapped into the box
+    (source/sepmol.c:683-729); centre-of-mass velocity (:731-748); spin
+    s = sum dcm x m v and the inertia tensor, with w = I^-1 s in the unsafe
+    mode (trace/3 for a singular tensor; :750-825); the dipole of the
+    positive and negative charges (:1036-1083; `pel` is updated in place and
+    keeps its value for a molecule without both signs).  Returns a dict of
+    (nmol, 3) arrays cm, v, s, w and the (nmol,) masses M and kinetic
+    energies ek."""
+    x = np.asarray(x, float); v = np.asarray(v, float); m = np.asarray(m, float)
+    z = np.asarray(z, float); L = np.asarray(L, float)
+    nmol = len(first)
+    out = {k: np.zeros((nmol, 3)) for k in ("cm", "v", "s", "w")}
+    out["M"] = np.zeros(nmol); out["ek"] = np.zeros(nmol)
+    eps = np.finfo(float).eps
+    for n in range(nmol):
+        idx = np.asarray(atoms[start[n]:start[n + 1]])
+        M = m[idx].sum()
+        i, k = int(first[n]), int(nuau[n])
+        chain = np.empty((k, 3))
+        chain[0] = x[i]
+        for q in range(1, k):
+            chain[q] = chain[q - 1] + _wrap(x[i + q] - x[i + q - 1], L)
+        cm = (m[i:i + k, None] * chain).sum(0) / M
+        cm = np.where(cm > L, cm - L, np.where(cm < 0.0, cm + L, cm))
+        vc = (v[idx] * m[idx, None]).sum(0) / M
+        dcm = _wrap(x[idx] - cm, L)
+        p = v[idx] * m[idx, None]
+        s = np.cross(dcm, p).sum(0)
+        if unsafe:
+            mi = m[idx]
+            I = np.zeros((3, 3))
+            I[0, 0] = (mi * (dcm[:, 1] ** 2 + dcm[:, 2] ** 2)).sum()
+            I[1, 1] = (mi * (dcm[:, 0] ** 2 + dcm[:, 2] ** 2)).sum()
+            I[2, 2] = (mi * (dcm[:, 0] ** 2 + dcm[:, 1] ** 2)).sum()
+            I[0, 1] = I[1, 0] = -(mi * dcm[:, 0] * dcm[:, 1]).sum()
+            I[0, 2] = I[2, 0] = -(mi * dcm[:, 0] * dcm[:, 2]).sum()
+            I[1, 2] = I[2, 1] = -(mi * dcm[:, 1] * dcm[:, 2]).sum()
+            if abs(np.linalg.det(I)) < eps:
+                out["w"][n] = s / (np.linalg.eigvalsh(I).sum() / 3.0)
+            else:
+                out["w"][n] = np.linalg.solve(I, s)
+        zq = z[idx]
+        pos, neg = zq > 0.0, zq < 0.0
+        if pos.any() and neg.any():
+            xa = cm + dcm
+            pel[n] = zq[pos].sum() * (xa[pos].mean(0) - xa[neg].mean(0))
+        out["cm"][n], out["v"][n], out["s"][n], out["M"][n] = cm, vc, s, M
+        out["ek"][n] = (0.5 * M * vc * vc).sum()
+    return out
+
+
+class MolSamplers:
+    """The reference's msacf (source/sepsampler.c:752-808), mvacf (:1782-1816)
+    and mgh (:1231-1410) samplers fed one sample at a time; `files()` gives
+    the numbers each writes at the end of a block.  The mgh energy sums are
+    not reset between blocks and the running mean kinetic energy starts at
+    `avekin0`, as in the reference."""
+
+    def __init__(self, lvec, dtsample, nk, Ly, volume, unsafe, avekin0=0.0):
+        self.lvec, self.dts, self.nk, self.V, self.unsafe = lvec, dtsample, nk, volume, unsafe
+        self.k = 2 * np.pi * np.arange(1, nk + 1) / Ly
+        self.avekin, self.ncalls = avekin0, 0
+        z = lambda: np.zeros((lvec, nk), complex)
+        self.fk = {q: z() for q in ("tv", "lv", "rho", "tav", "lav", "e", "dip", "X")}
+        self.c = {q: z() for q in ("tv", "lv", "scatt", "tav", "lav", "e", "vav", "dip", "X")}
+        self.im = self.iv = self.ia = 0
+        self.nm = self.nv = self.na = 0
+        self.vels = None
+        self.vacf = np.zeros(lvec)
+        self.sst = np.zeros((lvec, 3)); self.ast = np.zeros((lvec, 3))
+        self.sacf = np.zeros((lvec, 2))
+        self.out = {}
+
+    def mgh(self, props, pel):
+        i, nmol = self.im, len(props["M"])
+        self.ncalls += 1
+        self.avekin += props["ek"].sum() / (nmol * self.ncalls)
+        for j, kj in enumerate(self.k):
+            e = np.exp(1j * kj * props["cm"][:, 1])
+            M = props["M"]
+            self.fk["rho"][i, j] = (M * e).sum()
+            self.fk["tv"][i, j] = (M * props["v"][:, 0] * e).sum()
+            self.fk["lv"][i, j] = (M * props["v"][:, 1] * e).sum()
+            self.fk["e"][i, j] += ((props["ek"] - self.avekin) * e).sum()
+            self.fk["tav"][i, j] = (props["s"][:, 2] * e).sum()
+            self.fk["lav"][i, j] = (props["s"][:, 1] * e).sum()
+            self.fk["dip"][i, j] = (pel[:, 1] * e).sum()
+            self.fk["X"][i, j] = (props["w"][:, 0] * e).sum() if self.unsafe else 0.0
+        self.im += 1
+        if self.im == self.lvec:
+            f, c, lv = self.fk, self.c, self.lvec
+            for n in range(lv):
+                a, b = slice(0, lv - n), slice(n, lv)
+                c["tv"][n] += (np.conj(f["tv"][a]) * f["tv"][b]).sum(0)
+                c["lv"][n] += (np.conj(f["lv"][a]) * f["lv"][b]).sum(0)
+                c["scatt"][n] += (f["rho"][a] * np.conj(f["rho"][b])).sum(0)
+                c["e"][n] += (f["e"][a] * np.conj(f["e"][b])).sum(0)
+                c["tav"][n] += (np.conj(f["tav"][a]) * f["tav"][b]).sum(0)
+                c["lav"][n] += (np.conj(f["lav"][a]) * f["lav"][b]).sum(0)
+                c["vav"][n] += (np.conj(f["tv"][a]) * f["tav"][b]).sum(0)
+                c["dip"][n] += (np.conj(f["dip"][a]) * f["dip"][b]).sum(0)
+                if self.unsafe:
+                    c["X"][n] += (np.conj(f["X"][a]) * f["X"][b]).sum(0)
+            self.nm += 1
+            t = np.arange(lv) * self.dts
+            fac = 1.0 / (self.nm * self.V * (lv - np.arange(lv)))
+            for q, arr in c.items():
+                if q == "X" and not self.unsafe:
+                    continue
+                cols = np.empty((lv, 1 + 2 * self.nk))
+                cols[:, 0] = t
+                cols[:, 1::2] = (arr * fac[:, None]).real
+                cols[:, 2::2] = (arr * fac[:, None]).imag
+                self.out["mgh-" + q] = cols
+            self.im = 0
+
+    def mvacf(self, vcm_x):
+        if self.vels is None:
+            self.vels = np.zeros((self.lvec, len(vcm_x)))
+        self.vels[self.iv] = vcm_x
+        self.iv += 1
+        if self.iv == self.lvec:
+            lv, nmol = self.lvec, self.vels.shape[1]
+            for k in range(lv):
+                self.vacf[k] += (self.vels[:lv - k] * self.vels[k:]).sum()
+            self.nv += 1
+            fac = 1.0 / ((lv - np.arange(lv)) * nmol * self.nv)
+            self.out["mvacf"] = np.stack([np.arange(lv) * self.dts, self.vacf * fac], 1)
+            self.iv = 0
+
+    def msacf(self, P_mol):
+        P = np.asarray(P_mol).reshape(3, 3)
+        i = self.ia
+        self.sst[i] = 0.5 * np.array([P[0, 1] + P[1, 0], P[0, 2] + P[2, 0], P[1, 2] + P[2, 1]])
+        self.ast[i] = 0.5 * np.array([P[0, 1] - P[1, 0], P[0, 2] - P[2, 0], P[1, 2] - P[2, 1]])
+        self.ia += 1
+        if self.ia == self.lvec:
+            lv = self.lvec
+            for n in range(lv):
+                self.sacf[n, 0] += (self.sst[:lv - n] * self.sst[n:]).sum()
+                self.sacf[n, 1] += (self.ast[:lv - n] * self.ast[n:]).sum()
+            self.na += 1
+            fac = self.V / (3.0 * (lv - np.arange(lv)) * self.na)
+            self.out["msacf"] = np.column_stack([np.arange(lv) * self.dts, self.sacf * fac[:, None]])
+            self.ia = 0

@@ -1,0 +1,333 @@
+// dev_molsampler.cu - device parts of the molecular samplers mvacf and mgh.
+//
+// The reference (source/sepsampler.c:1231-1410 mgh, :1757-1816 mvacf)
+// downloads nothing itself but walks every molecule on the host at each
+// sample: centre of mass (source/sepmol.c:683-729), centre-of-mass velocity
+// (:731-748), spin angular momentum and inertia tensor (:750-825) and the
+// charge dipole (:1036-1083), then per wavevector sums over the molecules.
+// Here one thread per molecule forms these from the device state, a second
+// kernel sums them per wavevector with a fixed reduction order, and only
+// nk x 18 numbers come back per sample.  mvacf keeps the molecular
+// x-velocities of a block in a device ring (the vacf ring of dev_sampler.cu
+// sized by the molecule count).
+//
+// Positions are taken from the full 64-bit fixed-point words, as fractions
+// of the box in FP64; all molecular quantities are FP64.
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include "dev_common.cuh"
+
+#define MSB 128
+
+struct sepdev_moltab {
+	int nmol, nblk;
+	int *first, *nuau, *start, *atoms;
+	double *mass;
+	double *props;     // [nmol][MP_N]
+	double *pel;       // [nmol][3] last dipole (kept when a molecule has no +/- charges)
+	double *kvec;      // [nk]
+	int nk_alloc;
+	double *part;      // [nk][nblk][MG_N]
+	double *sum;       // [nk * MG_N]
+};
+
+enum { MP_Y, MP_M, MP_MVX, MP_MVY, MP_EK, MP_SZ, MP_SY, MP_PY, MP_WX, MP_N };
+#define MG_N 18
+
+__device__ __forceinline__ double frac64(int hi, unsigned lo)
+{
+	return ldexp((double)(((unsigned long long)(unsigned)hi << 32) | lo), -64);
+}
+
+__device__ __forceinline__ double wrap_half(double f)
+{
+	if (f > 0.5) return f - 1.0;
+	if (f < -0.5) return f + 1.0;
+	return f;
+}
+
+struct MolArgs {
+	int nmol;
+	const int *first, *nuau, *start, *atoms, *inv;
+	const double *mass;
+	const int4 *pos;
+	const uint4 *xlo;
+	const float4 *vhi, *vlo;
+	const float *charge;
+	double L[3];
+	int unsafe;
+	double *props, *pel;
+};
+
+// per molecule: the centre of mass (chain of consecutive user indices from
+// the first atom, bonds unwrapped by the minimum image, wrapped into the
+// box), velocity, kinetic energy M v^2 / 2, spin s = sum dcm x m v about the
+// centre of mass, the charge dipole and, in the unsafe mode, the angular
+// velocity I^-1 s
+__global__ void __launch_bounds__(MSB) k_mol_props(MolArgs a)
+{
+	const int m = blockIdx.x * MSB + threadIdx.x;
+	if (m >= a.nmol) return;
+	const int a0 = a.first[m];
+	double cmf[3];
+	{
+		const int s0 = a.inv[a0];
+		const int4 p0 = a.pos[s0];
+		const uint4 l0 = a.xlo[s0];
+		unsigned long long prev[3] = {((unsigned long long)(unsigned)p0.x << 32) | l0.x,
+					      ((unsigned long long)(unsigned)p0.y << 32) | l0.y,
+					      ((unsigned long long)(unsigned)p0.z << 32) | l0.z};
+		const double f0[3] = {ldexp((double)prev[0], -64), ldexp((double)prev[1], -64),
+				      ldexp((double)prev[2], -64)};
+		double off[3] = {0.0, 0.0, 0.0}, acc[3] = {0.0, 0.0, 0.0};
+		for (int q = 0; q < a.nuau[m]; q++) {
+			const int s = a.inv[a0 + q];
+			const int4 p = a.pos[s];
+			const uint4 l = a.xlo[s];
+			const unsigned long long X[3] = {((unsigned long long)(unsigned)p.x << 32) | l.x,
+							 ((unsigned long long)(unsigned)p.y << 32) | l.y,
+							 ((unsigned long long)(unsigned)p.z << 32) | l.z};
+			const double ma = (double)a.vhi[s].w;
+			for (int k = 0; k < 3; k++) {
+				if (q > 0) off[k] += ldexp((double)(long long)(X[k] - prev[k]), -64);
+				prev[k] = X[k];
+				acc[k] += ma * off[k];
+			}
+		}
+		const double M = a.mass[m];
+		for (int k = 0; k < 3; k++) {
+			double f = f0[k] + acc[k] / M;
+			if (f >= 1.0) f -= 1.0;
+			else if (f < 0.0) f += 1.0;
+			cmf[k] = f;
+		}
+	}
+	const double M = a.mass[m];
+	double v[3] = {0.0, 0.0, 0.0}, s[3] = {0.0, 0.0, 0.0};
+	double I00 = 0.0, I11 = 0.0, I22 = 0.0, I01 = 0.0, I02 = 0.0, I12 = 0.0;
+	double rpos[3] = {0.0, 0.0, 0.0}, rneg[3] = {0.0, 0.0, 0.0}, sumz = 0.0;
+	int npos = 0, nneg = 0;
+	for (int q = a.start[m]; q < a.start[m + 1]; q++) {
+		const int sl = a.inv[a.atoms[q]];
+		const int4 p = a.pos[sl];
+		const uint4 l = a.xlo[sl];
+		const float4 vh = a.vhi[sl], vl = a.vlo[sl];
+		const double ma = (double)vh.w;
+		const double va[3] = {(double)vh.x + (double)vl.x, (double)vh.y + (double)vl.y,
+				      (double)vh.z + (double)vl.z};
+		const double fx[3] = {frac64(p.x, l.x), frac64(p.y, l.y), frac64(p.z, l.z)};
+		double d[3], pm[3];
+		for (int k = 0; k < 3; k++) {
+			v[k] += va[k] * ma;
+			d[k] = wrap_half(fx[k] - cmf[k]) * a.L[k];
+			pm[k] = va[k] * ma;
+		}
+		s[0] += d[1] * pm[2] - d[2] * pm[1];
+		s[1] += d[2] * pm[0] - d[0] * pm[2];
+		s[2] += d[0] * pm[1] - d[1] * pm[0];
+		I00 += ma * (d[1] * d[1] + d[2] * d[2]);
+		I11 += ma * (d[0] * d[0] + d[2] * d[2]);
+		I22 += ma * (d[0] * d[0] + d[1] * d[1]);
+		I01 -= ma * d[0] * d[1];
+		I02 -= ma * d[0] * d[2];
+		I12 -= ma * d[1] * d[2];
+		if (a.charge) {
+			const double z = (double)a.charge[sl];
+			if (z > 0.0) {
+				for (int k = 0; k < 3; k++) rpos[k] += cmf[k] * a.L[k] + d[k];
+				sumz += z;
+				npos++;
+			} else if (z < 0.0) {
+				for (int k = 0; k < 3; k++) rneg[k] += cmf[k] * a.L[k] + d[k];
+				nneg++;
+			}
+		}
+	}
+	for (int k = 0; k < 3; k++) v[k] /= M;
+	if (npos > 0 && nneg > 0)
+		for (int k = 0; k < 3; k++) a.pel[3 * m + k] = sumz * (rpos[k] / npos - rneg[k] / nneg);
+	double ek = 0.0;
+	for (int k = 0; k < 3; k++) ek += 0.5 * M * v[k] * v[k];
+	double wx = 0.0;
+	if (a.unsafe) {
+		// I w = s; a singular tensor (a linear molecule) takes the mean
+		// principal moment, trace / 3
+		const double det = I00 * (I11 * I22 - I12 * I12) - I01 * (I01 * I22 - I12 * I02) +
+				   I02 * (I01 * I12 - I11 * I02);
+		if (fabs(det) < DBL_EPSILON)
+			wx = s[0] / ((I00 + I11 + I22) / 3.0);
+		else
+			wx = (s[0] * (I11 * I22 - I12 * I12) - I01 * (s[1] * I22 - I12 * s[2]) +
+			      I02 * (s[1] * I12 - I11 * s[2])) / det;
+	}
+	double *o = a.props + (long)m * MP_N;
+	o[MP_Y] = cmf[1] * a.L[1];
+	o[MP_M] = M;
+	o[MP_MVX] = M * v[0];
+	o[MP_MVY] = M * v[1];
+	o[MP_EK] = ek;
+	o[MP_SZ] = s[2];
+	o[MP_SY] = s[1];
+	o[MP_PY] = a.pel[3 * m + 1];
+	o[MP_WX] = wx;
+}
+
+// blockIdx.y = wavevector j: per block the sums over its molecules of
+// e^{i k_j y} times M, M vx, M vy, the kinetic energy, 1, s_z, s_y, the
+// dipole's y component and w_x (re, im interleaved)
+__global__ void __launch_bounds__(MSB) k_mgh_sums(int nmol, const double *props, const double *kvec,
+						  double *part)
+{
+	__shared__ double red[MSB / 32][MG_N];
+	const int m = blockIdx.x * MSB + threadIdx.x;
+	const int j = blockIdx.y;
+	double t[MG_N];
+	for (int q = 0; q < MG_N; q++) t[q] = 0.0;
+	if (m < nmol) {
+		const double *o = props + (long)m * MP_N;
+		double sn, cs;
+		sincos(kvec[j] * o[MP_Y], &sn, &cs);
+		const double w[9] = {o[MP_M], o[MP_MVX], o[MP_MVY], o[MP_EK], 1.0, o[MP_SZ], o[MP_SY], o[MP_PY],
+				     o[MP_WX]};
+		for (int q = 0; q < 9; q++) {
+			t[2 * q] = w[q] * cs;
+			t[2 * q + 1] = w[q] * sn;
+		}
+	}
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	for (int q = 0; q < MG_N; q++) {
+		double x = t[q];
+		for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+		if (lane == 0) red[wid][q] = x;
+	}
+	__syncthreads();
+	if (threadIdx.x < MG_N) {
+		double x = 0.0;
+		for (int w = 0; w < MSB / 32; w++) x += red[w][threadIdx.x];
+		part[((long)j * gridDim.x + blockIdx.x) * MG_N + threadIdx.x] = x;
+	}
+}
+
+// one thread per (j, q): the blocks' partial sums in order; row nk * MG_N
+// (an extra thread) sums the kinetic energies
+__global__ void k_mgh_rows(int nk, int nblk, int nmol, const double *part, const double *props, double *out)
+{
+	const int r = blockIdx.x * blockDim.x + threadIdx.x;
+	if (r < nk * MG_N) {
+		const int j = r / MG_N, q = r % MG_N;
+		double s = 0.0;
+		for (int b = 0; b < nblk; b++) s += part[((long)j * nblk + b) * MG_N + q];
+		out[r] = s;
+	} else if (r == nk * MG_N) {
+		double s = 0.0;
+		for (int m = 0; m < nmol; m++) s += props[(long)m * MP_N + MP_EK];
+		out[r] = s;
+	}
+}
+
+// mvacf: row[m] = x-velocity of molecule m's centre of mass
+__global__ void k_mol_vx(int nmol, const int *start, const int *atoms, const int *inv, const float4 *vhi,
+			 const float4 *vlo, const double *mass, double *row)
+{
+	const int m = blockIdx.x * blockDim.x + threadIdx.x;
+	if (m >= nmol) return;
+	double v = 0.0;
+	for (int q = start[m]; q < start[m + 1]; q++) {
+		const int s = inv[atoms[q]];
+		v += ((double)vhi[s].x + (double)vlo[s].x) * (double)vhi[s].w;
+	}
+	row[m] = v / mass[m];
+}
+
+// ---- host side ---------------------------------------------------------------
+
+extern "C" void sepdev_moltab_destroy(sepdev_moltab *t)
+{
+	if (!t) return;
+	void *b[] = {t->first, t->nuau, t->start, t->atoms, t->mass, t->props, t->pel, t->kvec, t->part, t->sum};
+	for (size_t k = 0; k < sizeof b / sizeof b[0]; k++)
+		if (b[k]) cudaFree(b[k]);
+	free(t);
+}
+
+extern "C" int sepdev_moltab_create(sepdev *d, int nmol, const int *first, const int *nuau, const int *start,
+				    const int *atoms, const double *mass, sepdev_moltab **out)
+{
+	*out = NULL;
+	if (nmol < 1) return SEPDEV_EINVAL;
+	for (int m = 0; m < nmol; m++)
+		if (nuau[m] < 1 || first[m] < 0 || first[m] + nuau[m] > d->n || start[m + 1] < start[m])
+			return SEPDEV_EINVAL;
+	for (int q = 0; q < start[nmol]; q++)
+		if (atoms[q] < 0 || atoms[q] >= d->n) return SEPDEV_EINVAL;
+	sepdev_moltab *t = (sepdev_moltab *)calloc(1, sizeof *t);
+	if (!t) return SEPDEV_ENOMEM;
+	t->nmol = nmol;
+	t->nblk = (nmol + MSB - 1) / MSB;
+	const int na = start[nmol] > 0 ? start[nmol] : 1;
+	cudaError_t e = cudaMalloc((void **)&t->first, sizeof(int) * nmol);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&t->nuau, sizeof(int) * nmol);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&t->start, sizeof(int) * (nmol + 1));
+	if (e == cudaSuccess) e = cudaMalloc((void **)&t->atoms, sizeof(int) * na);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&t->mass, sizeof(double) * nmol);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&t->props, sizeof(double) * MP_N * nmol);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&t->pel, sizeof(double) * 3 * nmol);
+	if (e == cudaSuccess) e = cudaMemcpy(t->first, first, sizeof(int) * nmol, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemcpy(t->nuau, nuau, sizeof(int) * nmol, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemcpy(t->start, start, sizeof(int) * (nmol + 1), cudaMemcpyHostToDevice);
+	if (e == cudaSuccess && start[nmol] > 0)
+		e = cudaMemcpy(t->atoms, atoms, sizeof(int) * start[nmol], cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemcpy(t->mass, mass, sizeof(double) * nmol, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemset(t->pel, 0, sizeof(double) * 3 * nmol);
+	if (e != cudaSuccess) {
+		sepdev_moltab_destroy(t);
+		sepdev_set_error("molecule tables", e);
+		return SEPDEV_ENOMEM;
+	}
+	*out = t;
+	return SEPDEV_OK;
+}
+
+extern "C" int sepdev_mvacf_store(sepdev *d, sepdev_moltab *t, sepdev_vacf *v, int index)
+{
+	double *row = sepdev_vacf_row(v, index);
+	if (!row || sepdev_vacf_count(v) != t->nmol) return SEPDEV_EINVAL;
+	k_mol_vx<<<grid_for(t->nmol, 128), 128, 0, d->st>>>(t->nmol, t->start, t->atoms, d->inv, d->vhi, d->vlo,
+							   t->mass, row);
+	CKL(d);
+	return SEPDEV_OK;
+}
+
+extern "C" int sepdev_mgh_sample(sepdev *d, sepdev_moltab *t, int nk, const double *k, int unsafe, double *out)
+{
+	if (nk < 1) return SEPDEV_EINVAL;
+	if (nk > t->nk_alloc) {
+		cudaFree(t->kvec); cudaFree(t->part); cudaFree(t->sum);
+		t->kvec = t->part = t->sum = NULL;
+		t->nk_alloc = 0;
+		cudaError_t e = cudaMalloc((void **)&t->kvec, sizeof(double) * nk);
+		if (e == cudaSuccess) e = cudaMalloc((void **)&t->part, sizeof(double) * MG_N * nk * t->nblk);
+		if (e == cudaSuccess) e = cudaMalloc((void **)&t->sum, sizeof(double) * (MG_N * nk + 1));
+		if (e != cudaSuccess) { sepdev_set_error("mgh buffers", e); return SEPDEV_ENOMEM; }
+		t->nk_alloc = nk;
+	}
+	CK(cudaMemcpyAsync(t->kvec, k, sizeof(double) * nk, cudaMemcpyHostToDevice, d->st));
+	MolArgs a;
+	a.nmol = t->nmol;
+	a.first = t->first; a.nuau = t->nuau; a.start = t->start; a.atoms = t->atoms; a.inv = d->inv;
+	a.mass = t->mass;
+	a.pos = d->pos[d->cur]; a.xlo = d->xlo; a.vhi = d->vhi; a.vlo = d->vlo;
+	a.charge = d->has_charge ? d->charge : NULL;
+	for (int q = 0; q < 3; q++) a.L[q] = d->L[q];
+	a.unsafe = unsafe;
+	a.props = t->props; a.pel = t->pel;
+	k_mol_props<<<t->nblk, MSB, 0, d->st>>>(a);
+	k_mgh_sums<<<dim3(t->nblk, nk), MSB, 0, d->st>>>(t->nmol, t->props, t->kvec, t->part);
+	k_mgh_rows<<<grid_for(MG_N * nk + 1, 128), 128, 0, d->st>>>(nk, t->nblk, t->nmol, t->part, t->props, t->sum);
+	d->launches += 2;
+	CKL(d);
+	CK(cudaMemcpyAsync(out, t->sum, sizeof(double) * (MG_N * nk + 1), cudaMemcpyDeviceToHost, d->st));
+	CK(cudaStreamSynchronize(d->st));
+	return SEPDEV_OK;
+}

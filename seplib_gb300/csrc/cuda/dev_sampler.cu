@@ -23,6 +23,7 @@ struct sepdev_vacf {
 	double *ring;     // [lvec][n]
 	double *part;     // [lvec][nblk] per-block partial sums
 	double *sum;      // [lvec]
+	long count;       // values per sample: particles, or molecules (mvacf)
 	int lvec;
 	int nblk;
 };
@@ -89,15 +90,17 @@ __global__ void k_rows_sum(int rows, int nblk, const double *part, double *out, 
 	out[r] = s;
 }
 
-extern "C" int sepdev_vacf_create(sepdev *d, int lvec, sepdev_vacf **out)
+extern "C" int sepdev_vacf_create_count(sepdev *d, int lvec, long count, sepdev_vacf **out)
 {
+	(void)d;
 	*out = NULL;
-	if (lvec < 1) return SEPDEV_EINVAL;
+	if (lvec < 1 || count < 1) return SEPDEV_EINVAL;
 	sepdev_vacf *v = (sepdev_vacf *)calloc(1, sizeof *v);
 	if (!v) return SEPDEV_ENOMEM;
 	v->lvec = lvec;
-	v->nblk = grid_for(d->n, SB);
-	cudaError_t e = cudaMalloc((void **)&v->ring, sizeof(double) * lvec * d->n);
+	v->count = count;
+	v->nblk = grid_for(count, SB);
+	cudaError_t e = cudaMalloc((void **)&v->ring, sizeof(double) * lvec * count);
 	if (e == cudaSuccess) e = cudaMalloc((void **)&v->part, sizeof(double) * lvec * v->nblk);
 	if (e == cudaSuccess) e = cudaMalloc((void **)&v->sum, sizeof(double) * lvec);
 	if (e != cudaSuccess) {
@@ -109,6 +112,19 @@ extern "C" int sepdev_vacf_create(sepdev *d, int lvec, sepdev_vacf **out)
 	return SEPDEV_OK;
 }
 
+extern "C" int sepdev_vacf_create(sepdev *d, int lvec, sepdev_vacf **out)
+{
+	return sepdev_vacf_create_count(d, lvec, d->n, out);
+}
+
+double *sepdev_vacf_row(sepdev_vacf *v, int index)
+{
+	if (index < 0 || index >= v->lvec) return NULL;
+	return v->ring + (long)index * v->count;
+}
+
+long sepdev_vacf_count(const sepdev_vacf *v) { return v->count; }
+
 extern "C" void sepdev_vacf_destroy(sepdev_vacf *v)
 {
 	if (!v) return;
@@ -118,7 +134,7 @@ extern "C" void sepdev_vacf_destroy(sepdev_vacf *v)
 
 extern "C" int sepdev_vacf_store(sepdev *d, sepdev_vacf *v, int index)
 {
-	if (index < 0 || index >= v->lvec) return SEPDEV_EINVAL;
+	if (index < 0 || index >= v->lvec || v->count != d->n) return SEPDEV_EINVAL;
 	k_vacf_store<<<grid_for(d->n, SB), SB, 0, d->st>>>(d->n, d->gid, d->vhi, d->vlo, v->ring + (long)index * d->n);
 	CKL(d);
 	return SEPDEV_OK;
@@ -128,7 +144,7 @@ extern "C" int sepdev_vacf_store(sepdev *d, sepdev_vacf *v, int index)
 extern "C" int sepdev_vacf_block(sepdev *d, sepdev_vacf *v, double *out)
 {
 	dim3 grid(v->nblk, v->lvec);
-	k_vacf_lags<<<grid, SB, 0, d->st>>>(d->n, v->lvec, v->ring, v->part);
+	k_vacf_lags<<<grid, SB, 0, d->st>>>(v->count, v->lvec, v->ring, v->part);
 	k_rows_sum<<<grid_for(v->lvec, 128), 128, 0, d->st>>>(v->lvec, v->nblk, v->part, v->sum, 1);
 	CKL(d);
 	CK(cudaMemcpyAsync(out, v->sum, sizeof(double) * v->lvec, cudaMemcpyDeviceToHost, d->st));

@@ -1,13 +1,17 @@
 /*
- * sep_api_sampler.c - the sacf, vacf and msd samplers of the sep C API.
+ * sep_api_sampler.c - the sacf, vacf, msd, msacf, mvacf and mgh samplers of
+ * the sep C API.
  *
  * Control flow, sampling intervals, normalisations and output files follow
  * the reference (source/sepsampler.c:4-242 dispatch, :280-351 sacf,
- * :471-641 msd, :658-714 vacf).  The stress autocorrelation works on the
- * sepret values the host already has after every sep_leapfrog; vacf and msd
- * keep their particle data on the GPU (dev_sampler.cu) and only their
- * per-sample or per-block sums come back to the host.
+ * :471-641 msd, :658-714 vacf, :725-818 msacf, :1110-1410 mgh, :1757-1825
+ * mvacf).  The stress autocorrelations work on the sepret values the host
+ * already has (the molecular one through sep_mol_pressure_tensor); vacf,
+ * msd, mvacf and mgh keep their particle data on the GPU (dev_sampler.cu,
+ * dev_molsampler.cu) and only their per-sample or per-block sums come back
+ * to the host.
  */
+#include <complex.h>
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -42,6 +46,41 @@ struct sepmsd {
 	double *Fs;            /* lvec x nk (real part) */
 	double *out;           /* 2 + nk, scratch */
 	sepdev_msd *dev;
+	rt_ctx *ctx;
+};
+
+struct sepmsacf {
+	int lvec, isample, i;
+	long nsample;
+	double dtsample;
+	double *sacf;          /* lvec x 2: symmetric, antisymmetric */
+	double *sstress;       /* lvec x 3 */
+	double *astress;       /* lvec x 3 */
+};
+
+struct sepmvacf {
+	int lvec, isample, i;
+	long nsample;
+	double dtsample;
+	double *vacf;          /* lvec */
+	double *block;         /* lvec, scratch */
+	sepdev_vacf *dev;
+	sepdev_moltab *tab;
+	rt_ctx *ctx;
+};
+
+/* the per-sample Fourier sums of one block (fk) and the accumulated
+ * correlations (c); the conjugate sums the reference also keeps (fkm) are
+ * the complex conjugates of these */
+struct sepmgh {
+	int lvec, isample, i, nk, safe;
+	long nsample, ncalls;
+	double dtsample, avekin;
+	double *k;
+	double complex *fk_tv, *fk_lv, *fk_rho, *fk_tav, *fk_lav, *fk_e, *fk_dip, *fk_X;
+	double complex *c_tv, *c_lv, *c_scatt, *c_tav, *c_lav, *c_e, *c_vav, *c_dip, *c_X;
+	double *out;           /* 18 nk + 1, scratch */
+	sepdev_moltab *tab;
 	rt_ctx *ctx;
 };
 
@@ -140,10 +179,64 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 			sptr->msd = p;
 			sptr->flag_msd = 1;
 		}
+	} else if (strcmp(sampler, "msacf") == 0) {
+		if (sptr->flag_msacf != 1) {
+			if (sptr->molptr == NULL) sep_error("%s: molpointer not initialized", __func__);
+			const double tsample = va_arg(args, double);
+			struct sepmsacf *p = xcalloc(1, sizeof *p);
+			p->lvec = lvec;
+			p->isample = sample_interval(tsample, lvec, sys.dt, &p->dtsample);
+			p->sacf = xcalloc(2 * (size_t)lvec, sizeof(double));
+			p->sstress = xcalloc(3 * (size_t)lvec, sizeof(double));
+			p->astress = xcalloc(3 * (size_t)lvec, sizeof(double));
+			sptr->msacf = p;
+			sptr->flag_msacf = 1;
+		}
+	} else if (strcmp(sampler, "mgh") == 0) {
+		if (sptr->flag_mgh != 1) {
+			if (sptr->molptr == NULL) sep_error("%s: molpointer not initialized", __func__);
+			const double tsample = va_arg(args, double);
+			const int nk = va_arg(args, int);
+			const int safe = va_arg(args, int);
+			struct sepmgh *p = xcalloc(1, sizeof *p);
+			p->lvec = lvec;
+			p->isample = sample_interval(tsample, lvec, sys.dt, &p->dtsample);
+			p->nk = nk;
+			p->k = xcalloc(nk, sizeof(double));
+			FILE *f = fopen("mgh-wavevector.dat", "w");
+			if (!f) sep_error("%s: couldn't open file", __func__);
+			for (int n = 1; n <= nk; n++) {
+				p->k[n - 1] = 2 * SEP_PI * n / sys.length[1];
+				fprintf(f, "%f\n", p->k[n - 1]);
+			}
+			fclose(f);
+			p->safe = safe ? 1 : 0;
+			if (!p->safe)
+				sep_warning("ACHTUNG - unsafe mode for mgh sampler. Assuming uniaxial single component system");
+			const size_t m = (size_t)lvec * (nk > 0 ? nk : 1);
+			double complex **arr[] = {&p->fk_tv, &p->fk_lv, &p->fk_rho, &p->fk_tav, &p->fk_lav, &p->fk_e,
+						  &p->fk_dip, &p->fk_X, &p->c_tv, &p->c_lv, &p->c_scatt, &p->c_tav,
+						  &p->c_lav, &p->c_e, &p->c_vav, &p->c_dip, &p->c_X};
+			for (size_t q = 0; q < sizeof arr / sizeof arr[0]; q++) *arr[q] = xcalloc(m, sizeof(double complex));
+			p->out = xcalloc(18 * (size_t)nk + 1, sizeof(double));
+			sptr->mgh = p;
+			sptr->flag_mgh = 1;
+		}
+	} else if (strcmp(sampler, "mvacf") == 0) {
+		if (sptr->flag_mvacf != 1) {
+			const double tsample = va_arg(args, double);
+			struct sepmvacf *p = xcalloc(1, sizeof *p);
+			p->lvec = lvec;
+			p->isample = sample_interval(tsample, lvec, sys.dt, &p->dtsample);
+			p->vacf = xcalloc(lvec, sizeof(double));
+			p->block = xcalloc(lvec, sizeof(double));
+			sptr->mvacf = p;
+			sptr->flag_mvacf = 1;
+		}
 	} else {
 		va_end(args);
 		sep_error("%s: sampler %s is not provided by this GPU implementation "
-			  "(available: sacf, vacf, msd)", __func__, sampler);
+			  "(available: sacf, vacf, msd, msacf, mvacf, mgh)", __func__, sampler);
 	}
 	va_end(args);
 }
@@ -258,11 +351,182 @@ static void msd_sample(struct sepmsd *s, seppart *pptr, sepsys sys)
 	s->i = index;
 }
 
-/* source/sepsampler.c:177-240 (the samplers provided here) */
+/* ---- msacf: source/sepsampler.c:752-808 ---- */
+static void msacf_sample(struct sepmsacf *s, seppart *pptr, sepmol *mols, sepret *ret, sepsys sys)
+{
+	sep_mol_pressure_tensor(pptr, mols, ret, &sys);
+	const int i = s->i;
+	s->sstress[3 * i] = 0.5 * (ret->P_mol[0][1] + ret->P_mol[1][0]);
+	s->sstress[3 * i + 1] = 0.5 * (ret->P_mol[0][2] + ret->P_mol[2][0]);
+	s->sstress[3 * i + 2] = 0.5 * (ret->P_mol[1][2] + ret->P_mol[2][1]);
+	s->astress[3 * i] = 0.5 * (ret->P_mol[0][1] - ret->P_mol[1][0]);
+	s->astress[3 * i + 1] = 0.5 * (ret->P_mol[0][2] - ret->P_mol[2][0]);
+	s->astress[3 * i + 2] = 0.5 * (ret->P_mol[1][2] - ret->P_mol[2][1]);
+	s->i++;
+	if (s->i == s->lvec) {
+		for (int n = 0; n < s->lvec; n++) {
+			double as = 0.0, aa = 0.0;
+			for (int k = 0; k < 3; k++)
+				for (int m = 0; m < s->lvec - n; m++) {
+					as += s->sstress[3 * m + k] * s->sstress[3 * (n + m) + k];
+					aa += s->astress[3 * m + k] * s->astress[3 * (n + m) + k];
+				}
+			s->sacf[2 * n] += as;
+			s->sacf[2 * n + 1] += aa;
+		}
+		s->nsample++;
+		FILE *f = fopen("msacf.dat", "w");
+		if (!f) sep_error("%s: couldn't open file", __func__);
+		for (int n = 0; n < s->lvec; n++) {
+			const double t = n * s->dtsample;
+			const double fac = sys.volume / (3.0 * (s->lvec - n) * s->nsample);
+			fprintf(f, "%f %f %f\n", t, s->sacf[2 * n] * fac, s->sacf[2 * n + 1] * fac);
+		}
+		fclose(f);
+		s->i = 0;
+	}
+}
+
+/* the molecule tables of the sampler's molecules on the context's device */
+static void mol_tables(sepdev_moltab **tab, rt_ctx **owner, rt_ctx *c, sepmol *mols, sepsys *sys)
+{
+	if (*tab && *owner == c) return;
+	if (*tab) sepdev_moltab_destroy(*tab);
+	*tab = NULL;
+	if (mols == NULL) sep_error("sep_sample: molpointer not initialized");
+	const int nm = (int)sys->molptr->num_mols;
+	int *first = xcalloc(nm, sizeof(int)), *nuau = xcalloc(nm, sizeof(int));
+	int *start = xcalloc(nm + 1, sizeof(int));
+	double *mass = xcalloc(nm, sizeof(double));
+	for (int m = 0; m < nm; m++) start[m + 1] = start[m] + (int)mols[m].nuau;
+	int *atoms = xcalloc(start[nm], sizeof(int));
+	for (int m = 0; m < nm; m++) {
+		first[m] = mols[m].nuau > 0 ? mols[m].index[0] : 0;
+		nuau[m] = (int)mols[m].nuau;
+		mass[m] = mols[m].m;
+		for (unsigned q = 0; q < mols[m].nuau; q++) atoms[start[m] + q] = mols[m].index[q];
+	}
+	rt_check(sepdev_moltab_create(c->dev, nm, first, nuau, start, atoms, mass, tab), "molecule tables");
+	*owner = c;
+	free(first); free(nuau); free(start); free(atoms); free(mass);
+}
+
+/* ---- mvacf: source/sepsampler.c:1782-1816 ---- */
+static void mvacf_sample(struct sepmvacf *s, seppart *pptr, sepmol *mols, sepsys sys)
+{
+	rt_ctx *c = sampler_ctx(pptr, &sys);
+	const int nm = (int)sys.molptr->num_mols;
+	if (s->ctx != c) {
+		if (s->dev) sepdev_vacf_destroy(s->dev);
+		s->dev = NULL;
+	}
+	mol_tables(&s->tab, &s->ctx, c, mols, &sys);
+	if (!s->dev) rt_check(sepdev_vacf_create_count(c->dev, s->lvec, nm, &s->dev), "mvacf sampler");
+	rt_check(sepdev_mvacf_store(c->dev, s->tab, s->dev, s->i), "mvacf sample");
+	s->i++;
+	if (s->i == s->lvec) {
+		rt_check(sepdev_vacf_block(c->dev, s->dev, s->block), "mvacf block");
+		for (int k = 0; k < s->lvec; k++) s->vacf[k] += s->block[k];
+		s->nsample++;
+		FILE *f = fopen("mvacf.dat", "w");
+		if (!f) sep_error("%s: couldn't open file", __func__);
+		for (int k = 0; k < s->lvec; k++) {
+			const double t = k * s->dtsample;
+			const double fac = 1.0 / ((double)(s->lvec - k) * nm * s->nsample);
+			fprintf(f, "%f %f\n", t, s->vacf[k] * fac);
+		}
+		fclose(f);
+		s->i = 0;
+	}
+}
+
+/* ---- mgh: source/sepsampler.c:1231-1410 ----
+ * The reference resets every per-sample sum at the start of a sample except
+ * the energy's, which therefore accumulates over the blocks at each index;
+ * the running mean kinetic energy starts at 0 here (the reference leaves it
+ * unset). */
+static void mgh_files(struct sepmgh *g, double volume)
+{
+	static const char *names[9] = {"mgh-trans-momentum-acf.dat", "mgh-long-momentum-acf.dat",
+				       "mgh-rho-acf.dat", "mgh-trans-angmomentum-acf.dat",
+				       "mgh-long-angmomentum-acf.dat", "mgh-energy-acf.dat",
+				       "mgh-momentum-angmomentum-ccf.dat", "mgh-dipole-acf.dat", "mgh-X-cf.dat"};
+	double complex *cs[9] = {g->c_tv, g->c_lv, g->c_scatt, g->c_tav, g->c_lav, g->c_e, g->c_vav, g->c_dip, g->c_X};
+	for (int f = 0; f < 9; f++) {
+		FILE *fp = fopen(names[f], "w");
+		if (!fp) sep_error("%s: Error opening files", __func__);
+		if (f == 8 && g->safe) { fclose(fp); continue; }
+		for (int n = 0; n < g->lvec; n++) {
+			fprintf(fp, "%f ", n * g->dtsample);
+			const double fac = 1.0 / (g->nsample * volume * (g->lvec - n));
+			for (int k = 0; k < g->nk; k++) {
+				const double complex v = cs[f][(size_t)n * g->nk + k] * fac;
+				fprintf(fp, "%f %f ", creal(v), cimag(v));
+			}
+			fprintf(fp, "\n");
+		}
+		fclose(fp);
+	}
+}
+
+static void mgh_sample(struct sepmgh *g, seppart *pptr, sepmol *mols, sepsys sys)
+{
+	rt_ctx *c = sampler_ctx(pptr, &sys);
+	mol_tables(&g->tab, &g->ctx, c, mols, &sys);
+	rt_check(sepdev_mgh_sample(c->dev, g->tab, g->nk, g->k, !g->safe, g->out), "mgh sample");
+	const int nm = (int)sys.molptr->num_mols, nk = g->nk;
+	g->ncalls++;
+	g->avekin += g->out[18 * nk] / ((double)nm * g->ncalls);
+	const size_t row = (size_t)g->i * nk;
+	for (int j = 0; j < nk; j++) {
+		const double *o = g->out + 18 * j;
+		double complex S[9];
+		for (int q = 0; q < 9; q++) S[q] = o[2 * q] + I * o[2 * q + 1];
+		g->fk_rho[row + j] = S[0];
+		g->fk_tv[row + j] = S[1];
+		g->fk_lv[row + j] = S[2];
+		g->fk_e[row + j] += S[3] - g->avekin * S[4];
+		g->fk_tav[row + j] = S[5];
+		g->fk_lav[row + j] = S[6];
+		g->fk_dip[row + j] = S[7];
+		g->fk_X[row + j] = g->safe ? 0.0 : S[8];
+	}
+	g->i++;
+	if (g->i == g->lvec) {
+		const int lv = g->lvec;
+		for (int k = 0; k < nk; k++)
+			for (int n = 0; n < lv; n++) {
+				const size_t o = (size_t)n * nk + k;
+				for (int m = 0; m < lv - n; m++) {
+					const size_t a = (size_t)m * nk + k, b = (size_t)(n + m) * nk + k;
+					g->c_tv[o] += conj(g->fk_tv[a]) * g->fk_tv[b];
+					g->c_lv[o] += conj(g->fk_lv[a]) * g->fk_lv[b];
+					g->c_scatt[o] += g->fk_rho[a] * conj(g->fk_rho[b]);
+					g->c_e[o] += g->fk_e[a] * conj(g->fk_e[b]);
+					g->c_tav[o] += conj(g->fk_tav[a]) * g->fk_tav[b];
+					g->c_lav[o] += conj(g->fk_lav[a]) * g->fk_lav[b];
+					/* the reference's vav pair: sums of s_z and of M v_x */
+					g->c_vav[o] += conj(g->fk_tv[a]) * g->fk_tav[b];
+					g->c_dip[o] += conj(g->fk_dip[a]) * g->fk_dip[b];
+					if (!g->safe) g->c_X[o] += conj(g->fk_X[a]) * g->fk_X[b];
+				}
+			}
+		g->nsample++;
+		mgh_files(g, sys.volume);
+		g->i = 0;
+	}
+}
+
+/* source/sepsampler.c:177-240 (the samplers provided here, in its order) */
 void sep_sample(seppart *pptr, sepsampler *sptr, sepret *ret, sepsys sys, unsigned n)
 {
 	if (sptr->flag_sacf == 1 && n % sptr->sacf->isample == 0) sacf_sample(sptr->sacf, ret, sys);
 	if (sptr->flag_vacf == 1 && n % sptr->vacf->isample == 0) vacf_sample(sptr->vacf, pptr, sys);
+	if (sptr->flag_msacf == 1 && n % sptr->msacf->isample == 0)
+		msacf_sample(sptr->msacf, pptr, sptr->molptr, ret, sys);
+	if (sptr->flag_mgh == 1 && n % sptr->mgh->isample == 0) mgh_sample(sptr->mgh, pptr, sptr->molptr, sys);
+	if (sptr->flag_mvacf == 1 && n % sptr->mvacf->isample == 0)
+		mvacf_sample(sptr->mvacf, pptr, sptr->molptr, sys);
 	if (sptr->flag_msd == 1) {
 		struct sepmsd *m = sptr->msd;
 		/* crossings: counted exactly on the device at every step */
@@ -288,6 +552,26 @@ void sep_close_sampler(sepsampler *ptr)
 		free(ptr->vacf->vacf);
 		free(ptr->vacf->block);
 		free(ptr->vacf);
+	}
+	if (ptr->flag_msacf == 1) {
+		free(ptr->msacf->sacf); free(ptr->msacf->sstress); free(ptr->msacf->astress);
+		free(ptr->msacf);
+	}
+	if (ptr->flag_mvacf == 1) {
+		if (ptr->mvacf->dev) sepdev_vacf_destroy(ptr->mvacf->dev);
+		if (ptr->mvacf->tab) sepdev_moltab_destroy(ptr->mvacf->tab);
+		free(ptr->mvacf->vacf); free(ptr->mvacf->block);
+		free(ptr->mvacf);
+	}
+	if (ptr->flag_mgh == 1) {
+		struct sepmgh *g = ptr->mgh;
+		if (g->tab) sepdev_moltab_destroy(g->tab);
+		double complex *arr[] = {g->fk_tv, g->fk_lv, g->fk_rho, g->fk_tav, g->fk_lav, g->fk_e, g->fk_dip,
+					 g->fk_X, g->c_tv, g->c_lv, g->c_scatt, g->c_tav, g->c_lav, g->c_e,
+					 g->c_vav, g->c_dip, g->c_X};
+		for (size_t q = 0; q < sizeof arr / sizeof arr[0]; q++) free(arr[q]);
+		free(g->k); free(g->out);
+		free(g);
 	}
 	if (ptr->flag_msd == 1) {
 		struct sepmsd *m = ptr->msd;

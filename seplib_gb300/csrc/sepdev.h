@@ -260,6 +260,27 @@ int sepdev_vacf_create(sepdev *d, int lvec, sepdev_vacf **out);
 void sepdev_vacf_destroy(sepdev_vacf *v);
 int sepdev_vacf_store(sepdev *d, sepdev_vacf *v, int index);
 int sepdev_vacf_block(sepdev *d, sepdev_vacf *v, double *out);
+/* a ring of count values per sample (mvacf: one per molecule) */
+int sepdev_vacf_create_count(sepdev *d, int lvec, long count, sepdev_vacf **out);
+double *sepdev_vacf_row(sepdev_vacf *v, int index);
+long sepdev_vacf_count(const sepdev_vacf *v);
+
+/* Molecule tables of the molecular samplers: first atom and length of each
+ * molecule's chain of consecutive user indices (centres of mass), its atoms
+ * as CSR over user indices, molecule masses. */
+typedef struct sepdev_moltab sepdev_moltab;
+int sepdev_moltab_create(sepdev *d, int nmol, const int *first, const int *nuau, const int *start,
+			 const int *atoms, const double *mass, sepdev_moltab **out);
+void sepdev_moltab_destroy(sepdev_moltab *t);
+/* mvacf: the molecules' centre-of-mass x-velocities into row index of a
+ * ring created with count nmol */
+int sepdev_mvacf_store(sepdev *d, sepdev_moltab *t, sepdev_vacf *v, int index);
+/* mgh: for each wavevector k[j] along y, out[18 j + 2 q + (0 re, 1 im)] =
+ * sum over molecules of e^{i k_j y_cm} w_q with w = (M, M vx, M vy, M v^2/2,
+ * 1, s_z, s_y, dipole_y, w_x) (w_x, the angular velocity, only when unsafe;
+ * else 0); out[18 nk] = sum of M v^2/2.  The dipole of a molecule without
+ * both signs of charge keeps its last value (initially 0). */
+int sepdev_mgh_sample(sepdev *d, sepdev_moltab *t, int nk, const double *k, int unsafe, double *out);
 int sepdev_msd_create(sepdev *d, int nk, const double *k, sepdev_msd **out);
 void sepdev_msd_destroy(sepdev_msd *m);
 int sepdev_msd_base(sepdev *d, sepdev_msd *m);

@@ -293,6 +293,34 @@ def molp_small(lib, tmp):
     return d
 
 
+def molsampler_small(lib, tmp):
+    """The msacf, mvacf and mgh (unsafe mode, 3 wavevectors) samplers on a
+    prgs/prg3.c-style run of 125 charged three-site molecules: two blocks of
+    4 samples, one every 2 steps.  The positions, velocities and molecular
+    pressure tensors at the sample steps, the spins, angular velocities and
+    dipoles the mgh sampler left in the molecule array, and the files the
+    reference wrote."""
+    from sephelp import water_mol_run
+    s = cfg.water_like(nmol=125, rho=0.09, seed=6)
+    top = os.path.join(tmp, "ms.top")
+    cfg.write_top(top, s)
+    cwd = os.getcwd()
+    run = os.path.join(tmp, "ms")
+    os.makedirs(run, exist_ok=True)
+    os.chdir(run)
+    try:
+        r = water_mol_run(lib, s, top, nsteps=16, lvec=4, tsample=0.0041, nk=3, unsafe=True, record_every=2,
+                          record_mols=True)
+    finally:
+        os.chdir(cwd)
+    d = dict(x0=s.x, v0=s.v, L=s.L, z=s.z, m=s.m, types=s.types.astype("S1"), bonds=s.bonds,
+             angles=s.angles, xs=r["x"], vs=r["v"], P=r["P"], molindex=r["molindex"], nmol=r["nmol"],
+             volume=r["volume"], mol_s=r["mol_s"], mol_w=r["mol_w"], mol_pel=r["mol_pel"])
+    for k, v in r["files"].items():
+        d["file_" + k] = v
+    return d
+
+
 def box_ops(lib):
     """sep_compress_box / _dir / _dir_length and sep_berendsen / _iso one at
     a time, then a Berendsen run (prgs/prg7.c) and a compression run
@@ -408,7 +436,8 @@ def main(only=()):
                          ("host_api", lambda: host_api(lib)),
                          ("stoch_small", lambda: stochastic(lib)),
                          ("box_small", lambda: box_ops(lib)),
-                         ("molp_small", lambda: molp_small(lib, tmp))):
+                         ("molp_small", lambda: molp_small(lib, tmp)),
+                         ("molsampler_small", lambda: molsampler_small(lib, tmp))):
             if only and name not in only:
                 continue
             d = fn()

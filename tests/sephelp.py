@@ -75,3 +75,86 @@ def boundary_mask(x, L, pairs, rlist, tol=1e-6):
     d -= L * np.round(d / L)
     r = np.sqrt((d * d).sum(1))
     return np.abs(r - rlist) < tol
+
+
+def bind_samplers(lib):
+    """ctypes signatures of the sampler API (sep_add_sampler is variadic:
+    callers pass ctypes-typed arguments)"""
+    for name, res, args in (("sep_init_sampler", A.SepSampler, []),
+                            ("sep_sample", None, [A.PART_P, C.POINTER(A.SepSampler), A.RET_P, A.SepSys,
+                                                  C.c_uint]),
+                            ("sep_close_sampler", None, [C.POINTER(A.SepSampler)]),
+                            ("sep_add_mol_sampler", None, [C.POINTER(A.SepSampler), C.c_void_p])):
+        f = getattr(lib, name)
+        f.restype, f.argtypes = res, args
+    lib.sep_add_sampler.restype = None
+    return lib
+
+
+MOLSAMPLER_FILES = {"msacf": "msacf.dat", "mvacf": "mvacf.dat",
+                    "mgh-tv": "mgh-trans-momentum-acf.dat", "mgh-lv": "mgh-long-momentum-acf.dat",
+                    "mgh-scatt": "mgh-rho-acf.dat", "mgh-tav": "mgh-trans-angmomentum-acf.dat",
+                    "mgh-lav": "mgh-long-angmomentum-acf.dat", "mgh-e": "mgh-energy-acf.dat",
+                    "mgh-vav": "mgh-momentum-angmomentum-ccf.dat", "mgh-dip": "mgh-dipole-acf.dat",
+                    "mgh-X": "mgh-X-cf.dat"}
+
+
+def water_mol_run(lib, s, top, nsteps, lvec, tsample, nk, unsafe, record_every, record_mols=False):
+    """A prgs/prg3.c-style run (LJ on O, SF Coulomb, bonds, cos^2 angles,
+    Nose-Hoover, leap-frog) with the msacf, mvacf and mgh samplers, in the
+    current directory.  Returns the positions, velocities and molecular
+    pressure tensors after the sampler call at every `record_every`-th step
+    (downloaded: an observation point), the molecule index of each atom and
+    the files the samplers wrote.  With `record_mols`, also the spin, angular
+    velocity and dipole the mgh sampler leaves in the molecule array (the
+    reference's side effect; this library's samplers keep them on the
+    device)."""
+    bind_samplers(lib)
+    h = Handle(lib, s, cf=3.0, update=A.SEP_LLIST_NEIGHBLIST, dt=0.0005)
+    lib.sep_read_topology_file(h.atoms, top.encode(), C.byref(h.sys), b"q")
+    mols = lib.sep_init_mol(h.atoms, C.byref(h.sys))
+    smp = lib.sep_init_sampler()
+    lib.sep_add_mol_sampler(C.byref(smp), C.cast(mols, C.c_void_p))
+    add = lib.sep_add_sampler
+    add(C.byref(smp), b"msacf", h.sys, C.c_int(lvec), C.c_double(tsample))
+    add(C.byref(smp), b"mvacf", h.sys, C.c_int(lvec), C.c_double(tsample))
+    add(C.byref(smp), b"mgh", h.sys, C.c_int(lvec), C.c_double(tsample), C.c_int(nk), C.c_int(0 if unsafe else 1))
+    xs, vs, Ps, mol_s, mol_w, mol_pel = [], [], [], [], [], []
+    nm = h.sys.molptr.contents.num_mols
+    mp = C.cast(mols, C.POINTER(A.SepMol))
+    for n in range(nsteps):
+        lib.sep_reset_retval(C.byref(h.ret))
+        lib.sep_reset_force(h.atoms, C.byref(h.sys))
+        lib.sep_reset_force_mol(C.byref(h.sys))
+        lib.sep_force_pairs(h.atoms, b"OO", 2.5, h.fun(), C.byref(h.sys), C.byref(h.ret), A.SEP_EXCL_SAME_MOL)
+        lib.sep_stretch_harmonic(h.atoms, 0, 0.316, 68421.0, C.byref(h.sys), C.byref(h.ret))
+        lib.sep_angle_cossq(h.atoms, 0, 1.97, 490.0, C.byref(h.sys), C.byref(h.ret))
+        lib.sep_coulomb_sf(h.atoms, 3.0, C.byref(h.sys), C.byref(h.ret), A.SEP_EXCL_SAME_MOL)
+        lib.sep_nosehoover(h.atoms, 3.0, C.byref(h.alpha), 0.01, C.byref(h.sys))
+        lib.sep_leapfrog(h.atoms, C.byref(h.sys), C.byref(h.ret))
+        lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, n)
+        if n % record_every == 0:
+            h.sync()
+            xs.append(h.view["x"].copy()); vs.append(h.view["v"].copy())
+            Ps.append(np.array(h.ret.P_mol))
+            if record_mols:
+                mol_s.append([list(mp[i].s) for i in range(nm)])
+                mol_w.append([list(mp[i].w) for i in range(nm)])
+                mol_pel.append([list(mp[i].pel) for i in range(nm)])
+    molindex = h.view["molindex"].copy()
+    nmol = h.sys.molptr.contents.num_mols
+    volume = h.sys.volume
+    lib.sep_close_sampler(C.byref(smp))
+    lib.sep_free_mol(mols, C.byref(h.sys))
+    h.close()
+    files = {}
+    for key, name in MOLSAMPLER_FILES.items():
+        if key == "mgh-X" and not unsafe:
+            continue
+        files[key] = np.atleast_2d(np.loadtxt(name))
+    files["mgh-k"] = np.loadtxt("mgh-wavevector.dat")
+    out = dict(x=np.array(xs), v=np.array(vs), P=np.array(Ps), molindex=molindex, nmol=nmol,
+               volume=volume, files=files)
+    if record_mols:
+        out.update(mol_s=np.array(mol_s), mol_w=np.array(mol_w), mol_pel=np.array(mol_pel))
+    return out

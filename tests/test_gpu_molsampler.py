@@ -1,0 +1,113 @@
+"""msacf, mvacf and mgh samplers on the GPU against the oracle's restatement
+of the reference's samplers (source/sepsampler.c:752-808, :1231-1410,
+:1782-1816), evaluated on the same trajectory.
+
+The run is the fixture molsampler_small's (125 charged three-site molecules,
+prgs/prg3.c forces, two blocks of 4 samples); at every sample step the state
+is downloaded (an observation point) and fed to the oracle.  Every number in
+the files must agree to the printing precision (%f, 5e-7 per side).  The
+energy correlation is included, with the mean kinetic energy starting at 0
+(the reference leaves it unset)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from seplib_gb300 import configs as cfg
+from sephelp import MOLSAMPLER_FILES, water_mol_run
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def g():
+    return np.load(os.path.join(HERE, "golden", "molsampler_small.npz"))
+
+
+@pytest.mark.parametrize("unsafe", [True, False])
+def test_molecular_sampler_files(gpu_lib, g, tmp_path, unsafe):
+    s = cfg.System(x=g["x0"].copy(), v=g["v0"].copy(), L=g["L"].copy(), types=g["types"].copy(),
+                   m=g["m"].copy(), z=g["z"].copy(), bonds=g["bonds"], angles=g["angles"])
+    top = str(tmp_path / "ms.top")
+    cfg.write_top(top, s)
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        r = water_mol_run(gpu_lib, s, top, nsteps=16, lvec=4, tsample=0.0041, nk=3, unsafe=unsafe,
+                          record_every=2)
+        x_size = os.path.getsize(MOLSAMPLER_FILES["mgh-X"])
+    finally:
+        os.chdir(cwd)
+    nmol = int(r["nmol"])
+    assert nmol == int(g["nmol"])
+    first, nuau, start, atoms = oracle.mol_tables(r["molindex"], nmol)
+    ms = oracle.MolSamplers(4, 0.0041 / 4, 3, g["L"][1], float(r["volume"]), unsafe)
+    pel = np.zeros((nmol, 3))
+    for k in range(len(r["x"])):
+        p = oracle.mol_props(r["x"][k], r["v"][k], g["m"], g["z"], first, nuau, start, atoms, g["L"], pel,
+                             unsafe)
+        ms.msacf(r["P"][k]); ms.mgh(p, pel); ms.mvacf(p["v"][:, 0])
+    files = r["files"]
+    np.testing.assert_allclose(files["mgh-k"], ms.k, rtol=0, atol=5.1e-7)
+    want = {"msacf", "mvacf", "mgh-tv", "mgh-lv", "mgh-scatt", "mgh-tav", "mgh-lav", "mgh-e", "mgh-vav",
+            "mgh-dip"} | ({"mgh-X"} if unsafe else set())
+    assert set(ms.out) == want
+    for key in want:
+        assert files[key].shape == ms.out[key].shape, key
+        np.testing.assert_allclose(files[key], ms.out[key], rtol=2e-7, atol=1.1e-6, err_msg=key)
+    if not unsafe:
+        assert x_size == 0          # opened and left empty, as the reference does
+    # the run is the reference's run up to FP32 forces: the trajectories stay close
+    np.testing.assert_allclose(r["x"][0], g["xs"][0], rtol=0, atol=1e-5)
+
+
+def test_mgh_full_size_butane(gpu_lib, tmp_path):
+    """one mgh and mvacf sample of 8000 butane chains (32000 beads; safe mode,
+    no charges) against the oracle on the same state"""
+    import ctypes as C
+    from seplib_gb300 import sepapi as A
+    from sephelp import Handle, bind_samplers
+    s = cfg.butane(nmol=8000, rho=0.6, seed=3)
+    top = str(tmp_path / "b.top")
+    cfg.write_top(top, s)
+    lib = bind_samplers(gpu_lib)
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        h = Handle(lib, s, cf=2.5, dt=0.002)
+        lib.sep_read_topology_file(h.atoms, top.encode(), C.byref(h.sys), b"q")
+        mols = lib.sep_init_mol(h.atoms, C.byref(h.sys))
+        smp = lib.sep_init_sampler()
+        lib.sep_add_mol_sampler(C.byref(smp), C.cast(mols, C.c_void_p))
+        # one sample per block: lvec 1
+        lib.sep_add_sampler(C.byref(smp), b"mgh", h.sys, C.c_int(1), C.c_double(0.002), C.c_int(10), C.c_int(1))
+        lib.sep_add_sampler(C.byref(smp), b"mvacf", h.sys, C.c_int(1), C.c_double(0.002))
+        for n in range(3):
+            h.forces(types=b"CC", opt=A.SEP_EXCL_SAME_MOL)
+            lib.sep_leapfrog(h.atoms, C.byref(h.sys), C.byref(h.ret))
+        lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, 0)
+        h.sync()
+        x, v = h.view["x"].copy(), h.view["v"].copy()
+        mi, nmol, vol = h.view["molindex"].copy(), h.sys.molptr.contents.num_mols, h.sys.volume
+        lib.sep_close_sampler(C.byref(smp))
+        lib.sep_free_mol(mols, C.byref(h.sys))
+        h.close()
+        tv = np.loadtxt("mgh-trans-momentum-acf.dat")
+        rho = np.loadtxt("mgh-rho-acf.dat")
+        lav = np.loadtxt("mgh-long-angmomentum-acf.dat")
+        mv = np.loadtxt("mvacf.dat")
+    finally:
+        os.chdir(cwd)
+    first, nuau, start, atoms = oracle.mol_tables(mi, nmol)
+    ms = oracle.MolSamplers(1, 0.002, 10, s.L[1], vol, False)
+    pel = np.zeros((nmol, 3))
+    p = oracle.mol_props(x, v, s.m, s.z, first, nuau, start, atoms, s.L, pel, False)
+    ms.mgh(p, pel)
+    ms.mvacf(p["v"][:, 0])
+    np.testing.assert_allclose(tv, ms.out["mgh-tv"][0], rtol=2e-7, atol=1.1e-6)
+    np.testing.assert_allclose(rho, ms.out["mgh-scatt"][0], rtol=2e-7, atol=1.1e-6)
+    np.testing.assert_allclose(lav, ms.out["mgh-lav"][0], rtol=2e-7, atol=1.1e-6)
+    np.testing.assert_allclose(mv, ms.out["mvacf"][0], rtol=2e-7, atol=1.1e-6)
+    assert np.abs(tv[1:]).max() > 1e-3
