@@ -83,6 +83,12 @@ void sep_compress_box_dir_length(sepatom *ptr, double length, double xi, int dir
 void sep_berendsen(sepatom *ptr, double Pd, double beta, sepret *ret, sepsys *sys);
 void sep_berendsen_iso(sepatom *ptr, double Pd, double beta, sepret *ret, sepsys *sys);
 
+/* Molecular Berendsen barostat (reference :216, source/sepmisc.c:948-990):
+ * xi = 1 - beta dt (Pd - p_mol) from sep_mol_pressure_tensor; L_z is scaled
+ * by xi, each molecule's centre-of-mass z by xi^(1/3) with its atoms keeping
+ * their offsets from it (wrapped once into the box), mol[].x[2] likewise. */
+void sep_berendsen_mol(sepatom *ptr, sepmol *mol, double Pd, double beta, sepret *ret, sepsys *sys);
+
 /* Sets the Langevin diffusion coefficient of every particle of a type
  * (reference :449, source/sepmisc.c:1162-1170). */
 void sep_set_ldiff(seppart *ptr, char type, double ldiff, sepsys sys);

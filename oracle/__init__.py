@@ -620,3 +620,62 @@ class MolSamplers:
             fac = self.V / (3.0 * (lv - np.arange(lv)) * self.na)
             self.out["msacf"] = np.column_stack([np.arange(lv) * self.dts, self.sacf * fac[:, None]])
             self.ia = 0
+
+
+def mol_cm_chain(x, m, first, nuau, L):
+    """centres of mass in the reference's order (source/sepmol.c:683-729):
+    the chain of consecutive indices from the first atom, each bond's minimum
+    image (sep_Wrap) added to the previous position, mass-weighted in order,
+    divided by the molecule mass (summed over the chain in order), wrapped
+    once (sep_Periodic)"""
+    x = np.asarray(x, float); m = np.asarray(m, float); L = np.asarray(L, float)
+    cm = np.zeros((len(first), 3))
+    for n in range(len(first)):
+        i, k = int(first[n]), int(nuau[n])
+        for d in range(3):
+            xp = chain = x[i, d]
+            acc = m[i] * chain
+            M = m[i]
+            for q in range(1, k):
+                r = x[i + q, d] - xp
+                if r > 0.5 * L[d]:
+                    r -= L[d]
+                elif r < -0.5 * L[d]:
+                    r += L[d]
+                chain = chain + r
+                acc = acc + m[i + q] * chain
+                M = M + m[i + q]
+                xp = x[i + q, d]
+            c = acc / M
+            if c > L[d]:
+                c -= L[d]
+            elif c < 0.0:
+                c += L[d]
+            cm[n, d] = c
+    return cm
+
+
+def berendsen_mol(x, m, molindex, first, nuau, L, p_mol, Pd, beta, dt):
+    """sep_berendsen_mol (source/sepmisc.c:948-990): xi = 1 - beta dt (Pd -
+    p_mol); L_z times xi; each molecule's centre-of-mass z times xi^(1/3),
+    its atoms keeping their (unwrapped) offsets from it, wrapped once into
+    the new box.  Returns the new positions, edges and centres of mass."""
+    x = np.array(x, float)
+    L = np.array(L, float)
+    cm = mol_cm_chain(x, m, first, nuau, L)
+    mi = np.asarray(molindex)
+    dr0 = np.where(mi >= 0, x[:, 2] - cm[np.maximum(mi, 0), 2], 0.0)
+    xi = 1 - beta * dt * (Pd - p_mol)
+    L1 = L.copy()
+    L1[2] = L[2] * xi
+    scale = xi ** (1.0 / 3.0)
+    cm[:, 2] = cm[:, 2] * scale
+    for a in range(len(x)):
+        if mi[a] != -1:
+            z = cm[mi[a], 2] + dr0[a]
+            if z > L1[2]:
+                z -= L1[2]
+            elif z < 0.0:
+                z += L1[2]
+            x[a, 2] = z
+    return x, L1, cm

@@ -1,4 +1,5 @@
-// dev_molsampler.cu - device parts of the molecular samplers mvacf and mgh.
+// dev_molsampler.cu - device parts of the molecular samplers mvacf and mgh,
+// and the molecular Berendsen barostat.
 //
 // The reference (source/sepsampler.c:1231-1410 mgh, :1757-1816 mvacf)
 // downloads nothing itself but walks every molecule on the host at each
@@ -329,5 +330,97 @@ extern "C" int sepdev_mgh_sample(sepdev *d, sepdev_moltab *t, int nk, const doub
 	CKL(d);
 	CK(cudaMemcpyAsync(out, t->sum, sizeof(double) * (MG_N * nk + 1), cudaMemcpyDeviceToHost, d->st));
 	CK(cudaStreamSynchronize(d->st));
+	return SEPDEV_OK;
+}
+
+// ---- molecular Berendsen barostat (source/sepmisc.c:948-990) ------------------
+//
+// The reference takes each molecule's centre of mass (source/sepmol.c:
+// 683-729), scales its z coordinate by xi^(1/3) while the box edge L_z is
+// scaled by xi, and moves every atom of the molecule with it, keeping its
+// offset from the centre of mass; the new z is wrapped once into the new box
+// without counting a crossing.  Atoms outside molecules keep their absolute
+// z (one beyond the new edge is wrapped and counted, as at the reference's
+// next integrator step).  Same FP64 operations as the reference.
+
+// z of the centre of mass, in the reference's order: the chain of
+// consecutive user indices from the first atom, each step's minimum image
+// added to the previous position
+__device__ double mol_cm_z(int m, const int *first, const int *nuau, const double *mass, const int4 *pos,
+			   const uint4 *xlo, const int *inv, const float4 *vhi, double L)
+{
+	const int a0 = first[m];
+	int s = inv[a0];
+	double xprev = from_fixed_dev((unsigned)pos[s].z, xlo[s].z, L), chain = xprev;
+	double acc = __dmul_rn((double)vhi[s].w, chain);
+	for (int q = 1; q < nuau[m]; q++) {
+		s = inv[a0 + q];
+		const double x = from_fixed_dev((unsigned)pos[s].z, xlo[s].z, L);
+		double r = __dsub_rn(x, xprev);
+		if (r > 0.5 * L) r = __dsub_rn(r, L);
+		else if (r < -0.5 * L) r = __dadd_rn(r, L);
+		chain = __dadd_rn(chain, r);
+		acc = __dadd_rn(acc, __dmul_rn((double)vhi[s].w, chain));
+		xprev = x;
+	}
+	double cm = __ddiv_rn(acc, mass[m]);
+	if (cm > L) cm = __dsub_rn(cm, L);
+	else if (cm < 0.0) cm = __dadd_rn(cm, L);
+	return cm;
+}
+
+__global__ void k_mol_cmz(int nmol, const int *first, const int *nuau, const double *mass, const int4 *pos,
+			  const uint4 *xlo, const int *inv, const float4 *vhi, double L, double *cmz)
+{
+	const int m = blockIdx.x * blockDim.x + threadIdx.x;
+	if (m < nmol) cmz[m] = mol_cm_z(m, first, nuau, mass, pos, xlo, inv, vhi, L);
+}
+
+__global__ void k_berendsen_mol(long n, int nmol, int4 *pos, uint4 *xlo, int4 *xn, int4 *cross, const int *mol,
+				const double *cmz, double L0, double L1, double scale)
+{
+	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const int4 p = pos[i];
+	const uint4 lo = xlo[i];
+	const int m = mol[i];
+	double x = from_fixed_dev((unsigned)p.z, lo.z, L0);
+	int cr = 0;
+	if (m >= 0 && m < nmol) {
+		const double dr0 = __dsub_rn(x, cmz[m]);
+		x = __dadd_rn(__dmul_rn(cmz[m], scale), dr0);
+		if (x > L1) x = __dsub_rn(x, L1);
+		else if (x < 0.0) x = __dadd_rn(x, L1);
+	} else if (x >= L1) {
+		x = __dsub_rn(x, L1);
+		cr = 1;
+	}
+	unsigned h, l, hn, ln;
+	to_fixed_dev(x, L1, h, l);
+	pos[i] = make_int4(p.x, p.y, (int)h, p.w);
+	xlo[i] = make_uint4(lo.x, lo.y, l, 0u);
+	const int4 q = xn[i];
+	to_fixed_dev(from_fixed_dev((unsigned)q.z, 0u, L0), L1, hn, ln);
+	xn[i] = make_int4(q.x, q.y, (int)hn, q.w);
+	if (cr) cross[i].z += 1;
+}
+
+extern void sepdev_runner_free(sepdev *d);
+
+extern "C" int sepdev_berendsen_mol(sepdev *d, sepdev_moltab *t, double L1z, double scale)
+{
+	if (!(L1z > 0.0) || !(scale > 0.0) || !d->mol) return SEPDEV_EINVAL;
+	double *cmz = t->props;      // scratch: nmol values
+	const int4 *pos = d->pos[d->cur];
+	k_mol_cmz<<<grid_for(t->nmol, 128), 128, 0, d->st>>>(t->nmol, t->first, t->nuau, t->mass, pos, d->xlo,
+							    d->inv, d->vhi, d->L[2], cmz);
+	k_berendsen_mol<<<grid_for(d->n, 256), 256, 0, d->st>>>(d->n, t->nmol, d->pos[d->cur], d->xlo, d->xn,
+								d->cross, d->mol, cmz, d->L[2], L1z, scale);
+	d->launches++;
+	CKL(d);
+	d->L[2] = L1z;
+	d->fscale[2] = (float)(L1z / 4294967296.0);
+	// captured loop graphs hold the old box's scale factors
+	sepdev_runner_free(d);
 	return SEPDEV_OK;
 }

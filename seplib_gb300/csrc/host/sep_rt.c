@@ -269,6 +269,9 @@ void rt_mv_drop(rt_ctx *c)
 	c->mv_mass = NULL;
 	c->mv_on = c->mv_uploaded = 0;
 	c->mv_info = NULL;
+	if (c->bm_tab) sepdev_moltab_destroy(c->bm_tab);
+	c->bm_tab = NULL;
+	c->bm_mols = NULL;
 	if (c->dev) sepdev_molvir_disable(c->dev);
 }
 

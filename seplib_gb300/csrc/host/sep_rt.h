@@ -129,6 +129,10 @@ typedef struct rt_ctx {
 	int *mv_first, *mv_nuau, *mv_start, *mv_atoms;
 	double *mv_mass;
 	double molW[9], molN[9];
+	/* molecule tables of sep_berendsen_mol's molecule array on the device */
+	sepdev_moltab *bm_tab;
+	const sepmol *bm_mols;
+	int bm_nmol;
 
 	/* statistics */
 	long nbuild;

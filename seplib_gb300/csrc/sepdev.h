@@ -281,6 +281,10 @@ int sepdev_mvacf_store(sepdev *d, sepdev_moltab *t, sepdev_vacf *v, int index);
  * else 0); out[18 nk] = sum of M v^2/2.  The dipole of a molecule without
  * both signs of charge keeps its last value (initially 0). */
 int sepdev_mgh_sample(sepdev *d, sepdev_moltab *t, int nk, const double *k, int unsafe, double *out);
+/* Molecular Berendsen step along z: each molecule's centre-of-mass z is
+ * scaled by `scale` and its atoms keep their offsets from it, the box edge
+ * L_z becomes L1z; atoms outside molecules keep their absolute z. */
+int sepdev_berendsen_mol(sepdev *d, sepdev_moltab *t, double L1z, double scale);
 int sepdev_msd_create(sepdev *d, int nk, const double *k, sepdev_msd **out);
 void sepdev_msd_destroy(sepdev_msd *m);
 int sepdev_msd_base(sepdev *d, sepdev_msd *m);

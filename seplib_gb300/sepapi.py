@@ -170,6 +170,7 @@ SIGNATURES = {
     "sep_compress_box_dir_length": (None, [PART_P, D, D, C.c_int, SYS_P]),
     "sep_berendsen": (None, [PART_P, D, D, RET_P, SYS_P]),
     "sep_berendsen_iso": (None, [PART_P, D, D, RET_P, SYS_P]),
+    "sep_berendsen_mol": (None, [PART_P, C.POINTER(SepMol), D, D, RET_P, SYS_P]),
 }
 
 

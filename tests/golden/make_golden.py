@@ -321,6 +321,50 @@ def molsampler_small(lib, tmp):
     return d
 
 
+def molbaro_small(lib, tmp):
+    """sep_berendsen_mol after a prgs/prg3.c step of 216 water-like molecules,
+    once compressing (Pd 0.4) and once expanding (Pd -0.25), beta 200, and
+    once compressing with every z shifted by 1.2 so that molecules straddle
+    the box edge: the positions and molecular pressure before the call, the
+    positions, box, sub-box grid and centres of mass after it."""
+    s = cfg.water_like(nmol=216, rho=0.09, seed=5)
+    top = os.path.join(tmp, "wb.top")
+    cfg.write_top(top, s)
+    d = dict(x=s.x, v=s.v, L=s.L, z=s.z, m=s.m, types=s.types.astype("S1"), bonds=s.bonds,
+             angles=s.angles)
+    for tag, Pd, dz in (("bmc", 0.4, 0.0), ("bme", -0.25, 0.0), ("bmw", 0.4, 1.2)):
+        s0 = cfg.water_like(nmol=216, rho=0.09, seed=5)
+        s0.x[:, 2] = np.mod(s0.x[:, 2] + dz, s0.L[2])
+        d[tag + "_xin"] = s0.x.copy()
+        h = Handle(lib, s0, cf=3.0, update=A.SEP_LLIST_NEIGHBLIST, dt=0.0005)
+        lib.sep_read_topology_file(h.atoms, top.encode(), C.byref(h.sys), b"q")
+        mols = lib.sep_init_mol(h.atoms, C.byref(h.sys))
+        d["molindex"] = h.view["molindex"].copy()
+        d["nmol"] = h.sys.molptr.contents.num_mols
+        lib.sep_reset_retval(C.byref(h.ret))
+        lib.sep_reset_force(h.atoms, C.byref(h.sys))
+        lib.sep_reset_force_mol(C.byref(h.sys))
+        lib.sep_force_pairs(h.atoms, b"OO", 2.5, h.fun(), C.byref(h.sys), C.byref(h.ret),
+                            A.SEP_EXCL_SAME_MOL)
+        lib.sep_stretch_harmonic(h.atoms, 0, 0.316, 68421.0, C.byref(h.sys), C.byref(h.ret))
+        lib.sep_angle_cossq(h.atoms, 0, 1.97, 490.0, C.byref(h.sys), C.byref(h.ret))
+        lib.sep_coulomb_sf(h.atoms, 3.0, C.byref(h.sys), C.byref(h.ret), A.SEP_EXCL_SAME_MOL)
+        lib.sep_nosehoover(h.atoms, 3.0, C.byref(h.alpha), 0.01, C.byref(h.sys))
+        lib.sep_leapfrog(h.atoms, C.byref(h.sys), C.byref(h.ret))
+        d[tag + "_x0"] = h.view["x"].copy()
+        d[tag + "_nsub0"] = np.array(h.sys.nsubbox)
+        lib.sep_berendsen_mol(h.atoms, mols, Pd, 200.0, C.byref(h.ret), C.byref(h.sys))
+        nm = d["nmol"]
+        d.update({tag + "_Pd": Pd, tag + "_p": h.ret.p_mol, tag + "_x1": h.view["x"].copy(),
+                  tag + "_L1": np.array(h.sys.length), tag + "_vol1": h.sys.volume,
+                  tag + "_nsub1": np.array(h.sys.nsubbox), tag + "_lsub1": np.array(h.sys.lsubbox),
+                  tag + "_cm": np.array([list(mols[i].x) for i in range(nm)]),
+                  tag + "_cross": h.view["crossings"].copy()})
+        lib.sep_free_mol(mols, C.byref(h.sys))
+        h.close()
+    return d
+
+
 def box_ops(lib):
     """sep_compress_box / _dir / _dir_length and sep_berendsen / _iso one at
     a time, then a Berendsen run (prgs/prg7.c) and a compression run
@@ -437,7 +481,8 @@ def main(only=()):
                          ("stoch_small", lambda: stochastic(lib)),
                          ("box_small", lambda: box_ops(lib)),
                          ("molp_small", lambda: molp_small(lib, tmp)),
-                         ("molsampler_small", lambda: molsampler_small(lib, tmp))):
+                         ("molsampler_small", lambda: molsampler_small(lib, tmp)),
+                         ("molbaro_small", lambda: molbaro_small(lib, tmp))):
             if only and name not in only:
                 continue
             d = fn()

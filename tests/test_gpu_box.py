@@ -133,3 +133,64 @@ def test_compression_run_matches_reference(gpu_lib, g):
     np.testing.assert_allclose(tr[:, :3], ref[:, :3], rtol=1e-5)
     assert np.abs(tr[:, 3] - ref[:, 3]).max() <= 1
     h.close()
+
+
+@pytest.mark.parametrize("tag", ["bmc", "bme", "bmw"])
+def test_berendsen_mol(gpu_lib, tag, tmp_path):
+    """sep_berendsen_mol on the device after a prgs/prg3.c step (fixture
+    molbaro_small): the move against the oracle on the device's own state
+    before the call (1e-12), the box, volume and sub-box grid against the
+    reference (the molecular pressure differs by the FP32 forces), the
+    crossings untouched, and a further step in the new box."""
+    import oracle
+    mb = np.load(os.path.join(HERE, "golden", "molbaro_small.npz"))
+    lib = gpu_lib
+    s = cfg.System(x=mb[tag + "_xin"].copy(), v=mb["v"].copy(), L=mb["L"].copy(), types=mb["types"].copy(),
+                   m=mb["m"].copy(), z=mb["z"].copy(), bonds=mb["bonds"], angles=mb["angles"])
+    top = str(tmp_path / "wb.top")
+    cfg.write_top(top, s)
+    h = Handle(lib, s, cf=3.0, update=A.SEP_LLIST_NEIGHBLIST, dt=0.0005)
+    lib.sep_read_topology_file(h.atoms, top.encode(), C.byref(h.sys), b"q")
+    mols = lib.sep_init_mol(h.atoms, C.byref(h.sys))
+    nm = int(mb["nmol"])
+
+    def step():
+        lib.sep_reset_retval(C.byref(h.ret))
+        lib.sep_reset_force(h.atoms, C.byref(h.sys))
+        lib.sep_reset_force_mol(C.byref(h.sys))
+        lib.sep_force_pairs(h.atoms, b"OO", 2.5, h.fun(), C.byref(h.sys), C.byref(h.ret), A.SEP_EXCL_SAME_MOL)
+        lib.sep_stretch_harmonic(h.atoms, 0, 0.316, 68421.0, C.byref(h.sys), C.byref(h.ret))
+        lib.sep_angle_cossq(h.atoms, 0, 1.97, 490.0, C.byref(h.sys), C.byref(h.ret))
+        lib.sep_coulomb_sf(h.atoms, 3.0, C.byref(h.sys), C.byref(h.ret), A.SEP_EXCL_SAME_MOL)
+        lib.sep_nosehoover(h.atoms, 3.0, C.byref(h.alpha), 0.01, C.byref(h.sys))
+        lib.sep_leapfrog(h.atoms, C.byref(h.sys), C.byref(h.ret))
+
+    step()
+    h.sync()
+    x0, cr0 = h.view["x"].copy(), h.view["crossings"].copy()
+    lib.sep_berendsen_mol(h.atoms, mols, float(mb[tag + "_Pd"]), 200.0, C.byref(h.ret), C.byref(h.sys))
+    p = h.ret.p_mol
+    h.sync()
+    x1 = h.view["x"].copy()
+    first, nuau, _, _ = oracle.mol_tables(h.view["molindex"], nm)
+    want, L1, cm = oracle.berendsen_mol(x0, mb["m"], h.view["molindex"], first, nuau, mb["L"], p,
+                                        float(mb[tag + "_Pd"]), 200.0, 0.0005)
+    d = x1 - want
+    d -= L1 * np.round(d / L1)
+    assert np.abs(d).max() < 1e-12
+    assert np.array_equal(np.array(h.sys.length), L1)
+    np.testing.assert_allclose(L1, mb[tag + "_L1"], rtol=1e-6)
+    assert h.sys.volume == pytest.approx(float(mb[tag + "_vol1"]), rel=1e-6)
+    assert np.array_equal(np.array(h.sys.nsubbox), mb[tag + "_nsub1"])
+    assert np.array_equal(h.view["crossings"], cr0)
+    assert p == pytest.approx(float(mb[tag + "_p"]), rel=1e-4)
+    mz = np.array([mols[i].x[2] for i in range(nm)])
+    dz = mz - cm[:, 2]
+    assert np.abs(dz - L1[2] * np.round(dz / L1[2])).max() < 1e-6
+    dref = x1 - mb[tag + "_x1"]
+    dref -= L1 * np.round(dref / L1)
+    assert np.abs(dref).max() < 1e-5
+    step()
+    assert np.isfinite(h.ret.epot) and np.isfinite(h.ret.ekin)
+    lib.sep_free_mol(mols, C.byref(h.sys))
+    h.close()
