@@ -68,16 +68,22 @@ __device__ __forceinline__ float3 sep64(const BondArgs &a, int sa, int sb)
 
 __device__ __forceinline__ float dot3(float3 u, float3 w) { return u.x * w.x + u.y * w.y + u.z * w.z; }
 
-// Each thread walks the incidence list of its particle once; every incident
-// term of a kind that is pending adds this atom's share.
+// BOND_LPA lanes share a particle: each walks every BOND_LPA-th entry of its
+// incidence list, and every incident term of a kind that is pending adds
+// this atom's share; the lanes' forces are summed by shuffles in a fixed
+// order.  The terms are independent chains of dependent loads, so the
+// lanes multiply the work in flight.
+#define BOND_LPA 4
 __global__ void __launch_bounds__(256) k_bonded(long n, BondArgs a)
 {
-	const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	const long s = gt / BOND_LPA;
+	const int sub = (int)(gt % BOND_LPA);
 	float fx = 0.f, fy = 0.f, fz = 0.f, eb = 0.f, ea = 0.f, ed = 0.f;
 	float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 	if (s < n) {
 		const int u = a.gid[s];
-		for (int t = a.inc_start[u], te = a.inc_start[u + 1]; t < te; t++) {
+		for (int t = a.inc_start[u] + sub, te = a.inc_start[u + 1]; t < te; t += BOND_LPA) {
 			const unsigned code = (unsigned)a.inc_term[t];
 			const int kind = (int)(code >> 30);
 			if (!a.has[kind]) continue;
@@ -163,6 +169,14 @@ __global__ void __launch_bounds__(256) k_bonded(long n, BondArgs a)
 				}
 			}
 		}
+	}
+#pragma unroll
+	for (int o = 1; o < BOND_LPA; o <<= 1) {
+		fx += __shfl_xor_sync(0xffffffffu, fx, o);
+		fy += __shfl_xor_sync(0xffffffffu, fy, o);
+		fz += __shfl_xor_sync(0xffffffffu, fz, o);
+	}
+	if (s < n && sub == 0) {
 		if (a.accumulate) {
 			if (fx != 0.f || fy != 0.f || fz != 0.f) {
 				float4 f = a.frc[s];
@@ -296,7 +310,7 @@ extern "C" int sepdev_bonded(sepdev *d, const sepdev_bterm *t, int nt, int accum
 	}
 	a.accumulate = accumulate;
 	a.slots = d->slots;
-	k_bonded<<<grid_for(d->n, 256), 256, 0, d->st>>>(d->n, a);
+	k_bonded<<<grid_for(d->n * BOND_LPA, 256), 256, 0, d->st>>>(d->n, a);
 	CKL(d);
 	return SEPDEV_OK;
 }
