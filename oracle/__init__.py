@@ -463,6 +463,29 @@ def mol_pressure(F, x, v, m, L, molindex, nmol):
     return kin.reshape(3, 3), pot.reshape(3, 3), cm, vcm
 
 
+def dpd_fij(x, L, molindex, nmol, cf, aij):
+    """dense F[i][j] (nmol, nmol, 3) of the O(N^2) DPD form's conservative
+    forces aij (1 - r) r_hat over every pair within cf of atoms in molecules
+    (source/sepprfrc.c:1134-1222; all atoms of the one type pair)"""
+    x = _f64(x); L = _f64(L); mi = np.asarray(molindex)
+    F = np.zeros((nmol, nmol, 3))
+    n = len(x)
+    for a in range(n - 1):
+        r = x[a] - x[a + 1:]
+        r = np.where(r > 0.5 * L, r - L, np.where(r < -0.5 * L, r + L, r))
+        r2 = (r * r).sum(1)
+        sel = np.nonzero(r2 < cf * cf)[0]
+        if mi[a] < 0 or len(sel) == 0:
+            continue
+        d = np.sqrt(r2[sel])
+        fC = aij * (1.0 - d)[:, None] * r[sel] / d[:, None]
+        mj = mi[a + 1 + sel]
+        ok = mj >= 0
+        np.add.at(F[mi[a]], mj[ok], fC[ok])
+        np.add.at(F[:, mi[a]], mj[ok], -fC[ok])
+    return F
+
+
 # ---- molecular samplers (msacf, mvacf, mgh) ---------------------------------------
 
 

@@ -25,6 +25,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include "dev_common.cuh"
+#include "dev_pair.cuh"
 
 #define SB 256
 
@@ -75,21 +76,42 @@ struct DpdArgs {
 	int accumulate;
 	long long *slot;
 	int off2;                            // slot2 - slot, in fields
+	// molecular sums (MOLV): molecule of each slot, centres of mass at the
+	// pass, per-atom intermolecular force (user order), mslot - slot
+	const int *mol;
+	const int4 *mcm;
+	float4 *finter;
+	int moff;
 };
 
 // Full list: particle i sums the pair terms of all its neighbours.  The
 // per-side energy is aij w^2 / 4 (each pair is seen from both ends).  VIR:
 // the O(N^2) form also accumulates the conservative, random and dissipative
-// virials f_k r_kk (halved for the same reason).
-template <bool VIR>
+// virials f_k r_kk (halved for the same reason).  MOLV (with VIR): the
+// conservative force of each pair of atoms in different molecules also
+// adds f (x) R_ij and f (x) n_ij to the molecular slot and f to the atom's
+// intermolecular force, as the pair kernels do for their forces (the
+// reference's O(N^2) form adds the conservative force to its molecular
+// force matrix, source/sepprfrc.c:1211-1222).
+template <bool VIR, bool MOLV = false>
 __global__ void __launch_bounds__(SB) k_dpd(long n, DpdArgs a)
 {
 	const long i = blockIdx.x * (long)SB + threadIdx.x;
 	float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
 	float wc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, wr[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 	float wd[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+	float wm[18];
+#pragma unroll
+	for (int k = 0; k < 18; k++) wm[k] = 0.f;
+	float gix = 0.f, giy = 0.f, giz = 0.f;
+	int mi = -1;
 	if (i < n) {
 		const int4 pi = a.pos[i];
+		int4 ci = make_int4(0, 0, 0, 0);
+		if (MOLV) {
+			mi = a.mol[i];
+			if (mi >= 0) ci = a.mcm[mi];
+		}
 		if (pi.w == a.tA || pi.w == a.tB) {
 			const float4 vi = a.pv[i];
 			const int gi = a.gid[i], cnt = a.ncnt[i];
@@ -127,22 +149,55 @@ __global__ void __launch_bounds__(SB) k_dpd(long n, DpdArgs a)
 							wc[q] += fc * rr; wr[q] += fr * rr; wd[q] += fd * rr;
 						}
 				}
+				if (MOLV && mi >= 0) {
+					const int mj = __ldg(&a.mol[j]);
+					if (mj >= 0 && mj != mi) {
+						const int4 cj = __ldg(&a.mcm[mj]);
+						const unsigned hi[3] = {(unsigned)ci.x, (unsigned)ci.y, (unsigned)ci.z};
+						const unsigned hj[3] = {(unsigned)cj.x, (unsigned)cj.y, (unsigned)cj.z};
+						const float g3[3] = {fc * rx, fc * ry, fc * rz};
+						float R[3], nim[3];
+#pragma unroll
+						for (int q = 0; q < 3; q++) {
+							const int dI = (int)(hi[q] - hj[q]);
+							R[q] = (float)dI * a.fs[q];
+							nim[q] = (float)((((long long)hi[q] - (long long)hj[q]) - dI) >> 32);
+						}
+#pragma unroll
+						for (int p = 0; p < 3; p++)
+#pragma unroll
+							for (int q = 0; q < 3; q++) {
+								wm[3 * p + q] += g3[p] * R[q];
+								wm[9 + 3 * p + q] += g3[p] * nim[q];
+							}
+						gix += g3[0]; giy += g3[1]; giz += g3[2];
+					}
+				}
 			}
+		}
+		if (MOLV && mi >= 0) {
+			const int u = a.gid[i];
+			float4 fo = a.finter[u];
+			fo.x += gix; fo.y += giy; fo.z += giz;
+			a.finter[u] = fo;
 		}
 		float4 f = a.accumulate ? a.frc[i] : make_float4(0.f, 0.f, 0.f, 0.f);
 		f.x += fx; f.y += fy; f.z += fz;
 		a.frc[i] = f;
 	}
 	if (VIR) {
-		float v[19];
-		int fld[19];
+		constexpr int NM = MOLV ? 18 : 0;
+		float v[19 + NM];
+		int fld[19 + NM];
 		v[0] = 0.25f * e; fld[0] = SLOT_EPOT0;
 		for (int q = 0; q < 6; q++) {
 			v[1 + q] = 0.5f * wc[q]; fld[1 + q] = SLOT_POTP + q;
 			v[7 + q] = 0.5f * wr[q]; fld[7 + q] = SLOT_POTPB + q;
 			v[13 + q] = 0.5f * wd[q]; fld[13 + q] = a.off2 + SLOT_POTP + q;
 		}
-		block_to_slot<19>(v, fld, a.slot, 0.f, -1);
+#pragma unroll
+		for (int k = 0; k < NM; k++) { v[19 + k] = 0.5f * wm[k]; fld[19 + k] = a.moff + k; }
+		block_to_slot<19 + NM>(v, fld, a.slot, 0.f, -1);
 	} else {
 		float v[1] = {0.25f * e};
 		const int fld[1] = {SLOT_EPOT0};
@@ -425,6 +480,8 @@ extern "C" int sepdev_dpd_forces(sepdev *d, const sepdev_dpd *p, int accumulate,
 	if (!d->ext[0] || !d->list_valid) return SEPDEV_EINVAL;
 	if (slot < 0 || slot >= d->nslots || (p->virial && (slot2 < 0 || slot2 >= d->nslots)))
 		return SEPDEV_EINVAL;
+	const bool molv = p->virial && p->mslot >= 0 && d->molvir_on;
+	if (molv && p->mslot >= d->nslots) return SEPDEV_EINVAL;
 	DpdArgs a;
 	memset(&a, 0, sizeof a);
 	a.pos = d->pos[d->cur];
@@ -443,8 +500,19 @@ extern "C" int sepdev_dpd_forces(sepdev *d, const sepdev_dpd *p, int accumulate,
 	a.accumulate = accumulate;
 	a.slot = d->slots + (long)slot * SLOT_FIELDS;
 	a.off2 = (slot2 - slot) * SLOT_FIELDS;
-	if (p->virial) k_dpd<true><<<grid_for(d->n, SB), SB, 0, d->st>>>(d->n, a);
-	else k_dpd<false><<<grid_for(d->n, SB), SB, 0, d->st>>>(d->n, a);
+	if (molv) {
+		// the centres of mass of this pass, as the pair passes take them
+		sepdev_molvir_cm(d, a.pos);
+		a.mol = d->mol;
+		a.mcm = d->mv_cm;
+		a.finter = d->mv_finter;
+		a.moff = (p->mslot - slot) * SLOT_FIELDS;
+		k_dpd<true, true><<<grid_for(d->n, SB), SB, 0, d->st>>>(d->n, a);
+	} else if (p->virial) {
+		k_dpd<true><<<grid_for(d->n, SB), SB, 0, d->st>>>(d->n, a);
+	} else {
+		k_dpd<false><<<grid_for(d->n, SB), SB, 0, d->st>>>(d->n, a);
+	}
 	CKL(d);
 	return SEPDEV_OK;
 }

@@ -53,8 +53,12 @@ static void dpd(const char *caller, seppart *ptr, const char *types, double cf, 
 	} else {
 		rt_materialize_forces(c);
 	}
-	if (c->nslots >= 14) rt_flush(c);
+	/* the O(N^2) form adds its conservative forces to the molecular tensor
+	 * (source/sepprfrc.c:1211-1222) */
+	const int molv = brute && c->mv_on && c->mv_uploaded;
+	if (c->nslots >= (molv ? 13 : 14)) rt_flush(c);
 	const int slot = rt_new_slot(c), slot2 = brute ? rt_new_slot(c) : -1;
+	const int mslot = molv ? rt_new_slot(c) : -1;
 	sepdev_dpd p;
 	p.tA = rt_type_id(c, types[0]);
 	p.tB = rt_type_id(c, types[1]);
@@ -63,9 +67,11 @@ static void dpd(const char *caller, seppart *ptr, const char *types, double cf, 
 	p.seed = c->seed;
 	p.call = c->ncall[RT_STREAM_DPD]++;
 	p.virial = brute;
+	p.mslot = mslot;
 	rt_check(sepdev_dpd_forces(c->dev, &p, accumulate, slot, slot2), "DPD forces");
 	rt_add_op(c, ret, brute ? OP_PAIR_ADD : OP_PAIR_ASSIGN, slot, 0);
 	if (brute) rt_add_op(c, ret, OP_DPD_VIR, slot, slot2);
+	if (molv) rt_add_op(c, NULL, OP_MOLVIR, mslot, 0);
 	c->host_valid = 0;
 }
 

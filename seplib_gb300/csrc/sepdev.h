@@ -306,6 +306,9 @@ typedef struct {
 	unsigned call;
 	int virial;              /* 1: pot_P (conservative) to slot, random and
 	                          * dissipative parts to slot2 (the O(N^2) form) */
+	int mslot;               /* with virial and the molecular tensor on: the
+	                          * slot of the conservative forces' molecular
+	                          * sums (as a pair pass's); -1 none */
 } sepdev_dpd;
 int sepdev_ext_enable(sepdev *d);
 int sepdev_ext_enabled(const sepdev *d);

@@ -365,6 +365,47 @@ def molbaro_small(lib, tmp):
     return d
 
 
+def dpd_dimers(seed=21, nmol=300, rho=3.0):
+    """DPD dimers (bond 0.5) at random positions, all type A, unit masses"""
+    rng = np.random.default_rng(seed)
+    n = 2 * nmol
+    L = (n / rho) ** (1.0 / 3.0)
+    a = rng.uniform(0, L, (nmol, 3))
+    u = rng.normal(size=(nmol, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    x = np.mod(np.stack([a, a + 0.5 * u], 1).reshape(-1, 3), L)
+    v = rng.normal(0, 1.0, (n, 3))
+    mol = np.arange(nmol)
+    bonds = np.stack([mol, 2 * mol, 2 * mol + 1, 0 * mol], 1)
+    return cfg.System(x=x, v=v, L=np.array([L, L, L]), types=np.full(n, b"A", dtype="S1"), m=np.ones(n),
+                      z=np.zeros(n), bonds=bonds, angles=np.zeros((0, 5), int))
+
+
+def dpdmol_small(lib, tmp):
+    """The O(N^2) DPD force (SEP_BRUTE) on 300 dimers, then
+    sep_mol_pressure_tensor: the conservative forces enter the molecular
+    tensor (source/sepprfrc.c:1211-1222); no integration between the two, so
+    the tensor depends on the positions and velocities only."""
+    s = dpd_dimers()
+    top = os.path.join(tmp, "dd.top")
+    cfg.write_top(top, s)
+    h = Handle(lib, s, cf=1.0, update=A.SEP_BRUTE, dt=0.01)
+    h.view["pv"] = s.v
+    lib.sep_read_topology_file(h.atoms, top.encode(), C.byref(h.sys), b"q")
+    mols = lib.sep_init_mol(h.atoms, C.byref(h.sys))
+    lib.sep_reset_retval(C.byref(h.ret))
+    lib.sep_reset_force(h.atoms, C.byref(h.sys))
+    lib.sep_reset_force_mol(C.byref(h.sys))
+    lib.sep_force_dpd(h.atoms, b"AA", 1.0, 25.0, 1.0, 3.0, C.byref(h.sys), C.byref(h.ret), A.SEP_ALL)
+    lib.sep_mol_pressure_tensor(h.atoms, mols, C.byref(h.ret), C.byref(h.sys))
+    d = dict(x=s.x, v=s.v, L=s.L, bonds=s.bonds, flag_Fij=h.sys.molptr.contents.flag_Fij,
+             kin=np.array(h.ret.kin_P_mol), pot=np.array(h.ret.pot_P_mol), P=np.array(h.ret.P_mol),
+             p=h.ret.p_mol, potP_cons=np.array(h.ret.pot_P_conservative), epot=h.ret.epot)
+    lib.sep_free_mol(mols, C.byref(h.sys))
+    h.close()
+    return d
+
+
 def box_ops(lib):
     """sep_compress_box / _dir / _dir_length and sep_berendsen / _iso one at
     a time, then a Berendsen run (prgs/prg7.c) and a compression run
@@ -482,7 +523,8 @@ def main(only=()):
                          ("box_small", lambda: box_ops(lib)),
                          ("molp_small", lambda: molp_small(lib, tmp)),
                          ("molsampler_small", lambda: molsampler_small(lib, tmp)),
-                         ("molbaro_small", lambda: molbaro_small(lib, tmp))):
+                         ("molbaro_small", lambda: molbaro_small(lib, tmp)),
+                         ("dpdmol_small", lambda: dpdmol_small(lib, tmp))):
             if only and name not in only:
                 continue
             d = fn()

@@ -74,3 +74,35 @@ def test_mol_pressure_matches_reference(gpu_lib, g, tag, tmp_path):
     lib.sep_free_mol(mols, C.byref(h.sys))
     h.close()
 
+
+
+def test_dpd_mol_pressure_matches_reference(gpu_lib, tmp_path):
+    """the O(N^2) DPD form (SEP_BRUTE) adds its conservative forces to the
+    molecular tensor as the reference's force matrix does (fixture
+    dpdmol_small: 300 dimers, the tensor right after the force call);
+    FP32 conservative forces: 1e-4 of the largest pot_P_mol entry"""
+    lib = gpu_lib
+    d = np.load(os.path.join(HERE, "golden", "dpdmol_small.npz"))
+    n = len(d["x"])
+    s = cfg.System(x=d["x"].copy(), v=d["v"].copy(), L=d["L"].copy(), types=np.full(n, b"A", "S1"),
+                   m=np.ones(n), z=np.zeros(n), bonds=d["bonds"], angles=np.zeros((0, 5), int))
+    top = str(tmp_path / "dd.top")
+    cfg.write_top(top, s)
+    h = Handle(lib, s, cf=1.0, update=A.SEP_BRUTE, dt=0.01)
+    h.view["pv"] = d["v"]
+    lib.sep_read_topology_file(h.atoms, top.encode(), C.byref(h.sys), b"q")
+    mols = lib.sep_init_mol(h.atoms, C.byref(h.sys))
+    assert h.sys.molptr.contents.flag_Fij == 1
+    lib.sep_reset_retval(C.byref(h.ret))
+    lib.sep_reset_force(h.atoms, C.byref(h.sys))
+    lib.sep_reset_force_mol(C.byref(h.sys))
+    lib.sep_force_dpd(h.atoms, b"AA", 1.0, 25.0, 1.0, 3.0, C.byref(h.sys), C.byref(h.ret), A.SEP_ALL)
+    lib.sep_mol_pressure_tensor(h.atoms, mols, C.byref(h.ret), C.byref(h.sys))
+    kin, pot = np.array(h.ret.kin_P_mol), np.array(h.ret.pot_P_mol)
+    np.testing.assert_allclose(kin, d["kin"], rtol=1e-5, atol=1e-5 * np.abs(d["kin"]).max())
+    assert np.abs(pot - d["pot"]).max() < 1e-4 * np.abs(d["pot"]).max()
+    assert h.ret.p_mol == pytest.approx(float(d["p"]), rel=1e-4)
+    np.testing.assert_allclose(np.array(h.ret.pot_P_conservative), d["potP_cons"], rtol=1e-4,
+                               atol=1e-4 * np.abs(d["potP_cons"]).max())
+    lib.sep_free_mol(mols, C.byref(h.sys))
+    h.close()

@@ -34,3 +34,25 @@ def test_mol_pressure_matches_reference(ora, g, tag):
     assert np.abs(pot - g[tag + "_pot"]).max() < 1e-5 * np.abs(g[tag + "_pot"]).max()
     P = (kin + pot) / np.prod(g[tag + "_L1"])
     assert np.trace(P) / 3 == pytest.approx(float(g[tag + "_p"]), rel=1e-5)
+
+
+def dimer_molindex(bonds, n):
+    mi = np.full(n, -1)
+    mi[bonds[:, 1]] = bonds[:, 0]
+    mi[bonds[:, 2]] = bonds[:, 0]
+    return mi
+
+
+def test_dpd_mol_pressure_matches_reference(ora):
+    """the O(N^2) DPD form's conservative forces in the molecular tensor
+    (fixture dpdmol_small: 300 dimers, sep_force_dpd under SEP_BRUTE, then
+    sep_mol_pressure_tensor)"""
+    d = np.load(os.path.join(HERE, "golden", "dpdmol_small.npz"))
+    n = len(d["x"])
+    nmol = len(d["bonds"])
+    mi = dimer_molindex(d["bonds"], n)
+    F = ora.dpd_fij(d["x"], d["L"], mi, nmol, 1.0, 25.0)
+    kin, pot, _, _ = ora.mol_pressure(F.ravel(), d["x"], d["v"], np.ones(n), d["L"], mi, nmol)
+    assert int(d["flag_Fij"]) == 1
+    np.testing.assert_allclose(kin, d["kin"], rtol=1e-12, atol=1e-12 * np.abs(d["kin"]).max())
+    assert np.abs(pot - d["pot"]).max() < 1e-5 * np.abs(d["pot"]).max()
