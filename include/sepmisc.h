@@ -95,6 +95,17 @@ void sep_set_ldiff(seppart *ptr, char type, double ldiff, sepsys sys);
 
 /* Removes the centre-of-mass momentum of one type (reference :338). */
 void sep_reset_momentum(seppart *ptr, const char type, sepsys *sys);
+
+/* Rescales the velocities of one type towards the temperature Td with
+ * relaxation time tau, then removes that type's momentum (reference :175,
+ * source/sepmisc.c:357-391). */
+void sep_relax_temp(seppart *ptr, char type, double Td, double tau, sepsys *sys);
+
+/* Tether force f -= fun(r2, 'f') r, r = x0 - x (minimum image), on the
+ * particles of one type (reference :262, source/sepmisc.c:645-670); this
+ * implementation takes linear tethers, fun(r2, 'f') independent of r2
+ * (sep_spring_x0), and ends the program with sep_error otherwise. */
+void sep_force_x0(seppart *ptr, char type, double (*fun)(double, char), sepsys *sys);
 void sep_set_ndof(size_t ndof, sepsys *sys);
 void sep_set_x0(seppart *ptr, int npart);
 void sep_set_xn(seppart *ptr, int npart);

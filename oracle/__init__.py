@@ -702,3 +702,77 @@ def berendsen_mol(x, m, molindex, first, nuau, L, p_mol, Pd, beta, dt):
                 z += L1[2]
             x[a, 2] = z
     return x, L1, cm
+
+
+# ---- per-type operations (tethers, temperature relaxation, profiles) -------------
+
+
+def tether_forces(x, x0, L, types, type_, k):
+    """sep_force_x0 with a linear tether fun(r2, 'f') = -k (source/sepmisc.c:
+    645-670): f = k (x0 - x), minimum image, on the particles of the type"""
+    L = np.asarray(L, float)
+    r = _wrap(np.asarray(x0, float) - np.asarray(x, float), L)
+    f = np.zeros_like(r)
+    sel = np.asarray(types) == type_
+    f[sel] = -(-k * r[sel])
+    return f
+
+
+def reset_momentum(v, m, types, type_):
+    """source/sepmisc.c:1173-1192: v -= sum m v / sum m over the type"""
+    v = np.array(v, float)
+    sel = np.asarray(types) == type_
+    mom = (v[sel] * np.asarray(m, float)[sel, None]).sum(0)
+    v[sel] -= mom / np.asarray(m, float)[sel].sum()
+    return v
+
+
+def relax_temp(v, m, types, type_, Td, tau, dt):
+    """source/sepmisc.c:357-391: v *= sqrt(1 + dt/tau (Td/Ta - 1)) over the
+    type, Ta = 2 ekin / (3 n_type), then the type's momentum reset"""
+    v = np.array(v, float)
+    m = np.asarray(m, float)
+    sel = np.asarray(types) == type_
+    ekin = 0.5 * (m[sel, None] * v[sel] ** 2).sum()
+    Ta = 2.0 * ekin / (3 * sel.sum())
+    v[sel] *= np.sqrt(1.0 + (dt / tau) * (Td / Ta - 1.0))
+    return reset_momentum(v, m, types, type_)
+
+
+class Profs:
+    """the profs sampler (source/sepsampler.c:1418-1510): bins of L_dir / lvec
+    along dir over one type; momentum density of v[dirvel], mass density and
+    the kinetic sums of the other two components, averaged over samples;
+    `out` holds the file's columns after every 100th sample"""
+
+    def __init__(self, lvec, type_, dir_=2, dirvel=0):
+        self.lvec, self.type, self.dir, self.dirvel = lvec, type_, dir_, dirvel
+        self.momc = np.zeros(lvec); self.dens = np.zeros(lvec)
+        self.temp = np.zeros(lvec); self.svel = np.zeros(lvec)
+        self.nsample = 0
+        self.out = None
+
+    def sample(self, x, v, m, types, L):
+        L = np.asarray(L, float)
+        d, lv = self.dir, self.lvec
+        dl = L[d] / lv
+        dV = dl * np.prod(np.delete(L, d))
+        sel = np.asarray(types) == self.type
+        b = np.minimum((np.asarray(x)[sel, d] / dl).astype(int), lv - 1)
+        mm = np.asarray(m, float)[sel]
+        vv = np.asarray(v, float)[sel]
+        j = np.bincount(b, mm * vv[:, self.dirvel], lv)
+        rho = np.bincount(b, mm, lv)
+        other = [k for k in range(3) if k != self.dirvel]
+        s2 = np.bincount(b, mm * (vv[:, other] ** 2).sum(1), lv)
+        nb = np.bincount(b, minlength=lv)
+        self.nsample += 1
+        self.momc += j / dV
+        self.dens += rho / dV
+        self.temp += np.where(nb > 0, s2, 0.0)
+        if self.nsample % 100 == 0:
+            pos = self.dens > 0.0
+            self.svel[pos] = self.momc[pos] / self.dens[pos]
+            tfac = np.where(pos, 1.0 / (2.0 * dV * np.where(pos, self.dens, 1.0)), 0.0)
+            self.out = np.column_stack([(np.arange(lv) + 0.5) * dl, self.momc / self.nsample,
+                                        self.dens / self.nsample, self.temp * tfac, self.svel])

@@ -56,6 +56,12 @@ struct sepdev {
 	// molecular pressure tensor (sepdev_molvir_enable): molecule tables in
 	// user indices, centres of mass of the last pair pass and its box, the
 	// per-atom intermolecular force since the last reset (user order)
+	// per-type operations (dev_typeops.cu): tether positions x0 (user
+	// order, 3 doubles each), scratch for sums and profile histograms
+	double *x0;
+	void *tscr;
+	size_t tscr_cap;
+
 	int molvir_on, nmolv;
 	int *mv_first, *mv_nuau, *mv_start, *mv_atoms;
 	double *mv_mass;

@@ -101,7 +101,7 @@ extern "C" void sepdev_destroy(sepdev *d)
 			d->celloff, d->cellcount, d->cellstart, d->perm, d->nl, d->ncnt, d->exb_start,
 			d->exb_idx, d->exa_start, d->exa_idx, d->bonds, d->angles, d->diheds_abcd,
 			d->dihed_type, d->inc_start, d->inc_term, d->term_out, d->slots, d->flags,
-			d->d_ps, d->flush_buf, d->hio_scr};
+			d->d_ps, d->flush_buf, d->hio_scr, d->x0, d->tscr};
 	for (size_t k = 0; k < sizeof bufs / sizeof bufs[0]; k++)
 		if (bufs[k]) cudaFree(bufs[k]);
 	for (int k = 0; k < SEPDEV_MAXTAB; k++)

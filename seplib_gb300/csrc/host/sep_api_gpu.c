@@ -32,6 +32,7 @@ int sep_gpu_invalidate(seppart *ptr)
 	rt_flush(c);
 	c->host_valid = 1;
 	c->dev_valid = 0;
+	c->x0_valid = 0;
 	c->forces_zero = 0;
 	return 0;
 }

@@ -281,25 +281,11 @@ void sep_set_mass(seppart *ptr, char type, double m, sepsys sys)
 		if (ptr[i].type == type) ptr[i].m = m;
 }
 
-void sep_reset_momentum(seppart *ptr, const char type, sepsys *sys)
-{
-	rt_ctx *c = rt_get(ptr, __func__);
-	rt_host_modified(c);
-	double mom[3] = {0, 0, 0}, mass = 0.0;
-	for (long i = 0; i < sys->npart; i++)
-		if (ptr[i].type == type) {
-			for (int k = 0; k < 3; k++) mom[k] += ptr[i].v[k] * ptr[i].m;
-			mass += ptr[i].m;
-		}
-	for (long i = 0; i < sys->npart; i++)
-		if (ptr[i].type == type)
-			for (int k = 0; k < 3; k++) ptr[i].v[k] -= mom[k] / mass;
-}
-
 void sep_set_x0(seppart *ptr, int npart)
 {
 	rt_ctx *c = rt_get(ptr, __func__);
 	rt_need_host(c);
+	c->x0_valid = 0;
 	for (int i = 0; i < npart; i++)
 		for (int k = 0; k < 3; k++) ptr[i].x0[k] = ptr[i].x[k];
 }

@@ -4,8 +4,8 @@
  *
  * Control flow, sampling intervals, normalisations and output files follow
  * the reference (source/sepsampler.c:4-242 dispatch, :280-351 sacf,
- * :471-641 msd, :658-714 vacf, :725-818 msacf, :1110-1410 mgh, :1757-1825
- * mvacf).  The stress autocorrelations work on the sepret values the host
+ * :471-641 msd, :658-714 vacf, :725-818 msacf, :1110-1410 mgh, :1418-1510
+ * profs, :1757-1825 mvacf).  The stress autocorrelations work on the sepret values the host
  * already has (the molecular one through sep_mol_pressure_tensor); vacf,
  * msd, mvacf and mgh keep their particle data on the GPU (dev_sampler.cu,
  * dev_molsampler.cu) and only their per-sample or per-block sums come back
@@ -47,6 +47,14 @@ struct sepmsd {
 	double *out;           /* 2 + nk, scratch */
 	sepdev_msd *dev;
 	rt_ctx *ctx;
+};
+
+struct sepprofs {
+	int lvec, isample, dir, dirvel;
+	long nsample;
+	char type;
+	double *momc, *svel, *dens, *temp;   /* lvec each */
+	double *hist;                        /* 4 lvec, scratch */
 };
 
 struct sepmsacf {
@@ -222,6 +230,25 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 			sptr->mgh = p;
 			sptr->flag_mgh = 1;
 		}
+	} else if (strcmp(sampler, "profs") == 0) {
+		if (sptr->flag_profs != 1) {
+			const char type = (char)va_arg(args, int);
+			const int isample = va_arg(args, int);
+			struct sepprofs *p = xcalloc(1, sizeof *p);
+			p->lvec = lvec;
+			p->isample = isample;
+			p->type = type;
+			/* the reference's defaults: profiles along z of v_x */
+			p->dir = 2;
+			p->dirvel = 0;
+			p->momc = xcalloc(lvec, sizeof(double));
+			p->svel = xcalloc(lvec, sizeof(double));
+			p->dens = xcalloc(lvec, sizeof(double));
+			p->temp = xcalloc(lvec, sizeof(double));
+			p->hist = xcalloc(4 * (size_t)lvec, sizeof(double));
+			sptr->profs = p;
+			sptr->flag_profs = 1;
+		}
 	} else if (strcmp(sampler, "mvacf") == 0) {
 		if (sptr->flag_mvacf != 1) {
 			const double tsample = va_arg(args, double);
@@ -236,7 +263,7 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 	} else {
 		va_end(args);
 		sep_error("%s: sampler %s is not provided by this GPU implementation "
-			  "(available: sacf, vacf, msd, msacf, mvacf, mgh)", __func__, sampler);
+			  "(available: sacf, vacf, msd, msacf, mvacf, mgh, profs)", __func__, sampler);
 	}
 	va_end(args);
 }
@@ -517,6 +544,46 @@ static void mgh_sample(struct sepmgh *g, seppart *pptr, sepmol *mols, sepsys sys
 	}
 }
 
+/* ---- profs: source/sepsampler.c:1453-1510 ----
+ * The bin of a particle is floor(x_dir / dl), the last bin for a coordinate
+ * that rounds to L_dir. */
+static void profs_sample(struct sepprofs *p, seppart *pptr, sepsys sys)
+{
+	rt_ctx *c = sampler_ctx(pptr, &sys);
+	const int lv = p->lvec, dir = p->dir;
+	const double dl = sys.length[dir] / lv;
+	double dV;
+	if (dir == 0) dV = dl * sys.length[1] * sys.length[2];
+	else if (dir == 1) dV = sys.length[0] * dl * sys.length[2];
+	else dV = sys.length[0] * sys.length[1] * dl;
+	const int tid = rt_type_id(c, p->type);
+	for (int k = 0; k < 4 * lv; k++) p->hist[k] = 0.0;
+	if (tid >= 0) rt_check(sepdev_profile(c->dev, tid, dir, p->dirvel, lv, p->hist), "profile");
+	p->nsample++;
+	const double idV = 1.0 / dV;
+	for (int n = 0; n < lv; n++) {
+		p->momc[n] += p->hist[4 * n] * idV;
+		p->dens[n] += p->hist[4 * n + 1] * idV;
+		if (p->hist[4 * n + 3] > 0) p->temp[n] += p->hist[4 * n + 2];
+	}
+	if (p->nsample % 100 == 0) {
+		FILE *f = fopen("profs.dat", "w");
+		if (!f) sep_error("%s: Couldn't open file", __func__);
+		for (int n = 0; n < lv; n++) {
+			const double insample = 1.0 / p->nsample;
+			double temp_fac = 0;
+			if (p->dens[n] > 0.0) {
+				p->svel[n] = p->momc[n] / p->dens[n];
+				temp_fac = 1.0 / (2.0 * dV * p->dens[n]);
+			}
+			const double z = (n + 0.5) * dl;
+			fprintf(f, "%f %f %f %f %f\n", z, p->momc[n] * insample, p->dens[n] * insample,
+				p->temp[n] * temp_fac, p->svel[n]);
+		}
+		fclose(f);
+	}
+}
+
 /* source/sepsampler.c:177-240 (the samplers provided here, in its order) */
 void sep_sample(seppart *pptr, sepsampler *sptr, sepret *ret, sepsys sys, unsigned n)
 {
@@ -525,6 +592,7 @@ void sep_sample(seppart *pptr, sepsampler *sptr, sepret *ret, sepsys sys, unsign
 	if (sptr->flag_msacf == 1 && n % sptr->msacf->isample == 0)
 		msacf_sample(sptr->msacf, pptr, sptr->molptr, ret, sys);
 	if (sptr->flag_mgh == 1 && n % sptr->mgh->isample == 0) mgh_sample(sptr->mgh, pptr, sptr->molptr, sys);
+	if (sptr->flag_profs == 1 && n % sptr->profs->isample == 0) profs_sample(sptr->profs, pptr, sys);
 	if (sptr->flag_mvacf == 1 && n % sptr->mvacf->isample == 0)
 		mvacf_sample(sptr->mvacf, pptr, sptr->molptr, sys);
 	if (sptr->flag_msd == 1) {
@@ -552,6 +620,11 @@ void sep_close_sampler(sepsampler *ptr)
 		free(ptr->vacf->vacf);
 		free(ptr->vacf->block);
 		free(ptr->vacf);
+	}
+	if (ptr->flag_profs == 1) {
+		struct sepprofs *p = ptr->profs;
+		free(p->momc); free(p->svel); free(p->dens); free(p->temp); free(p->hist);
+		free(p);
 	}
 	if (ptr->flag_msacf == 1) {
 		free(ptr->msacf->sacf); free(ptr->msacf->sstress); free(ptr->msacf->astress);

@@ -325,6 +325,7 @@ void rt_host_modified(rt_ctx *c)
 {
 	rt_need_host(c);
 	c->dev_valid = 0;
+	c->x0_valid = 0;
 	c->forces_zero = 0;
 }
 

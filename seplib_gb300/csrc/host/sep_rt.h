@@ -90,6 +90,7 @@ typedef struct rt_ctx {
 	int pass_slot;          /* slot of the pending pair pass, -1 if none */
 	int mv_slot;            /* its molecular sums' slot (molecular tensor on) */
 	int forces_zero;        /* stored forces are logically zero */
+	int x0_valid;           /* the device holds the tether positions x0 */
 	sepdev_bterm bq[3];     /* pending bonded terms, at most one per kind */
 	int nbq;
 	int friction;           /* Nose-Hoover friction pending */

@@ -265,6 +265,19 @@ int sepdev_vacf_create_count(sepdev *d, int lvec, long count, sepdev_vacf **out)
 double *sepdev_vacf_row(sepdev_vacf *v, int index);
 long sepdev_vacf_count(const sepdev_vacf *v);
 
+/* Per-type operations.  _set_x0: tether positions (user order, 3 n
+ * doubles); _tether: f += k (x0 - x) (minimum image) on the particles of
+ * type id tid; _type_sums: out[0..2] sum m v, out[3] sum m, out[4] sum m v^2,
+ * out[5] count over the type; _type_scale: v = v fact - shift on the type;
+ * _profile: lvec bins of L_dir / lvec along dir over the type, out[4 b + q]
+ * = sum m v[dirvel], sum m, sum m v^2 over the other two components, count
+ * (4 lvec doubles; lvec <= 1536). */
+int sepdev_set_x0(sepdev *d, const double *x0);
+int sepdev_tether(sepdev *d, int tid, double k);
+int sepdev_type_sums(sepdev *d, int tid, double *out);
+int sepdev_type_scale(sepdev *d, int tid, double fact, const double *shift);
+int sepdev_profile(sepdev *d, int tid, int dir, int dirvel, int lvec, double *out);
+
 /* Molecule tables of the molecular samplers: first atom and length of each
  * molecule's chain of consecutive user indices (centres of mass), its atoms
  * as CSR over user indices, molecule masses. */

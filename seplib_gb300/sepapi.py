@@ -171,6 +171,11 @@ SIGNATURES = {
     "sep_berendsen": (None, [PART_P, D, D, RET_P, SYS_P]),
     "sep_berendsen_iso": (None, [PART_P, D, D, RET_P, SYS_P]),
     "sep_berendsen_mol": (None, [PART_P, C.POINTER(SepMol), D, D, RET_P, SYS_P]),
+    "sep_set_x0": (None, [PART_P, C.c_int]),
+    "sep_force_x0": (None, [PART_P, C.c_char, C.c_void_p, SYS_P]),
+    "sep_relax_temp": (None, [PART_P, C.c_char, D, D, SYS_P]),
+    "sep_reset_momentum": (None, [PART_P, C.c_char, SYS_P]),
+    "sep_spring_x0": (D, [D, C.c_char]),
 }
 
 

@@ -25,7 +25,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 import oracle  # noqa: E402
 from seplib_gb300 import configs as cfg  # noqa: E402
 from seplib_gb300 import sepapi as A  # noqa: E402
-from sephelp import Handle  # noqa: E402
+from sephelp import Handle, bind_samplers, slit_step  # noqa: E402
 
 
 def ref_lib():
@@ -406,6 +406,79 @@ def dpdmol_small(lib, tmp):
     return d
 
 
+def slit_system(seed=31, ncell=6, rho=0.8, wall=2.0):
+    """fcc lattice with the particles below z = wall typed W (wall), the rest
+    F (fluid), Maxwell-Boltzmann velocities at T = 1"""
+    rng = np.random.default_rng(seed)
+    x, L = cfg.fcc(ncell, rho)
+    n = len(x)
+    types = np.where(x[:, 2] < wall, b"W", b"F").astype("S1")
+    v = cfg.maxwell_boltzmann(n, 1.0, rng)
+    return cfg.System(x=x, v=v, L=np.asarray(L, float), types=types, m=np.ones(n), z=np.zeros(n)), rng
+
+
+def slit_small(lib, tmp):
+    """prgs/prg8.c's per-type operations one at a time (sep_force_x0 with
+    sep_spring_x0, sep_relax_temp, sep_reset_momentum, the profs sampler on a
+    fixed state) and 100 steps of its loop (LJ F-F and W-F, WCA W-W, tethers
+    on W, leap-frog, temperature relaxation of W, profs of F every step)."""
+    s, rng = slit_system()
+    n = s.n
+    d = dict(x=s.x, v=s.v, L=s.L, types=s.types)
+    h = Handle(lib, s, cf=2.5, update=A.SEP_LLIST_NEIGHBLIST, dt=0.005)
+    lib.sep_set_x0(h.atoms, n)
+    xp = np.mod(s.x + rng.normal(0, 0.05, s.x.shape), s.L)
+    h.view["x"] = xp
+    d["xp"] = xp
+    lib.sep_reset_force(h.atoms, C.byref(h.sys))
+    lib.sep_force_x0(h.atoms, b"W", A.fun_ptr(lib, "sep_spring_x0"), C.byref(h.sys))
+    d["f_tether"] = h.view["f"].copy()
+    vp = s.v + rng.normal(0, 0.3, s.v.shape)
+    h.view["v"] = vp
+    d["vp"] = vp
+    lib.sep_relax_temp(h.atoms, b"W", 2.0, 0.01, C.byref(h.sys))
+    d["v_relax_W"] = h.view["v"].copy()
+    lib.sep_reset_momentum(h.atoms, b"F", C.byref(h.sys))
+    d["v_mom_F"] = h.view["v"].copy()
+    # profs of F on this state: 100 samples, the file is written at the 100th
+    bind_samplers(lib)
+    cwd = os.getcwd()
+    run = os.path.join(tmp, "slit")
+    os.makedirs(run, exist_ok=True)
+    os.chdir(run)
+    try:
+        smp = lib.sep_init_sampler()
+        lib.sep_add_sampler(C.byref(smp), b"profs", h.sys, C.c_int(20), C.c_int(ord("F")), C.c_int(1))
+        for k in range(100):
+            lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, k)
+        lib.sep_close_sampler(C.byref(smp))
+        d["profs_static"] = np.loadtxt("profs.dat")
+        os.remove("profs.dat")
+    finally:
+        os.chdir(cwd)
+    h.close()
+    # the prg8 loop from the unperturbed state
+    s, _ = slit_system()
+    h = Handle(lib, s, cf=2.5, update=A.SEP_LLIST_NEIGHBLIST, dt=0.005)
+    lib.sep_set_x0(h.atoms, n)
+    os.chdir(run)
+    try:
+        smp = lib.sep_init_sampler()
+        lib.sep_add_sampler(C.byref(smp), b"profs", h.sys, C.c_int(20), C.c_int(ord("F")), C.c_int(1))
+        tr = []
+        for k in range(100):
+            slit_step(lib, h)
+            lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, k)
+            tr.append([h.ret.epot, h.ret.ekin])
+        lib.sep_close_sampler(C.byref(smp))
+        d["profs_run"] = np.loadtxt("profs.dat")
+    finally:
+        os.chdir(cwd)
+    d["run_trace"], d["run_x"], d["run_v"] = np.array(tr), h.view["x"].copy(), h.view["v"].copy()
+    h.close()
+    return d
+
+
 def box_ops(lib):
     """sep_compress_box / _dir / _dir_length and sep_berendsen / _iso one at
     a time, then a Berendsen run (prgs/prg7.c) and a compression run
@@ -524,7 +597,8 @@ def main(only=()):
                          ("molp_small", lambda: molp_small(lib, tmp)),
                          ("molsampler_small", lambda: molsampler_small(lib, tmp)),
                          ("molbaro_small", lambda: molbaro_small(lib, tmp)),
-                         ("dpdmol_small", lambda: dpdmol_small(lib, tmp))):
+                         ("dpdmol_small", lambda: dpdmol_small(lib, tmp)),
+                         ("slit_small", lambda: slit_small(lib, tmp))):
             if only and name not in only:
                 continue
             d = fn()

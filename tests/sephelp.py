@@ -158,3 +158,18 @@ def water_mol_run(lib, s, top, nsteps, lvec, tsample, nk, unsafe, record_every, 
     if record_mols:
         out.update(mol_s=np.array(mol_s), mol_w=np.array(mol_w), mol_pel=np.array(mol_pel))
     return out
+
+
+def slit_step(lib, h):
+    """one step of the prgs/prg8.c loop: LJ F-F and W-F (rc 2.5), WCA W-W,
+    tethers of W to x0, leap-frog, temperature relaxation of W towards
+    T = 1.0 with tau 0.01"""
+    lib.sep_reset_retval(C.byref(h.ret))
+    lib.sep_reset_force(h.atoms, C.byref(h.sys))
+    lib.sep_force_pairs(h.atoms, b"FF", 2.5, h.fun(), C.byref(h.sys), C.byref(h.ret), A.SEP_ALL)
+    lib.sep_force_pairs(h.atoms, b"WF", 2.5, h.fun(), C.byref(h.sys), C.byref(h.ret), A.SEP_ALL)
+    lib.sep_force_pairs(h.atoms, b"WW", 2 ** (1 / 6), h.fun("sep_wca"), C.byref(h.sys), C.byref(h.ret),
+                        A.SEP_ALL)
+    lib.sep_force_x0(h.atoms, b"W", A.fun_ptr(lib, "sep_spring_x0"), C.byref(h.sys))
+    lib.sep_leapfrog(h.atoms, C.byref(h.sys), C.byref(h.ret))
+    lib.sep_relax_temp(h.atoms, b"W", 1.0, 0.01, C.byref(h.sys))

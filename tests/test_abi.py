@@ -50,7 +50,7 @@ def test_struct_layout(tmp_path):
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_PRGS), reason="reference programs not present")
-@pytest.mark.parametrize("prg", ["prg0.c", "prg1.c", "prg2.c", "prg3.c", "prg4.c", "prg6.c", "prg7.c", "prg9.c"])
+@pytest.mark.parametrize("prg", ["prg0.c", "prg1.c", "prg2.c", "prg3.c", "prg4.c", "prg6.c", "prg7.c", "prg8.c", "prg9.c"])
 @pytest.mark.parametrize("headers", ["ours", "reference"])
 def test_reference_programs_link_unchanged(lib, tmp_path, prg, headers):
     """prgs/prg0.c, prg1.c (with the vacf, sacf and msd samplers), prg4.c,
