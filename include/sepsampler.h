@@ -11,11 +11,12 @@
  * molecular "msacf" (molecular stress autocorrelation), "mvacf" (centre-of-
  * mass velocity autocorrelation) and "mgh" (molecular generalised
  * hydrodynamics: momentum, density, energy, spin and dipole correlations
- * per wavevector along y) and "profs" (density, momentum and temperature
- * profiles of one type along z).  They write the reference's files
- * (sacf.dat, vacf.dat, msd.dat, msd-gaussparam.dat, msd-incoherent.dat,
- * msd-k.dat, msacf.dat, mvacf.dat, mgh-*.dat, profs.dat) in the same
- * formats.  The particle data
+ * per wavevector along y), "profs" (density, momentum and temperature
+ * profiles of one type along z) and "radial" (pair distances histogrammed
+ * per type combination).  They write the reference's files (sacf.dat,
+ * vacf.dat, msd.dat, msd-gaussparam.dat, msd-incoherent.dat, msd-k.dat,
+ * msacf.dat, mvacf.dat, mgh-*.dat, profs.dat, radial.dat,
+ * radial_info.dat) in the same formats.  The particle data
  * a sample needs stays on the GPU: vacf and mvacf keep their window of
  * velocities in device memory, msd and mgh reduce on the device, so sampling
  * costs no download of the particle arrays.  Unlike the reference, mgh does
@@ -81,7 +82,8 @@ sepsampler sep_init_sampler(void);
  * particle type (char); "mgh": lvec samples over a time span (double),
  * number of wave vectors (int), safe (int; 0 also evaluates the angular
  * velocities); "profs": lvec bins, particle type (char), sampling interval
- * in steps (int).  The molecular samplers need sep_add_mol_sampler first. */
+ * in steps (int); "radial": lvec bins, sampling interval in steps (int),
+ * the types (char *, 1 to 7).  The molecular samplers need sep_add_mol_sampler first. */
 void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec, ...);
 
 /* Reference include/sepsampler.h:281. */

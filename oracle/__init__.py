@@ -776,3 +776,41 @@ class Profs:
             tfac = np.where(pos, 1.0 / (2.0 * dV * np.where(pos, self.dens, 1.0)), 0.0)
             self.out = np.column_stack([(np.arange(lv) + 0.5) * dl, self.momc / self.nsample,
                                         self.dens / self.nsample, self.temp * tfac, self.svel])
+
+
+def radial_counts(x, types, L, lvec, typestr):
+    """one sample of the radial sampler (source/sepsampler.c:396-434): for
+    every pair i < j, r from the differences wrapped by L_x on every axis
+    (the squares summed in order), bin floor(r / dg), dg = L_x / (2 lvec);
+    one count per matching type combination (t1 <= t2 in the string's
+    order).  Returns (lvec, ncomb) integer counts."""
+    x = np.asarray(x, float)
+    lb = float(np.asarray(L, float)[0])
+    dg = 0.5 * lb / lvec
+    ty = [bytes([c]) for c in typestr]
+    combos = [(a, b) for i, a in enumerate(ty) for b in ty[i:]]
+    tarr = np.asarray(types)
+    hist = np.zeros((lvec, len(combos)), np.int64)
+    n = len(x)
+    for i in range(n - 1):
+        rv = x[i] - x[i + 1:]
+        rv = np.where(rv > 0.5 * lb, rv - lb, np.where(rv < -0.5 * lb, rv + lb, rv))
+        r2 = rv[:, 0] * rv[:, 0]
+        r2 = r2 + rv[:, 1] * rv[:, 1]
+        r2 = r2 + rv[:, 2] * rv[:, 2]
+        idx = (np.sqrt(r2) / dg).astype(np.int64)
+        ok = idx < lvec
+        tj = tarr[i + 1:]
+        for c, (a, b) in enumerate(combos):
+            m = ok & (((tarr[i] == a) & (tj == b)) | ((tarr[i] == b) & (tj == a)))
+            np.add.at(hist[:, c], idx[m], 1)
+    return hist
+
+
+def radial_file(hist_sum, nsample, L, lvec):
+    """radial.dat's columns from the accumulated counts (source/sepsampler.c:
+    438-457): r = (i + 1/2) dg, counts / ((r_{i+1}^3 - r_i^3) nsample)"""
+    dg = 0.5 * float(np.asarray(L, float)[0]) / lvec
+    i = np.arange(lvec)
+    fac = 1.0 / ((((i + 1) * dg) ** 3.0 - (i * dg) ** 3.0) * nsample)
+    return np.column_stack([(i + 0.5) * dg, hist_sum * fac[:, None]])

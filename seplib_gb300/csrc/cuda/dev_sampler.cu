@@ -283,3 +283,150 @@ extern "C" int sepdev_msd_sample(sepdev *d, sepdev_msd *m, int type_id, double *
 	CK(cudaStreamSynchronize(d->st));
 	return SEPDEV_OK;
 }
+
+// ---- radial distribution (source/sepsampler.c:396-461) -------------------------
+//
+// Every pair i < j within half the box: bin floor(r / dg), one count for
+// each requested type combination the pair matches.  The bin is found in
+// FP32 from the exact fixed-point differences; a pair whose r / dg lies
+// within RAD_EPS of a bin edge is recomputed with the reference's own FP64
+// operations (positions as doubles, sep_Wrap by L_x on every axis, the
+// squares summed in order, correctly rounded sqrt and division), so the
+// counts are the reference's exactly.  A non-cubic box takes the FP64 path
+// for every pair.  Blocks keep 32-bit counts in shared memory and add them
+// to the 64-bit global histogram once.
+
+#define RAD_B 256
+#define RAD_G 16           // j tiles per block
+#define RAD_EPS 1e-3f
+
+struct RadArgs {
+	long n;
+	int lvec, ncomb, nt;
+	double L, dg;          // the reference's lbox = L_x and bin width
+	float fsx, fsy, fsz;   // L_k / 2^32
+	float idg;             // 1 / dg
+	int cubic;
+	const int4 *pos;
+	const uint4 *xlo;
+	const unsigned *mask;  // [type i][type j] -> bit c: combination c matches
+	unsigned long long *hist;   // [lvec][ncomb]
+};
+
+__device__ __forceinline__ int rad_bin64(const RadArgs &a, int4 pi, uint4 li, int4 pj, uint4 lj, double Ly, double Lz)
+{
+	const unsigned hi[3] = {(unsigned)pi.x, (unsigned)pi.y, (unsigned)pi.z};
+	const unsigned lo[3] = {li.x, li.y, li.z};
+	const unsigned hj[3] = {(unsigned)pj.x, (unsigned)pj.y, (unsigned)pj.z};
+	const unsigned lj_[3] = {lj.x, lj.y, lj.z};
+	const double Lk[3] = {a.L, Ly, Lz};
+	double r2 = 0.0;
+	for (int k = 0; k < 3; k++) {
+		double rv = __dsub_rn(from_fixed_dev(hi[k], lo[k], Lk[k]), from_fixed_dev(hj[k], lj_[k], Lk[k]));
+		if (rv > 0.5 * a.L) rv = __dsub_rn(rv, a.L);
+		else if (rv < -0.5 * a.L) rv = __dadd_rn(rv, a.L);
+		r2 = __dadd_rn(r2, __dmul_rn(rv, rv));
+	}
+	return (int)__ddiv_rn(__dsqrt_rn(r2), a.dg);
+}
+
+__global__ void __launch_bounds__(RAD_B) k_radial(RadArgs a, double Ly, double Lz)
+{
+	extern __shared__ unsigned char rsh[];
+	int4 *sp = (int4 *)rsh;
+	uint4 *sl = (uint4 *)(rsh + sizeof(int4) * RAD_B);
+	unsigned *h = (unsigned *)(rsh + (sizeof(int4) + sizeof(uint4)) * RAD_B);
+	const int nh = a.lvec * a.ncomb;
+	for (int k = threadIdx.x; k < nh; k += RAD_B) h[k] = 0u;
+	const int nb = (int)((a.n + RAD_B - 1) / RAD_B);
+	const int bi = blockIdx.x;
+	const int bj0 = max(bi, (int)blockIdx.y * RAD_G), bj1 = min(nb, ((int)blockIdx.y + 1) * RAD_G);
+	const long i = (long)bi * RAD_B + threadIdx.x;
+	const bool act = i < a.n;
+	int4 pi = make_int4(0, 0, 0, 0);
+	uint4 li = make_uint4(0, 0, 0, 0);
+	if (act) { pi = a.pos[i]; li = a.xlo[i]; }
+	const float lim = (float)a.lvec;
+	__syncthreads();
+	for (int bj = bj0; bj < bj1; bj++) {
+		const long j0 = (long)bj * RAD_B;
+		const long jl = j0 + threadIdx.x;
+		if (jl < a.n) { sp[threadIdx.x] = a.pos[jl]; sl[threadIdx.x] = a.xlo[jl]; }
+		__syncthreads();
+		const int cnt = (int)min((long)RAD_B, a.n - j0);
+		if (act) {
+			const int k0 = bj == bi ? threadIdx.x + 1 : 0;
+			for (int k = k0; k < cnt; k++) {
+				const int4 pj = sp[k];
+				int bin;
+				if (a.cubic) {
+					const float dx = (float)(int)((unsigned)pi.x - (unsigned)pj.x) * a.fsx;
+					const float dy = (float)(int)((unsigned)pi.y - (unsigned)pj.y) * a.fsy;
+					const float dz = (float)(int)((unsigned)pi.z - (unsigned)pj.z) * a.fsz;
+					const float q = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) * a.idg;
+					if (q > lim + 1.0f) continue;
+					const float fl = floorf(q);
+					if (q - fl < RAD_EPS || fl + 1.0f - q < RAD_EPS) bin = rad_bin64(a, pi, li, pj, sl[k], Ly, Lz);
+					else bin = (int)fl;
+				} else {
+					bin = rad_bin64(a, pi, li, pj, sl[k], Ly, Lz);
+				}
+				if (bin >= a.lvec) continue;
+				unsigned m = a.mask[pi.w * a.nt + pj.w];
+				while (m) {
+					const int c = __ffs(m) - 1;
+					m &= m - 1;
+					atomicAdd(&h[bin * a.ncomb + c], 1u);
+				}
+			}
+		}
+		__syncthreads();
+	}
+	for (int k = threadIdx.x; k < nh; k += RAD_B)
+		if (h[k]) atomicAdd(&a.hist[k], (unsigned long long)h[k]);
+}
+
+// out (host, lvec x ncomb): the counts of one sample; mask[ti * nt + tj]
+// (nt = the device's type count) holds the bits of the combinations the
+// pair of type ids matches
+extern "C" int sepdev_radial(sepdev *d, int lvec, int ncomb, int nt, const unsigned *mask, double *out)
+{
+	if (lvec < 1 || ncomb < 1 || ncomb > 32 || nt < 1 || nt > SEPDEV_MAXTYPES) return SEPDEV_EINVAL;
+	const size_t hbytes = sizeof(unsigned) * lvec * ncomb;
+	const size_t shm = (sizeof(int4) + sizeof(uint4)) * RAD_B + hbytes;
+	if (shm > 200 * 1024) return SEPDEV_EINVAL;
+	unsigned long long *hist = NULL;
+	unsigned *dmask = NULL;
+	cudaError_t e = cudaMalloc((void **)&hist, sizeof(unsigned long long) * lvec * ncomb);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&dmask, sizeof(unsigned) * nt * nt);
+	if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, sizeof(unsigned long long) * lvec * ncomb, d->st);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(dmask, mask, sizeof(unsigned) * nt * nt, cudaMemcpyHostToDevice, d->st);
+	if (e == cudaSuccess && shm > 48 * 1024)
+		e = cudaFuncSetAttribute(k_radial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+	if (e != cudaSuccess) {
+		cudaFree(hist); cudaFree(dmask);
+		sepdev_set_error("radial distribution", e);
+		return SEPDEV_ECUDA;
+	}
+	RadArgs a;
+	a.n = d->n; a.lvec = lvec; a.ncomb = ncomb; a.nt = nt;
+	a.L = d->L[0];
+	a.dg = 0.5 * d->L[0] / lvec;
+	a.fsx = d->fscale[0]; a.fsy = d->fscale[1]; a.fsz = d->fscale[2];
+	a.idg = (float)(1.0 / a.dg);
+	a.cubic = d->L[0] == d->L[1] && d->L[1] == d->L[2];
+	a.pos = d->pos[d->cur]; a.xlo = d->xlo;
+	a.mask = dmask; a.hist = hist;
+	const int nb = grid_for(d->n, RAD_B);
+	k_radial<<<dim3(nb, (nb + RAD_G - 1) / RAD_G), RAD_B, shm, d->st>>>(a, d->L[1], d->L[2]);
+	CKL(d);
+	unsigned long long *hh = (unsigned long long *)malloc(sizeof(unsigned long long) * lvec * ncomb);
+	if (!hh) { cudaFree(hist); cudaFree(dmask); return SEPDEV_ENOMEM; }
+	e = cudaMemcpyAsync(hh, hist, sizeof(unsigned long long) * lvec * ncomb, cudaMemcpyDeviceToHost, d->st);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(d->st);
+	cudaFree(hist); cudaFree(dmask);
+	if (e != cudaSuccess) { free(hh); sepdev_set_error("radial distribution", e); return SEPDEV_ECUDA; }
+	for (int k = 0; k < lvec * ncomb; k++) out[k] = (double)hh[k];
+	free(hh);
+	return SEPDEV_OK;
+}

@@ -4,8 +4,8 @@
  *
  * Control flow, sampling intervals, normalisations and output files follow
  * the reference (source/sepsampler.c:4-242 dispatch, :280-351 sacf,
- * :471-641 msd, :658-714 vacf, :725-818 msacf, :1110-1410 mgh, :1418-1510
- * profs, :1757-1825 mvacf).  The stress autocorrelations work on the sepret values the host
+ * :361-470 radial, :471-641 msd, :658-714 vacf, :725-818 msacf, :1110-1410
+ * mgh, :1418-1510 profs, :1757-1825 mvacf).  The stress autocorrelations work on the sepret values the host
  * already has (the molecular one through sep_mol_pressure_tensor); vacf,
  * msd, mvacf and mgh keep their particle data on the GPU (dev_sampler.cu,
  * dev_molsampler.cu) and only their per-sample or per-block sums come back
@@ -47,6 +47,15 @@ struct sepmsd {
 	double *out;           /* 2 + nk, scratch */
 	sepdev_msd *dev;
 	rt_ctx *ctx;
+};
+
+struct sepradial {
+	int lvec, isample, ntypes, ncomb;
+	long nsample;
+	char types[8];
+	double *hist;          /* lvec x ncomb accumulated counts */
+	double *out;           /* lvec x ncomb, scratch */
+	unsigned *mask;        /* [SEPDEV_MAXTYPES]^2, scratch */
 };
 
 struct sepprofs {
@@ -249,6 +258,30 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 			sptr->profs = p;
 			sptr->flag_profs = 1;
 		}
+	} else if (strcmp(sampler, "radial") == 0) {
+		if (sptr->flag_radial != 1) {
+			const int isample = va_arg(args, int);
+			const char *t = va_arg(args, char *);
+			struct sepradial *p = xcalloc(1, sizeof *p);
+			p->lvec = lvec;
+			p->isample = isample;
+			p->ntypes = (int)strlen(t);
+			if (p->ntypes < 1 || p->ntypes > 7)
+				sep_error("%s: radial takes 1 to 7 types (got \"%s\")", __func__, t);
+			memcpy(p->types, t, p->ntypes);
+			for (int k = 1; k <= p->ntypes; k++) p->ncomb += k;
+			p->hist = xcalloc((size_t)lvec * p->ncomb, sizeof(double));
+			p->out = xcalloc((size_t)lvec * p->ncomb, sizeof(double));
+			p->mask = xcalloc(SEPDEV_MAXTYPES * SEPDEV_MAXTYPES, sizeof(unsigned));
+			FILE *f = fopen("radial_info.dat", "w");
+			if (!f) sep_error("%s: Couldn't open file", __func__);
+			fprintf(f, "Pairs in radial.dat columns are\n");
+			for (int a = 0; a < p->ntypes; a++)
+				for (int b = a; b < p->ntypes; b++) fprintf(f, "%c%c  ", p->types[a], p->types[b]);
+			fclose(f);
+			sptr->radial = p;
+			sptr->flag_radial = 1;
+		}
 	} else if (strcmp(sampler, "mvacf") == 0) {
 		if (sptr->flag_mvacf != 1) {
 			const double tsample = va_arg(args, double);
@@ -263,7 +296,7 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 	} else {
 		va_end(args);
 		sep_error("%s: sampler %s is not provided by this GPU implementation "
-			  "(available: sacf, vacf, msd, msacf, mvacf, mgh, profs)", __func__, sampler);
+			  "(available: sacf, vacf, msd, msacf, mvacf, mgh, profs, radial)", __func__, sampler);
 	}
 	va_end(args);
 }
@@ -584,6 +617,40 @@ static void profs_sample(struct sepprofs *p, seppart *pptr, sepsys sys)
 	}
 }
 
+/* ---- radial: source/sepsampler.c:396-461 ---- */
+static void radial_sample(struct sepradial *p, seppart *pptr, sepsys sys)
+{
+	rt_ctx *c = sampler_ctx(pptr, &sys);
+	const int nt = c->ntypes > 0 ? c->ntypes : 1;
+	for (int a = 0; a < nt; a++)
+		for (int b = 0; b < nt; b++) {
+			unsigned m = 0;
+			int cc = 0;
+			for (int t1 = 0; t1 < p->ntypes; t1++)
+				for (int t2 = t1; t2 < p->ntypes; t2++, cc++)
+					if ((c->tchar[a] == p->types[t1] && c->tchar[b] == p->types[t2]) ||
+					    (c->tchar[a] == p->types[t2] && c->tchar[b] == p->types[t1]))
+						m |= 1u << cc;
+			p->mask[a * nt + b] = m;
+		}
+	rt_check(sepdev_radial(c->dev, p->lvec, p->ncomb, nt, p->mask, p->out), "radial distribution");
+	for (int k = 0; k < p->lvec * p->ncomb; k++) p->hist[k] += p->out[k];
+	p->nsample++;
+	const double dg = 0.5 * sys.length[0] / p->lvec;
+	FILE *f = fopen("radial.dat", "w");
+	if (!f) sep_error("%s: Couldn't open file", __func__);
+	for (int i = 0; i < p->lvec; i++) {
+		const double vi = pow(i * dg, 3.0), vii = pow((i + 1) * dg, 3.0);
+		fprintf(f, "%f ", (i + 0.5) * dg);
+		for (int n = 0; n < p->ncomb; n++) {
+			const double fac = 1.0 / ((vii - vi) * p->nsample);
+			fprintf(f, "%f ", p->hist[(size_t)i * p->ncomb + n] * fac);
+		}
+		fprintf(f, "\n");
+	}
+	fclose(f);
+}
+
 /* source/sepsampler.c:177-240 (the samplers provided here, in its order) */
 void sep_sample(seppart *pptr, sepsampler *sptr, sepret *ret, sepsys sys, unsigned n)
 {
@@ -595,6 +662,7 @@ void sep_sample(seppart *pptr, sepsampler *sptr, sepret *ret, sepsys sys, unsign
 	if (sptr->flag_profs == 1 && n % sptr->profs->isample == 0) profs_sample(sptr->profs, pptr, sys);
 	if (sptr->flag_mvacf == 1 && n % sptr->mvacf->isample == 0)
 		mvacf_sample(sptr->mvacf, pptr, sptr->molptr, sys);
+	if (sptr->flag_radial == 1 && n % sptr->radial->isample == 0) radial_sample(sptr->radial, pptr, sys);
 	if (sptr->flag_msd == 1) {
 		struct sepmsd *m = sptr->msd;
 		/* crossings: counted exactly on the device at every step */
@@ -620,6 +688,10 @@ void sep_close_sampler(sepsampler *ptr)
 		free(ptr->vacf->vacf);
 		free(ptr->vacf->block);
 		free(ptr->vacf);
+	}
+	if (ptr->flag_radial == 1) {
+		free(ptr->radial->hist); free(ptr->radial->out); free(ptr->radial->mask);
+		free(ptr->radial);
 	}
 	if (ptr->flag_profs == 1) {
 		struct sepprofs *p = ptr->profs;

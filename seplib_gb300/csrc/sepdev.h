@@ -260,6 +260,10 @@ int sepdev_vacf_create(sepdev *d, int lvec, sepdev_vacf **out);
 void sepdev_vacf_destroy(sepdev_vacf *v);
 int sepdev_vacf_store(sepdev *d, sepdev_vacf *v, int index);
 int sepdev_vacf_block(sepdev *d, sepdev_vacf *v, double *out);
+/* radial distribution: out[b * ncomb + c] = the number of pairs i < j with
+ * floor(r / dg) = b (dg = L_x / (2 lvec)) whose type ids (ti, tj) have bit c
+ * set in mask[ti * nt + tj] (ncomb <= 32, lvec * ncomb <= 49152) */
+int sepdev_radial(sepdev *d, int lvec, int ncomb, int nt, const unsigned *mask, double *out);
 /* a ring of count values per sample (mvacf: one per molecule) */
 int sepdev_vacf_create_count(sepdev *d, int lvec, long count, sepdev_vacf **out);
 double *sepdev_vacf_row(sepdev_vacf *v, int index);

@@ -479,6 +479,40 @@ def slit_small(lib, tmp):
     return d
 
 
+def radial_small(lib, tmp):
+    """the radial sampler (types "AB", 50 bins) on an LJ liquid of 500
+    particles with random A/B types: three samples, 20 steps apart; the
+    states sampled and the file after the last one"""
+    rng = np.random.default_rng(41)
+    x, L = cfg.fcc(5, 0.8)
+    n = len(x)
+    types = np.where(rng.random(n) < 0.3, b"B", b"A").astype("S1")
+    s = cfg.System(x=x, v=cfg.maxwell_boltzmann(n, 1.0, rng), L=np.asarray(L, float), types=types,
+                   m=np.ones(n), z=np.zeros(n))
+    h = Handle(lib, s, cf=2.5, dt=0.005)
+    bind_samplers(lib)
+    cwd = os.getcwd()
+    run = os.path.join(tmp, "radial")
+    os.makedirs(run, exist_ok=True)
+    os.chdir(run)
+    xs = []
+    try:
+        smp = lib.sep_init_sampler()
+        lib.sep_add_sampler(C.byref(smp), b"radial", h.sys, C.c_int(50), C.c_int(20), C.c_char_p(b"AB"))
+        for k in range(41):
+            h.step(types=b"AB", nh=(1.0, 10.0))
+            lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, k)
+            if k % 20 == 0:
+                xs.append(h.view["x"].copy())
+        lib.sep_close_sampler(C.byref(smp))
+        d = dict(xs=np.array(xs), L=s.L, types=types, radial=np.loadtxt("radial.dat"),
+                 info=open("radial_info.dat").read())
+    finally:
+        os.chdir(cwd)
+    h.close()
+    return d
+
+
 def box_ops(lib):
     """sep_compress_box / _dir / _dir_length and sep_berendsen / _iso one at
     a time, then a Berendsen run (prgs/prg7.c) and a compression run
@@ -598,7 +632,8 @@ def main(only=()):
                          ("molsampler_small", lambda: molsampler_small(lib, tmp)),
                          ("molbaro_small", lambda: molbaro_small(lib, tmp)),
                          ("dpdmol_small", lambda: dpdmol_small(lib, tmp)),
-                         ("slit_small", lambda: slit_small(lib, tmp))):
+                         ("slit_small", lambda: slit_small(lib, tmp)),
+                         ("radial_small", lambda: radial_small(lib, tmp))):
             if only and name not in only:
                 continue
             d = fn()
