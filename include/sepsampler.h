@@ -11,11 +11,12 @@
  * molecular "msacf" (molecular stress autocorrelation), "mvacf" (centre-of-
  * mass velocity autocorrelation) and "mgh" (molecular generalised
  * hydrodynamics: momentum, density, energy, spin and dipole correlations
- * per wavevector along y), "profs" (density, momentum and temperature
+ * per wavevector along y), "gh" (the atomic counterpart: density,
+ * momentum and energy correlations along y), "profs" (density, momentum and temperature
  * profiles of one type along z) and "radial" (pair distances histogrammed
  * per type combination).  They write the reference's files (sacf.dat,
  * vacf.dat, msd.dat, msd-gaussparam.dat, msd-incoherent.dat, msd-k.dat,
- * msacf.dat, mvacf.dat, mgh-*.dat, profs.dat, radial.dat,
+ * msacf.dat, mvacf.dat, gh-*.dat, mgh-*.dat, profs.dat, radial.dat,
  * radial_info.dat) in the same formats.  The particle data
  * a sample needs stays on the GPU: vacf and mvacf keep their window of
  * velocities in device memory, msd and mgh reduce on the device, so sampling
@@ -77,7 +78,8 @@ typedef struct {
 sepsampler sep_init_sampler(void);
 
 /* Reference include/sepsampler.h:275: "sacf", "vacf", "msacf", "mvacf":
- * lvec samples over a time span (double); "msd": lvec samples (0:
+ * lvec samples over a time span (double); "gh": lvec samples over a time
+ * span (double), number of wave vectors (int); "msd": lvec samples (0:
  * log-spaced) over a time span (double), number of wave vectors (int),
  * particle type (char); "mgh": lvec samples over a time span (double),
  * number of wave vectors (int), safe (int; 0 also evaluates the angular

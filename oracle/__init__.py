@@ -814,3 +814,66 @@ def radial_file(hist_sum, nsample, L, lvec):
     i = np.arange(lvec)
     fac = 1.0 / ((((i + 1) * dg) ** 3.0 - (i * dg) ** 3.0) * nsample)
     return np.column_stack([(i + 0.5) * dg, hist_sum * fac[:, None]])
+
+
+class GH:
+    """the gh sampler (source/sepsampler.c:957-1105) fed one sample at a
+    time: Fourier sums along y of the unwrapped positions over all particles
+    (mass, transverse and longitudinal momentum, kinetic energy minus its
+    running mean, and the auxiliary m (a_y - i k v_y^2)), auto- and
+    cross-correlations per block; `out` maps each file's name (without the
+    gh- prefix and .dat) to its columns"""
+
+    NAMES = ["rho-acf", "trans-momentum-acf", "long-momentum-acf", "energy-acf", "rho-energy-ccf",
+             "rho-long-momentum-ccf", "energy-long-momentum-ccf", "energy-rho-ccf", "long-momentum-rho-ccf",
+             "long-momentum-energy-ccf", "X-acf"]
+
+    def __init__(self, lvec, dtsample, nk, Ly, volume):
+        self.lvec, self.dts, self.V = lvec, dtsample, volume
+        self.k = 2 * np.pi * np.arange(1, nk + 1) / Ly
+        self.avekin, self.ncalls, self.i, self.nsample = 0.0, 0, 0, 0
+        z = lambda: np.zeros((lvec, nk), complex)
+        self.fk = {q: z() for q in ("tv", "lv", "rho", "e", "X")}
+        self.c = {q: z() for q in self.NAMES}
+        self.out = {}
+
+    def sample(self, xt, v, a, m):
+        m = np.asarray(m, float); v = np.asarray(v, float); a = np.asarray(a, float)
+        ek = 0.5 * (m[:, None] * v * v).sum(1)
+        self.ncalls += 1
+        self.avekin += ek.sum() / (len(m) * self.ncalls)
+        i = self.i
+        for j, kj in enumerate(self.k):
+            e = np.exp(1j * kj * np.asarray(xt, float)[:, 1])
+            self.fk["rho"][i, j] = (m * e).sum()
+            self.fk["tv"][i, j] = (m * v[:, 0] * e).sum()
+            self.fk["lv"][i, j] = (m * v[:, 1] * e).sum()
+            self.fk["e"][i, j] = ((ek - self.avekin) * e).sum()
+            self.fk["X"][i, j] = (m * (a[:, 1] - 1j * kj * v[:, 1] ** 2) * e).sum()
+        self.i += 1
+        if self.i < self.lvec:
+            return
+        f, c, lv = self.fk, self.c, self.lvec
+        cj = np.conj
+        for n in range(lv):
+            p, q = slice(0, lv - n), slice(n, lv)
+            c["trans-momentum-acf"][n] += (cj(f["tv"][p]) * f["tv"][q]).sum(0)
+            c["long-momentum-acf"][n] += (cj(f["lv"][p]) * f["lv"][q]).sum(0)
+            c["rho-acf"][n] += (f["rho"][p] * cj(f["rho"][q])).sum(0)
+            c["energy-acf"][n] += (f["e"][p] * cj(f["e"][q])).sum(0)
+            c["rho-energy-ccf"][n] += (f["rho"][p] * cj(f["e"][q])).sum(0)
+            c["rho-long-momentum-ccf"][n] += (f["rho"][p] * cj(f["lv"][q])).sum(0)
+            c["energy-long-momentum-ccf"][n] += (f["e"][p] * cj(f["lv"][q])).sum(0)
+            c["energy-rho-ccf"][n] += (f["rho"][q] * cj(f["e"][p])).sum(0)
+            c["long-momentum-rho-ccf"][n] += (f["rho"][q] * cj(f["lv"][p])).sum(0)
+            c["long-momentum-energy-ccf"][n] += (f["e"][q] * cj(f["lv"][p])).sum(0)
+            c["X-acf"][n] += (f["X"][p] * cj(f["lv"][q])).sum(0)
+        self.nsample += 1
+        fac = 1.0 / (self.nsample * self.V * (lv - np.arange(lv)))
+        for name, arr in c.items():
+            cols = np.empty((lv, 1 + 2 * len(self.k)))
+            cols[:, 0] = np.arange(lv) * self.dts
+            cols[:, 1::2] = (arr * fac[:, None]).real
+            cols[:, 2::2] = (arr * fac[:, None]).imag
+            self.out[name] = cols
+        self.i = 0

@@ -430,3 +430,102 @@ extern "C" int sepdev_radial(sepdev *d, int lvec, int ncomb, int nt, const unsig
 	free(hh);
 	return SEPDEV_OK;
 }
+
+// ---- atomic generalised hydrodynamics (source/sepsampler.c:957-1098) -----------
+//
+// Per wavevector k_j along y, over all particles, the sums of e^{i k_j y}
+// (y unwrapped by the crossings, as the reference's xtrue) times m, m v_x,
+// m v_y, the kinetic energy, 1, m a_y and m v_y^2; the reference's
+// auxiliary sum m (a_y - i k v_y^2) e^{iky} is formed from the last two on
+// the host.  FP64 with a fixed reduction order; nk x 14 numbers (plus the
+// kinetic energy) come back per sample.
+
+#define GH_N 15
+
+struct sepdev_gh {
+	double *kvec, *part, *sum;
+	int nk, nblk;
+};
+
+__global__ void __launch_bounds__(SB) k_gh_sums(long n, double Ly, const int4 *pos, const uint4 *xlo,
+						 const int4 *cross, const float4 *vhi, const float4 *vlo,
+						 const float4 *frc, const double *kvec, double *part)
+{
+	__shared__ double red[SB / 32][GH_N];
+	const long i = blockIdx.x * (long)SB + threadIdx.x;
+	const int j = blockIdx.y;
+	double t[GH_N];
+	for (int q = 0; q < GH_N; q++) t[q] = 0.0;
+	if (i < n) {
+		const float4 h = vhi[i], l = vlo[i];
+		const double m = (double)h.w;
+		const double v[3] = {(double)h.x + (double)l.x, (double)h.y + (double)l.y, (double)h.z + (double)l.z};
+		double ek = 0.0;
+		for (int k = 0; k < 3; k++) ek += 0.5 * m * v[k] * v[k];
+		const double y = Ly * cross[i].y + from_fixed_dev((unsigned)pos[i].y, xlo[i].y, Ly);
+		double sn, cs;
+		sincos(kvec[j] * y, &sn, &cs);
+		const double ay = (double)frc[i].y / m;
+		const double w[7] = {m, m * v[0], m * v[1], ek, 1.0, m * ay, m * v[1] * v[1]};
+		for (int q = 0; q < 7; q++) {
+			t[2 * q] = w[q] * cs;
+			t[2 * q + 1] = w[q] * sn;
+		}
+		t[14] = ek;
+	}
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	for (int q = 0; q < GH_N; q++) {
+		double x = t[q];
+		for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+		if (lane == 0) red[wid][q] = x;
+	}
+	__syncthreads();
+	if (threadIdx.x < GH_N) {
+		double x = 0.0;
+		for (int w = 0; w < SB / 32; w++) x += red[w][threadIdx.x];
+		part[((long)blockIdx.x * gridDim.y + j) * GH_N + threadIdx.x] = x;
+	}
+}
+
+extern "C" int sepdev_gh_create(sepdev *d, int nk, const double *k, sepdev_gh **out)
+{
+	*out = NULL;
+	if (nk < 1) return SEPDEV_EINVAL;
+	sepdev_gh *g = (sepdev_gh *)calloc(1, sizeof *g);
+	if (!g) return SEPDEV_ENOMEM;
+	g->nk = nk;
+	g->nblk = grid_for(d->n, SB);
+	cudaError_t e = cudaMalloc((void **)&g->kvec, sizeof(double) * nk);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&g->part, sizeof(double) * GH_N * nk * g->nblk);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&g->sum, sizeof(double) * GH_N * nk);
+	if (e == cudaSuccess) e = cudaMemcpy(g->kvec, k, sizeof(double) * nk, cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) {
+		cudaFree(g->kvec); cudaFree(g->part); cudaFree(g->sum); free(g);
+		sepdev_set_error("gh buffers", e);
+		return SEPDEV_ENOMEM;
+	}
+	*out = g;
+	return SEPDEV_OK;
+}
+
+extern "C" void sepdev_gh_destroy(sepdev_gh *g)
+{
+	if (!g) return;
+	cudaFree(g->kvec); cudaFree(g->part); cudaFree(g->sum);
+	free(g);
+}
+
+// out (host, 15 nk): for wavevector j, out[15 j + 2 q + (0 re, 1 im)] with q
+// over (m, m v_x, m v_y, kinetic energy, 1, m a_y, m v_y^2) and
+// out[15 j + 14] the sum of the kinetic energies
+extern "C" int sepdev_gh_sample(sepdev *d, sepdev_gh *g, double *out)
+{
+	k_gh_sums<<<dim3(g->nblk, g->nk), SB, 0, d->st>>>(d->n, d->L[1], d->pos[d->cur], d->xlo, d->cross, d->vhi,
+							  d->vlo, d->frc, g->kvec, g->part);
+	// partials are [block][j][q]: row j * GH_N + q summed over the blocks in order
+	k_rows_sum<<<grid_for(GH_N * g->nk, 128), 128, 0, d->st>>>(GH_N * g->nk, g->nblk, g->part, g->sum, 0);
+	CKL(d);
+	CK(cudaMemcpyAsync(out, g->sum, sizeof(double) * GH_N * g->nk, cudaMemcpyDeviceToHost, d->st));
+	CK(cudaStreamSynchronize(d->st));
+	return SEPDEV_OK;
+}

@@ -4,8 +4,8 @@
  *
  * Control flow, sampling intervals, normalisations and output files follow
  * the reference (source/sepsampler.c:4-242 dispatch, :280-351 sacf,
- * :361-470 radial, :471-641 msd, :658-714 vacf, :725-818 msacf, :1110-1410
- * mgh, :1418-1510 profs, :1757-1825 mvacf).  The stress autocorrelations work on the sepret values the host
+ * :361-470 radial, :471-641 msd, :658-714 vacf, :725-818 msacf, :822-1105
+ * gh, :1110-1410 mgh, :1418-1510 profs, :1757-1825 mvacf).  The stress autocorrelations work on the sepret values the host
  * already has (the molecular one through sep_mol_pressure_tensor); vacf,
  * msd, mvacf and mgh keep their particle data on the GPU (dev_sampler.cu,
  * dev_molsampler.cu) and only their per-sample or per-block sums come back
@@ -46,6 +46,21 @@ struct sepmsd {
 	double *Fs;            /* lvec x nk (real part) */
 	double *out;           /* 2 + nk, scratch */
 	sepdev_msd *dev;
+	rt_ctx *ctx;
+};
+
+/* per-sample Fourier sums of one block and the accumulated correlations;
+ * the reference's conjugate sums (fkm) are the complex conjugates of fk for
+ * the real weights, and its conjugate auxiliary sum is never used */
+struct sepgh {
+	int lvec, isample, i, nk;
+	long nsample, ncalls;
+	double dtsample, avekin;
+	double *k;
+	double complex *fk_tv, *fk_lv, *fk_rho, *fk_e, *fk_X;
+	double complex *c_tv, *c_lv, *c_scatt, *c_e, *c_re, *c_rj, *c_ej, *c_er, *c_jr, *c_je, *c_X;
+	double *out;           /* 15 nk, scratch */
+	sepdev_gh *dev;
 	rt_ctx *ctx;
 };
 
@@ -258,6 +273,31 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 			sptr->profs = p;
 			sptr->flag_profs = 1;
 		}
+	} else if (strcmp(sampler, "gh") == 0) {
+		if (sptr->flag_gh != 1) {
+			const double tsample = va_arg(args, double);
+			const int nk = va_arg(args, int);
+			struct sepgh *p = xcalloc(1, sizeof *p);
+			p->lvec = lvec;
+			p->isample = sample_interval(tsample, lvec, sys.dt, &p->dtsample);
+			p->nk = nk;
+			p->k = xcalloc(nk, sizeof(double));
+			FILE *f = fopen("gh-wavevector.dat", "w");
+			if (!f) sep_error("%s: couldn't open file", __func__);
+			for (int n = 1; n <= nk; n++) {
+				p->k[n - 1] = 2 * SEP_PI * n / sys.length[1];
+				fprintf(f, "%f\n", p->k[n - 1]);
+			}
+			fclose(f);
+			const size_t m = (size_t)lvec * (nk > 0 ? nk : 1);
+			double complex **arr[] = {&p->fk_tv, &p->fk_lv, &p->fk_rho, &p->fk_e, &p->fk_X, &p->c_tv, &p->c_lv,
+						  &p->c_scatt, &p->c_e, &p->c_re, &p->c_rj, &p->c_ej, &p->c_er, &p->c_jr,
+						  &p->c_je, &p->c_X};
+			for (size_t q = 0; q < sizeof arr / sizeof arr[0]; q++) *arr[q] = xcalloc(m, sizeof(double complex));
+			p->out = xcalloc(15 * (size_t)(nk > 0 ? nk : 1), sizeof(double));
+			sptr->gh = p;
+			sptr->flag_gh = 1;
+		}
 	} else if (strcmp(sampler, "radial") == 0) {
 		if (sptr->flag_radial != 1) {
 			const int isample = va_arg(args, int);
@@ -296,7 +336,7 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 	} else {
 		va_end(args);
 		sep_error("%s: sampler %s is not provided by this GPU implementation "
-			  "(available: sacf, vacf, msd, msacf, mvacf, mgh, profs, radial)", __func__, sampler);
+			  "(available: sacf, vacf, msd, msacf, mvacf, gh, mgh, profs, radial)", __func__, sampler);
 	}
 	va_end(args);
 }
@@ -617,6 +657,77 @@ static void profs_sample(struct sepprofs *p, seppart *pptr, sepsys sys)
 	}
 }
 
+/* ---- gh: source/sepsampler.c:957-1105 ---- */
+static void gh_sample(struct sepgh *g, seppart *pptr, sepsys sys)
+{
+	rt_ctx *c = sampler_ctx(pptr, &sys);
+	if (!g->dev || g->ctx != c) {
+		if (g->dev) sepdev_gh_destroy(g->dev);
+		rt_check(sepdev_gh_create(c->dev, g->nk, g->k, &g->dev), "gh sampler");
+		g->ctx = c;
+	}
+	/* the accelerations are those of the last integrator step: the stored
+	 * forces, which calls deferred since then have not touched */
+	rt_check(sepdev_gh_sample(c->dev, g->dev, g->out), "gh sample");
+	const int nk = g->nk;
+	g->ncalls++;
+	g->avekin += g->out[14] / ((double)sys.npart * g->ncalls);
+	const size_t row = (size_t)g->i * nk;
+	for (int j = 0; j < nk; j++) {
+		const double *o = g->out + 15 * j;
+		double complex S[7];
+		for (int q = 0; q < 7; q++) S[q] = o[2 * q] + I * o[2 * q + 1];
+		g->fk_rho[row + j] = S[0];
+		g->fk_tv[row + j] = S[1];
+		g->fk_lv[row + j] = S[2];
+		g->fk_e[row + j] = S[3] - g->avekin * S[4];
+		g->fk_X[row + j] = S[5] - I * g->k[j] * S[6];
+	}
+	g->i++;
+	if (g->i < g->lvec) return;
+	const int lv = g->lvec;
+	for (int k = 0; k < nk; k++)
+		for (int n = 0; n < lv; n++) {
+			const size_t o = (size_t)n * nk + k;
+			for (int m = 0; m < lv - n; m++) {
+				const size_t a = (size_t)m * nk + k, b = (size_t)(n + m) * nk + k;
+				g->c_tv[o] += conj(g->fk_tv[a]) * g->fk_tv[b];
+				g->c_lv[o] += conj(g->fk_lv[a]) * g->fk_lv[b];
+				g->c_scatt[o] += g->fk_rho[a] * conj(g->fk_rho[b]);
+				g->c_e[o] += g->fk_e[a] * conj(g->fk_e[b]);
+				g->c_re[o] += g->fk_rho[a] * conj(g->fk_e[b]);
+				g->c_rj[o] += g->fk_rho[a] * conj(g->fk_lv[b]);
+				g->c_ej[o] += g->fk_e[a] * conj(g->fk_lv[b]);
+				g->c_er[o] += g->fk_rho[b] * conj(g->fk_e[a]);
+				g->c_jr[o] += g->fk_rho[b] * conj(g->fk_lv[a]);
+				g->c_je[o] += g->fk_e[b] * conj(g->fk_lv[a]);
+				g->c_X[o] += g->fk_X[a] * conj(g->fk_lv[b]);
+			}
+		}
+	g->nsample++;
+	static const char *names[11] = {"gh-rho-acf.dat", "gh-trans-momentum-acf.dat", "gh-long-momentum-acf.dat",
+					"gh-energy-acf.dat", "gh-rho-energy-ccf.dat", "gh-rho-long-momentum-ccf.dat",
+					"gh-energy-long-momentum-ccf.dat", "gh-energy-rho-ccf.dat",
+					"gh-long-momentum-rho-ccf.dat", "gh-long-momentum-energy-ccf.dat", "gh-X-acf.dat"};
+	double complex *cs[11] = {g->c_scatt, g->c_tv, g->c_lv, g->c_e, g->c_re, g->c_rj, g->c_ej, g->c_er, g->c_jr,
+				  g->c_je, g->c_X};
+	for (int f = 0; f < 11; f++) {
+		FILE *fp = fopen(names[f], "w");
+		if (!fp) sep_error("%s: Error opening files", __func__);
+		for (int n = 0; n < lv; n++) {
+			fprintf(fp, "%f ", n * g->dtsample);
+			const double fac = 1.0 / (g->nsample * sys.volume * (lv - n));
+			for (int k = 0; k < nk; k++) {
+				const double complex v = cs[f][(size_t)n * nk + k] * fac;
+				fprintf(fp, "%f %f ", creal(v), cimag(v));
+			}
+			fprintf(fp, "\n");
+		}
+		fclose(fp);
+	}
+	g->i = 0;
+}
+
 /* ---- radial: source/sepsampler.c:396-461 ---- */
 static void radial_sample(struct sepradial *p, seppart *pptr, sepsys sys)
 {
@@ -658,6 +769,7 @@ void sep_sample(seppart *pptr, sepsampler *sptr, sepret *ret, sepsys sys, unsign
 	if (sptr->flag_vacf == 1 && n % sptr->vacf->isample == 0) vacf_sample(sptr->vacf, pptr, sys);
 	if (sptr->flag_msacf == 1 && n % sptr->msacf->isample == 0)
 		msacf_sample(sptr->msacf, pptr, sptr->molptr, ret, sys);
+	if (sptr->flag_gh == 1 && n % sptr->gh->isample == 0) gh_sample(sptr->gh, pptr, sys);
 	if (sptr->flag_mgh == 1 && n % sptr->mgh->isample == 0) mgh_sample(sptr->mgh, pptr, sptr->molptr, sys);
 	if (sptr->flag_profs == 1 && n % sptr->profs->isample == 0) profs_sample(sptr->profs, pptr, sys);
 	if (sptr->flag_mvacf == 1 && n % sptr->mvacf->isample == 0)
@@ -688,6 +800,15 @@ void sep_close_sampler(sepsampler *ptr)
 		free(ptr->vacf->vacf);
 		free(ptr->vacf->block);
 		free(ptr->vacf);
+	}
+	if (ptr->flag_gh == 1) {
+		struct sepgh *g = ptr->gh;
+		if (g->dev) sepdev_gh_destroy(g->dev);
+		double complex *arr[] = {g->fk_tv, g->fk_lv, g->fk_rho, g->fk_e, g->fk_X, g->c_tv, g->c_lv, g->c_scatt,
+					 g->c_e, g->c_re, g->c_rj, g->c_ej, g->c_er, g->c_jr, g->c_je, g->c_X};
+		for (size_t q = 0; q < sizeof arr / sizeof arr[0]; q++) free(arr[q]);
+		free(g->k); free(g->out);
+		free(g);
 	}
 	if (ptr->flag_radial == 1) {
 		free(ptr->radial->hist); free(ptr->radial->out); free(ptr->radial->mask);

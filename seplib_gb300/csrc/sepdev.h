@@ -264,6 +264,14 @@ int sepdev_vacf_block(sepdev *d, sepdev_vacf *v, double *out);
  * floor(r / dg) = b (dg = L_x / (2 lvec)) whose type ids (ti, tj) have bit c
  * set in mask[ti * nt + tj] (ncomb <= 32, lvec * ncomb <= 49152) */
 int sepdev_radial(sepdev *d, int lvec, int ncomb, int nt, const unsigned *mask, double *out);
+/* atomic generalised hydrodynamics: per wavevector k[j] along y (unwrapped
+ * by the crossings), out[15 j + 2 q + (0 re, 1 im)] = sum over particles of
+ * e^{i k_j y} w_q with w = (m, m v_x, m v_y, m v^2/2, 1, m a_y, m v_y^2),
+ * a = f / m of the stored forces; out[15 j + 14] = sum m v^2/2 */
+typedef struct sepdev_gh sepdev_gh;
+int sepdev_gh_create(sepdev *d, int nk, const double *k, sepdev_gh **out);
+void sepdev_gh_destroy(sepdev_gh *g);
+int sepdev_gh_sample(sepdev *d, sepdev_gh *g, double *out);
 /* a ring of count values per sample (mvacf: one per molecule) */
 int sepdev_vacf_create_count(sepdev *d, int lvec, long count, sepdev_vacf **out);
 double *sepdev_vacf_row(sepdev_vacf *v, int index);

@@ -513,6 +513,47 @@ def radial_small(lib, tmp):
     return d
 
 
+def gh_small(lib, tmp):
+    """the gh sampler (3 wavevectors, two blocks of 4 samples every 2 steps)
+    on an NVE WCA fluid of 108 particles: the positions (unwrapped),
+    velocities and accelerations at the sample steps and the files"""
+    rng = np.random.default_rng(43)
+    x, L = cfg.fcc(3, 0.8)
+    n = len(x)
+    x = np.mod(x + rng.normal(0, 0.05, x.shape), L)
+    s = cfg.System(x=x, v=cfg.maxwell_boltzmann(n, 1.5, rng), L=np.asarray(L, float),
+                   types=np.full(n, b"A", "S1"), m=np.ones(n), z=np.zeros(n))
+    h = Handle(lib, s, cf=2 ** (1 / 6), dt=0.005)
+    bind_samplers(lib)
+    cwd = os.getcwd()
+    run = os.path.join(tmp, "gh")
+    os.makedirs(run, exist_ok=True)
+    os.chdir(run)
+    xt, vs, acc = [], [], []
+    names = ["gh-rho-acf.dat", "gh-trans-momentum-acf.dat", "gh-long-momentum-acf.dat", "gh-energy-acf.dat",
+             "gh-rho-energy-ccf.dat", "gh-rho-long-momentum-ccf.dat", "gh-energy-long-momentum-ccf.dat",
+             "gh-energy-rho-ccf.dat", "gh-long-momentum-rho-ccf.dat", "gh-long-momentum-energy-ccf.dat",
+             "gh-X-acf.dat"]
+    try:
+        smp = lib.sep_init_sampler()
+        lib.sep_add_sampler(C.byref(smp), b"gh", h.sys, C.c_int(4), C.c_double(0.041), C.c_int(3))
+        for k in range(16):
+            h.step(cf=2 ** (1 / 6), fun="sep_wca")
+            lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, k)
+            if k % 2 == 0:
+                xt.append(h.view["x"] + h.view["crossings"] * s.L)
+                vs.append(h.view["v"].copy())
+                acc.append(h.view["a"].copy())
+        lib.sep_close_sampler(C.byref(smp))
+        d = dict(L=s.L, xt=np.array(xt), v=np.array(vs), a=np.array(acc), k=np.loadtxt("gh-wavevector.dat"))
+        for nm in names:
+            d["file_" + nm[3:-4]] = np.loadtxt(nm)
+    finally:
+        os.chdir(cwd)
+    h.close()
+    return d
+
+
 def box_ops(lib):
     """sep_compress_box / _dir / _dir_length and sep_berendsen / _iso one at
     a time, then a Berendsen run (prgs/prg7.c) and a compression run
@@ -633,7 +674,8 @@ def main(only=()):
                          ("molbaro_small", lambda: molbaro_small(lib, tmp)),
                          ("dpdmol_small", lambda: dpdmol_small(lib, tmp)),
                          ("slit_small", lambda: slit_small(lib, tmp)),
-                         ("radial_small", lambda: radial_small(lib, tmp))):
+                         ("radial_small", lambda: radial_small(lib, tmp)),
+                         ("gh_small", lambda: gh_small(lib, tmp))):
             if only and name not in only:
                 continue
             d = fn()

@@ -111,3 +111,40 @@ def test_mgh_full_size_butane(gpu_lib, tmp_path):
     np.testing.assert_allclose(lav, ms.out["mgh-lav"][0], rtol=2e-7, atol=1.1e-6)
     np.testing.assert_allclose(mv, ms.out["mvacf"][0], rtol=2e-7, atol=1.1e-6)
     assert np.abs(tv[1:]).max() > 1e-3
+
+
+def test_gh_files(gpu_lib, tmp_path):
+    """the atomic gh sampler (source/sepsampler.c:957-1105) on the fixture
+    gh_small's run (108 WCA particles, two blocks of 4 samples) against the
+    oracle fed the device's own states at the sample steps"""
+    import ctypes as C
+    from sephelp import Handle, bind_samplers
+    g = np.load(os.path.join(HERE, "golden", "gh_small.npz"))
+    lib = bind_samplers(gpu_lib)
+    n = g["xt"].shape[1]
+    rng = np.random.default_rng(43)
+    x, L = cfg.fcc(3, 0.8)
+    x = np.mod(x + rng.normal(0, 0.05, x.shape), L)
+    s = cfg.System(x=x, v=cfg.maxwell_boltzmann(n, 1.5, rng), L=np.asarray(L, float),
+                   types=np.full(n, b"A", "S1"), m=np.ones(n), z=np.zeros(n))
+    h = Handle(lib, s, cf=2 ** (1 / 6), dt=0.005)
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    gh = oracle.GH(4, 0.041 / 4, 3, s.L[1], float(np.prod(s.L)))
+    try:
+        smp = lib.sep_init_sampler()
+        lib.sep_add_sampler(C.byref(smp), b"gh", h.sys, C.c_int(4), C.c_double(0.041), C.c_int(3))
+        for k in range(16):
+            h.step(cf=2 ** (1 / 6), fun="sep_wca")
+            lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, k)
+            if k % 2 == 0:
+                h.sync()
+                gh.sample(h.view["x"] + h.view["crossings"] * s.L, h.view["v"], h.view["a"], np.ones(n))
+        lib.sep_close_sampler(C.byref(smp))
+        files = {nm: np.loadtxt("gh-" + nm + ".dat") for nm in oracle.GH.NAMES}
+    finally:
+        os.chdir(cwd)
+    h.close()
+    for nm in oracle.GH.NAMES:
+        np.testing.assert_allclose(files[nm], gh.out[nm], rtol=2e-7, atol=1.1e-6, err_msg=nm)
+        np.testing.assert_allclose(files[nm], g["file_" + nm], rtol=0, atol=1e-4, err_msg=nm)
