@@ -14,10 +14,11 @@
  * per wavevector along y), "gh" (the atomic counterpart: density,
  * momentum and energy correlations along y), "profs" (density, momentum and temperature
  * profiles of one type along z) and "radial" (pair distances histogrammed
- * per type combination).  They write the reference's files (sacf.dat,
+ * per type combination) and "mmsd" (molecular mean square displacement).
+ * They write the reference's files (sacf.dat,
  * vacf.dat, msd.dat, msd-gaussparam.dat, msd-incoherent.dat, msd-k.dat,
  * msacf.dat, mvacf.dat, gh-*.dat, mgh-*.dat, profs.dat, radial.dat,
- * radial_info.dat) in the same formats.  The particle data
+ * radial_info.dat, mmsd*.dat) in the same formats.  The particle data
  * a sample needs stays on the GPU: vacf and mvacf keep their window of
  * velocities in device memory, msd and mgh reduce on the device, so sampling
  * costs no download of the particle arrays.  Unlike the reference, mgh does
@@ -85,7 +86,8 @@ sepsampler sep_init_sampler(void);
  * number of wave vectors (int), safe (int; 0 also evaluates the angular
  * velocities); "profs": lvec bins, particle type (char), sampling interval
  * in steps (int); "radial": lvec bins, sampling interval in steps (int),
- * the types (char *, 1 to 7).  The molecular samplers need sep_add_mol_sampler first. */
+ * the types (char *, 1 to 7); "mmsd": as "msd", over the molecules of a
+ * molecule type.  The molecular samplers need sep_add_mol_sampler first. */
 void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec, ...);
 
 /* Reference include/sepsampler.h:281. */

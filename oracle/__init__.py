@@ -877,3 +877,37 @@ class GH:
             cols[:, 2::2] = (arr * fac[:, None]).imag
             self.out[name] = cols
         self.i = 0
+
+
+class MMSD:
+    """the mmsd sampler (source/sepsampler.c:1958-2036) fed the centres of
+    mass at each sample: crossings from jumps of more than half the box
+    since the last sample, displacements from the block's first sample over
+    the molecules of the sampled type; `out` holds mmsd.dat and
+    mmsd-incoherent.dat's columns after each block"""
+
+    def __init__(self, lvec, dtsample, nk, Lx):
+        self.lvec, self.dts, self.nk = lvec, dtsample, nk
+        self.k = 2 * np.pi / Lx * np.arange(1, nk + 1)
+        self.msd = np.zeros(lvec); self.Fs = np.zeros((lvec, nk))
+        self.i, self.nsample = 0, 0
+        self.out = {}
+
+    def sample(self, cm, sel, L):
+        cm = np.asarray(cm, float); L = np.asarray(L, float); sel = np.asarray(sel, bool)
+        if self.i == 0:
+            self.prev = cm.copy(); self.pos0 = cm.copy(); self.cross = np.zeros(cm.shape, int)
+        d = self.prev - cm
+        self.cross[sel] += (d[sel] > 0.5 * L).astype(int) - (d[sel] < -0.5 * L).astype(int)
+        dr = cm + self.cross * L - self.pos0
+        self.prev[sel] = cm[sel]
+        self.msd[self.i] += (dr[sel] ** 2).sum()
+        self.Fs[self.i] += np.cos(np.outer(dr[sel, 0], self.k)).sum(0)
+        self.i += 1
+        if self.i == self.lvec:
+            self.nsample += 1
+            ntype = sel.sum()
+            t = np.arange(self.lvec) * self.dts
+            self.out["mmsd"] = np.column_stack([t, self.msd / (ntype * self.nsample)])
+            self.out["mmsd-incoherent"] = np.column_stack([t, self.Fs / (self.nsample * ntype)])
+            self.i = 0

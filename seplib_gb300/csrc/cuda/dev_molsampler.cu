@@ -343,19 +343,25 @@ extern "C" int sepdev_mgh_sample(sepdev *d, sepdev_moltab *t, int nk, const doub
 // z (one beyond the new edge is wrapped and counted, as at the reference's
 // next integrator step).  Same FP64 operations as the reference.
 
-// z of the centre of mass, in the reference's order: the chain of
-// consecutive user indices from the first atom, each step's minimum image
-// added to the previous position
-__device__ double mol_cm_z(int m, const int *first, const int *nuau, const double *mass, const int4 *pos,
+__device__ __forceinline__ double coord(const int4 &p, const uint4 &l, int k, double L)
+{
+	return k == 0 ? from_fixed_dev((unsigned)p.x, l.x, L)
+		      : (k == 1 ? from_fixed_dev((unsigned)p.y, l.y, L) : from_fixed_dev((unsigned)p.z, l.z, L));
+}
+
+// coordinate k of the centre of mass, in the reference's order: the chain
+// of consecutive user indices from the first atom, each step's minimum
+// image added to the previous position
+__device__ double mol_cm_k(int m, int k, const int *first, const int *nuau, const double *mass, const int4 *pos,
 			   const uint4 *xlo, const int *inv, const float4 *vhi, double L)
 {
 	const int a0 = first[m];
 	int s = inv[a0];
-	double xprev = from_fixed_dev((unsigned)pos[s].z, xlo[s].z, L), chain = xprev;
+	double xprev = coord(pos[s], xlo[s], k, L), chain = xprev;
 	double acc = __dmul_rn((double)vhi[s].w, chain);
 	for (int q = 1; q < nuau[m]; q++) {
 		s = inv[a0 + q];
-		const double x = from_fixed_dev((unsigned)pos[s].z, xlo[s].z, L);
+		const double x = coord(pos[s], xlo[s], k, L);
 		double r = __dsub_rn(x, xprev);
 		if (r > 0.5 * L) r = __dsub_rn(r, L);
 		else if (r < -0.5 * L) r = __dadd_rn(r, L);
@@ -373,7 +379,7 @@ __global__ void k_mol_cmz(int nmol, const int *first, const int *nuau, const dou
 			  const uint4 *xlo, const int *inv, const float4 *vhi, double L, double *cmz)
 {
 	const int m = blockIdx.x * blockDim.x + threadIdx.x;
-	if (m < nmol) cmz[m] = mol_cm_z(m, first, nuau, mass, pos, xlo, inv, vhi, L);
+	if (m < nmol) cmz[m] = mol_cm_k(m, 2, first, nuau, mass, pos, xlo, inv, vhi, L);
 }
 
 __global__ void k_berendsen_mol(long n, int nmol, int4 *pos, uint4 *xlo, int4 *xn, int4 *cross, const int *mol,
@@ -422,5 +428,130 @@ extern "C" int sepdev_berendsen_mol(sepdev *d, sepdev_moltab *t, double L1z, dou
 	d->fscale[2] = (float)(L1z / 4294967296.0);
 	// captured loop graphs hold the old box's scale factors
 	sepdev_runner_free(d);
+	return SEPDEV_OK;
+}
+
+// ---- molecular mean square displacement (source/sepsampler.c:1958-2036) --------
+//
+// Per molecule of the sampled type: the centre of mass now, crossings
+// counted from its jumps of more than half the box since the last sample
+// (as the reference does), the displacement dr from the block's first
+// sample; per block the sums of |dr|^2 and cos(k_j dr_x), FP64, fixed order.
+
+struct sepdev_mmsd {
+	double *prev, *pos0;   // [nmol][3]
+	int *cross;            // [nmol][3]
+	unsigned char *sel;    // [nmol] 1: the molecule has the sampled type
+	double *kvec, *part, *sum;
+	int nk, nblk;
+};
+
+__global__ void __launch_bounds__(MSB) k_mmsd(int nmol, const int *first, const int *nuau, const double *mass,
+					       const int4 *pos, const uint4 *xlo, const int *inv, const float4 *vhi,
+					       double L0, double L1, double L2, int reset, sepdev_mmsd m, double *part)
+{
+	extern __shared__ double red[];       // [MSB / 32][1 + nk]
+	const int i = blockIdx.x * MSB + threadIdx.x;
+	const int nf = 1 + m.nk;
+	const double L[3] = {L0, L1, L2};
+	double sd = 0.0, dr0 = 0.0;
+	bool on = false;
+	if (i < nmol) {
+		double cm[3];
+		for (int k = 0; k < 3; k++) cm[k] = mol_cm_k(i, k, first, nuau, mass, pos, xlo, inv, vhi, L[k]);
+		if (reset)
+			for (int k = 0; k < 3; k++) {
+				m.prev[3 * i + k] = m.pos0[3 * i + k] = cm[k];
+				m.cross[3 * i + k] = 0;
+			}
+		if (m.sel[i]) {
+			on = true;
+			double dr[3];
+			for (int k = 0; k < 3; k++) {
+				const double d = __dsub_rn(m.prev[3 * i + k], cm[k]);
+				if (d > 0.5 * L[k]) m.cross[3 * i + k]++;
+				else if (d < -0.5 * L[k]) m.cross[3 * i + k]--;
+				dr[k] = __dsub_rn(__dadd_rn(cm[k], __dmul_rn((double)m.cross[3 * i + k], L[k])), m.pos0[3 * i + k]);
+				m.prev[3 * i + k] = cm[k];
+			}
+			sd = __dadd_rn(__dadd_rn(__dmul_rn(dr[0], dr[0]), __dmul_rn(dr[1], dr[1])), __dmul_rn(dr[2], dr[2]));
+			dr0 = dr[0];
+		}
+	}
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	for (int q = 0; q < nf; q++) {
+		double x = on ? (q == 0 ? sd : cos(m.kvec[q - 1] * dr0)) : 0.0;
+		for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+		if (lane == 0) red[wid * nf + q] = x;
+	}
+	__syncthreads();
+	for (int q = threadIdx.x; q < nf; q += MSB) {
+		double x = 0.0;
+		for (int w = 0; w < MSB / 32; w++) x += red[w * nf + q];
+		part[(long)blockIdx.x * nf + q] = x;
+	}
+}
+
+__global__ void k_mmsd_rows(int nf, int nblk, const double *part, double *out)
+{
+	const int q = blockIdx.x * blockDim.x + threadIdx.x;
+	if (q >= nf) return;
+	double s = 0.0;
+	for (int b = 0; b < nblk; b++) s += part[(long)b * nf + q];
+	out[q] = s;
+}
+
+extern "C" void sepdev_mmsd_destroy(sepdev_mmsd *m)
+{
+	if (!m) return;
+	void *b[] = {m->prev, m->pos0, m->cross, m->sel, m->kvec, m->part, m->sum};
+	for (size_t k = 0; k < sizeof b / sizeof b[0]; k++)
+		if (b[k]) cudaFree(b[k]);
+	free(m);
+}
+
+extern "C" int sepdev_mmsd_create(sepdev *d, sepdev_moltab *t, int nk, const double *k, sepdev_mmsd **out)
+{
+	(void)d;
+	*out = NULL;
+	if (nk < 0 || (1 + nk) * (MSB / 32) * 8 > 40 * 1024) return SEPDEV_EINVAL;
+	sepdev_mmsd *m = (sepdev_mmsd *)calloc(1, sizeof *m);
+	if (!m) return SEPDEV_ENOMEM;
+	m->nk = nk;
+	m->nblk = (t->nmol + MSB - 1) / MSB;
+	const int nm = t->nmol;
+	cudaError_t e = cudaMalloc((void **)&m->prev, sizeof(double) * 3 * nm);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&m->pos0, sizeof(double) * 3 * nm);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&m->cross, sizeof(int) * 3 * nm);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&m->sel, nm);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&m->kvec, sizeof(double) * (nk > 0 ? nk : 1));
+	if (e == cudaSuccess) e = cudaMalloc((void **)&m->part, sizeof(double) * (1 + nk) * m->nblk);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&m->sum, sizeof(double) * (1 + nk));
+	if (e == cudaSuccess && nk > 0) e = cudaMemcpy(m->kvec, k, sizeof(double) * nk, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemset(m->cross, 0, sizeof(int) * 3 * nm);
+	if (e != cudaSuccess) {
+		sepdev_mmsd_destroy(m);
+		sepdev_set_error("mmsd buffers", e);
+		return SEPDEV_ENOMEM;
+	}
+	*out = m;
+	return SEPDEV_OK;
+}
+
+// sel (host, nmol): 1 for the molecules of the sampled type; reset: the
+// sample starts a block.  out (host, 1 + nk): sum |dr|^2, sum cos(k_j dr_x)
+extern "C" int sepdev_mmsd_sample(sepdev *d, sepdev_moltab *t, sepdev_mmsd *m, const unsigned char *sel, int reset,
+				  double *out)
+{
+	const int nf = 1 + m->nk;
+	CK(cudaMemcpyAsync(m->sel, sel, t->nmol, cudaMemcpyHostToDevice, d->st));
+	k_mmsd<<<m->nblk, MSB, sizeof(double) * nf * (MSB / 32), d->st>>>(
+		t->nmol, t->first, t->nuau, t->mass, d->pos[d->cur], d->xlo, d->inv, d->vhi, d->L[0], d->L[1], d->L[2],
+		reset, *m, m->part);
+	k_mmsd_rows<<<grid_for(nf, 64), 64, 0, d->st>>>(nf, m->nblk, m->part, m->sum);
+	d->launches++;
+	CKL(d);
+	CK(cudaMemcpyAsync(out, m->sum, sizeof(double) * nf, cudaMemcpyDeviceToHost, d->st));
+	CK(cudaStreamSynchronize(d->st));
 	return SEPDEV_OK;
 }

@@ -5,7 +5,7 @@
  * Control flow, sampling intervals, normalisations and output files follow
  * the reference (source/sepsampler.c:4-242 dispatch, :280-351 sacf,
  * :361-470 radial, :471-641 msd, :658-714 vacf, :725-818 msacf, :822-1105
- * gh, :1110-1410 mgh, :1418-1510 profs, :1757-1825 mvacf).  The stress autocorrelations work on the sepret values the host
+ * gh, :1110-1410 mgh, :1418-1510 profs, :1757-1825 mvacf, :1918-2051 mmsd).  The stress autocorrelations work on the sepret values the host
  * already has (the molecular one through sep_mol_pressure_tensor); vacf,
  * msd, mvacf and mgh keep their particle data on the GPU (dev_sampler.cu,
  * dev_molsampler.cu) and only their per-sample or per-block sums come back
@@ -61,6 +61,19 @@ struct sepgh {
 	double complex *c_tv, *c_lv, *c_scatt, *c_e, *c_re, *c_rj, *c_ej, *c_er, *c_jr, *c_je, *c_X;
 	double *out;           /* 15 nk, scratch */
 	sepdev_gh *dev;
+	rt_ctx *ctx;
+};
+
+struct sepmmsd {
+	int lvec, isample, i, nk, nmol;
+	long nsample;
+	char type;
+	double dtsample;
+	double *k, *msd, *Fs;  /* Fs: lvec x nk (real part) */
+	double *out;           /* 1 + nk, scratch */
+	unsigned char *sel;    /* nmol, scratch */
+	sepdev_moltab *tab;
+	sepdev_mmsd *dev;
 	rt_ctx *ctx;
 };
 
@@ -322,6 +335,32 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 			sptr->radial = p;
 			sptr->flag_radial = 1;
 		}
+	} else if (strcmp(sampler, "mmsd") == 0) {
+		if (sptr->flag_mmsd != 1) {
+			const double tsample = va_arg(args, double);
+			const int nk = va_arg(args, int);
+			const char type = (char)va_arg(args, int);
+			struct sepmmsd *p = xcalloc(1, sizeof *p);
+			p->lvec = lvec;
+			p->isample = sample_interval(tsample, lvec, sys.dt, &p->dtsample);
+			p->nk = nk;
+			p->type = type;
+			p->nmol = (int)sys.molptr->num_mols;
+			p->k = xcalloc(nk, sizeof(double));
+			FILE *f = fopen("mmsd-wavevector.dat", "w");
+			if (!f) sep_error("%s: Couldn't open file", __func__);
+			for (int n = 1; n <= nk; n++) {
+				p->k[n - 1] = 2 * SEP_PI / sys.length[0] * n;
+				fprintf(f, "%f\n", p->k[n - 1]);
+			}
+			fclose(f);
+			p->msd = xcalloc(lvec, sizeof(double));
+			p->Fs = xcalloc((size_t)lvec * (nk > 0 ? nk : 1), sizeof(double));
+			p->out = xcalloc(1 + nk, sizeof(double));
+			p->sel = xcalloc(p->nmol, 1);
+			sptr->mmsd = p;
+			sptr->flag_mmsd = 1;
+		}
 	} else if (strcmp(sampler, "mvacf") == 0) {
 		if (sptr->flag_mvacf != 1) {
 			const double tsample = va_arg(args, double);
@@ -336,7 +375,7 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 	} else {
 		va_end(args);
 		sep_error("%s: sampler %s is not provided by this GPU implementation "
-			  "(available: sacf, vacf, msd, msacf, mvacf, gh, mgh, profs, radial)", __func__, sampler);
+			  "(available: sacf, vacf, msd, msacf, mvacf, gh, mgh, profs, radial, mmsd)", __func__, sampler);
 	}
 	va_end(args);
 }
@@ -728,6 +767,45 @@ static void gh_sample(struct sepgh *g, seppart *pptr, sepsys sys)
 	g->i = 0;
 }
 
+/* ---- mmsd: source/sepsampler.c:1958-2036 ---- */
+static void mmsd_sample(struct sepmmsd *p, seppart *pptr, sepmol *mols, sepsys sys)
+{
+	rt_ctx *c = sampler_ctx(pptr, &sys);
+	if (p->ctx != c) {
+		if (p->dev) sepdev_mmsd_destroy(p->dev);
+		p->dev = NULL;
+	}
+	mol_tables(&p->tab, &p->ctx, c, mols, &sys);
+	if (!p->dev) rt_check(sepdev_mmsd_create(c->dev, p->tab, p->nk, p->k, &p->dev), "mmsd sampler");
+	int ntype = 0;
+	for (int n = 0; n < p->nmol; n++) {
+		p->sel[n] = mols[n].type == p->type;
+		ntype += p->sel[n];
+	}
+	int index = p->i;
+	rt_check(sepdev_mmsd_sample(c->dev, p->tab, p->dev, p->sel, index == 0, p->out), "mmsd sample");
+	p->msd[index] += p->out[0];
+	for (int j = 0; j < p->nk; j++) p->Fs[(size_t)index * p->nk + j] += p->out[1 + j];
+	index++;
+	if (index == p->lvec) {
+		p->nsample++;
+		FILE *f = fopen("mmsd.dat", "w");
+		if (!f) sep_error("%s: Couldn't open file", __func__);
+		for (int n = 0; n < p->lvec; n++) fprintf(f, "%f %f \n", n * p->dtsample, p->msd[n] / (ntype * p->nsample));
+		fclose(f);
+		f = fopen("mmsd-incoherent.dat", "w");
+		if (!f) sep_error("%s: Couldn't open file", __func__);
+		for (int n = 0; n < p->lvec; n++) {
+			fprintf(f, "%f ", n * p->dtsample);
+			for (int j = 0; j < p->nk; j++) fprintf(f, "%f ", p->Fs[(size_t)n * p->nk + j] / (p->nsample * ntype));
+			fprintf(f, "\n");
+		}
+		fclose(f);
+		index = 0;
+	}
+	p->i = index;
+}
+
 /* ---- radial: source/sepsampler.c:396-461 ---- */
 static void radial_sample(struct sepradial *p, seppart *pptr, sepsys sys)
 {
@@ -786,6 +864,7 @@ void sep_sample(seppart *pptr, sepsampler *sptr, sepret *ret, sepsys sys, unsign
 		}
 		sptr->msd_counter++;
 	}
+	if (sptr->flag_mmsd == 1 && n % sptr->mmsd->isample == 0) mmsd_sample(sptr->mmsd, pptr, sptr->molptr, sys);
 }
 
 void sep_close_sampler(sepsampler *ptr)
@@ -800,6 +879,13 @@ void sep_close_sampler(sepsampler *ptr)
 		free(ptr->vacf->vacf);
 		free(ptr->vacf->block);
 		free(ptr->vacf);
+	}
+	if (ptr->flag_mmsd == 1) {
+		struct sepmmsd *p = ptr->mmsd;
+		if (p->dev) sepdev_mmsd_destroy(p->dev);
+		if (p->tab) sepdev_moltab_destroy(p->tab);
+		free(p->k); free(p->msd); free(p->Fs); free(p->out); free(p->sel);
+		free(p);
 	}
 	if (ptr->flag_gh == 1) {
 		struct sepgh *g = ptr->gh;

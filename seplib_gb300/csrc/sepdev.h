@@ -306,6 +306,15 @@ int sepdev_mvacf_store(sepdev *d, sepdev_moltab *t, sepdev_vacf *v, int index);
  * else 0); out[18 nk] = sum of M v^2/2.  The dipole of a molecule without
  * both signs of charge keeps its last value (initially 0). */
 int sepdev_mgh_sample(sepdev *d, sepdev_moltab *t, int nk, const double *k, int unsafe, double *out);
+/* Molecular mean square displacement: sel (host, nmol) marks the
+ * molecules of the sampled type, reset starts a block (the centres of mass
+ * become the reference and the crossing counts restart); out (host, 1 + nk)
+ * = sum |dr|^2 and sum cos(k_j dr_x) over the marked molecules. */
+typedef struct sepdev_mmsd sepdev_mmsd;
+int sepdev_mmsd_create(sepdev *d, sepdev_moltab *t, int nk, const double *k, sepdev_mmsd **out);
+void sepdev_mmsd_destroy(sepdev_mmsd *m);
+int sepdev_mmsd_sample(sepdev *d, sepdev_moltab *t, sepdev_mmsd *m, const unsigned char *sel, int reset,
+		       double *out);
 /* Molecular Berendsen step along z: each molecule's centre-of-mass z is
  * scaled by `scale` and its atoms keep their offsets from it, the box edge
  * L_z becomes L1z; atoms outside molecules keep their absolute z. */

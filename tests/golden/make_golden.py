@@ -25,7 +25,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 import oracle  # noqa: E402
 from seplib_gb300 import configs as cfg  # noqa: E402
 from seplib_gb300 import sepapi as A  # noqa: E402
-from sephelp import Handle, bind_samplers, slit_step  # noqa: E402
+from sephelp import Handle, bind_samplers, slit_step, water_step  # noqa: E402
 
 
 def ref_lib():
@@ -554,6 +554,49 @@ def gh_small(lib, tmp):
     return d
 
 
+def mmsd_small(lib, tmp):
+    """the mmsd sampler (3 wavevectors, two blocks of 4 samples over a time
+    span of 0.41) on a prgs/prg3.c-style run of 125 charged three-site molecules,
+    every third molecule of type B and the sampler taking type A: the
+    positions at the sample steps and the files"""
+    s = cfg.water_like(nmol=125, rho=0.09, seed=7)
+    top = os.path.join(tmp, "mm.top")
+    cfg.write_top(top, s)
+    h = Handle(lib, s, cf=3.0, update=A.SEP_LLIST_NEIGHBLIST, dt=0.0005)
+    lib.sep_read_topology_file(h.atoms, top.encode(), C.byref(h.sys), b"q")
+    mols = lib.sep_init_mol(h.atoms, C.byref(h.sys))
+    nm = h.sys.molptr.contents.num_mols
+    for i in range(0, nm, 3):
+        mols[i].type = b"B"
+    bind_samplers(lib)
+    cwd = os.getcwd()
+    run = os.path.join(tmp, "mmsd")
+    os.makedirs(run, exist_ok=True)
+    os.chdir(run)
+    xs = []
+    try:
+        smp = lib.sep_init_sampler()
+        lib.sep_add_mol_sampler(C.byref(smp), C.cast(mols, C.c_void_p))
+        lib.sep_add_sampler(C.byref(smp), b"mmsd", h.sys, C.c_int(4), C.c_double(0.41), C.c_int(3),
+                            C.c_int(ord("A")))
+        isample = int((0.41 / 4) / 0.0005)
+        for n in range(8 * isample):
+            water_step(lib, h)
+            lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, n)
+            if n % isample == 0:
+                xs.append(h.view["x"].copy())
+        lib.sep_close_sampler(C.byref(smp))
+        d = dict(x0=s.x, v0=s.v, L=s.L, z=s.z, m=s.m, types=s.types.astype("S1"), bonds=s.bonds,
+                 angles=s.angles, xs=np.array(xs), molindex=h.view["molindex"].copy(), nmol=nm,
+                 mmsd=np.loadtxt("mmsd.dat"), mmsd_inc=np.loadtxt("mmsd-incoherent.dat"),
+                 k=np.loadtxt("mmsd-wavevector.dat"))
+    finally:
+        os.chdir(cwd)
+    lib.sep_free_mol(mols, C.byref(h.sys))
+    h.close()
+    return d
+
+
 def box_ops(lib):
     """sep_compress_box / _dir / _dir_length and sep_berendsen / _iso one at
     a time, then a Berendsen run (prgs/prg7.c) and a compression run
@@ -675,7 +718,8 @@ def main(only=()):
                          ("dpdmol_small", lambda: dpdmol_small(lib, tmp)),
                          ("slit_small", lambda: slit_small(lib, tmp)),
                          ("radial_small", lambda: radial_small(lib, tmp)),
-                         ("gh_small", lambda: gh_small(lib, tmp))):
+                         ("gh_small", lambda: gh_small(lib, tmp)),
+                         ("mmsd_small", lambda: mmsd_small(lib, tmp))):
             if only and name not in only:
                 continue
             d = fn()

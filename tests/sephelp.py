@@ -99,6 +99,20 @@ MOLSAMPLER_FILES = {"msacf": "msacf.dat", "mvacf": "mvacf.dat",
                     "mgh-X": "mgh-X-cf.dat"}
 
 
+def water_step(lib, h):
+    """one prgs/prg3.c-style step of the water-like molecules: LJ on O,
+    bonds, cos^2 angles, SF Coulomb, Nose-Hoover, leap-frog"""
+    lib.sep_reset_retval(C.byref(h.ret))
+    lib.sep_reset_force(h.atoms, C.byref(h.sys))
+    lib.sep_reset_force_mol(C.byref(h.sys))
+    lib.sep_force_pairs(h.atoms, b"OO", 2.5, h.fun(), C.byref(h.sys), C.byref(h.ret), A.SEP_EXCL_SAME_MOL)
+    lib.sep_stretch_harmonic(h.atoms, 0, 0.316, 68421.0, C.byref(h.sys), C.byref(h.ret))
+    lib.sep_angle_cossq(h.atoms, 0, 1.97, 490.0, C.byref(h.sys), C.byref(h.ret))
+    lib.sep_coulomb_sf(h.atoms, 3.0, C.byref(h.sys), C.byref(h.ret), A.SEP_EXCL_SAME_MOL)
+    lib.sep_nosehoover(h.atoms, 3.0, C.byref(h.alpha), 0.01, C.byref(h.sys))
+    lib.sep_leapfrog(h.atoms, C.byref(h.sys), C.byref(h.ret))
+
+
 def water_mol_run(lib, s, top, nsteps, lvec, tsample, nk, unsafe, record_every, record_mols=False):
     """A prgs/prg3.c-style run (LJ on O, SF Coulomb, bonds, cos^2 angles,
     Nose-Hoover, leap-frog) with the msacf, mvacf and mgh samplers, in the
@@ -123,15 +137,7 @@ def water_mol_run(lib, s, top, nsteps, lvec, tsample, nk, unsafe, record_every, 
     nm = h.sys.molptr.contents.num_mols
     mp = C.cast(mols, C.POINTER(A.SepMol))
     for n in range(nsteps):
-        lib.sep_reset_retval(C.byref(h.ret))
-        lib.sep_reset_force(h.atoms, C.byref(h.sys))
-        lib.sep_reset_force_mol(C.byref(h.sys))
-        lib.sep_force_pairs(h.atoms, b"OO", 2.5, h.fun(), C.byref(h.sys), C.byref(h.ret), A.SEP_EXCL_SAME_MOL)
-        lib.sep_stretch_harmonic(h.atoms, 0, 0.316, 68421.0, C.byref(h.sys), C.byref(h.ret))
-        lib.sep_angle_cossq(h.atoms, 0, 1.97, 490.0, C.byref(h.sys), C.byref(h.ret))
-        lib.sep_coulomb_sf(h.atoms, 3.0, C.byref(h.sys), C.byref(h.ret), A.SEP_EXCL_SAME_MOL)
-        lib.sep_nosehoover(h.atoms, 3.0, C.byref(h.alpha), 0.01, C.byref(h.sys))
-        lib.sep_leapfrog(h.atoms, C.byref(h.sys), C.byref(h.ret))
+        water_step(lib, h)
         lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, n)
         if n % record_every == 0:
             h.sync()

@@ -148,3 +148,53 @@ def test_gh_files(gpu_lib, tmp_path):
     for nm in oracle.GH.NAMES:
         np.testing.assert_allclose(files[nm], gh.out[nm], rtol=2e-7, atol=1.1e-6, err_msg=nm)
         np.testing.assert_allclose(files[nm], g["file_" + nm], rtol=0, atol=1e-4, err_msg=nm)
+
+
+def test_mmsd_files(gpu_lib, tmp_path):
+    """the molecular mean square displacement (source/sepsampler.c:1958-2036)
+    on the fixture mmsd_small's run against the oracle fed the device's own
+    states at the sample steps (the printing precision), and against the
+    reference's files within the FP32 trajectories' spread"""
+    import ctypes as C
+    from seplib_gb300 import sepapi as A
+    from sephelp import Handle, bind_samplers, water_step
+    g = np.load(os.path.join(HERE, "golden", "mmsd_small.npz"))
+    lib = bind_samplers(gpu_lib)
+    s = cfg.System(x=g["x0"].copy(), v=g["v0"].copy(), L=g["L"].copy(), types=g["types"].copy(),
+                   m=g["m"].copy(), z=g["z"].copy(), bonds=g["bonds"], angles=g["angles"])
+    top = str(tmp_path / "mm.top")
+    cfg.write_top(top, s)
+    h = Handle(lib, s, cf=3.0, update=A.SEP_LLIST_NEIGHBLIST, dt=0.0005)
+    lib.sep_read_topology_file(h.atoms, top.encode(), C.byref(h.sys), b"q")
+    mols = lib.sep_init_mol(h.atoms, C.byref(h.sys))
+    nm = h.sys.molptr.contents.num_mols
+    for i in range(0, nm, 3):
+        mols[i].type = b"B"
+    sel = np.ones(nm, bool)
+    sel[::3] = False
+    first, nuau, _, _ = oracle.mol_tables(h.view["molindex"], nm)
+    mm = oracle.MMSD(4, 0.41 / 4, 3, s.L[0])
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        smp = lib.sep_init_sampler()
+        lib.sep_add_mol_sampler(C.byref(smp), C.cast(mols, C.c_void_p))
+        lib.sep_add_sampler(C.byref(smp), b"mmsd", h.sys, C.c_int(4), C.c_double(0.41), C.c_int(3),
+                            C.c_int(ord("A")))
+        isample = int((0.41 / 4) / 0.0005)
+        for n in range(8 * isample):
+            water_step(lib, h)
+            lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, n)
+            if n % isample == 0:
+                h.sync()
+                mm.sample(oracle.mol_cm_chain(h.view["x"], s.m, first, nuau, s.L), sel, s.L)
+        lib.sep_close_sampler(C.byref(smp))
+        msd = np.loadtxt("mmsd.dat")
+        inc = np.loadtxt("mmsd-incoherent.dat")
+    finally:
+        os.chdir(cwd)
+    lib.sep_free_mol(mols, C.byref(h.sys))
+    h.close()
+    np.testing.assert_allclose(msd, mm.out["mmsd"], rtol=1e-9, atol=1.1e-6)
+    np.testing.assert_allclose(inc, mm.out["mmsd-incoherent"], rtol=1e-9, atol=1.1e-6)
+    np.testing.assert_allclose(msd[:, 1], g["mmsd"][:, 1], rtol=0.05, atol=1e-3)
