@@ -14,11 +14,12 @@
  * per wavevector along y), "gh" (the atomic counterpart: density,
  * momentum and energy correlations along y), "profs" (density, momentum and temperature
  * profiles of one type along z) and "radial" (pair distances histogrammed
- * per type combination) and "mmsd" (molecular mean square displacement).
- * They write the reference's files (sacf.dat,
+ * per type combination), "mmsd" (molecular mean square displacement) and
+ * "scatt" (partial coherent scattering functions per type pair).  They
+ * write the reference's files (sacf.dat,
  * vacf.dat, msd.dat, msd-gaussparam.dat, msd-incoherent.dat, msd-k.dat,
  * msacf.dat, mvacf.dat, gh-*.dat, mgh-*.dat, profs.dat, radial.dat,
- * radial_info.dat, mmsd*.dat) in the same formats.  The particle data
+ * radial_info.dat, mmsd*.dat, scatt-*.dat) in the same formats.  The particle data
  * a sample needs stays on the GPU: vacf and mvacf keep their window of
  * velocities in device memory, msd and mgh reduce on the device, so sampling
  * costs no download of the particle arrays.  Unlike the reference, mgh does
@@ -87,7 +88,8 @@ sepsampler sep_init_sampler(void);
  * velocities); "profs": lvec bins, particle type (char), sampling interval
  * in steps (int); "radial": lvec bins, sampling interval in steps (int),
  * the types (char *, 1 to 7); "mmsd": as "msd", over the molecules of a
- * molecule type.  The molecular samplers need sep_add_mol_sampler first. */
+ * molecule type; "scatt": lvec samples, the types (char *, 1 to 7), number
+ * of wave vectors (int), time span (double).  The molecular samplers need sep_add_mol_sampler first. */
 void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec, ...);
 
 /* Reference include/sepsampler.h:281. */
@@ -98,6 +100,11 @@ void sep_sample(seppart *pptr, sepsampler *sptr, sepret *ret, sepsys sys, unsign
 
 /* Reference include/sepsampler.h:299: the molecules of msacf, mvacf and mgh. */
 void sep_add_mol_sampler(sepsampler *sptr, sepmol *mols);
+
+/* Reference include/sepsampler.h:383: the scatt sampler takes its first type
+ * from molecules of even index and its second from molecules of odd index
+ * (or none) instead of all particles. */
+void sep_set_inter_scatt(sepsampler *sampler);
 
 #ifdef __cplusplus
 }

@@ -911,3 +911,46 @@ class MMSD:
             self.out["mmsd"] = np.column_stack([t, self.msd / (ntype * self.nsample)])
             self.out["mmsd-incoherent"] = np.column_stack([t, self.Fs / (self.nsample * ntype)])
             self.i = 0
+
+
+class Scatt:
+    """the scatt sampler (source/sepsampler.c:2142-2213): per type pair t1 <=
+    t2 of the string, sums of m e^{+ikx} over t1 and m e^{-ikx} over t2 (x
+    unwrapped, k = 2 pi (n+1) / L_x), their time correlation per block; in
+    the 'i' mode t1 from molecules of even index, t2 from odd index or
+    none; `out` maps scatt-XY to the file's columns (real parts)"""
+
+    def __init__(self, typestr, lvec, nk, tspan, Lx, volume, opt="a"):
+        self.ty = [bytes([c]) for c in typestr]
+        self.combos = [(a, b) for i, a in enumerate(self.ty) for b in self.ty[i:]]
+        self.lvec, self.nk, self.tspan, self.V, self.opt = lvec, nk, tspan, volume, opt
+        self.k = 2.0 * 3.14159265358979 * np.arange(1, nk + 1) / Lx
+        z = lambda: np.zeros((lvec, nk), complex)
+        self.p1 = [z() for _ in self.combos]; self.m2 = [z() for _ in self.combos]
+        self.sc = [z() for _ in self.combos]
+        self.index, self.nsample = 0, 0
+        self.out = {}
+
+    def sample(self, xt, m, types, molindex):
+        m = np.asarray(m, float); ty = np.asarray(types); mi = np.asarray(molindex)
+        e = np.exp(1j * np.outer(np.asarray(xt, float), self.k))
+        for c, (a, b) in enumerate(self.combos):
+            s1 = ty == a
+            s2 = ty == b
+            if self.opt == "i":
+                s1 = s1 & (mi >= 0) & (mi % 2 == 0)
+                s2 = s2 & (((mi + 1) % 2) == 0)
+            self.p1[c][self.index] = (m[s1, None] * e[s1]).sum(0)
+            self.m2[c][self.index] = (m[s2, None] * np.conj(e[s2])).sum(0)
+        self.index += 1
+        if self.index < self.lvec:
+            return
+        self.index = 0
+        self.nsample += 1
+        lv = self.lvec
+        fac = 1.0 / (self.nsample * self.V * (lv - np.arange(lv)))
+        for c, (a, b) in enumerate(self.combos):
+            for n in range(lv):
+                self.sc[c][n] += (self.p1[c][:lv - n] * self.m2[c][n:]).sum(0)
+            cols = np.column_stack([np.arange(lv) * (self.tspan / lv), (self.sc[c] * fac[:, None]).real])
+            self.out["scatt-" + (a + b).decode()] = cols

@@ -529,3 +529,92 @@ extern "C" int sepdev_gh_sample(sepdev *d, sepdev_gh *g, double *out)
 	CK(cudaStreamSynchronize(d->st));
 	return SEPDEV_OK;
 }
+
+// ---- partial coherent scattering (source/sepsampler.c:2142-2213) ----------------
+//
+// Per wavevector k_j = 2 pi (j + 1) / L_x and per requested type u (and, in
+// the reference's 'i' mode, per molecule-index class: even, or odd or none)
+// the sums of m e^{i k_j x} over the particles, x unwrapped by the
+// crossings.  Warp shuffles and ordered block partials keep the FP64 sums
+// independent of scheduling.
+
+#define SC_MAXV 28     // 7 types x 2 classes x (re, im)
+
+struct ScattArgs {
+	long n;
+	double Lx;
+	const int4 *pos;
+	const uint4 *xlo;
+	const int4 *cross;
+	const float4 *vhi;
+	const int *mol;
+	int umap[SEPDEV_MAXTYPES];     // device type id -> requested type index, -1
+	int nu, nclass;                // requested types, classes (1: all; 2: even, odd-or-none)
+	double *part;                  // [block][j][2 nu nclass]
+};
+
+__global__ void __launch_bounds__(SB) k_scatt(ScattArgs a)
+{
+	__shared__ double red[SB / 32][SC_MAXV];
+	const long i = blockIdx.x * (long)SB + threadIdx.x;
+	const int j = blockIdx.y;
+	const int nv = 2 * a.nu * a.nclass;
+	int u = -1, cls = 0;
+	double re = 0.0, im = 0.0;
+	if (i < a.n) {
+		const int4 p = a.pos[i];
+		u = a.umap[p.w];
+		if (u >= 0) {
+			const double m = (double)a.vhi[i].w;
+			const double x = a.Lx * a.cross[i].x + from_fixed_dev((unsigned)p.x, a.xlo[i].x, a.Lx);
+			const double k = 2.0 * 3.14159265358979 * (j + 1) / a.Lx;
+			double sn, cs;
+			sincos(k * x, &sn, &cs);
+			re = m * cs;
+			im = m * sn;
+			const int mi = a.mol[i];
+			// class bits: 1 = even molecule index, 2 = odd or no molecule
+			cls = (mi >= 0 && mi % 2 == 0 ? 1 : 0) | ((mi + 1) % 2 == 0 ? 2 : 0);
+		}
+	}
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	for (int q = 0; q < nv; q++) {
+		const int uq = q / (2 * a.nclass), cq = (q / 2) % a.nclass;
+		const bool hit = u == uq && (a.nclass == 1 || (cls >> cq) & 1);
+		double x = hit ? ((q & 1) ? im : re) : 0.0;
+		for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+		if (lane == 0) red[wid][q] = x;
+	}
+	__syncthreads();
+	if ((int)threadIdx.x < nv) {
+		double x = 0.0;
+		for (int w = 0; w < SB / 32; w++) x += red[w][threadIdx.x];
+		a.part[((long)blockIdx.x * gridDim.y + j) * nv + threadIdx.x] = x;
+	}
+}
+
+// umap (host, SEPDEV_MAXTYPES): requested type index of each device type id
+// or -1; out (host, nk x 2 nu nclass): for wavevector j, type u, class c:
+// out[j * 2 nu nclass + 2 (u nclass + c) + (0 re, 1 im)]
+extern "C" int sepdev_scatt(sepdev *d, int nk, int nu, int nclass, const int *umap, double *out)
+{
+	if (nk < 1 || nu < 1 || (nclass != 1 && nclass != 2) || 2 * nu * nclass > SC_MAXV) return SEPDEV_EINVAL;
+	const int nv = 2 * nu * nclass, nblk = grid_for(d->n, SB);
+	double *part = NULL, *sum = NULL;
+	cudaError_t e = cudaMalloc((void **)&part, sizeof(double) * nv * nk * nblk);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&sum, sizeof(double) * nv * nk);
+	if (e != cudaSuccess) { cudaFree(part); sepdev_set_error("scatt buffers", e); return SEPDEV_ENOMEM; }
+	ScattArgs a;
+	a.n = d->n; a.Lx = d->L[0];
+	a.pos = d->pos[d->cur]; a.xlo = d->xlo; a.cross = d->cross; a.vhi = d->vhi; a.mol = d->mol;
+	for (int t = 0; t < SEPDEV_MAXTYPES; t++) a.umap[t] = umap[t];
+	a.nu = nu; a.nclass = nclass; a.part = part;
+	k_scatt<<<dim3(nblk, nk), SB, 0, d->st>>>(a);
+	k_rows_sum<<<grid_for(nv * nk, 128), 128, 0, d->st>>>(nv * nk, nblk, part, sum, 0);
+	CKL(d);
+	e = cudaMemcpyAsync(out, sum, sizeof(double) * nv * nk, cudaMemcpyDeviceToHost, d->st);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(d->st);
+	cudaFree(part); cudaFree(sum);
+	if (e != cudaSuccess) { sepdev_set_error("scatt", e); return SEPDEV_ECUDA; }
+	return SEPDEV_OK;
+}

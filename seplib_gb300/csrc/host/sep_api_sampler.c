@@ -5,7 +5,8 @@
  * Control flow, sampling intervals, normalisations and output files follow
  * the reference (source/sepsampler.c:4-242 dispatch, :280-351 sacf,
  * :361-470 radial, :471-641 msd, :658-714 vacf, :725-818 msacf, :822-1105
- * gh, :1110-1410 mgh, :1418-1510 profs, :1757-1825 mvacf, :1918-2051 mmsd).  The stress autocorrelations work on the sepret values the host
+ * gh, :1110-1410 mgh, :1418-1510 profs, :1757-1825 mvacf, :1918-2051 mmsd,
+ * :2055-2213 scatt).  The stress autocorrelations work on the sepret values the host
  * already has (the molecular one through sep_mol_pressure_tensor); vacf,
  * msd, mvacf and mgh keep their particle data on the GPU (dev_sampler.cu,
  * dev_molsampler.cu) and only their per-sample or per-block sums come back
@@ -75,6 +76,20 @@ struct sepmmsd {
 	sepdev_moltab *tab;
 	sepdev_mmsd *dev;
 	rt_ctx *ctx;
+};
+
+/* all type combinations of one scatt sampler; the program's sepsampler
+ * holds a one-element array pointing to it.  intropt 'a': every particle of
+ * the types; 'i': the first type from molecules of even index, the second
+ * from molecules of odd index or none (sep_set_inter_scatt). */
+struct sepscatt {
+	int lvec, isample, nk, ntypes, ncomb, index;
+	long nsample;
+	char types[8], intropt;
+	double tspan;
+	double complex *p1, *m2;   /* ncomb x lvec x nk */
+	double complex *sc;        /* ncomb x lvec x nk */
+	double *out;               /* nk x 28, scratch */
 };
 
 struct sepradial {
@@ -361,6 +376,32 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 			sptr->mmsd = p;
 			sptr->flag_mmsd = 1;
 		}
+	} else if (strcmp(sampler, "scatt") == 0) {
+		if (sptr->flag_scatt != 1) {
+			const char *t = va_arg(args, char *);
+			const int nk = va_arg(args, int);
+			const double tsample = va_arg(args, double);
+			struct sepscatt *p = xcalloc(1, sizeof *p);
+			p->ntypes = (int)strlen(t);
+			if (p->ntypes < 1 || p->ntypes > 7)
+				sep_error("%s: scatt takes 1 to 7 types (got \"%s\")", __func__, t);
+			memcpy(p->types, t, p->ntypes);
+			p->ncomb = p->ntypes * (p->ntypes + 1) / 2;
+			p->lvec = lvec;
+			p->nk = nk;
+			p->tspan = tsample;
+			p->isample = (int)(tsample / (lvec * sys.dt));
+			if (p->isample < 1) sep_error("%s: isample is too small - CHECK lvec argument", __func__);
+			p->intropt = 'a';
+			const size_t m = (size_t)p->ncomb * lvec * (nk > 0 ? nk : 1);
+			p->p1 = xcalloc(m, sizeof(double complex));
+			p->m2 = xcalloc(m, sizeof(double complex));
+			p->sc = xcalloc(m, sizeof(double complex));
+			p->out = xcalloc(28 * (size_t)(nk > 0 ? nk : 1), sizeof(double));
+			sptr->scatt = xcalloc(1, sizeof(struct sepscatt *));
+			sptr->scatt[0] = p;
+			sptr->flag_scatt = 1;
+		}
 	} else if (strcmp(sampler, "mvacf") == 0) {
 		if (sptr->flag_mvacf != 1) {
 			const double tsample = va_arg(args, double);
@@ -375,7 +416,8 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 	} else {
 		va_end(args);
 		sep_error("%s: sampler %s is not provided by this GPU implementation "
-			  "(available: sacf, vacf, msd, msacf, mvacf, gh, mgh, profs, radial, mmsd)", __func__, sampler);
+			  "(available: sacf, vacf, msd, msacf, mvacf, gh, mgh, profs, radial, mmsd, scatt)", __func__,
+			  sampler);
 	}
 	va_end(args);
 }
@@ -806,6 +848,69 @@ static void mmsd_sample(struct sepmmsd *p, seppart *pptr, sepmol *mols, sepsys s
 	p->i = index;
 }
 
+/* source/sepsampler.c:2107-2114 */
+void sep_set_inter_scatt(sepsampler *sampler)
+{
+	if (sampler->flag_scatt == 1) sampler->scatt[0]->intropt = 'i';
+	else sep_error("%s: Couldn't set option since scatt in not initialized", __func__);
+}
+
+/* ---- scatt: source/sepsampler.c:2142-2213 ---- */
+static void scatt_sample(struct sepscatt *p, seppart *pptr, sepsys sys)
+{
+	rt_ctx *c = sampler_ctx(pptr, &sys);
+	/* the requested types by their first position in the string */
+	int umap[SEPDEV_MAXTYPES], first[8];
+	for (int t = 0; t < SEPDEV_MAXTYPES; t++) umap[t] = -1;
+	for (int u = 0; u < p->ntypes; u++) {
+		first[u] = u;
+		for (int v = 0; v < u; v++)
+			if (p->types[v] == p->types[u]) { first[u] = first[v]; break; }
+		const int tid = rt_type_id(c, p->types[u]);
+		if (tid >= 0 && first[u] == u) umap[tid] = u;
+	}
+	const int inter = p->intropt == 'i', ncl = inter ? 2 : 1;
+	const int nv = 2 * p->ntypes * ncl, nk = p->nk;
+	rt_check(sepdev_scatt(c->dev, nk, p->ntypes, ncl, umap, p->out), "scatt sample");
+	int cb = 0;
+	for (int a = 0; a < p->ntypes; a++)
+		for (int b = a; b < p->ntypes; b++, cb++)
+			for (int j = 0; j < nk; j++) {
+				const double *o = p->out + (size_t)j * nv;
+				const int qa = 2 * (first[a] * ncl + 0), qb = 2 * (first[b] * ncl + (inter ? 1 : 0));
+				const size_t at = ((size_t)cb * p->lvec + p->index) * nk + j;
+				p->p1[at] = o[qa] + I * o[qa + 1];
+				p->m2[at] = o[qb] - I * o[qb + 1];
+			}
+	p->index++;
+	if (p->index < p->lvec) return;
+	p->index = 0;
+	p->nsample++;
+	const int lv = p->lvec;
+	cb = 0;
+	for (int a = 0; a < p->ntypes; a++)
+		for (int b = a; b < p->ntypes; b++, cb++) {
+			const size_t base = (size_t)cb * lv * nk;
+			for (int k = 0; k < nk; k++)
+				for (int n = 0; n < lv; n++)
+					for (int m = 0; m < lv - n; m++)
+						p->sc[base + (size_t)n * nk + k] +=
+							p->p1[base + (size_t)m * nk + k] * p->m2[base + (size_t)(n + m) * nk + k];
+			char name[64];
+			snprintf(name, sizeof name, "scatt-%c%c.dat", p->types[a], p->types[b]);
+			FILE *f = fopen(name, "w");
+			if (!f) sep_error("Couldn't open file");
+			const double dt = p->tspan / lv;
+			for (int n = 0; n < lv; n++) {
+				fprintf(f, "%f ", n * dt);
+				const double fac = 1.0 / (p->nsample * sys.volume * (lv - n));
+				for (int k = 0; k < nk; k++) fprintf(f, "%f ", creal(p->sc[base + (size_t)n * nk + k] * fac));
+				fprintf(f, "\n");
+			}
+			fclose(f);
+		}
+}
+
 /* ---- radial: source/sepsampler.c:396-461 ---- */
 static void radial_sample(struct sepradial *p, seppart *pptr, sepsys sys)
 {
@@ -865,6 +970,7 @@ void sep_sample(seppart *pptr, sepsampler *sptr, sepret *ret, sepsys sys, unsign
 		sptr->msd_counter++;
 	}
 	if (sptr->flag_mmsd == 1 && n % sptr->mmsd->isample == 0) mmsd_sample(sptr->mmsd, pptr, sptr->molptr, sys);
+	if (sptr->flag_scatt == 1 && n % sptr->scatt[0]->isample == 0) scatt_sample(sptr->scatt[0], pptr, sys);
 }
 
 void sep_close_sampler(sepsampler *ptr)
@@ -879,6 +985,12 @@ void sep_close_sampler(sepsampler *ptr)
 		free(ptr->vacf->vacf);
 		free(ptr->vacf->block);
 		free(ptr->vacf);
+	}
+	if (ptr->flag_scatt == 1) {
+		struct sepscatt *p = ptr->scatt[0];
+		free(p->p1); free(p->m2); free(p->sc); free(p->out);
+		free(p);
+		free(ptr->scatt);
 	}
 	if (ptr->flag_mmsd == 1) {
 		struct sepmmsd *p = ptr->mmsd;

@@ -272,6 +272,12 @@ typedef struct sepdev_gh sepdev_gh;
 int sepdev_gh_create(sepdev *d, int nk, const double *k, sepdev_gh **out);
 void sepdev_gh_destroy(sepdev_gh *g);
 int sepdev_gh_sample(sepdev *d, sepdev_gh *g, double *out);
+/* partial coherent scattering: per wavevector k_j = 2 pi (j+1) / L_x, per
+ * requested type u (umap: device type id -> u or -1) and class c (nclass
+ * 1: all particles; 2: even molecule index, odd or no molecule) the sum of
+ * m e^{i k_j x} (x unwrapped): out[j * 2 nu nclass + 2 (u nclass + c) + (0
+ * re, 1 im)]; 2 nu nclass <= 28 */
+int sepdev_scatt(sepdev *d, int nk, int nu, int nclass, const int *umap, double *out);
 /* a ring of count values per sample (mvacf: one per molecule) */
 int sepdev_vacf_create_count(sepdev *d, int lvec, long count, sepdev_vacf **out);
 double *sepdev_vacf_row(sepdev_vacf *v, int index);

@@ -597,6 +597,51 @@ def mmsd_small(lib, tmp):
     return d
 
 
+def scatt_small(lib, tmp):
+    """the scatt sampler (types "AB", 3 wavevectors, two blocks of 4 samples
+    every 2 steps) on an A/B LJ liquid of 500 particles, in the default mode
+    and, on a second run with molecule indices i // 2, the 'i' mode
+    (sep_set_inter_scatt): the unwrapped x at the sample steps and the files"""
+    rng = np.random.default_rng(47)
+    x, L = cfg.fcc(5, 0.8)
+    n = len(x)
+    x = np.mod(x + rng.normal(0, 0.05, x.shape), L)
+    types = np.where(rng.random(n) < 0.4, b"B", b"A").astype("S1")
+    v = cfg.maxwell_boltzmann(n, 1.5, rng)
+    d = dict(x0=x, v0=v, L=np.asarray(L, float), types=types)
+    bind_samplers(lib)
+    cwd = os.getcwd()
+    for tag in ("a", "i"):
+        s = cfg.System(x=x.copy(), v=v.copy(), L=np.asarray(L, float), types=types.copy(), m=np.ones(n),
+                       z=np.zeros(n))
+        h = Handle(lib, s, cf=2.5, dt=0.005)
+        if tag == "i":
+            h.view["molindex"] = np.arange(n) // 2
+        run = os.path.join(tmp, "scatt_" + tag)
+        os.makedirs(run, exist_ok=True)
+        os.chdir(run)
+        xt = []
+        try:
+            smp = lib.sep_init_sampler()
+            lib.sep_add_sampler(C.byref(smp), b"scatt", h.sys, C.c_int(4), C.c_char_p(b"AB"), C.c_int(3),
+                                C.c_double(0.041))
+            if tag == "i":
+                lib.sep_set_inter_scatt(C.byref(smp))
+            for k in range(16):
+                h.step(types=b"AB")
+                lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, k)
+                if k % 2 == 0:
+                    xt.append(h.view["x"][:, 0] + h.view["crossings"][:, 0] * s.L[0])
+            lib.sep_close_sampler(C.byref(smp))
+            d[tag + "_xt"] = np.array(xt)
+            for pair in ("AA", "AB", "BB"):
+                d[tag + "_" + pair] = np.loadtxt("scatt-%s.dat" % pair)
+        finally:
+            os.chdir(cwd)
+        h.close()
+    return d
+
+
 def box_ops(lib):
     """sep_compress_box / _dir / _dir_length and sep_berendsen / _iso one at
     a time, then a Berendsen run (prgs/prg7.c) and a compression run
@@ -719,7 +764,8 @@ def main(only=()):
                          ("slit_small", lambda: slit_small(lib, tmp)),
                          ("radial_small", lambda: radial_small(lib, tmp)),
                          ("gh_small", lambda: gh_small(lib, tmp)),
-                         ("mmsd_small", lambda: mmsd_small(lib, tmp))):
+                         ("mmsd_small", lambda: mmsd_small(lib, tmp)),
+                         ("scatt_small", lambda: scatt_small(lib, tmp))):
             if only and name not in only:
                 continue
             d = fn()

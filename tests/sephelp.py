@@ -84,7 +84,8 @@ def bind_samplers(lib):
                             ("sep_sample", None, [A.PART_P, C.POINTER(A.SepSampler), A.RET_P, A.SepSys,
                                                   C.c_uint]),
                             ("sep_close_sampler", None, [C.POINTER(A.SepSampler)]),
-                            ("sep_add_mol_sampler", None, [C.POINTER(A.SepSampler), C.c_void_p])):
+                            ("sep_add_mol_sampler", None, [C.POINTER(A.SepSampler), C.c_void_p]),
+                            ("sep_set_inter_scatt", None, [C.POINTER(A.SepSampler)])):
         f = getattr(lib, name)
         f.restype, f.argtypes = res, args
     lib.sep_add_sampler.restype = None

@@ -198,3 +198,45 @@ def test_mmsd_files(gpu_lib, tmp_path):
     np.testing.assert_allclose(msd, mm.out["mmsd"], rtol=1e-9, atol=1.1e-6)
     np.testing.assert_allclose(inc, mm.out["mmsd-incoherent"], rtol=1e-9, atol=1.1e-6)
     np.testing.assert_allclose(msd[:, 1], g["mmsd"][:, 1], rtol=0.05, atol=1e-3)
+
+
+@pytest.mark.parametrize("tag", ["a", "i"])
+def test_scatt_files(gpu_lib, tmp_path, tag):
+    """the partial coherent scattering sampler (source/sepsampler.c:
+    2142-2213) on the fixture scatt_small's runs against the oracle fed the
+    device's own unwrapped positions, in the default and the 'i' mode"""
+    import ctypes as C
+    from sephelp import Handle, bind_samplers
+    g = np.load(os.path.join(HERE, "golden", "scatt_small.npz"))
+    lib = bind_samplers(gpu_lib)
+    n = len(g["types"])
+    s = cfg.System(x=g["x0"].copy(), v=g["v0"].copy(), L=g["L"].copy(), types=g["types"].copy(), m=np.ones(n),
+                   z=np.zeros(n))
+    h = Handle(lib, s, cf=2.5, dt=0.005)
+    mi = np.full(n, -1)
+    if tag == "i":
+        mi = np.arange(n) // 2
+        h.view["molindex"] = mi
+    sc = oracle.Scatt(b"AB", 4, 3, 0.041, s.L[0], float(np.prod(s.L)), opt=tag)
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        smp = lib.sep_init_sampler()
+        lib.sep_add_sampler(C.byref(smp), b"scatt", h.sys, C.c_int(4), C.c_char_p(b"AB"), C.c_int(3),
+                            C.c_double(0.041))
+        if tag == "i":
+            lib.sep_set_inter_scatt(C.byref(smp))
+        for k in range(16):
+            h.step(types=b"AB")
+            lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, k)
+            if k % 2 == 0:
+                h.sync()
+                sc.sample(h.view["x"][:, 0] + h.view["crossings"][:, 0] * s.L[0], np.ones(n), s.types, mi)
+        lib.sep_close_sampler(C.byref(smp))
+        files = {p: np.loadtxt("scatt-%s.dat" % p) for p in ("AA", "AB", "BB")}
+    finally:
+        os.chdir(cwd)
+    h.close()
+    for p in ("AA", "AB", "BB"):
+        np.testing.assert_allclose(files[p], sc.out["scatt-" + p], rtol=2e-7, atol=1.1e-6, err_msg=p)
+        np.testing.assert_allclose(files[p], g[tag + "_" + p], rtol=0, atol=1e-4, err_msg=p)
