@@ -15,11 +15,13 @@
  * momentum and energy correlations along y), "profs" (density, momentum and temperature
  * profiles of one type along z) and "radial" (pair distances histogrammed
  * per type combination), "mmsd" (molecular mean square displacement) and
- * "scatt" (partial coherent scattering functions per type pair).  They
- * write the reference's files (sacf.dat,
+ * "scatt" (partial coherent scattering functions per type pair), and
+ * "mprofs" (molecular density, momentum, temperature, spin and inertia
+ * profiles along z).  They write the reference's files (sacf.dat,
  * vacf.dat, msd.dat, msd-gaussparam.dat, msd-incoherent.dat, msd-k.dat,
  * msacf.dat, mvacf.dat, gh-*.dat, mgh-*.dat, profs.dat, radial.dat,
- * radial_info.dat, mmsd*.dat, scatt-*.dat) in the same formats.  The particle data
+ * radial_info.dat, mmsd*.dat, scatt-*.dat, mprofs.dat) in the same
+ * formats.  The particle data
  * a sample needs stays on the GPU: vacf and mvacf keep their window of
  * velocities in device memory, msd and mgh reduce on the device, so sampling
  * costs no download of the particle arrays.  Unlike the reference, mgh does
@@ -89,7 +91,8 @@ sepsampler sep_init_sampler(void);
  * in steps (int); "radial": lvec bins, sampling interval in steps (int),
  * the types (char *, 1 to 7); "mmsd": as "msd", over the molecules of a
  * molecule type; "scatt": lvec samples, the types (char *, 1 to 7), number
- * of wave vectors (int), time span (double).  The molecular samplers need sep_add_mol_sampler first. */
+ * of wave vectors (int), time span (double); "mprofs": as "profs", over
+ * the molecules of a molecule type.  The molecular samplers need sep_add_mol_sampler first. */
 void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec, ...);
 
 /* Reference include/sepsampler.h:281. */

@@ -954,3 +954,69 @@ class Scatt:
                 self.sc[c][n] += (self.p1[c][:lv - n] * self.m2[c][n:]).sum(0)
             cols = np.column_stack([np.arange(lv) * (self.tspan / lv), (self.sc[c] * fac[:, None]).real])
             self.out["scatt-" + (a + b).decode()] = cols
+
+
+def mol_spin_inertia(x, v, m, first, nuau, start, atoms, L):
+    """centres of mass (chain order, source/sepmol.c:683-729), velocities
+    (:731-748), spins and inertia tensors about the centres of mass
+    (:750-799) of every molecule"""
+    x = np.asarray(x, float); v = np.asarray(v, float); m = np.asarray(m, float); L = np.asarray(L, float)
+    cm = mol_cm_chain(x, m, first, nuau, L)
+    nmol = len(first)
+    vc = np.zeros((nmol, 3)); s = np.zeros((nmol, 3)); In = np.zeros((nmol, 3, 3)); M = np.zeros(nmol)
+    for n in range(nmol):
+        idx = np.asarray(atoms[start[n]:start[n + 1]])
+        mi = m[idx]
+        M[n] = mi.sum()
+        vc[n] = (v[idx] * mi[:, None]).sum(0) / M[n]
+        d = _wrap(x[idx] - cm[n], L)
+        s[n] = np.cross(d, v[idx] * mi[:, None]).sum(0)
+        In[n, 0, 0] = (mi * (d[:, 1] ** 2 + d[:, 2] ** 2)).sum()
+        In[n, 1, 1] = (mi * (d[:, 0] ** 2 + d[:, 2] ** 2)).sum()
+        In[n, 2, 2] = (mi * (d[:, 0] ** 2 + d[:, 1] ** 2)).sum()
+        In[n, 0, 1] = In[n, 1, 0] = -(mi * d[:, 0] * d[:, 1]).sum()
+        In[n, 0, 2] = In[n, 2, 0] = -(mi * d[:, 0] * d[:, 2]).sum()
+        In[n, 1, 2] = In[n, 2, 1] = -(mi * d[:, 1] * d[:, 2]).sum()
+    return cm, vc, s, In, M
+
+
+class MProfs:
+    """the mprofs sampler (source/sepsampler.c:1571-1666) with the
+    reference's fixed directions (bins along z, momentum of v_x, angular
+    velocity's y component); `lines` holds mprofs.dat's lines after every
+    100th sample"""
+
+    def __init__(self, lvec):
+        self.lvec = lvec
+        self.acc = np.zeros((lvec, 16))
+        self.nsample = 0
+        self.lines = None
+
+    def sample(self, cm, vc, s, In, M, sel, L):
+        L = np.asarray(L, float)
+        dl = L[2] / self.lvec
+        for n in np.nonzero(np.asarray(sel))[0]:
+            b = min(int(cm[n, 2] / dl), self.lvec - 1)
+            t = M[n] * (vc[n, 1] ** 2 + vc[n, 2] ** 2)
+            self.acc[b] += np.concatenate([[M[n] * vc[n, 0], M[n], 1.0], s[n], [t], In[n].ravel()])
+        self.nsample += 1
+        if self.nsample % 100:
+            return
+        dV = L[0] * L[1] * dl
+        fac = 1 / (self.nsample * dV)
+        out = []
+        for n in range(self.lvec):
+            q = self.acc[n]
+            x = (n + 0.5) * dl
+            if q[2] > 0:
+                a, b = q[1] * fac, q[0] * fac
+                c = q[6] / (2 * self.nsample * (q[2] / self.nsample))
+                spin = q[3:6] * fac
+                In_ = (q[7:16] * fac).reshape(3, 3)
+                w = np.linalg.solve(In_, spin)
+                out.append("%e %e %e %e %e " % (x, a, b / a, c, w[1]) +
+                           "%e %e %e %e %e %e %e %e %e %e %e %e" % (tuple(spin) + tuple(In_.ravel())))
+            else:
+                out.append("%e %e %e %e %e %e " % (x, 0.0, 0.0, 0.0, 0.0, 0.0) +
+                           "%e %e % e%e %e %e %e %e %e %e %e %e" % ((0.0,) * 12))
+        self.lines = out

@@ -555,3 +555,95 @@ extern "C" int sepdev_mmsd_sample(sepdev *d, sepdev_moltab *t, sepdev_mmsd *m, c
 	CK(cudaStreamSynchronize(d->st));
 	return SEPDEV_OK;
 }
+
+// ---- molecular profiles (source/sepsampler.c:1571-1666) -------------------------
+//
+// Per molecule of the sampled type: the centre of mass (chain order, as
+// the reference's sep_mol_spin takes it), velocity, spin about the centre
+// of mass and inertia tensor; binned by the centre of mass along dir into
+// 64-bit fixed-point sums (2^-32 units), so the order of the atomics does
+// not matter: m v[dirvel], m, count, s (3), m v^2 over the other two
+// components, the inertia tensor (9, row-major).
+
+#define MPF 16
+
+__global__ void __launch_bounds__(MSB) k_mprofs(int nmol, const int *first, const int *nuau, const int *start,
+						 const int *atoms, const double *mass, const int *inv, const int4 *pos,
+						 const uint4 *xlo, const float4 *vhi, const float4 *vlo, double L0,
+						 double L1, double L2, const unsigned char *sel, int dir, int dirvel,
+						 int lvec, unsigned long long *hist)
+{
+	const int m = blockIdx.x * MSB + threadIdx.x;
+	if (m >= nmol || !sel[m]) return;
+	const double L[3] = {L0, L1, L2};
+	double cm[3];
+	for (int k = 0; k < 3; k++) cm[k] = mol_cm_k(m, k, first, nuau, mass, pos, xlo, inv, vhi, L[k]);
+	double v[3] = {0.0, 0.0, 0.0}, s[3] = {0.0, 0.0, 0.0}, I[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+	for (int q = start[m]; q < start[m + 1]; q++) {
+		const int sl = inv[atoms[q]];
+		const int4 p = pos[sl];
+		const uint4 l = xlo[sl];
+		const float4 vh = vhi[sl], vl = vlo[sl];
+		const double ma = (double)vh.w;
+		const double va[3] = {(double)vh.x + (double)vl.x, (double)vh.y + (double)vl.y,
+				      (double)vh.z + (double)vl.z};
+		double d[3];
+		for (int k = 0; k < 3; k++) {
+			double r = coord(p, l, k, L[k]) - cm[k];
+			if (r > 0.5 * L[k]) r -= L[k];
+			else if (r < -0.5 * L[k]) r += L[k];
+			d[k] = r;
+			v[k] += va[k] * ma;
+		}
+		const double pm[3] = {va[0] * ma, va[1] * ma, va[2] * ma};
+		s[0] += d[1] * pm[2] - d[2] * pm[1];
+		s[1] += d[2] * pm[0] - d[0] * pm[2];
+		s[2] += d[0] * pm[1] - d[1] * pm[0];
+		I[0] += ma * (d[1] * d[1] + d[2] * d[2]);
+		I[4] += ma * (d[0] * d[0] + d[2] * d[2]);
+		I[8] += ma * (d[0] * d[0] + d[1] * d[1]);
+		I[1] -= ma * d[0] * d[1];
+		I[2] -= ma * d[0] * d[2];
+		I[5] -= ma * d[1] * d[2];
+	}
+	I[3] = I[1]; I[6] = I[2]; I[7] = I[5];
+	const double M = mass[m];
+	for (int k = 0; k < 3; k++) v[k] /= M;
+	const double dl = L[dir] / lvec;
+	int b = (int)(cm[dir] / dl);
+	b = b < 0 ? 0 : (b >= lvec ? lvec - 1 : b);
+	double t = 0.0;
+	for (int k = 0; k < 3; k++)
+		if (k != dirvel) t += M * v[k] * v[k];
+	const double val[MPF] = {M * v[dirvel], M, 1.0, s[0], s[1], s[2], t,
+				 I[0], I[1], I[2], I[3], I[4], I[5], I[6], I[7], I[8]};
+	for (int q = 0; q < MPF; q++)
+		atomicAdd(&hist[(long)b * MPF + q], (unsigned long long)llrint(ldexp(val[q], 32)));
+}
+
+// sel (host, nmol): the molecules of the sampled type; out (host, lvec x 16)
+extern "C" int sepdev_mprofs(sepdev *d, sepdev_moltab *t, const unsigned char *sel, int dir, int dirvel, int lvec,
+			     double *out)
+{
+	if (dir < 0 || dir > 2 || dirvel < 0 || dirvel > 2 || lvec < 1) return SEPDEV_EINVAL;
+	unsigned long long *hist = NULL;
+	unsigned char *dsel = NULL;
+	cudaError_t e = cudaMalloc((void **)&hist, sizeof(long long) * MPF * lvec);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&dsel, t->nmol);
+	if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, sizeof(long long) * MPF * lvec, d->st);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(dsel, sel, t->nmol, cudaMemcpyHostToDevice, d->st);
+	if (e != cudaSuccess) { cudaFree(hist); cudaFree(dsel); sepdev_set_error("mprofs", e); return SEPDEV_ECUDA; }
+	k_mprofs<<<t->nblk, MSB, 0, d->st>>>(t->nmol, t->first, t->nuau, t->start, t->atoms, t->mass, d->inv,
+					     d->pos[d->cur], d->xlo, d->vhi, d->vlo, d->L[0], d->L[1], d->L[2], dsel,
+					     dir, dirvel, lvec, hist);
+	CKL(d);
+	long long *h = (long long *)malloc(sizeof(long long) * MPF * lvec);
+	if (!h) { cudaFree(hist); cudaFree(dsel); return SEPDEV_ENOMEM; }
+	e = cudaMemcpyAsync(h, hist, sizeof(long long) * MPF * lvec, cudaMemcpyDeviceToHost, d->st);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(d->st);
+	cudaFree(hist); cudaFree(dsel);
+	if (e != cudaSuccess) { free(h); sepdev_set_error("mprofs", e); return SEPDEV_ECUDA; }
+	for (int k = 0; k < MPF * lvec; k++) out[k] = ldexp((double)h[k], -32);
+	free(h);
+	return SEPDEV_OK;
+}

@@ -5,7 +5,8 @@
  * Control flow, sampling intervals, normalisations and output files follow
  * the reference (source/sepsampler.c:4-242 dispatch, :280-351 sacf,
  * :361-470 radial, :471-641 msd, :658-714 vacf, :725-818 msacf, :822-1105
- * gh, :1110-1410 mgh, :1418-1510 profs, :1757-1825 mvacf, :1918-2051 mmsd,
+ * gh, :1110-1410 mgh, :1418-1510 profs, :1531-1666 mprofs, :1757-1825 mvacf,
+ * :1918-2051 mmsd,
  * :2055-2213 scatt).  The stress autocorrelations work on the sepret values the host
  * already has (the molecular one through sep_mol_pressure_tensor); vacf,
  * msd, mvacf and mgh keep their particle data on the GPU (dev_sampler.cu,
@@ -90,6 +91,17 @@ struct sepscatt {
 	double complex *p1, *m2;   /* ncomb x lvec x nk */
 	double complex *sc;        /* ncomb x lvec x nk */
 	double *out;               /* nk x 28, scratch */
+};
+
+struct sepmprofs {
+	int lvec, isample, dir, dirvel, diramom, nmol;
+	long nsample;
+	char type;
+	double *acc;           /* lvec x 16 accumulated sums */
+	double *out;           /* lvec x 16, scratch */
+	unsigned char *sel;    /* nmol, scratch */
+	sepdev_moltab *tab;
+	rt_ctx *ctx;
 };
 
 struct sepradial {
@@ -402,6 +414,26 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 			sptr->scatt[0] = p;
 			sptr->flag_scatt = 1;
 		}
+	} else if (strcmp(sampler, "mprofs") == 0) {
+		if (sptr->flag_mprofs != 1) {
+			const char type = (char)va_arg(args, int);
+			const int isample = va_arg(args, int);
+			struct sepmprofs *p = xcalloc(1, sizeof *p);
+			p->lvec = lvec;
+			p->isample = isample;
+			p->type = type;
+			/* the reference's fixed choice: profiles along z of v_x, the
+			 * angular velocity's y component */
+			p->dir = 2;
+			p->dirvel = 0;
+			p->diramom = 1;
+			p->nmol = (int)sys.molptr->num_mols;
+			p->acc = xcalloc(16 * (size_t)lvec, sizeof(double));
+			p->out = xcalloc(16 * (size_t)lvec, sizeof(double));
+			p->sel = xcalloc(p->nmol > 0 ? p->nmol : 1, 1);
+			sptr->mprofs = p;
+			sptr->flag_mprofs = 1;
+		}
 	} else if (strcmp(sampler, "mvacf") == 0) {
 		if (sptr->flag_mvacf != 1) {
 			const double tsample = va_arg(args, double);
@@ -416,7 +448,7 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 	} else {
 		va_end(args);
 		sep_error("%s: sampler %s is not provided by this GPU implementation "
-			  "(available: sacf, vacf, msd, msacf, mvacf, gh, mgh, profs, radial, mmsd, scatt)", __func__,
+			  "(available: sacf, vacf, msd, msacf, mvacf, gh, mgh, profs, mprofs, radial, mmsd, scatt)", __func__,
 			  sampler);
 	}
 	va_end(args);
@@ -911,6 +943,77 @@ static void scatt_sample(struct sepscatt *p, seppart *pptr, sepsys sys)
 		}
 }
 
+/* w solving in w = s by Gaussian elimination with partial pivoting */
+static void solve3(double w[3], const double s[3], const double in[9])
+{
+	double a[3][4];
+	for (int r = 0; r < 3; r++) {
+		for (int c = 0; c < 3; c++) a[r][c] = in[3 * r + c];
+		a[r][3] = s[r];
+	}
+	for (int c = 0; c < 3; c++) {
+		int piv = c;
+		for (int r = c + 1; r < 3; r++)
+			if (fabs(a[r][c]) > fabs(a[piv][c])) piv = r;
+		if (piv != c)
+			for (int k = 0; k < 4; k++) { const double t = a[c][k]; a[c][k] = a[piv][k]; a[piv][k] = t; }
+		for (int r = c + 1; r < 3; r++) {
+			const double f = a[r][c] / a[c][c];
+			for (int k = c; k < 4; k++) a[r][k] -= f * a[c][k];
+		}
+	}
+	for (int r = 2; r >= 0; r--) {
+		double t = a[r][3];
+		for (int k = r + 1; k < 3; k++) t -= a[r][k] * w[k];
+		w[r] = t / a[r][r];
+	}
+}
+
+/* ---- mprofs: source/sepsampler.c:1571-1666 ----
+ * The bin of a molecule is floor(x_cm / dl), the last bin for a centre at
+ * the box edge (where the reference ends the program). */
+static void mprofs_sample(struct sepmprofs *p, seppart *pptr, sepmol *mols, sepsys sys)
+{
+	rt_ctx *c = sampler_ctx(pptr, &sys);
+	mol_tables(&p->tab, &p->ctx, c, mols, &sys);
+	for (int n = 0; n < p->nmol; n++) p->sel[n] = mols[n].type == p->type;
+	rt_check(sepdev_mprofs(c->dev, p->tab, p->sel, p->dir, p->dirvel, p->lvec, p->out), "mprofs");
+	for (int k = 0; k < 16 * p->lvec; k++) p->acc[k] += p->out[k];
+	p->nsample++;
+	if (p->nsample % 100 != 0) return;
+	const int dir = p->dir;
+	const double dl = sys.length[dir] / p->lvec;
+	double dV;
+	if (dir == 0) dV = dl * sys.length[1] * sys.length[2];
+	else if (dir == 1) dV = sys.length[0] * dl * sys.length[2];
+	else dV = sys.length[0] * sys.length[1] * dl;
+	FILE *f = fopen("mprofs.dat", "w");
+	if (!f) sep_error("%s: Couldn't open file", __func__);
+	const double fac = 1 / (p->nsample * dV);
+	for (int n = 0; n < p->lvec; n++) {
+		const double *q = p->acc + 16 * (size_t)n;
+		const double x = (n + 0.5) * dl;
+		if (q[2] > 0) {
+			const double a = q[1] * fac, b = q[0] * fac;
+			const double av_numb = q[2] / p->nsample;
+			const double tc = q[6] / (2 * p->nsample * av_numb);
+			double spin[3], in[9], w[3] = {0.0, 0.0, 0.0};
+			for (int k = 0; k < 3; k++) spin[k] = q[3 + k] * fac;
+			for (int k = 0; k < 9; k++) in[k] = q[7 + k] * fac;
+			solve3(w, spin, in);
+			fprintf(f, "%e %e %e %e %e ", x, a, b / a, tc, w[p->diramom]);
+			fprintf(f, "%e %e %e %e %e %e %e %e %e %e %e %e\n", spin[0], spin[1], spin[2], in[0], in[1],
+				in[2], in[3], in[4], in[5], in[6], in[7], in[8]);
+		} else {
+			/* the reference's empty-bin line, spacing included */
+			fprintf(f, "%e %e %e %e %e %e ", x, 0.0, 0.0, 0.0, 0.0, 0.0);
+			fprintf(f, "%e %e % e%e %e %e %e %e %e %e %e %e\n", 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0,
+				0.0, 0.0, 0.0);
+		}
+	}
+	fclose(f);
+}
+
 /* ---- radial: source/sepsampler.c:396-461 ---- */
 static void radial_sample(struct sepradial *p, seppart *pptr, sepsys sys)
 {
@@ -955,6 +1058,8 @@ void sep_sample(seppart *pptr, sepsampler *sptr, sepret *ret, sepsys sys, unsign
 	if (sptr->flag_gh == 1 && n % sptr->gh->isample == 0) gh_sample(sptr->gh, pptr, sys);
 	if (sptr->flag_mgh == 1 && n % sptr->mgh->isample == 0) mgh_sample(sptr->mgh, pptr, sptr->molptr, sys);
 	if (sptr->flag_profs == 1 && n % sptr->profs->isample == 0) profs_sample(sptr->profs, pptr, sys);
+	if (sptr->flag_mprofs == 1 && n % sptr->mprofs->isample == 0)
+		mprofs_sample(sptr->mprofs, pptr, sptr->molptr, sys);
 	if (sptr->flag_mvacf == 1 && n % sptr->mvacf->isample == 0)
 		mvacf_sample(sptr->mvacf, pptr, sptr->molptr, sys);
 	if (sptr->flag_radial == 1 && n % sptr->radial->isample == 0) radial_sample(sptr->radial, pptr, sys);
@@ -985,6 +1090,12 @@ void sep_close_sampler(sepsampler *ptr)
 		free(ptr->vacf->vacf);
 		free(ptr->vacf->block);
 		free(ptr->vacf);
+	}
+	if (ptr->flag_mprofs == 1) {
+		struct sepmprofs *p = ptr->mprofs;
+		if (p->tab) sepdev_moltab_destroy(p->tab);
+		free(p->acc); free(p->out); free(p->sel);
+		free(p);
 	}
 	if (ptr->flag_scatt == 1) {
 		struct sepscatt *p = ptr->scatt[0];

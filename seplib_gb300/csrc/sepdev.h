@@ -321,6 +321,12 @@ int sepdev_mmsd_create(sepdev *d, sepdev_moltab *t, int nk, const double *k, sep
 void sepdev_mmsd_destroy(sepdev_mmsd *m);
 int sepdev_mmsd_sample(sepdev *d, sepdev_moltab *t, sepdev_mmsd *m, const unsigned char *sel, int reset,
 		       double *out);
+/* Molecular profiles: over the molecules marked in sel (host, nmol),
+ * binned by the centre of mass along dir into lvec bins, out[16 b + q]
+ * (host) = sum m v[dirvel], m, count, spin (3), m v^2 over the other two
+ * components, inertia tensor (9, row-major). */
+int sepdev_mprofs(sepdev *d, sepdev_moltab *t, const unsigned char *sel, int dir, int dirvel, int lvec,
+		  double *out);
 /* Molecular Berendsen step along z: each molecule's centre-of-mass z is
  * scaled by `scale` and its atoms keep their offsets from it, the box edge
  * L_z becomes L1z; atoms outside molecules keep their absolute z. */

@@ -642,6 +642,38 @@ def scatt_small(lib, tmp):
     return d
 
 
+def mprofs_small(lib, tmp):
+    """the mprofs sampler (40 bins, type A, every step) sampled 100 times on
+    one state of 216 water-like molecules (layered, so some bins are empty):
+    the state and the file's lines"""
+    s = cfg.water_like(nmol=216, rho=0.09, seed=9)
+    top = os.path.join(tmp, "mp.top")
+    cfg.write_top(top, s)
+    h = Handle(lib, s, cf=3.0, update=A.SEP_LLIST_NEIGHBLIST, dt=0.0005)
+    lib.sep_read_topology_file(h.atoms, top.encode(), C.byref(h.sys), b"q")
+    mols = lib.sep_init_mol(h.atoms, C.byref(h.sys))
+    bind_samplers(lib)
+    cwd = os.getcwd()
+    run = os.path.join(tmp, "mprofs")
+    os.makedirs(run, exist_ok=True)
+    os.chdir(run)
+    try:
+        smp = lib.sep_init_sampler()
+        lib.sep_add_mol_sampler(C.byref(smp), C.cast(mols, C.c_void_p))
+        lib.sep_add_sampler(C.byref(smp), b"mprofs", h.sys, C.c_int(40), C.c_int(ord("A")), C.c_int(1))
+        for k in range(100):
+            lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, k)
+        lib.sep_close_sampler(C.byref(smp))
+        d = dict(x=s.x, v=s.v, L=s.L, z=s.z, m=s.m, types=s.types.astype("S1"), bonds=s.bonds,
+                 angles=s.angles, molindex=h.view["molindex"].copy(), nmol=h.sys.molptr.contents.num_mols,
+                 lines=np.array(open("mprofs.dat").read().splitlines()))
+    finally:
+        os.chdir(cwd)
+    lib.sep_free_mol(mols, C.byref(h.sys))
+    h.close()
+    return d
+
+
 def box_ops(lib):
     """sep_compress_box / _dir / _dir_length and sep_berendsen / _iso one at
     a time, then a Berendsen run (prgs/prg7.c) and a compression run
@@ -765,7 +797,8 @@ def main(only=()):
                          ("radial_small", lambda: radial_small(lib, tmp)),
                          ("gh_small", lambda: gh_small(lib, tmp)),
                          ("mmsd_small", lambda: mmsd_small(lib, tmp)),
-                         ("scatt_small", lambda: scatt_small(lib, tmp))):
+                         ("scatt_small", lambda: scatt_small(lib, tmp)),
+                         ("mprofs_small", lambda: mprofs_small(lib, tmp))):
             if only and name not in only:
                 continue
             d = fn()

@@ -240,3 +240,48 @@ def test_scatt_files(gpu_lib, tmp_path, tag):
     for p in ("AA", "AB", "BB"):
         np.testing.assert_allclose(files[p], sc.out["scatt-" + p], rtol=2e-7, atol=1.1e-6, err_msg=p)
         np.testing.assert_allclose(files[p], g[tag + "_" + p], rtol=0, atol=1e-4, err_msg=p)
+
+
+def test_mprofs_file(gpu_lib, tmp_path):
+    """molecular profiles (source/sepsampler.c:1571-1666) of the fixture
+    mprofs_small's state on the device against the reference's lines and the
+    oracle on the device's own state"""
+    import ctypes as C
+    from seplib_gb300 import sepapi as A
+    from sephelp import Handle, bind_samplers
+    from test_oracle_mprofs import compare_lines
+    g = np.load(os.path.join(HERE, "golden", "mprofs_small.npz"))
+    lib = bind_samplers(gpu_lib)
+    s = cfg.System(x=g["x"].copy(), v=g["v"].copy(), L=g["L"].copy(), types=g["types"].copy(), m=g["m"].copy(),
+                   z=g["z"].copy(), bonds=g["bonds"], angles=g["angles"])
+    top = str(tmp_path / "mp.top")
+    cfg.write_top(top, s)
+    h = Handle(lib, s, cf=3.0, update=A.SEP_LLIST_NEIGHBLIST, dt=0.0005)
+    lib.sep_read_topology_file(h.atoms, top.encode(), C.byref(h.sys), b"q")
+    mols = lib.sep_init_mol(h.atoms, C.byref(h.sys))
+    # put the particles on the device
+    lib.sep_reset_force(h.atoms, C.byref(h.sys))
+    lib.sep_force_pairs(h.atoms, b"OO", 2.5, h.fun(), C.byref(h.sys), C.byref(h.ret), A.SEP_EXCL_SAME_MOL)
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        smp = lib.sep_init_sampler()
+        lib.sep_add_mol_sampler(C.byref(smp), C.cast(mols, C.c_void_p))
+        lib.sep_add_sampler(C.byref(smp), b"mprofs", h.sys, C.c_int(40), C.c_int(ord("A")), C.c_int(1))
+        for k in range(100):
+            lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, k)
+        lib.sep_close_sampler(C.byref(smp))
+        lines = open("mprofs.dat").read().splitlines()
+    finally:
+        os.chdir(cwd)
+    h.sync()
+    nm = int(g["nmol"])
+    first, nuau, start, atoms = oracle.mol_tables(h.view["molindex"], nm)
+    cm, vc, sp, In, M = oracle.mol_spin_inertia(h.view["x"], h.view["v"], s.m, first, nuau, start, atoms, s.L)
+    mp = oracle.MProfs(40)
+    for _ in range(100):
+        mp.sample(cm, vc, sp, In, M, np.ones(nm, bool), s.L)
+    lib.sep_free_mol(mols, C.byref(h.sys))
+    h.close()
+    assert compare_lines(lines, mp.lines) >= 6
+    assert compare_lines(lines, list(g["lines"])) >= 6
