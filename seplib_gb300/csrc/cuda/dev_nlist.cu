@@ -228,8 +228,12 @@ __device__ __forceinline__ float warp_max_f(float v, unsigned mask)
 // WRAPFAST: runs whose region wraps around the box (small boxes: the batched
 // systems) also get the branch-free test loop; without it they take the
 // general loop, which keeps the common in-box loop's code tight.
-template <bool WRAPFAST>
-__device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, float4 *sp, int *ring)
+// MOLX (same-molecule exclusions): the candidates' molecule indices are
+// staged in spm beside their positions, and in-box runs take a branch-free
+// loop that tests them from shared memory.
+template <bool WRAPFAST, bool MOLX = false>
+__device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, float4 *sp, int *ring,
+					   int *spm = nullptr)
 {
 	const unsigned FULL = 0xffffffffu;
 	const int lane = threadIdx.x & 31;
@@ -278,7 +282,18 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 		const int span = __reduce_max_sync(FULL, act ? cnt - flushed : 0);
 		if (span + fill > BT_RING) flush();
 		if (me) {
-			if (local && a.excl == SEPDEV_EXCL_NONE) {
+			if (MOLX && local) {
+#pragma unroll 4
+				for (int c = 0; c < fill; c++) {
+					const float4 q = sp[c];
+					const float dx = mx - q.x, dy = my - q.y, dz = mz - q.z;
+					const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+					const int j = __float_as_int(q.w);
+					const bool hit = (r2 < a.rl2) & (j != (int)i) & !((mi != -1) & (mi == spm[c]));
+					ring[(cnt & (BT_RING - 1)) * 32 + lane] = j;
+					cnt += hit ? 1 : 0;
+				}
+			} else if (local && a.excl == SEPDEV_EXCL_NONE) {
 #pragma unroll 4
 				for (int c = 0; c < fill; c++) {
 					const float4 q = sp[c];
@@ -385,7 +400,11 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 							}
 						}
 						const unsigned kb = __ballot_sync(FULL, keep);
-						if (keep) sp[fill + __popc(kb & ((1u << lane) - 1u))] = q;
+						if (keep) {
+							const int slot = fill + __popc(kb & ((1u << lane) - 1u));
+							sp[slot] = q;
+							if (MOLX) spm[slot] = a.mol[jj + lane];
+						}
 						fill += __popc(kb);
 					}
 				}
@@ -409,6 +428,17 @@ __global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles(long n, BuildArgs
 	__shared__ int ring_all[BT_WARPS][BT_RING * 32];
 	const int w = threadIdx.x >> 5;
 	build_tile<false>(n, a, ((long)blockIdx.x * BT_WARPS + w) * 32, sp_all[w], ring_all[w]);
+}
+
+// Same-molecule exclusions (the butane-type workloads): molecule indices
+// staged with the candidates.
+__global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles_mol(long n, BuildArgs a)
+{
+	__shared__ float4 sp_all[BT_WARPS][BT_CAP];
+	__shared__ int spm_all[BT_WARPS][BT_CAP];
+	__shared__ int ring_all[BT_WARPS][BT_RING * 32];
+	const int w = threadIdx.x >> 5;
+	build_tile<false, true>(n, a, ((long)blockIdx.x * BT_WARPS + w) * 32, sp_all[w], ring_all[w], spm_all[w]);
 }
 
 // Batched systems: each warp builds its tile with its own system's cell grid
@@ -494,7 +524,10 @@ static int grow(sepdev *d, void **p, size_t bytes, size_t *cap)
 static int launch_build(sepdev *d, const BuildArgs &a)
 {
 	const int grid = grid_for((d->n + 31) / 32, BT_WARPS);
-	k_build_tiles<<<grid, BT_WARPS * 32, 0, d->st>>>(d->n, a);
+	if (a.excl == SEPDEV_EXCL_SAMEMOL)
+		k_build_tiles_mol<<<grid, BT_WARPS * 32, 0, d->st>>>(d->n, a);
+	else
+		k_build_tiles<<<grid, BT_WARPS * 32, 0, d->st>>>(d->n, a);
 	CKL(d);
 	return SEPDEV_OK;
 }
