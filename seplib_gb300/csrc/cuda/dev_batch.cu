@@ -114,19 +114,20 @@ __global__ void kb_scatter(const int *wsys, int nwarps, const unsigned *flag, co
 	perm[start[cellof[t]] + celloff[t]] = (int)t;
 }
 
-// a warp per cell: members ordered by their index in the system
-// (dev_cellsort.cuh); launched with 256 threads
+// a warp per cell: members ordered by x, ties by their index in the
+// system (dev_cellsort.cuh); launched with 256 threads
 __global__ void __launch_bounds__(256) kb_cellsort(long ncells, const int *csys, const unsigned *flag,
-						   const int *start, const int *gid, int *perm)
+						   const int *start, const int *gid, const int4 *pos, int *perm)
 {
-	__shared__ int sk[8][CS_MAX], sv[8][CS_MAX];
+	__shared__ unsigned long long sk[8][CS_MAX];
+	__shared__ int sv[8][CS_MAX];
 	const long c = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
 	if (c >= ncells) return;
 	const int s = csys[c];
 	if (s < 0 || !flag[s]) return;
 	const int w = threadIdx.x >> 5;
 	const int lo = start[c];
-	cell_sort_warp(lo, start[c + 1] - lo, gid, perm, sk[w], sv[w]);
+	cell_sort_warp(lo, start[c + 1] - lo, gid, pos, perm, sk[w], sv[w]);
 }
 
 struct BGather {
@@ -553,7 +554,7 @@ int batch_cells_launch(sepb *b, int parity)
 	kb_scatter<<<grid_for(nt, B), B, 0, d->st>>>(b->wsys, b->nwarps, b->flag, d->cellof, d->celloff,
 						    b->cellstart, d->perm);
 	kb_cellsort<<<grid_for(b->ncells * 32, B), B, 0, d->st>>>(b->ncells, b->csys, b->flag, b->cellstart,
-								 d->gid, d->perm);
+								 d->gid, d->pos[parity], d->perm);
 	CKL(d);
 	return SEPDEV_OK;
 }
@@ -570,7 +571,7 @@ int batch_rebuild_launch(sepb *b, int parity)
 	kb_scatter<<<grid_for(nt, B), B, 0, d->st>>>(b->wsys, b->nwarps, b->flag, d->cellof, d->celloff,
 						    b->cellstart, d->perm);
 	kb_cellsort<<<grid_for(b->ncells * 32, B), B, 0, d->st>>>(b->ncells, b->csys, b->flag, b->cellstart,
-								 d->gid, d->perm);
+								 d->gid, d->pos[parity], d->perm);
 	BGather g = gather_args(b, parity);
 	kb_gather<<<grid_for(nt, B), B, 0, d->st>>>(g);
 	kb_copyback<<<grid_for(nt, B), B, 0, d->st>>>(g);

@@ -462,16 +462,18 @@ __global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles_batch(BuildArgs a
 }
 
 // Deterministic order inside each cell: one warp per cell ranks its members
-// by user index (dev_cellsort.cuh).  Launched with 256 threads.
+// by x, ties by user index (dev_cellsort.cuh).  Launched with 256 threads.
 __global__ void __launch_bounds__(256) k_cellsort_w(long m, const int *__restrict__ start,
-						    const int *__restrict__ gid, int *__restrict__ perm)
+						    const int *__restrict__ gid, const int4 *__restrict__ pos,
+						    int *__restrict__ perm)
 {
-	__shared__ int sk[8][CS_MAX], sv[8][CS_MAX];
+	__shared__ unsigned long long sk[8][CS_MAX];
+	__shared__ int sv[8][CS_MAX];
 	const long c = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
 	if (c >= m) return;
 	const int w = threadIdx.x >> 5;
 	const int lo = start[c];
-	cell_sort_warp(lo, start[c + 1] - lo, gid, perm, sk[w], sv[w]);
+	cell_sort_warp(lo, start[c + 1] - lo, gid, pos, perm, sk[w], sv[w]);
 }
 
 // Copy the gathered arrays back into the primary buffers, so buffer
@@ -570,7 +572,8 @@ int sepdev_sort_async(sepdev *d, int parity, int trigger)
 	CKL(d);
 	k_scatter<<<grid_for(n, B), B, 0, d->st>>>(n, d->cellof, d->celloff, d->cellstart, d->perm);
 	CKL(d);
-	k_cellsort_w<<<grid_for(d->ncells * 32, B), B, 0, d->st>>>(d->ncells, d->cellstart, d->gid, d->perm);
+	k_cellsort_w<<<grid_for(d->ncells * 32, B), B, 0, d->st>>>(d->ncells, d->cellstart, d->gid, d->pos[parity],
+								  d->perm);
 	CKL(d);
 	GatherArgs g;
 	const int o = parity ^ 1;
