@@ -17,7 +17,8 @@
  * per type combination), "mmsd" (molecular mean square displacement) and
  * "scatt" (partial coherent scattering functions per type pair), and
  * "mprofs" (molecular density, momentum, temperature, spin and inertia
- * profiles along z).  They write the reference's files (sacf.dat,
+ * profiles along z) and "mavacf" (the reference's molecular end-to-end
+ * dipole-like quantity, autocorrelated).  They write the reference's files (sacf.dat,
  * vacf.dat, msd.dat, msd-gaussparam.dat, msd-incoherent.dat, msd-k.dat,
  * msacf.dat, mvacf.dat, gh-*.dat, mgh-*.dat, profs.dat, radial.dat,
  * radial_info.dat, mmsd*.dat, scatt-*.dat, mprofs.dat) in the same
@@ -81,7 +82,8 @@ typedef struct {
 /* Reference include/sepsampler.h:247. */
 sepsampler sep_init_sampler(void);
 
-/* Reference include/sepsampler.h:275: "sacf", "vacf", "msacf", "mvacf":
+/* Reference include/sepsampler.h:275: "sacf", "vacf", "msacf", "mvacf",
+ * "mavacf":
  * lvec samples over a time span (double); "gh": lvec samples over a time
  * span (double), number of wave vectors (int); "msd": lvec samples (0:
  * log-spaced) over a time span (double), number of wave vectors (int),

@@ -1020,3 +1020,40 @@ class MProfs:
                 out.append("%e %e %e %e %e %e " % (x, 0.0, 0.0, 0.0, 0.0, 0.0) +
                            "%e %e % e%e %e %e %e %e %e %e %e %e" % ((0.0,) * 12))
         self.lines = out
+
+
+class MAVACF:
+    """the mavacf sampler (source/sepsampler.c:1853-1906): per molecule of
+    type A the y component of the end-to-end vector (atom 0 to atom b, b =
+    the first molecule's atom count - 1; minimum image) times the first
+    particle's |charge| times the molecule mass (others 0), correlated over
+    blocks like mvacf; times at (k + 1/2) dt_sample"""
+
+    def __init__(self, lvec, dtsample):
+        self.lvec, self.dts = lvec, dtsample
+        self.acf = np.zeros(lvec)
+        self.i, self.nsample, self.rows = 0, 0, None
+        self.out = None
+
+    def sample(self, x, molidx, M, sel, q, Ly):
+        x = np.asarray(x, float)
+        b = len(molidx[0]) - 1
+        val = np.zeros(len(molidx))
+        for n, idx in enumerate(molidx):
+            if sel[n]:
+                r = x[idx[0], 1] - x[idx[min(b, len(idx) - 1)], 1]
+                r = r - Ly if r > 0.5 * Ly else (r + Ly if r < -0.5 * Ly else r)
+                val[n] = r * q * M[n]
+        if self.rows is None:
+            self.rows = np.zeros((self.lvec, len(molidx)))
+        self.rows[self.i] = val
+        self.i += 1
+        if self.i < self.lvec:
+            return
+        lv = self.lvec
+        for k in range(lv):
+            self.acf[k] += (self.rows[:lv - k] * self.rows[k:]).sum()
+        self.nsample += 1
+        fac = 1.0 / ((lv - np.arange(lv)) * len(molidx) * self.nsample)
+        self.out = np.column_stack([(np.arange(lv) + 0.5) * self.dts, self.acf * fac])
+        self.i = 0

@@ -647,3 +647,48 @@ extern "C" int sepdev_mprofs(sepdev *d, sepdev_moltab *t, const unsigned char *s
 	free(h);
 	return SEPDEV_OK;
 }
+
+// ---- mavacf (source/sepsampler.c:1853-1906) ----------------------------------------
+//
+// The reference's sampled quantity: for each molecule of type A, the y
+// component of the end-to-end vector from its atom 0 to its atom b (b the
+// first molecule's atom count - 1; minimum image, source/sepmol.c:1106-1124)
+// times the first particle's |charge| times the molecule mass; molecules of
+// other types give 0.  A molecule with fewer atoms takes its last one.
+
+__global__ void k_mol_ete_y(int nmol, const int *start, const int *atoms, const int *inv, const int4 *pos,
+			    const uint4 *xlo, const double *mass, const unsigned char *sel, int b, double Ly,
+			    double q, double *row)
+{
+	const int m = blockIdx.x * blockDim.x + threadIdx.x;
+	if (m >= nmol) return;
+	if (!sel[m]) { row[m] = 0.0; return; }
+	const int last = start[m + 1] - 1;
+	const int sa = inv[atoms[start[m]]], sb = inv[atoms[min(start[m] + b, last)]];
+	double r = __dsub_rn(from_fixed_dev((unsigned)pos[sa].y, xlo[sa].y, Ly),
+			     from_fixed_dev((unsigned)pos[sb].y, xlo[sb].y, Ly));
+	if (r > 0.5 * Ly) r = __dsub_rn(r, Ly);
+	else if (r < -0.5 * Ly) r = __dadd_rn(r, Ly);
+	row[m] = r * q * mass[m];
+}
+
+// sel (host, nmol): the molecules of type A; q: |charge| of particle 0
+extern "C" int sepdev_mavacf_store(sepdev *d, sepdev_moltab *t, sepdev_vacf *v, int index, const unsigned char *sel,
+				   int b, double q)
+{
+	double *row = sepdev_vacf_row(v, index);
+	if (!row || sepdev_vacf_count(v) != t->nmol) return SEPDEV_EINVAL;
+	unsigned char *dsel = NULL;
+	CK(cudaMalloc((void **)&dsel, t->nmol));
+	cudaError_t e = cudaMemcpyAsync(dsel, sel, t->nmol, cudaMemcpyHostToDevice, d->st);
+	if (e == cudaSuccess) {
+		k_mol_ete_y<<<grid_for(t->nmol, 128), 128, 0, d->st>>>(t->nmol, t->start, t->atoms, d->inv, d->pos[d->cur],
+								      d->xlo, t->mass, dsel, b, d->L[1], q, row);
+		e = cudaGetLastError();
+		d->launches++;
+	}
+	if (e == cudaSuccess) e = cudaStreamSynchronize(d->st);
+	cudaFree(dsel);
+	if (e != cudaSuccess) { sepdev_set_error("mavacf sample", e); return SEPDEV_ECUDA; }
+	return SEPDEV_OK;
+}

@@ -6,7 +6,7 @@
  * the reference (source/sepsampler.c:4-242 dispatch, :280-351 sacf,
  * :361-470 radial, :471-641 msd, :658-714 vacf, :725-818 msacf, :822-1105
  * gh, :1110-1410 mgh, :1418-1510 profs, :1531-1666 mprofs, :1757-1825 mvacf,
- * :1918-2051 mmsd,
+ * :1828-1916 mavacf, :1918-2051 mmsd,
  * :2055-2213 scatt).  The stress autocorrelations work on the sepret values the host
  * already has (the molecular one through sep_mol_pressure_tensor); vacf,
  * msd, mvacf and mgh keep their particle data on the GPU (dev_sampler.cu,
@@ -128,6 +128,18 @@ struct sepmsacf {
 	double *sacf;          /* lvec x 2: symmetric, antisymmetric */
 	double *sstress;       /* lvec x 3 */
 	double *astress;       /* lvec x 3 */
+};
+
+/* mavacf keeps the same window as mvacf (its own quantity per molecule) */
+struct sepmavacf {
+	int lvec, isample, i;
+	long nsample;
+	double dtsample;
+	double *vacf, *block;
+	unsigned char *sel;
+	sepdev_vacf *dev;
+	sepdev_moltab *tab;
+	rt_ctx *ctx;
 };
 
 struct sepmvacf {
@@ -434,6 +446,18 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 			sptr->mprofs = p;
 			sptr->flag_mprofs = 1;
 		}
+	} else if (strcmp(sampler, "mavacf") == 0) {
+		if (sptr->flag_mavacf != 1) {
+			const double tsample = va_arg(args, double);
+			struct sepmavacf *p = xcalloc(1, sizeof *p);
+			p->lvec = lvec;
+			p->isample = sample_interval(tsample, lvec, sys.dt, &p->dtsample);
+			p->vacf = xcalloc(lvec, sizeof(double));
+			p->block = xcalloc(lvec, sizeof(double));
+			p->sel = xcalloc(sys.molptr->num_mols > 0 ? sys.molptr->num_mols : 1, 1);
+			sptr->mavacf = p;
+			sptr->flag_mavacf = 1;
+		}
 	} else if (strcmp(sampler, "mvacf") == 0) {
 		if (sptr->flag_mvacf != 1) {
 			const double tsample = va_arg(args, double);
@@ -448,7 +472,8 @@ void sep_add_sampler(sepsampler *sptr, const char *sampler, sepsys sys, int lvec
 	} else {
 		va_end(args);
 		sep_error("%s: sampler %s is not provided by this GPU implementation "
-			  "(available: sacf, vacf, msd, msacf, mvacf, gh, mgh, profs, mprofs, radial, mmsd, scatt)", __func__,
+			  "(available: sacf, vacf, msd, msacf, mvacf, mavacf, gh, mgh, profs, mprofs, radial, mmsd, scatt)",
+			  __func__,
 			  sampler);
 	}
 	va_end(args);
@@ -645,6 +670,43 @@ static void mvacf_sample(struct sepmvacf *s, seppart *pptr, sepmol *mols, sepsys
 		if (!f) sep_error("%s: couldn't open file", __func__);
 		for (int k = 0; k < s->lvec; k++) {
 			const double t = k * s->dtsample;
+			const double fac = 1.0 / ((double)(s->lvec - k) * nm * s->nsample);
+			fprintf(f, "%f %f\n", t, s->vacf[k] * fac);
+		}
+		fclose(f);
+		s->i = 0;
+	}
+}
+
+/* ---- mavacf: source/sepsampler.c:1853-1906 ----
+ * The reference's body samples, per molecule, the y component of the
+ * end-to-end vector of the type-A molecules times the first particle's
+ * |charge| times the molecule mass (its angular-velocity variant is
+ * commented out); the block correlation and file follow mvacf's with the
+ * times at (k + 1/2) dt_sample. */
+static void mavacf_sample(struct sepmavacf *s, seppart *pptr, sepmol *mols, sepsys sys)
+{
+	rt_ctx *c = sampler_ctx(pptr, &sys);
+	const int nm = (int)sys.molptr->num_mols;
+	if (s->ctx != c) {
+		if (s->dev) sepdev_vacf_destroy(s->dev);
+		s->dev = NULL;
+	}
+	mol_tables(&s->tab, &s->ctx, c, mols, &sys);
+	if (!s->dev) rt_check(sepdev_vacf_create_count(c->dev, s->lvec, nm, &s->dev), "mavacf sampler");
+	for (int i = 0; i < nm; i++) s->sel[i] = mols[i].type == 'A';
+	/* charges live on the host; the device never changes them */
+	const double q = fabs(pptr[0].z);
+	rt_check(sepdev_mavacf_store(c->dev, s->tab, s->dev, s->i, s->sel, (int)mols[0].nuau - 1, q), "mavacf sample");
+	s->i++;
+	if (s->i == s->lvec) {
+		rt_check(sepdev_vacf_block(c->dev, s->dev, s->block), "mavacf block");
+		for (int k = 0; k < s->lvec; k++) s->vacf[k] += s->block[k];
+		s->nsample++;
+		FILE *f = fopen("mavacf.dat", "w");
+		if (!f) sep_error("%s: couldn't open file", __func__);
+		for (int k = 0; k < s->lvec; k++) {
+			const double t = (k + 0.5) * s->dtsample;
 			const double fac = 1.0 / ((double)(s->lvec - k) * nm * s->nsample);
 			fprintf(f, "%f %f\n", t, s->vacf[k] * fac);
 		}
@@ -1062,6 +1124,8 @@ void sep_sample(seppart *pptr, sepsampler *sptr, sepret *ret, sepsys sys, unsign
 		mprofs_sample(sptr->mprofs, pptr, sptr->molptr, sys);
 	if (sptr->flag_mvacf == 1 && n % sptr->mvacf->isample == 0)
 		mvacf_sample(sptr->mvacf, pptr, sptr->molptr, sys);
+	if (sptr->flag_mavacf == 1 && n % sptr->mavacf->isample == 0)
+		mavacf_sample(sptr->mavacf, pptr, sptr->molptr, sys);
 	if (sptr->flag_radial == 1 && n % sptr->radial->isample == 0) radial_sample(sptr->radial, pptr, sys);
 	if (sptr->flag_msd == 1) {
 		struct sepmsd *m = sptr->msd;
@@ -1090,6 +1154,13 @@ void sep_close_sampler(sepsampler *ptr)
 		free(ptr->vacf->vacf);
 		free(ptr->vacf->block);
 		free(ptr->vacf);
+	}
+	if (ptr->flag_mavacf == 1) {
+		struct sepmavacf *p = ptr->mavacf;
+		if (p->dev) sepdev_vacf_destroy(p->dev);
+		if (p->tab) sepdev_moltab_destroy(p->tab);
+		free(p->vacf); free(p->block); free(p->sel);
+		free(p);
 	}
 	if (ptr->flag_mprofs == 1) {
 		struct sepmprofs *p = ptr->mprofs;

@@ -306,6 +306,11 @@ void sepdev_moltab_destroy(sepdev_moltab *t);
 /* mvacf: the molecules' centre-of-mass x-velocities into row index of a
  * ring created with count nmol */
 int sepdev_mvacf_store(sepdev *d, sepdev_moltab *t, sepdev_vacf *v, int index);
+/* mavacf: the type-A molecules' (sel) end-to-end y component (atom 0 to
+ * atom b) times q times the molecule mass into row index of a ring created
+ * with count nmol */
+int sepdev_mavacf_store(sepdev *d, sepdev_moltab *t, sepdev_vacf *v, int index, const unsigned char *sel,
+			int b, double q);
 /* mgh: for each wavevector k[j] along y, out[18 j + 2 q + (0 re, 1 im)] =
  * sum over molecules of e^{i k_j y_cm} w_q with w = (M, M vx, M vy, M v^2/2,
  * 1, s_z, s_y, dipole_y, w_x) (w_x, the angular velocity, only when unsafe;

@@ -674,6 +674,46 @@ def mprofs_small(lib, tmp):
     return d
 
 
+def mavacf_small(lib, tmp):
+    """the mavacf sampler (lvec 4 over 0.41, two blocks) on the mmsd_small
+    run's system (125 charged three-site molecules, every third of type B):
+    the positions at the sample steps and the file"""
+    s = cfg.water_like(nmol=125, rho=0.09, seed=7)
+    top = os.path.join(tmp, "ma.top")
+    cfg.write_top(top, s)
+    h = Handle(lib, s, cf=3.0, update=A.SEP_LLIST_NEIGHBLIST, dt=0.0005)
+    lib.sep_read_topology_file(h.atoms, top.encode(), C.byref(h.sys), b"q")
+    mols = lib.sep_init_mol(h.atoms, C.byref(h.sys))
+    nm = h.sys.molptr.contents.num_mols
+    for i in range(0, nm, 3):
+        mols[i].type = b"B"
+    bind_samplers(lib)
+    cwd = os.getcwd()
+    run = os.path.join(tmp, "mavacf")
+    os.makedirs(run, exist_ok=True)
+    os.chdir(run)
+    xs = []
+    try:
+        smp = lib.sep_init_sampler()
+        lib.sep_add_mol_sampler(C.byref(smp), C.cast(mols, C.c_void_p))
+        lib.sep_add_sampler(C.byref(smp), b"mavacf", h.sys, C.c_int(4), C.c_double(0.41))
+        isample = int((0.41 / 4) / 0.0005)
+        for n in range(8 * isample):
+            water_step(lib, h)
+            lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, n)
+            if n % isample == 0:
+                xs.append(h.view["x"].copy())
+        lib.sep_close_sampler(C.byref(smp))
+        d = dict(x0=s.x, v0=s.v, L=s.L, z=s.z, m=s.m, types=s.types.astype("S1"), bonds=s.bonds,
+                 angles=s.angles, xs=np.array(xs), molindex=h.view["molindex"].copy(), nmol=nm,
+                 mavacf=np.loadtxt("mavacf.dat"))
+    finally:
+        os.chdir(cwd)
+    lib.sep_free_mol(mols, C.byref(h.sys))
+    h.close()
+    return d
+
+
 def box_ops(lib):
     """sep_compress_box / _dir / _dir_length and sep_berendsen / _iso one at
     a time, then a Berendsen run (prgs/prg7.c) and a compression run
@@ -798,7 +838,8 @@ def main(only=()):
                          ("gh_small", lambda: gh_small(lib, tmp)),
                          ("mmsd_small", lambda: mmsd_small(lib, tmp)),
                          ("scatt_small", lambda: scatt_small(lib, tmp)),
-                         ("mprofs_small", lambda: mprofs_small(lib, tmp))):
+                         ("mprofs_small", lambda: mprofs_small(lib, tmp)),
+                         ("mavacf_small", lambda: mavacf_small(lib, tmp))):
             if only and name not in only:
                 continue
             d = fn()

@@ -285,3 +285,51 @@ def test_mprofs_file(gpu_lib, tmp_path):
     h.close()
     assert compare_lines(lines, mp.lines) >= 6
     assert compare_lines(lines, list(g["lines"])) >= 6
+
+
+def test_mavacf_file(gpu_lib, tmp_path):
+    """mavacf (source/sepsampler.c:1853-1906) on the fixture mavacf_small's
+    run against the oracle fed the device's own states, and against the
+    reference's file within the FP32 trajectories' spread"""
+    import ctypes as C
+    from seplib_gb300 import sepapi as A
+    from sephelp import Handle, bind_samplers, water_step
+    g = np.load(os.path.join(HERE, "golden", "mavacf_small.npz"))
+    lib = bind_samplers(gpu_lib)
+    s = cfg.System(x=g["x0"].copy(), v=g["v0"].copy(), L=g["L"].copy(), types=g["types"].copy(),
+                   m=g["m"].copy(), z=g["z"].copy(), bonds=g["bonds"], angles=g["angles"])
+    top = str(tmp_path / "ma.top")
+    cfg.write_top(top, s)
+    h = Handle(lib, s, cf=3.0, update=A.SEP_LLIST_NEIGHBLIST, dt=0.0005)
+    lib.sep_read_topology_file(h.atoms, top.encode(), C.byref(h.sys), b"q")
+    mols = lib.sep_init_mol(h.atoms, C.byref(h.sys))
+    nm = h.sys.molptr.contents.num_mols
+    for i in range(0, nm, 3):
+        mols[i].type = b"B"
+    sel = np.ones(nm, bool)
+    sel[::3] = False
+    _, _, start, atoms = oracle.mol_tables(h.view["molindex"], nm)
+    molidx = [atoms[start[i]:start[i + 1]] for i in range(nm)]
+    M = np.array([s.m[ix].sum() for ix in molidx])
+    ma = oracle.MAVACF(4, 0.41 / 4)
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        smp = lib.sep_init_sampler()
+        lib.sep_add_mol_sampler(C.byref(smp), C.cast(mols, C.c_void_p))
+        lib.sep_add_sampler(C.byref(smp), b"mavacf", h.sys, C.c_int(4), C.c_double(0.41))
+        isample = int((0.41 / 4) / 0.0005)
+        for n in range(8 * isample):
+            water_step(lib, h)
+            lib.sep_sample(h.atoms, C.byref(smp), C.byref(h.ret), h.sys, n)
+            if n % isample == 0:
+                h.sync()
+                ma.sample(h.view["x"], molidx, M, sel, abs(s.z[0]), s.L[1])
+        lib.sep_close_sampler(C.byref(smp))
+        out = np.loadtxt("mavacf.dat")
+    finally:
+        os.chdir(cwd)
+    lib.sep_free_mol(mols, C.byref(h.sys))
+    h.close()
+    np.testing.assert_allclose(out, ma.out, rtol=1e-9, atol=1.1e-6)
+    np.testing.assert_allclose(out[:, 1], g["mavacf"][:, 1], rtol=0, atol=2e-3)
