@@ -1,0 +1,94 @@
+"""Edge cases of the plain pair path on the GPU against the FP64 oracle:
+systems of 1 to 131 particles (ragged warps, a box of two cells a side),
+and a dense cluster in a dilute fluid whose neighbour counts overflow the
+list capacity estimated from the mean density, so the build grows the list
+and retries.  Bars as in test_gpu_lj.py: forces within 1e-5 relative L2 of
+FP64, energies within 1e-6 relative (plus, for the few-particle systems
+whose whole energy comes from pairs at the cut-off, an absolute 1e-7 per
+particle: FP32 resolution of the per-pair energy)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import seplib_gb300
+from seplib_gb300 import configs as cfg
+from sephelp import Handle, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def spread(n, L, rng, dmin=0.95, lo=None, hi=None):
+    """n random positions in [lo, hi) (default the box) at least dmin apart
+    (minimum image)"""
+    lo = np.zeros(3) if lo is None else lo
+    hi = L if hi is None else hi
+    x = []
+    while len(x) < n:
+        p = lo + rng.random(3) * (hi - lo)
+        if x:
+            d = np.asarray(x) - p
+            d -= L * np.round(d / L)
+            if (d * d).sum(1).min() < dmin * dmin:
+                continue
+        x.append(p)
+    return np.array(x).reshape(-1, 3)
+
+
+def oracle_forces(ora, x, L, types, cf=2.5):
+    pairs = ora.pairs_brute(x, L, cf)
+    st, nb = ora.csr_from_pairs(len(x), pairs)
+    return ora.pair_forces(x, types, L, "AA", ora.POT_LJSHIFT, None, cf, st, nb)
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 33, 131])
+def test_tiny_and_ragged_systems(gpu_lib, ora, n):
+    rng = np.random.default_rng(100 + n)
+    L = np.array([7.0, 7.0, 7.0])
+    x = spread(n, L, rng)
+    s = cfg.System(x=x, v=np.zeros((n, 3)), L=L, types=np.full(n, b"A", "S1"), m=np.ones(n), z=np.zeros(n))
+    h = Handle(gpu_lib, s, skin=0.3)
+    h.forces()
+    h.sync()
+    f, e, _ = oracle_forces(ora, x, L, s.types)
+    if np.linalg.norm(f) == 0.0:
+        # no pair within the cut-off (one particle, or two far apart)
+        assert np.abs(h.view["f"]).max() == 0.0 and abs(h.ret.epot - e) <= 1e-12
+    else:
+        assert rel_l2(h.view["f"], f) < 1e-5
+        # pairs near the cut-off have energies that are differences of
+        # O(0.01) terms in FP32: an absolute floor of 1e-7 per particle
+        assert abs(h.ret.epot - e) <= 1e-6 * abs(e) + 1e-7 * n
+    # one step through the integrator keeps the system finite
+    gpu_lib.sep_leapfrog(h.atoms, C.byref(h.sys), C.byref(h.ret))
+    h.sync()
+    assert np.isfinite(h.view["x"]).all() and np.isfinite(h.view["v"]).all()
+    h.close()
+
+
+def test_list_overflow_grows(gpu_lib, ora):
+    rng = np.random.default_rng(17)
+    L = np.array([16.0, 16.0, 16.0])
+    cl, _ = cfg.fcc(6, 1.6)
+    cl = cl - cl.mean(0) + 0.5 * L
+    dil = []
+    while len(dil) < 1000:
+        p = spread(1, L, rng)[0]
+        d = cl - p
+        if (d * d).sum(1).min() > 0.95 ** 2 and (not dil or ((np.asarray(dil) - p) ** 2).sum(1).min() > 0.95 ** 2):
+            dil.append(p)
+    x = np.concatenate([cl, np.array(dil)])
+    n = len(x)
+    s = cfg.System(x=x, v=np.zeros((n, 3)), L=L, types=np.full(n, b"A", "S1"), m=np.ones(n), z=np.zeros(n))
+    h = Handle(gpu_lib, s, skin=0.3)
+    h.forces()
+    h.sync()
+    info = seplib_gb300.GpuInfo()
+    gpu_lib.sep_gpu_info_get(h.atoms, C.byref(info))
+    est = 1.35 * 4.18879020479 * 2.8 ** 3 * n / np.prod(L) + 32
+    assert info.list_max > est          # the mean-density estimate would have overflowed
+    assert info.list_capacity >= info.list_max
+    f, e, _ = oracle_forces(ora, x, L, s.types)
+    assert rel_l2(h.view["f"], f) < 1e-5
+    assert abs(h.ret.epot - e) <= 1e-6 * abs(e)
+    h.close()
