@@ -688,6 +688,7 @@ static void mavacf_sample(struct sepmavacf *s, seppart *pptr, sepmol *mols, seps
 {
 	rt_ctx *c = sampler_ctx(pptr, &sys);
 	const int nm = (int)sys.molptr->num_mols;
+	if (nm < 1 || mols == NULL) sep_error("%s: no molecules to sample", __func__);
 	if (s->ctx != c) {
 		if (s->dev) sepdev_vacf_destroy(s->dev);
 		s->dev = NULL;
