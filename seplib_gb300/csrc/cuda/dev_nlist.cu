@@ -231,6 +231,10 @@ __device__ __forceinline__ float warp_max_f(float v, unsigned mask)
 // MOLX (same-molecule exclusions): the candidates' molecule indices are
 // staged in spm beside their positions, and in-box runs take a branch-free
 // loop that tests them from shared memory.
+// NSPLIT > 1: NSPLIT warps share the tile, warp `half` taking its runs
+// half, half + NSPLIT, ...  A tile that spans two cell rows stages two
+// neighbourhoods; split, no warp carries both.  Each particle is built by
+// one warp in the same order, so the lists do not change.
 template <bool WRAPFAST, bool MOLX = false>
 __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, float4 *sp, int *ring,
 					   int *spm = nullptr)
@@ -369,7 +373,9 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 			else if (s1 > nc0) { sA0 = s0; sA1 = nc0; sB1 = s1 - nc0; }
 			else { sA0 = s0; sA1 = s1; }
 		}
-		int fill = 0;
+		// the run's candidate segments, in staging order: up to 9 rows x 2
+		// x-ranges; lane k loads segment k's bounds, all in one round
+		int nseg = 0, seg_b = 0, seg_e = 0;
 		for (int oz = lo2; oz <= hi2; oz++) {
 			const int zz = wrapc(rz + oz, nc2);
 			for (int oy = lo1; oy <= hi1; oy++) {
@@ -378,37 +384,63 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 				for (int sg = 0; sg < 2; sg++) {
 					const int c0 = sg ? sB0 : sA0, c1 = sg ? sB1 : sA1;
 					if (c1 <= c0) continue;
-					const int jb = a.cellstart[rb + c0], je = a.cellstart[rb + c1];
-					for (int jj = jb; jj < je; jj += 32) {
-						const int take = min(32, je - jj);
-						if (fill + take > BT_CAP) { test(fill); fill = 0; }
-						bool keep = lane < take;
-						float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-						if (keep) {
-							const int4 pj = a.pos[jj + lane];
-							if (local) {
-								q = make_float4(sep_hi(pj.x, ref.x, a.fs[0]), sep_hi(pj.y, ref.y, a.fs[1]),
-										sep_hi(pj.z, ref.z, a.fs[2]), __int_as_float(jj + lane));
-								const float ex = fmaxf(fmaxf(bx0 - q.x, q.x - bx1), 0.f);
-								const float ey = fmaxf(fmaxf(by0 - q.y, q.y - by1), 0.f);
-								const float ez = fmaxf(fmaxf(bz0 - q.z, q.z - bz1), 0.f);
-								keep = ex < rl && ey < rl && ez < rl &&
-								       fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < a.rl2;
-							} else {
-								q = make_float4(__int_as_float(pj.x), __int_as_float(pj.y),
-										__int_as_float(pj.z), __int_as_float(jj + lane));
-							}
-						}
-						const unsigned kb = __ballot_sync(FULL, keep);
-						if (keep) {
-							const int slot = fill + __popc(kb & ((1u << lane) - 1u));
-							sp[slot] = q;
-							if (MOLX) spm[slot] = a.mol[jj + lane];
-						}
-						fill += __popc(kb);
-					}
+					if (lane == nseg) { seg_b = a.cellstart[rb + c0]; seg_e = a.cellstart[rb + c1]; }
+					nseg++;
 				}
 			}
+		}
+		// chunks of up to 32 consecutive candidates; the loads of the next
+		// chunk are issued before the current one is filtered and tested
+		int sidx = 0, jj = 0, je = 0;
+		auto next_seg = [&]() {
+			while (sidx < nseg) {
+				jj = __shfl_sync(FULL, seg_b, sidx);
+				je = __shfl_sync(FULL, seg_e, sidx);
+				if (jj < je) return;
+				sidx++;
+			}
+		};
+		next_seg();
+		int4 pn = make_int4(0, 0, 0, 0);
+		int mn = 0;
+		if (sidx < nseg && lane < je - jj) {
+			pn = a.pos[jj + lane];
+			if (MOLX) mn = a.mol[jj + lane];
+		}
+		int fill = 0;
+		while (sidx < nseg) {
+			const int jc = jj, take = min(32, je - jj);
+			const int4 pj = pn;
+			const int mj = mn;
+			jj += 32;
+			if (jj >= je) { sidx++; next_seg(); }
+			if (sidx < nseg && lane < min(32, je - jj)) {
+				pn = a.pos[jj + lane];
+				if (MOLX) mn = a.mol[jj + lane];
+			}
+			if (fill + take > BT_CAP) { test(fill); fill = 0; }
+			bool keep = lane < take;
+			float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+			if (keep) {
+				if (local) {
+					q = make_float4(sep_hi(pj.x, ref.x, a.fs[0]), sep_hi(pj.y, ref.y, a.fs[1]),
+							sep_hi(pj.z, ref.z, a.fs[2]), __int_as_float(jc + lane));
+					const float ex = fmaxf(fmaxf(bx0 - q.x, q.x - bx1), 0.f);
+					const float ey = fmaxf(fmaxf(by0 - q.y, q.y - by1), 0.f);
+					const float ez = fmaxf(fmaxf(bz0 - q.z, q.z - bz1), 0.f);
+					keep = ex < rl && ey < rl && ez < rl && fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < a.rl2;
+				} else {
+					q = make_float4(__int_as_float(pj.x), __int_as_float(pj.y), __int_as_float(pj.z),
+							__int_as_float(jc + lane));
+				}
+			}
+			const unsigned kb = __ballot_sync(FULL, keep);
+			if (keep) {
+				const int slot = fill + __popc(kb & ((1u << lane) - 1u));
+				sp[slot] = q;
+				if (MOLX) spm[slot] = mj;
+			}
+			fill += __popc(kb);
 		}
 		test(fill);
 	}
@@ -526,7 +558,7 @@ static int grow(sepdev *d, void **p, size_t bytes, size_t *cap)
 static int launch_build(sepdev *d, const BuildArgs &a)
 {
 	const int grid = grid_for((d->n + 31) / 32, BT_WARPS);
-	if (a.excl == SEPDEV_EXCL_SAMEMOL)
+	if (a.excl == SEPDEV_EXCL_SAMEMOL)      // two warps per tile
 		k_build_tiles_mol<<<grid, BT_WARPS * 32, 0, d->st>>>(d->n, a);
 	else
 		k_build_tiles<<<grid, BT_WARPS * 32, 0, d->st>>>(d->n, a);
