@@ -46,10 +46,23 @@ sys.path.insert(0, HERE)
 RHO, TEMP, RC, SKIN, DT, T0, TAU = 0.8442, 1.0, 2.5, 0.3, 0.005, 1.0, 10.0
 L2_BYTES = 129 * 2 ** 20
 FLUSH_BYTES = 256 * 2 ** 20     # written between timed steps: about twice the L2
-# DRAM bytes (read + write) per launch of the fused step kernel, from one ncu
-# capture of this workload after an L2 flush (profiles/k_lj_fcc256000.md);
-# keyed by fcc cells per edge
-K_LJ_TRAFFIC = {40: 105.6e6}
+# DRAM bytes (read + write) per launch of the step kernels, measured by ncu:
+# one line per kernel and workload in profiles/traffic.txt, with the command
+# that measured it
+TRAFFIC_FILE = os.path.join(HERE, "profiles", "traffic.txt")
+
+
+def measured_traffic(kernel, workload):
+    """Bytes per launch recorded for (kernel, workload), or None."""
+    try:
+        with open(TRAFFIC_FILE) as fh:
+            for line in fh:
+                f = line.split()
+                if len(f) >= 3 and not line.startswith("#") and f[0] == kernel and f[1] == workload:
+                    return float(f[2])
+    except OSError:
+        pass
+    return None
 
 
 def parse():
@@ -61,6 +74,8 @@ def parse():
     ap.add_argument("--ncell", type=int, default=40, help="fcc cells per edge (40: N=256000)")
     ap.add_argument("--cpu-steps", type=int, default=0, help="oracle steps for cpu_baseline (0: auto)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="skip the batched, adjoint and butane sub-objects of the headline line")
     ap.add_argument("--tpp", type=int, default=0)
     ap.add_argument("--workload", default="plain", choices=["plain", "batched", "adjoint", "butane"],
                     help="plain: one N=4 ncell^3 system (the headline); batched: 512 independent "
@@ -117,11 +132,11 @@ class Clocks:
 
     def __init__(self):
         self.p = None
-        self.path = os.path.join(HERE, "gpurun_out", "clocks_bench.csv")
+        fd, self.path = tempfile.mkstemp(prefix="sep_clocks_", suffix=".csv")
+        os.close(fd)
 
     def start(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -151,6 +166,10 @@ class Clocks:
             for k, name in enumerate(names):
                 if f[5 + k].lower() == "active":
                     reasons.add(name)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
         if not sm:
             return None
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
@@ -229,11 +248,13 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
-def run_batched(args, rank, world):
+def run_batched(args, rank, world, steps=None, single_every=1, emit=True):
     """512 independent LJ systems (N log-uniform in [108, 4000], rho* in
     [0.70, 0.95], T* in [0.7, 1.5], Nose-Hoover) stepped together with the
     sepb_* API, against the same systems run one at a time through
-    sep_gpu_run (one graph per system)."""
+    sep_gpu_run (one graph per system; with single_every > 1, every
+    single_every-th system, the rate taken over their particles)."""
+    steps = steps or args.steps
     from seplib_gb300 import build, configs, load, sepapi as A
     from seplib_gb300.batch import Batch
     build.build()
@@ -245,14 +266,14 @@ def run_batched(args, rank, world):
     clocks = Clocks()
     clocks.start()
     barrier(world)
-    ms = b.run_timed(args.steps, FLUSH_BYTES)
+    ms = b.run_timed(steps, FLUSH_BYTES)
     barrier(world)
     clk = clocks.stop()
     t_dev = allmax(world, ms / 1e3)
-    value = world * ntot * args.steps / t_dev
+    value = world * ntot * steps / t_dev
     # the production loop (one graph, no flush), wall clock around the call
     t0 = time.perf_counter()
-    b.run(args.steps)
+    b.run(steps)
     t_graph = time.perf_counter() - t0
     slots = b.slots()
     b.close()
@@ -260,7 +281,11 @@ def run_batched(args, rank, world):
     fun = A.fun_ptr(lib, "sep_lj_shift")
     ks = args.single_steps
     t_single = 0.0
+    n_single = 0
     for k, s in enumerate(systems):
+        if k % single_every:
+            continue
+        n_single += s.n
         atoms, sys_ = new_system(lib, s)
         ret = A.SepRet()
         alpha = C.c_double(0.0)
@@ -272,12 +297,12 @@ def run_batched(args, rank, world):
         assert run(ks) == 0
         t_single += time.perf_counter() - t0
         lib.sep_close(atoms, s.n)
-    single_pss = ntot * ks / t_single
+    single_pss = n_single * ks / t_single
     if rank == 0:
         line = {
             "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
+            "n_gpus": world, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_dev / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 pair / fixed-point x / f64-exact sums",
             "data": "synthetic (seeded fcc lattices with vacancies, Maxwell-Boltzmann velocities)",
             "config": {"workload": "%d independent LJ NVT systems, N log-uniform in [108, 4000] "
@@ -286,20 +311,23 @@ def run_batched(args, rank, world):
                                    % (args.nsys, ntot, TAU, RC, SKIN, DT),
                        "n_systems": args.nsys, "n_particles": ntot, "device_slots": slots,
                        "l2": "flushed: %d MiB before every timed step, outside the spans" % (FLUSH_BYTES >> 20),
-                       "graph_loop_no_flush": {"value": ntot * args.steps / t_graph,
+                       "graph_loop_no_flush": {"value": ntot * steps / t_graph,
                                                "unit": "particle-steps/s",
                                                "what": "sepb_run, wall clock around the call"},
                        "one_system_per_launch": {"value": single_pss, "unit": "particle-steps/s",
                                                  "steps_per_system": ks,
+                                                 "systems": len(range(0, len(systems), single_every)),
                                                  "what": "each system through sep_gpu_run in turn, "
                                                          "wall clock"},
                        "speedup_vs_one_system_per_launch": value / single_pss},
             "clocks": clk,
         }
-        print(json.dumps(line))
+        if emit:
+            print(json.dumps(line))
+        return line
 
 
-def run_adjoint(args, rank, world):
+def run_adjoint(args, rank, world, steps=None, emit=True):
     """64 NVE replicas of N=4000 (fcc 10^3 cells at rho*=0.8442, T*=1.0,
     seeded), 200 steps, loss (1/K) sum_n (epot_n + p_n), gradients wrt eps,
     sigma and x0, checkpoints every 20 steps: wall time of the forward pass,
@@ -308,7 +336,7 @@ def run_adjoint(args, rank, world):
     from seplib_gb300.adjoint import Adjoint
     build.build()
     lib = load()
-    nrep, steps = 64, args.steps
+    nrep, steps = 64, steps or args.steps
     systems = [configs.plain_lj_large(10, seed=100 + 64 * rank + k, temp=1.0) for k in range(nrep)]
     param = (RC, 1.0, 1.0, 1.0)
     a = Adjoint(lib, systems, param, rc=RC, skin=SKIN, dt=DT, ckpt=args.ckpt)
@@ -341,10 +369,12 @@ def run_adjoint(args, rank, world):
                        "mean_loss": float(np.mean(loss)), "mean_dloss_deps": float(np.mean(de)),
                        "mean_dloss_dsigma": float(np.mean(ds))},
         }
-        print(json.dumps(line))
+        if emit:
+            print(json.dumps(line))
+        return line
 
 
-def run_butane(args, rank, world):
+def run_butane(args, rank, world, steps=None, emit=True):
     """8000 united-atom butane chains (32000 beads) at rho*=0.6, T*=4.0,
     dt=0.002: the prgs/prg2.c step (LJ with intramolecular exclusions, bonds,
     angles, Ryckaert-Bellemans torsions, Nose-Hoover, leap-frog) through the
@@ -353,6 +383,7 @@ def run_butane(args, rank, world):
     step ends in a synchronous read-back of its sepret)."""
     from seplib_gb300 import build, configs
     build.build()
+    steps = steps or args.steps
     s = configs.butane(nmol=8000, rho=0.6, temp=4.0, seed=3 + rank)
     n = s.n
     clocks = Clocks()
@@ -363,15 +394,15 @@ def run_butane(args, rank, world):
         write_state(state, s)
         clocks.start()
         barrier(world)
-        run = run_driver(state, args.steps, max(3, args.warmup), RC, 0.002, 0.25, 4.0, 0.1, top)
+        run = run_driver(state, steps, max(3, args.warmup), RC, 0.002, 0.25, 4.0, 0.1, top)
         barrier(world)
         clk = clocks.stop()
     t = allmax(world, run["seconds"])
     temp = 2.0 * run["ekin"] / (3.0 * n)
     if rank == 0:
         line = {
-            "metric": "particle-steps/s", "value": world * n * args.steps / t, "unit": "particle-steps/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "metric": "particle-steps/s", "value": world * n * steps / t, "unit": "particle-steps/s",
+            "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 pair and bonded / fixed-point x / f64-exact sums",
             "data": "synthetic (8000 planar zig-zag butane chains on a lattice, seeded velocities)",
@@ -385,7 +416,33 @@ def run_butane(args, rank, world):
                        "list_updates": run["rebuilds"], "final_temperature": temp},
             "clocks": clk,
         }
-        print(json.dumps(line))
+        if emit:
+            print(json.dumps(line))
+        return line
+
+
+def other_workloads(args, rank, world):
+    """The batched, adjoint and butane workloads, each bounded to a few
+    seconds, as sub-objects of the headline line (their own --workload
+    modes give the full runs)."""
+    def brief(line, keep):
+        out = {k: line[k] for k in ("value", "unit", "steps", "ms_per_step", "dtype") if k in line}
+        out["workload"] = line["config"]["workload"]
+        for k in keep:
+            out[k] = line["config"].get(k)
+        if line.get("clocks"):
+            out["clocks"] = line["clocks"]
+        return out
+    out = {}
+    b = run_batched(args, rank, world, steps=200, single_every=4, emit=False)
+    out["batched"] = brief(b, ("speedup_vs_one_system_per_launch", "one_system_per_launch",
+                               "graph_loop_no_flush", "n_particles"))
+    a = run_adjoint(args, rank, world, steps=200, emit=False)
+    out["adjoint"] = brief(a, ("forward_s", "backward_s", "backward_over_forward",
+                               "forward_particle_steps_per_s"))
+    u = run_butane(args, rank, world, steps=500, emit=False)
+    out["butane"] = brief(u, ("list_updates", "final_temperature"))
+    return out
 
 
 def main():
@@ -532,7 +589,7 @@ def main():
                             "read-back and the final download timed; L2 flushed between steps, "
                             "untimed"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": K_LJ_TRAFFIC.get(args.ncell),
+                         "frac": achieved / peak, "traffic": measured_traffic("k_lj", "fcc%d" % args.ncell),
                          "traffic_unit": "bytes per launch", "peak_source": peak_kind,
                          "kernel": "k_lj<fused step>", "kernel_ms": kernel_ms,
                          "bytes_per_launch": alg_bytes,
@@ -544,6 +601,8 @@ def main():
             # k_cellsort_w, k_gather, k_copyback, k_build_tiles
             "gpu_launches": args.steps + (args.steps + 63) // 64 + 7 * rebuilds,
         }
+        if world == 1 and not args.no_workloads:
+            line["workloads"] = other_workloads(args, rank, world)
         print(json.dumps(line))
 
 

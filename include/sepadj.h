@@ -36,8 +36,23 @@ typedef struct sepadj sepadj;
 sepadj *sepadj_create(int nrep, const int *npart, const double *L, double rc, double skin,
 		      double dt, const double *ljparam, int ckpt_every);
 
+/*
+ * Mixtures: ntypes (at most 4) particle types with one parameter set
+ * {cf, eps, sigma, aw} per type pair, the loop being one sep_force_lj call
+ * per pair of types ("ab", param_ab; the energies add) and sep_leapfrog.
+ * ljparams holds ntypes x ntypes sets of four doubles, set [a][b] equal to
+ * set [b][a]; eps = 0 leaves a type pair without a term.  The list cut-off
+ * is the largest cf plus skin.  Gradients come from sepadj_backward_typed.
+ */
+sepadj *sepadj_create_typed(int nrep, const int *npart, const double *L, double skin, double dt,
+			    int ntypes, const double *ljparams, int ckpt_every);
+
 /* Initial positions (3 n), velocities (3 n) and masses (n or NULL) of replica r. */
 int sepadj_set_state(sepadj *a, int r, const double *x, const double *v, const double *m);
+
+/* Type ids (0 .. ntypes-1) of the particles of replica r (typed adjoint);
+ * after sepadj_set_state of that replica. */
+int sepadj_set_types(sepadj *a, int r, const int *type);
 
 /* nsteps NVE steps of every replica from the initial states; loss[r]. */
 int sepadj_forward(sepadj *a, long nsteps, double *loss);
@@ -45,6 +60,16 @@ int sepadj_forward(sepadj *a, long nsteps, double *loss);
 /* Gradients of the last forward's losses: dloss_deps[r], dloss_dsigma[r]
  * and dloss_dx0 (3 n of replica 0, then replica 1, ...; may be NULL). */
 int sepadj_backward(sepadj *a, double *dloss_deps, double *dloss_dsigma, double *dloss_dx0);
+
+/* The same for a typed adjoint: dloss_deps and dloss_dsigma hold
+ * nrep x ntypes x ntypes values, [r][a][b] = [r][b][a] the gradient with
+ * respect to the one eps (sigma) of type pair {a, b}. */
+int sepadj_backward_typed(sepadj *a, double *dloss_deps, double *dloss_dsigma, double *dloss_dx0);
+
+/* Positions and velocities (3 n each, either may be NULL) of replica r at
+ * the end of the last forward pass; call it before sepadj_backward, whose
+ * recomputation leaves other states on the device. */
+int sepadj_get_state(sepadj *a, int r, double *x, double *v);
 
 void sepadj_destroy(sepadj *a);
 

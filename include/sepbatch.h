@@ -38,6 +38,22 @@ typedef struct {
 sepb *sepb_create(int nsys, const int *npart, const double *L, double rc, double skin, double dt,
 		  const double *ljparam);
 
+/*
+ * A batch of mixtures: ntypes (at most 4) particle types with one
+ * Lennard-Jones parameter set {cf, eps, sigma, aw} per type pair, as one
+ * sep_force_lj(ptr, "ab", param_ab, ...) call per pair of types would give
+ * (the energies of the calls add).  ljparams holds ntypes x ntypes sets of
+ * four doubles, set [a][b] equal to set [b][a]; eps = 0 leaves a type pair
+ * without a term.  The list cut-off is the largest cf plus skin.  Types are
+ * set per system with sepb_set_types (all type 0 otherwise).
+ */
+sepb *sepb_create_typed(int nsys, const int *npart, const double *L, double skin, double dt,
+			int ntypes, const double *ljparams);
+
+/* Type ids (0 .. ntypes-1) of the n particles of system s of a typed batch;
+ * call it after sepb_set_state of that system and before the next run. */
+int sepb_set_types(sepb *b, int s, const int *type);
+
 /* Positions (3 n, wrapped into the box), velocities (3 n) and masses (n, or
  * NULL for 1) of system s.  A system set here starts afresh: its first step
  * reports a list update, as the first sep_leapfrog of a program does. */

@@ -145,12 +145,21 @@ int sep_gpu_flush_l2(seppart *ptr, long bytes);
  * host arrays.  All work is queued on `stream` (a cudaStream_t; NULL is the
  * legacy default stream) and the call returns without waiting.
  *
+ * The cut-off param[0] may be at most half the shortest box side; larger
+ * cut-offs are rejected.
+ *
  * The fixed array is shared by every call and keeps the last call's
  * contents; each call clears what it needs.  Calls whose work overlaps on
  * the GPU (different streams, or several host threads) race on it and give
  * wrong results: order them on one stream.  The first call on each device,
- * with that device current, looks up the array's address and keeps it;
- * make that first call before any stream capture.
+ * with that device current, looks up the array's address and keeps it.
+ * Under CUDA's default lazy module loading, that first call is also when
+ * the array (and the code it runs) is placed on the device: the first call
+ * takes about 5 MB of device memory, later calls take none.  So make the
+ * first call before a pool allocator takes the device's memory, and before
+ * any stream capture.  Particles are binned with atomics, so the summation
+ * order of a particle's pair terms, and with it the last bits of the
+ * results, can differ from call to call.
  *
  * Returns 0, or a negative code with the message in sep_gpu_error().
  */

@@ -22,8 +22,13 @@ _lib = None
 
 
 def build(ref=False):
-    """Compile the restatement (and, if `ref`, the reference library)."""
-    targets = ["all"] + (["ref"] if ref else [])
+    """Compile the restatement and, with `ref` True, the reference library
+    from its sources (the Makefile's REF, overridable through the
+    SEPLIB_REFERENCE environment variable); with `ref` "auto", the reference
+    library only where its sources are present."""
+    targets = ["all"] + ({True: ["ref"], "auto": ["ref-if-present"]}.get(ref, []))
+    if os.environ.get("SEPLIB_REFERENCE"):
+        targets.append("REF=" + os.environ["SEPLIB_REFERENCE"])
     subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
 
 
@@ -179,6 +184,18 @@ def leapfrog(st, f, L, dt, skin, max_dist2=0.0):
     return flag, md.value, ek.value, kP.reshape(3, 3)
 
 
+def kinetic_sums(v, f, m, dt):
+    """Kinetic energy and tensor that sep_leapfrog reports for a step that
+    left velocities v (time t + dt/2) from forces f: v(t) = v - a dt / 2 with
+    a = f / m, ekin = sum m v(t)^2 / 2, kin_P = sum m v(t) v(t)^T (reference
+    source/sepintgr.c:50-65), in FP64 with pairwise summation."""
+    v = _f64(v); f = _f64(f); m = _f64(m)
+    a = f / m[:, None]
+    vt = v - 0.5 * a * dt
+    kP = np.array([[np.sum(m * vt[:, k] * vt[:, l]) for l in range(3)] for k in range(3)])
+    return 0.5 * float(np.sum(m[:, None] * vt * vt)), kP
+
+
 def stretch_harmonic(blist, btype, l0, ks, x, L):
     x = _f64(x); n = len(x); L = _f64(L); bl = np.ascontiguousarray(blist, np.uint32)
     f = np.zeros((n, 3)); e = C.c_double(0.0); pP = np.zeros(9); pB = np.zeros(9)
@@ -246,6 +263,51 @@ def lj_adjoint(x, v, m, L, param, dt, nsteps):
     if rc != 0:
         raise MemoryError("ora_lj_adjoint")
     return de.value, ds.value, gx
+
+
+def _ljt_args(x, v, m, types, L, params):
+    x = _f64(x); v = _f64(v); m = _f64(m); L = _f64(L)
+    t = _i32(types)
+    P = _f64(params)
+    nt = int(round(np.sqrt(P.size // 4)))
+    assert P.size == 4 * nt * nt
+    return x, v, m, t, L, P, nt
+
+
+def ljt_loss(x, v, m, types, L, params, dt, nsteps):
+    """FP64 loss of the NVE loop with one sep_force_lj term per type pair:
+    params has shape (nt, nt, 4) = {cf, eps, sigma, aw} per pair (symmetric),
+    types are ids 0..nt-1; linked-cell pairs, so large systems are cheap."""
+    x, v, m, t, L, P, nt = _ljt_args(x, v, m, types, L, params)
+    f = lib().ora_ljt_loss
+    f.restype = C.c_double
+    return f(len(x), _p(x, C.c_double), _p(v, C.c_double), _p(m, C.c_double), _p(t, C.c_int),
+             _p(L, C.c_double), nt, _p(P, C.c_double), C.c_double(dt), C.c_long(nsteps))
+
+
+def ljt_adjoint(x, v, m, types, L, params, dt, nsteps):
+    """FP64 gradient of ljt_loss: (dL/deps (nt, nt), dL/dsigma (nt, nt), dL/dx0)."""
+    x, v, m, t, L, P, nt = _ljt_args(x, v, m, types, L, params)
+    ge = np.zeros((nt, nt)); gs = np.zeros((nt, nt)); gx = np.zeros_like(x)
+    rc = lib().ora_ljt_adjoint(len(x), _p(x, C.c_double), _p(v, C.c_double), _p(m, C.c_double),
+                               _p(t, C.c_int), _p(L, C.c_double), nt, _p(P, C.c_double),
+                               C.c_double(dt), C.c_long(nsteps), _p(ge, C.c_double),
+                               _p(gs, C.c_double), _p(gx, C.c_double))
+    if rc != 0:
+        raise MemoryError("ora_ljt_adjoint")
+    return ge, gs, gx
+
+
+def lj_loss_cells(x, v, m, L, param, dt, nsteps):
+    """lj_loss through the linked-cell pair search of ljt_loss (one type)."""
+    return ljt_loss(x, v, m, np.zeros(len(x)), L, np.asarray(param, float).reshape(1, 1, 4), dt, nsteps)
+
+
+def lj_adjoint_cells(x, v, m, L, param, dt, nsteps):
+    """lj_adjoint through the linked-cell pair search of ljt_adjoint (one type)."""
+    ge, gs, gx = ljt_adjoint(x, v, m, np.zeros(len(x)), L, np.asarray(param, float).reshape(1, 1, 4),
+                             dt, nsteps)
+    return ge[0, 0], gs[0, 0], gx
 
 
 # ---- stochastic dynamics -------------------------------------------------------

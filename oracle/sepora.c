@@ -734,6 +734,224 @@ int ora_lj_adjoint(long n, const double *x0, const double *v0, const double *m, 
 	return 0;
 }
 
+/* ---- typed loss and adjoint: one LJ parameter set per type pair ------------
+ *
+ * The NVE prgs loop with one sep_force_lj call per unordered type pair {a, b}
+ * (param_ab = {cf, eps, sigma, aw}; source/sepprfrc.c:743-1000: the term of
+ * types "ab" applies to every pair whose types are a and b in either order,
+ * and the energies of the calls add) and sep_leapfrog
+ * (source/sepintgr.c:42-88).  P holds nt x nt parameter sets of 4 doubles,
+ * symmetric (P[a][b] == P[b][a]); eps = 0 switches a pair type off.  Pairs
+ * are found each step through a linked-cell list of cells at least the
+ * largest cut-off wide (every pair once, i < j), or by brute force when a
+ * box side holds fewer than three such cells. */
+
+typedef struct { long np, cap; int *ij; } ora_plist;
+
+static int ora_plist_push(ora_plist *pl, long i, long j)
+{
+	if (pl->np == pl->cap) {
+		long nc = pl->cap ? 2 * pl->cap : 4096;
+		int *q = realloc(pl->ij, sizeof(int) * 2 * nc);
+		if (!q) return -1;
+		pl->ij = q;
+		pl->cap = nc;
+	}
+	pl->ij[2 * pl->np] = (int)i;
+	pl->ij[2 * pl->np + 1] = (int)j;
+	pl->np++;
+	return 0;
+}
+
+/* every unordered pair i < j with r^2 < rmax^2 (minimum image) */
+static int ora_halfpairs(long n, const double *x, const double L[3], double rmax, ora_plist *pl)
+{
+	const double r2max = rmax * rmax;
+	int nc[3];
+	double d[3];
+	pl->np = 0;
+	for (int k = 0; k < 3; k++) nc[k] = (int)floor(L[k] / rmax);
+	if (nc[0] < 3 || nc[1] < 3 || nc[2] < 3) {
+		for (long i = 0; i < n; i++)
+			for (long j = i + 1; j < n; j++)
+				if (ora_sep(x, i, j, L, d) < r2max && ora_plist_push(pl, i, j)) return -1;
+		return 0;
+	}
+	const long ncell = (long)nc[0] * nc[1] * nc[2];
+	long *head = malloc(sizeof(long) * ncell), *next = malloc(sizeof(long) * n);
+	if (!head || !next) { free(head); free(next); return -1; }
+	for (long c = 0; c < ncell; c++) head[c] = -1;
+	int (*cell)[3] = malloc(sizeof(int) * 3 * n);
+	if (!cell) { free(head); free(next); return -1; }
+	for (long i = 0; i < n; i++) {
+		for (int k = 0; k < 3; k++) {
+			int c = (int)floor(x[3 * i + k] / L[k] * nc[k]);
+			c = c < 0 ? 0 : (c >= nc[k] ? nc[k] - 1 : c);
+			cell[i][k] = c;
+		}
+		const long c = cell[i][0] + (long)nc[0] * (cell[i][1] + (long)nc[1] * cell[i][2]);
+		next[i] = head[c];
+		head[c] = i;
+	}
+	int rc = 0;
+	for (long i = 0; i < n && !rc; i++)
+		for (int oz = -1; oz <= 1; oz++)
+			for (int oy = -1; oy <= 1; oy++)
+				for (int ox = -1; ox <= 1; ox++) {
+					const int cx = (cell[i][0] + ox + nc[0]) % nc[0];
+					const int cy = (cell[i][1] + oy + nc[1]) % nc[1];
+					const int cz = (cell[i][2] + oz + nc[2]) % nc[2];
+					for (long j = head[cx + (long)nc[0] * (cy + (long)nc[1] * cz)]; j != -1; j = next[j])
+						if (j > i && ora_sep(x, i, j, L, d) < r2max && ora_plist_push(pl, i, j))
+							rc = -1;
+				}
+	free(head); free(next); free(cell);
+	return rc;
+}
+
+static double ora_maxcf(int nt, const double *P)
+{
+	double c = 0.0;
+	for (int k = 0; k < nt * nt; k++)
+		if (P[4 * k + 1] != 0.0 && P[4 * k] > c) c = P[4 * k];
+	return c;
+}
+
+/* forces, energy and tr pot_P of the typed terms over the pairs of pl */
+static void ora_ljt_forces(long n, const double *x, const int *type, const double L[3], int nt,
+			   const double *P, const ora_plist *pl, double *F, double *epot, double *trw)
+{
+	memset(F, 0, sizeof(double) * 3 * n);
+	double e = 0.0, w = 0.0, d[3];
+	for (long k = 0; k < pl->np; k++) {
+		const long i = pl->ij[2 * k], j = pl->ij[2 * k + 1];
+		const double *p = P + 4 * (type[i] * nt + type[j]);
+		if (p[1] == 0.0) continue;
+		const double s = ora_sep(x, i, j, L, d);
+		if (s >= p[0] * p[0]) continue;
+		ora_pairfn f;
+		ora_lj_pairfn(p, s, &f);
+		for (int q = 0; q < 3; q++) {
+			F[3 * i + q] += f.phi * d[q];
+			F[3 * j + q] -= f.phi * d[q];
+		}
+		e += f.u;
+		w += f.phi * s;
+	}
+	*epot = e;
+	*trw = w;
+}
+
+double ora_ljt_loss(long n, const double *x0, const double *v0, const double *m, const int *type,
+		    const double L[3], int nt, const double *P, double dt, long nsteps)
+{
+	double *x = malloc(sizeof(double) * 3 * n), *u = malloc(sizeof(double) * 3 * n);
+	double *F = malloc(sizeof(double) * 3 * n);
+	ora_plist pl = {0, 0, NULL};
+	if (!x || !u || !F) { free(x); free(u); free(F); return NAN; }
+	memcpy(x, x0, sizeof(double) * 3 * n);
+	memcpy(u, v0, sizeof(double) * 3 * n);
+	const double V = L[0] * L[1] * L[2], rmax = ora_maxcf(nt, P);
+	double loss = 0.0;
+	for (long step = 0; step < nsteps; step++) {
+		double ep, trw, trk = 0.0;
+		if (ora_halfpairs(n, x, L, rmax, &pl)) { loss = NAN; break; }
+		ora_ljt_forces(n, x, type, L, nt, P, &pl, F, &ep, &trw);
+		for (long i = 0; i < n; i++)
+			for (int k = 0; k < 3; k++) {
+				const double a = F[3 * i + k] / m[i];
+				u[3 * i + k] += a * dt;
+				x[3 * i + k] += u[3 * i + k] * dt;
+				const double vt = u[3 * i + k] - 0.5 * a * dt;
+				trk += m[i] * vt * vt;
+			}
+		ora_wrap_all(x, L, n);
+		loss += ep + (trk + trw) / (3.0 * V);
+	}
+	free(x); free(u); free(F); free(pl.ij);
+	return loss / nsteps;
+}
+
+/* gradient of ora_ljt_loss: dL_deps[a * nt + b] and dL_dsig[a * nt + b]
+ * (both orders filled with the gradient of the one shared parameter) and
+ * dL_dx0 (3n) */
+int ora_ljt_adjoint(long n, const double *x0, const double *v0, const double *m, const int *type,
+		    const double L[3], int nt, const double *P, double dt, long nsteps, double *dL_deps,
+		    double *dL_dsig, double *dL_dx0)
+{
+	const long K = nsteps;
+	double *X = malloc(sizeof(double) * 3 * n * (K + 1)), *U = malloc(sizeof(double) * 3 * n * (K + 1));
+	double *F = malloc(sizeof(double) * 3 * n), *lx = calloc(3 * n, sizeof(double));
+	double *lu = calloc(3 * n, sizeof(double)), *h = malloc(sizeof(double) * 3 * n);
+	double *ge = calloc(nt * nt, sizeof(double)), *gs = calloc(nt * nt, sizeof(double));
+	ora_plist pl = {0, 0, NULL};
+	int rc = -1;
+	if (!X || !U || !F || !lx || !lu || !h || !ge || !gs) goto out;
+	memcpy(X, x0, sizeof(double) * 3 * n);
+	memcpy(U, v0, sizeof(double) * 3 * n);
+	const double V = L[0] * L[1] * L[2], cK = 1.0 / K, rmax = ora_maxcf(nt, P);
+	for (long s = 0; s < K; s++) {
+		double *x = X + 3 * n * s, *u = U + 3 * n * s, *x1 = X + 3 * n * (s + 1), *u1 = U + 3 * n * (s + 1);
+		double ep, trw;
+		if (ora_halfpairs(n, x, L, rmax, &pl)) goto out;
+		ora_ljt_forces(n, x, type, L, nt, P, &pl, F, &ep, &trw);
+		for (long q = 0; q < 3 * n; q++) {
+			u1[q] = u[q] + F[q] / m[q / 3] * dt;
+			x1[q] = x[q] + u1[q] * dt;
+		}
+		ora_wrap_all(x1, L, n);
+	}
+	for (long s = K - 1; s >= 0; s--) {
+		const double *x = X + 3 * n * s, *u = U + 3 * n * s, *u1 = U + 3 * n * (s + 1);
+		for (long q = 0; q < 3 * n; q++) {
+			const double mi = m[q / 3];
+			const double kin = cK * mi * 0.5 * (u[q] + u1[q]) / (3.0 * V);
+			const double g = lu[q] + dt * lx[q] + kin;
+			lu[q] = g + kin;
+			h[q] = dt / mi * g;
+		}
+		if (ora_halfpairs(n, x, L, rmax, &pl)) goto out;
+		for (long k = 0; k < pl.np; k++) {
+			const long i = pl.ij[2 * k], j = pl.ij[2 * k + 1];
+			const int tp = type[i] * nt + type[j];
+			const double *p = P + 4 * tp;
+			if (p[1] == 0.0) continue;
+			double d[3];
+			const double sq = ora_sep(x, i, j, L, d);
+			if (sq >= p[0] * p[0]) continue;
+			ora_pairfn f;
+			ora_lj_pairfn(p, sq, &f);
+			double dh[3], ddh = 0.0, dhi = 0.0, dhj = 0.0;
+			for (int q = 0; q < 3; q++) {
+				dh[q] = h[3 * i + q] - h[3 * j + q];
+				ddh += d[q] * dh[q];
+				dhi += d[q] * h[3 * i + q];
+				dhj += d[q] * h[3 * j + q];
+			}
+			const double c2 = 2.0 * f.phis * ddh + 2.0 * cK * (f.us + f.ws / (3.0 * V));
+			for (int q = 0; q < 3; q++) {
+				const double t = f.phi * dh[q] + c2 * d[q];
+				lx[3 * i + q] += t;
+				lx[3 * j + q] -= t;
+			}
+			const int tu = type[i] < type[j] ? type[i] * nt + type[j] : type[j] * nt + type[i];
+			ge[tu] += f.phie * (dhi - dhj) + cK * (f.ue + f.phie * sq / (3.0 * V));
+			gs[tu] += f.phisg * (dhi - dhj) + cK * (f.usg + f.phisg * sq / (3.0 * V));
+		}
+	}
+	for (int a = 0; a < nt; a++)
+		for (int b = 0; b < nt; b++) {
+			const int tu = a < b ? a * nt + b : b * nt + a;
+			dL_deps[a * nt + b] = ge[tu];
+			dL_dsig[a * nt + b] = gs[tu];
+		}
+	memcpy(dL_dx0, lx, sizeof(double) * 3 * n);
+	rc = 0;
+out:
+	free(X); free(U); free(F); free(lx); free(lu); free(h); free(ge); free(gs); free(pl.ij);
+	return rc;
+}
+
 /* ======================================================================
  * Stochastic dynamics: DPD pair force, Groot-Warren integrator,
  * Fokker-Planck and Langevin (GJF) integrators.

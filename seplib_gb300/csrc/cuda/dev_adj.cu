@@ -78,6 +78,9 @@ __global__ void ka_build(const BatchSys *sys, const int *wsys, int nwarps, const
 	}
 	ncnt[t] = cnt < maxnb ? cnt : maxnb;
 	if (cnt > maxnb) atomicOr(oflow, 1u);
+	// the last group of four is padded with the particle itself, as the
+	// list builder pads it (the step kernel reads whole groups)
+	for (int k = cnt; k < ((cnt + 3) & ~3) && k < maxnb; k++) nl[nl_index(t, k, maxnb)] = (int)t;
 }
 
 // a rebuilt system measures displacements from here on (skin test)
@@ -131,31 +134,48 @@ __global__ void ka_h(const BatchSys *sys, const int *wsys, int nwarps, AdjState 
 	h[t] = make_float4((float)(w * g[0]), (float)(w * g[1]), (float)(w * g[2]), 0.f);
 }
 
+// per type pair: the force parameters and what the gradient terms need
+struct AdjPot {
+	float rc2, sig2, eps48, eps4, aw, awh, ushift;
+	float inv_eps, inv_sig, dsh_sig;   // 1/eps, 1/sigma, d ushift / d sigma
+	int tu;                            // unordered type-pair index (gradient slot)
+};
+
+#define ADJ_MAXT SEPB_MAXTYPES
+
 struct AdjPair {
 	const BatchSys *sys;
 	const int *wsys;
 	int nwarps;
-	const int4 *pos;         // x_n (high words)
+	const int4 *pos;         // x_n (high words; .w = type id)
 	const int *pool;         // stored lists
 	const long *lbase;       // per system: offset of its list at this step (ints)
 	int maxnb;
 	const float4 *h;
 	double *lx;
-	long long *gslots;       // per system: d/deps, d/dsigma (fixed point)
-	float rc2, sig2, eps48, eps4, aw, awh, ushift;
-	float inv_eps, inv_sig, dsh_sig;   // 1/eps, 1/sigma, d ushift / d sigma
+	long long *gslots;       // per system: d/deps (NTP), then d/dsigma (NTP), fixed point
+	const AdjPot *pot;       // NT x NT
 	float cK;
 };
 
+// NT particle types, NTP = NT (NT + 1) / 2 type pairs, each with its own
+// eps and sigma gradient
+template <int NT>
 __global__ void __launch_bounds__(256) ka_pair(AdjPair a)
 {
+	constexpr int NTP = NT * (NT + 1) / 2;
+	__shared__ AdjPot sp[NT * NT];
+	for (int k = threadIdx.x; k < NT * NT; k += blockDim.x) sp[k] = a.pot[k];
+	__syncthreads();
 	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
 	const long wg = i >> 5;
 	if (wg >= a.nwarps) return;                   // whole warps
 	const int sidx = a.wsys[wg];
 	const BatchSys S = a.sys[sidx];
 	const bool act = i - S.off < S.n;
-	float lxx = 0.f, lxy = 0.f, lxz = 0.f, ge = 0.f, gs = 0.f;
+	float lxx = 0.f, lxy = 0.f, lxz = 0.f, ge[NTP], gs[NTP];
+#pragma unroll
+	for (int t = 0; t < NTP; t++) { ge[t] = 0.f; gs[t] = 0.f; }
 	if (act) {
 		const float fs = S.fs;
 		const float inv3V = (float)(1.0 / (3.0 * S.L * S.L * S.L));
@@ -164,20 +184,22 @@ __global__ void __launch_bounds__(256) ka_pair(AdjPair a)
 		const int cnt = lp[(long)S.npad * a.maxnb + li];
 		const int4 pi = a.pos[i];
 		const float4 hi = a.h[i];
+		const int row = NT > 1 ? pi.w * NT : 0;
 		for (int k = 0; k < cnt; k++) {
 			const int j = lp[nl_index(li, k, a.maxnb)];
 			const int4 pj = a.pos[j];
+			const AdjPot &pp = sp[NT > 1 ? row + pj.w : 0];
 			const float dx = sep_hi(pi.x, pj.x, fs), dy = sep_hi(pi.y, pj.y, fs), dz = sep_hi(pi.z, pj.z, fs);
 			const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-			if (s >= a.rc2) continue;
+			if (s >= pp.rc2) continue;
 			const float is = 1.0f / s;
-			const float q = a.sig2 * is;
+			const float q = pp.sig2 * is;
 			const float s6 = q * q * q;
-			const float phi = a.eps48 * q * s6 * (s6 - a.awh);
-			const float phis = -a.eps48 * q * s6 * (7.f * s6 - 4.f * a.awh) * is;
-			const float us = -0.25f * a.eps48 * s6 * (2.f * s6 - a.aw) * is;
-			const float ws = -3.f * a.eps48 * q * s6 * (2.f * s6 - a.awh);
-			const float u = a.eps4 * s6 * (s6 - a.aw) + a.ushift;
+			const float phi = pp.eps48 * q * s6 * (s6 - pp.awh);
+			const float phis = -pp.eps48 * q * s6 * (7.f * s6 - 4.f * pp.awh) * is;
+			const float us = -0.25f * pp.eps48 * s6 * (2.f * s6 - pp.aw) * is;
+			const float ws = -3.f * pp.eps48 * q * s6 * (2.f * s6 - pp.awh);
+			const float u = pp.eps4 * s6 * (s6 - pp.aw) + pp.ushift;
 			const float4 hj = a.h[j];
 			const float dhx = hi.x - hj.x, dhy = hi.y - hj.y, dhz = hi.z - hj.z;
 			const float ddh = dx * dhx + dy * dhy + dz * dhz;
@@ -186,23 +208,29 @@ __global__ void __launch_bounds__(256) ka_pair(AdjPair a)
 			lxy += phi * dhy + c2 * dy;
 			lxz += phi * dhz + c2 * dz;
 			const float dhi = dx * hi.x + dy * hi.y + dz * hi.z;
-			const float phie = phi * a.inv_eps, ue = u * a.inv_eps;
-			const float phisg = 2.f * a.eps48 * q * s6 * (7.f * s6 - 4.f * a.awh) * a.inv_sig;
-			const float usg = 0.5f * a.eps48 * a.inv_sig * s6 * (2.f * s6 - a.aw) + a.dsh_sig;
-			ge += phie * dhi + 0.5f * a.cK * (ue + phie * s * inv3V);
-			gs += phisg * dhi + 0.5f * a.cK * (usg + phisg * s * inv3V);
+			const float phie = phi * pp.inv_eps, ue = u * pp.inv_eps;
+			const float phisg = 2.f * pp.eps48 * q * s6 * (7.f * s6 - 4.f * pp.awh) * pp.inv_sig;
+			const float usg = 0.5f * pp.eps48 * pp.inv_sig * s6 * (2.f * s6 - pp.aw) + pp.dsh_sig;
+			const float te = phie * dhi + 0.5f * a.cK * (ue + phie * s * inv3V);
+			const float ts = phisg * dhi + 0.5f * a.cK * (usg + phisg * s * inv3V);
+#pragma unroll
+			for (int t = 0; t < NTP; t++) {
+				const bool mine = NTP == 1 || pp.tu == t;
+				ge[t] += mine ? te : 0.f;
+				gs[t] += mine ? ts : 0.f;
+			}
 		}
 		a.lx[3 * i] += (double)lxx;
 		a.lx[3 * i + 1] += (double)lxy;
 		a.lx[3 * i + 2] += (double)lxz;
 	}
-	float v[2] = {ge, gs};
-	warp_sum<2>(v);
-	if ((threadIdx.x & 31) == 0) {
-		long long *g = a.gslots + 2 * (long)sidx;
-		for (int k = 0; k < 2; k++) {
-			const long long q = __float2ll_rn(v[k] * FX_SCALE);
-			if (q != 0) atomicAdd((unsigned long long *)&g[k], (unsigned long long)q);
+	long long *g = a.gslots + 2 * NTP * (long)sidx;
+#pragma unroll
+	for (int t = 0; t < NTP; t++) {
+		const long long qe = warp_sum_fx(to_fx(ge[t])), qs = warp_sum_fx(to_fx(gs[t]));
+		if ((threadIdx.x & 31) == 0) {
+			if (qe != 0) atomicAdd((unsigned long long *)&g[t], (unsigned long long)qe);
+			if (qs != 0) atomicAdd((unsigned long long *)&g[NTP + t], (unsigned long long)qs);
 		}
 	}
 }
@@ -221,7 +249,6 @@ struct sepadj {
 	sepb *b;
 	int C;
 	long K;
-	double eps, sigma, aw, cf;
 	std::vector<Ckpt> ck;
 	size_t ck_bytes;
 	char *seg;                       // (C + 1) stored steps
@@ -232,10 +259,13 @@ struct sepadj {
 	long *d_lbase;
 	double *lx, *lu;
 	float4 *h;
-	long long *gslots;
+	long long *gslots;               // per replica: 2 NTP fixed-point gradients
+	int nt, ntp;                     // particle types, type pairs
+	AdjPot *dpot;                    // nt x nt
 	unsigned *h_flag;                // pinned
 	std::vector<double> loss;
 	int have_forward;
+	int at_end;                      // the device holds the state the last forward ended in
 };
 
 static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -269,7 +299,7 @@ extern "C" void sepadj_destroy(sepadj *A)
 	if (A->b && A->b->d) cudaStreamSynchronize(A->b->d->st);
 	for (auto &c : A->ck)
 		if (c.dev) cudaFree(c.dev);
-	void *dv[] = {A->seg, A->pool, A->d_lbase, A->lx, A->lu, A->h, A->gslots};
+	void *dv[] = {A->seg, A->pool, A->d_lbase, A->lx, A->lu, A->h, A->gslots, A->dpot};
 	for (size_t k = 0; k < sizeof dv / sizeof dv[0]; k++)
 		if (dv[k]) cudaFree(dv[k]);
 	if (A->h_flag) cudaFreeHost(A->h_flag);
@@ -277,24 +307,54 @@ extern "C" void sepadj_destroy(sepadj *A)
 	delete A;
 }
 
-extern "C" sepadj *sepadj_create(int nrep, const int *npart, const double *L, double rc, double skin,
-				 double dt, const double *ljparam, int ckpt_every)
+// the per-type-pair table of the gradient kernel (params: nt x nt sets of
+// {cf, eps, sigma, aw}; eps = 0: no term)
+static int adj_pot_table(sepadj *A, int nt, const double *params)
 {
-	if (!ljparam || ckpt_every < 1) {
-		batch_fail("sepadj_create: ljparam and ckpt_every >= 1 are required", SEPDEV_EINVAL);
-		return NULL;
-	}
-	sepb *b = sepb_create(nrep, npart, L, rc, skin, dt, ljparam);
+	std::vector<AdjPot> t(nt * nt);
+	for (int a = 0; a < nt; a++)
+		for (int c = 0; c < nt; c++) {
+			const double *p = params + 4 * (a * nt + c);
+			AdjPot &q = t[a * nt + c];
+			memset(&q, 0, sizeof q);
+			const int lo = a < c ? a : c, hi = a < c ? c : a;
+			q.tu = lo * nt - lo * (lo - 1) / 2 + (hi - lo);
+			if (p[1] == 0.0) continue;           // rc2 = 0: the pair is skipped
+			const double cf = p[0], eps = p[1], sig = p[2], aw = p[3];
+			const double sr6 = pow(sig / cf, 6.0);
+			q.rc2 = (float)(cf * cf);
+			q.sig2 = (float)(sig * sig);
+			q.eps48 = (float)(48.0 * eps);
+			q.eps4 = (float)(4.0 * eps);
+			q.aw = (float)aw;
+			q.awh = (float)(0.5 * aw);
+			q.ushift = (float)(-4.0 * eps * (sr6 * sr6 - aw * sr6));
+			q.inv_eps = (float)(1.0 / eps);
+			q.inv_sig = (float)(1.0 / sig);
+			q.dsh_sig = (float)(-24.0 * eps / sig * (2.0 * sr6 * sr6 - aw * sr6));
+		}
+	A->nt = nt;
+	A->ntp = nt * (nt + 1) / 2;
+	CK(cudaMalloc((void **)&A->dpot, sizeof(AdjPot) * nt * nt));
+	CK(cudaMemcpy(A->dpot, t.data(), sizeof(AdjPot) * nt * nt, cudaMemcpyHostToDevice));
+	return SEPDEV_OK;
+}
+
+static sepadj *adj_make(sepb *b, int nrep, int nt, const double *params, int ckpt_every)
+{
 	if (!b) return NULL;
 	sepadj *A = new sepadj();
 	A->b = b;
 	A->C = ckpt_every;
-	A->cf = ljparam[0]; A->eps = ljparam[1]; A->sigma = ljparam[2]; A->aw = ljparam[3];
 	const long n = b->ntot;
+	if (adj_pot_table(A, nt, params)) {
+		sepadj_destroy(A);
+		return NULL;
+	}
 	cudaError_t e = cudaMalloc((void **)&A->lx, sizeof(double) * 3 * n);
 	if (e == cudaSuccess) e = cudaMalloc((void **)&A->lu, sizeof(double) * 3 * n);
 	if (e == cudaSuccess) e = cudaMalloc((void **)&A->h, sizeof(float4) * n);
-	if (e == cudaSuccess) e = cudaMalloc((void **)&A->gslots, sizeof(long long) * 2 * nrep);
+	if (e == cudaSuccess) e = cudaMalloc((void **)&A->gslots, sizeof(long long) * 2 * A->ntp * nrep);
 	if (e == cudaSuccess) e = cudaMallocHost((void **)&A->h_flag, sizeof(unsigned) * nrep);
 	if (e != cudaSuccess) {
 		sepdev_set_error("sepadj_create", e);
@@ -305,6 +365,28 @@ extern "C" sepadj *sepadj_create(int nrep, const int *npart, const double *L, do
 	return A;
 }
 
+extern "C" sepadj *sepadj_create(int nrep, const int *npart, const double *L, double rc, double skin,
+				 double dt, const double *ljparam, int ckpt_every)
+{
+	if (!ljparam || ckpt_every < 1) {
+		batch_fail("sepadj_create: ljparam and ckpt_every >= 1 are required", SEPDEV_EINVAL);
+		return NULL;
+	}
+	return adj_make(sepb_create(nrep, npart, L, rc, skin, dt, ljparam), nrep, 1, ljparam, ckpt_every);
+}
+
+extern "C" sepadj *sepadj_create_typed(int nrep, const int *npart, const double *L, double skin, double dt,
+				       int ntypes, const double *ljparams, int ckpt_every)
+{
+	if (!ljparams || ckpt_every < 1 || ntypes < 1 || ntypes > ADJ_MAXT) {
+		batch_fail("sepadj_create_typed: 1 to 4 types, their parameters and ckpt_every >= 1 are required",
+			   SEPDEV_EINVAL);
+		return NULL;
+	}
+	return adj_make(sepb_create_typed(nrep, npart, L, skin, dt, ntypes, ljparams), nrep, ntypes, ljparams,
+			ckpt_every);
+}
+
 extern "C" int sepadj_set_state(sepadj *A, int r, const double *x, const double *v, const double *m)
 {
 	if (!A) return batch_fail("sepadj_set_state: no adjoint", SEPDEV_EINVAL);
@@ -312,6 +394,15 @@ extern "C" int sepadj_set_state(sepadj *A, int r, const double *x, const double 
 	for (auto &c : A->ck) { if (c.dev) cudaFree(c.dev); c.dev = NULL; }
 	A->ck.clear();
 	return sepb_set_state(A->b, r, x, v, m);
+}
+
+extern "C" int sepadj_set_types(sepadj *A, int r, const int *type)
+{
+	if (!A) return batch_fail("sepadj_set_types: no adjoint", SEPDEV_EINVAL);
+	A->have_forward = 0;
+	for (auto &c : A->ck) { if (c.dev) cudaFree(c.dev); c.dev = NULL; }
+	A->ck.clear();
+	return sepb_set_types(A->b, r, type);
 }
 
 // sort-free list rebuild of the flagged systems from buffer `parity`
@@ -459,6 +550,7 @@ extern "C" int sepadj_forward(sepadj *A, long nsteps, double *loss)
 	}
 	A->K = nsteps;
 	A->have_forward = 1;
+	A->at_end = 1;
 	return SEPDEV_OK;
 }
 
@@ -509,7 +601,7 @@ static int seg_store(sepadj *A, int k)
 	return SEPDEV_OK;
 }
 
-extern "C" int sepadj_backward(sepadj *A, double *dloss_deps, double *dloss_dsigma, double *dloss_dx0)
+static int adj_backward(sepadj *A, double *dloss_deps, double *dloss_dsigma, double *dloss_dx0)
 {
 	if (!A || !A->have_forward) return batch_fail("sepadj_backward: no forward pass", SEPDEV_EINVAL);
 	sepb *b = A->b;
@@ -520,23 +612,15 @@ extern "C" int sepadj_backward(sepadj *A, double *dloss_deps, double *dloss_dsig
 	if ((rc = seg_alloc(A))) return rc;
 	CK(cudaMemsetAsync(A->lx, 0, sizeof(double) * 3 * n, d->st));
 	CK(cudaMemsetAsync(A->lu, 0, sizeof(double) * 3 * n, d->st));
-	CK(cudaMemsetAsync(A->gslots, 0, sizeof(long long) * 2 * nsys, d->st));
+	const int ntp = A->ntp;
+	A->at_end = 0;
+	CK(cudaMemsetAsync(A->gslots, 0, sizeof(long long) * 2 * ntp * nsys, d->st));
 	const double cK = 1.0 / (double)A->K;
 	AdjPair P;
 	memset(&P, 0, sizeof P);
 	P.sys = b->sys; P.wsys = b->wsys; P.nwarps = b->nwarps; P.pool = A->pool;
 	P.maxnb = d->maxnb; P.h = A->h; P.lx = A->lx; P.gslots = A->gslots;
-	P.rc2 = (float)(A->cf * A->cf);
-	P.sig2 = (float)(A->sigma * A->sigma);
-	P.eps48 = (float)(48.0 * A->eps);
-	P.eps4 = (float)(4.0 * A->eps);
-	P.aw = (float)A->aw;
-	P.awh = (float)(0.5 * A->aw);
-	P.ushift = (float)b->ushift;
-	P.inv_eps = (float)(1.0 / A->eps);
-	P.inv_sig = (float)(1.0 / A->sigma);
-	const double sr = A->sigma / A->cf, sr6 = pow(sr, 6.0);
-	P.dsh_sig = (float)(-24.0 * A->eps / A->sigma * (2.0 * sr6 * sr6 - A->aw * sr6));
+	P.pot = A->dpot;
 	P.cK = (float)cK;
 	const long nseg = (A->K + A->C - 1) / A->C;
 	for (long sg = nseg - 1; sg >= 0; sg--) {
@@ -570,13 +654,20 @@ extern "C" int sepadj_backward(sepadj *A, double *dloss_deps, double *dloss_dsig
 								 seg_state(A, k + 1), A->lx, A->lu, A->h, b->dt, cK);
 			P.pos = seg_state(A, k).pos;
 			P.lbase = A->d_lbase + (size_t)k * nsys;
-			ka_pair<<<grid_for(n, 256), 256, 0, d->st>>>(P);
+			const int g = grid_for(n, 256);
+			switch (A->nt) {
+			case 1: ka_pair<1><<<g, 256, 0, d->st>>>(P); break;
+			case 2: ka_pair<2><<<g, 256, 0, d->st>>>(P); break;
+			case 3: ka_pair<3><<<g, 256, 0, d->st>>>(P); break;
+			default: ka_pair<4><<<g, 256, 0, d->st>>>(P); break;
+			}
 			CKL(d);
 		}
 	}
 	// gradients out
-	std::vector<long long> g(2 * nsys);
-	CK(cudaMemcpyAsync(g.data(), A->gslots, sizeof(long long) * 2 * nsys, cudaMemcpyDeviceToHost, d->st));
+	std::vector<long long> g(2 * ntp * nsys);
+	CK(cudaMemcpyAsync(g.data(), A->gslots, sizeof(long long) * 2 * ntp * nsys, cudaMemcpyDeviceToHost,
+			   d->st));
 	std::vector<double> lx;
 	std::vector<int> gid;
 	if (dloss_dx0) {
@@ -587,9 +678,17 @@ extern "C" int sepadj_backward(sepadj *A, double *dloss_deps, double *dloss_dsig
 	}
 	CK(cudaStreamSynchronize(d->st));
 	long out = 0;
+	const int nt = A->nt;
 	for (int s = 0; s < nsys; s++) {
-		if (dloss_deps) dloss_deps[s] = (double)g[2 * s] * FX_ISCALE;
-		if (dloss_dsigma) dloss_dsigma[s] = (double)g[2 * s + 1] * FX_ISCALE;
+		// every ordered type pair gets the gradient of its unordered pair's parameter
+		for (int a = 0; a < nt; a++)
+			for (int c = 0; c < nt; c++) {
+				const int lo = a < c ? a : c, hi = a < c ? c : a;
+				const int tu = lo * nt - lo * (lo - 1) / 2 + (hi - lo);
+				const size_t o = ((size_t)s * nt + a) * nt + c;
+				if (dloss_deps) dloss_deps[o] = (double)g[2 * ntp * s + tu] * FX_ISCALE;
+				if (dloss_dsigma) dloss_dsigma[o] = (double)g[2 * ntp * s + ntp + tu] * FX_ISCALE;
+			}
 		if (dloss_dx0) {
 			const BatchSys &S = b->hsys[s];
 			for (int t = 0; t < S.n; t++) {
@@ -601,4 +700,24 @@ extern "C" int sepadj_backward(sepadj *A, double *dloss_deps, double *dloss_dsig
 		}
 	}
 	return SEPDEV_OK;
+}
+
+extern "C" int sepadj_backward(sepadj *A, double *dloss_deps, double *dloss_dsigma, double *dloss_dx0)
+{
+	if (A && A->nt > 1)
+		return batch_fail("sepadj_backward: a typed adjoint returns its gradients through "
+				  "sepadj_backward_typed", SEPDEV_EINVAL);
+	return adj_backward(A, dloss_deps, dloss_dsigma, dloss_dx0);
+}
+
+extern "C" int sepadj_backward_typed(sepadj *A, double *dloss_deps, double *dloss_dsigma, double *dloss_dx0)
+{
+	return adj_backward(A, dloss_deps, dloss_dsigma, dloss_dx0);
+}
+
+extern "C" int sepadj_get_state(sepadj *A, int r, double *x, double *v)
+{
+	if (!A || !A->at_end)
+		return batch_fail("sepadj_get_state: call it after sepadj_forward, before sepadj_backward", SEPDEV_EINVAL);
+	return sepb_get_state(A->b, r, x, v, NULL);
 }

@@ -338,6 +338,7 @@ extern "C" sepb *sepb_create(int nsys, const int *npart, const double *L, double
 	const double rlist = rc + skin;
 	b->hsys.resize(nsys);
 	b->have.assign(nsys, 0);
+	b->fresh.assign(nsys, 0);
 	b->nupd.assign(nsys, 0u);
 	b->alpha0.assign(nsys, 0.0);
 	long off = 0, coff = 0;
@@ -350,6 +351,9 @@ extern "C" sepb *sepb_create(int nsys, const int *npart, const double *L, double
 		S.off = (int)off;
 		S.L = L[s];
 		S.fs = (float)(L[s] / 4294967296.0);
+		// from the FP32 sigma^2 and cut-off the single-system path holds, so a
+		// system computes with the same constants in a batch and alone
+		S.sc = lj_scale(L[s], (double)(float)(b->sigma * b->sigma), (double)(float)(b->cf * b->cf));
 		const double sc = dt * 18446744073709551616.0 / L[s];
 		S.shi = (float)sc;
 		S.slo = (float)(sc - (double)S.shi);
@@ -464,7 +468,87 @@ extern "C" int sepb_set_state(sepb *b, int s, const double *x, const double *v, 
 	st.force_trig = 1;
 	b->nupd[s] = 0;
 	b->have[s] = 1;
+	b->fresh[s] = 1;
 	b->list_ok = 0;
+	return SEPDEV_OK;
+}
+
+extern "C" sepb *sepb_create_typed(int nsys, const int *npart, const double *L, double skin, double dt,
+				   int ntypes, const double *ljparams)
+{
+	if (ntypes < 1 || ntypes > SEPB_MAXTYPES || !ljparams) {
+		batch_fail("sepb_create_typed: 1 to 4 types and their parameters are required", SEPDEV_EINVAL);
+		return NULL;
+	}
+	double rc = 0.0;
+	const double *p0 = NULL;
+	for (int a = 0; a < ntypes; a++)
+		for (int c = 0; c < ntypes; c++) {
+			const double *p = ljparams + 4 * (a * ntypes + c), *q = ljparams + 4 * (c * ntypes + a);
+			if (p[0] != q[0] || p[1] != q[1] || p[2] != q[2] || p[3] != q[3]) {
+				batch_fail("sepb_create_typed: the parameters of a type pair must not depend on its order",
+					   SEPDEV_EINVAL);
+				return NULL;
+			}
+			if (p[1] == 0.0) continue;
+			if (!(p[0] > 0) || !(p[2] > 0)) {
+				batch_fail("sepb_create_typed: cut-off and sigma must be positive", SEPDEV_EINVAL);
+				return NULL;
+			}
+			if (p[0] > rc) rc = p[0];
+			if (!p0) p0 = p;
+		}
+	if (!p0) {
+		batch_fail("sepb_create_typed: no type pair interacts", SEPDEV_EINVAL);
+		return NULL;
+	}
+	sepb *b = sepb_create(nsys, npart, L, rc, skin, dt, p0);
+	if (!b) return NULL;
+	b->ntypes = ntypes;
+	memcpy(b->tparam, ljparams, sizeof(double) * 4 * ntypes * ntypes);
+	// the parameter table, unscaled: every pair's own cut-off and shift
+	sepdev_pairset ps;
+	memset(&ps, 0, sizeof ps);
+	ps.ntypes = ntypes;
+	for (int k = 0; k < ntypes * ntypes; k++) {
+		const double *p = ljparams + 4 * k;
+		sepdev_pot &P = ps.pot[k];
+		P.kind = SEPDEV_POT_LJ;
+		if (p[1] == 0.0) continue;           // no term: rc2 = 0, eps = 0
+		P.rc2 = (float)(p[0] * p[0]);
+		P.eps48 = (float)(48.0 * p[1]);
+		P.eps4 = (float)(4.0 * p[1]);
+		P.sig2 = (float)(p[2] * p[2]);
+		P.aw = (float)p[3];
+		P.awh = (float)(0.5 * p[3]);
+		P.ushift = (float)(-4.0 * p[1] * (pow(p[2] / p[0], 12.) - p[3] * pow(p[2] / p[0], 6.)));
+	}
+	int rc0 = sepdev_upload_pairset(b->d, &ps);
+	if (!rc0) rc0 = cudaStreamSynchronize(b->d->st) == cudaSuccess ? SEPDEV_OK : SEPDEV_ECUDA;
+	if (rc0) {
+		sepb_destroy(b);
+		return NULL;
+	}
+	return b;
+}
+
+extern "C" int sepb_set_types(sepb *b, int s, const int *type)
+{
+	if (!b || s < 0 || s >= b->nsys || !type) return batch_fail("sepb_set_types: invalid arguments", SEPDEV_EINVAL);
+	if (!b->fresh[s])
+		return batch_fail("sepb_set_types: call it after sepb_set_state of the system, before a run",
+				  SEPDEV_EINVAL);
+	const BatchSys &S = b->hsys[s];
+	sepdev *d = b->d;
+	std::vector<int4> hp(S.npad);
+	CK(cudaMemcpy(hp.data(), d->pos[0] + S.off, sizeof(int4) * S.npad, cudaMemcpyDeviceToHost));
+	for (int i = 0; i < S.n; i++) {
+		if (type[i] < 0 || type[i] >= b->ntypes)
+			return batch_fail("sepb_set_types: type id outside 0..ntypes-1", SEPDEV_EINVAL);
+		hp[i].w = type[i];           // slots are in the system's own order until its first run
+	}
+	CK(cudaMemcpy(d->pos[0] + S.off, hp.data(), sizeof(int4) * S.npad, cudaMemcpyHostToDevice));
+	CK(cudaMemcpy(d->pos[1] + S.off, hp.data(), sizeof(int4) * S.npad, cudaMemcpyHostToDevice));
 	return SEPDEV_OK;
 }
 
@@ -498,6 +582,7 @@ PairArgs batch_pair_args(sepb *b, int parity)
 	P.aw = (float)b->aw;
 	P.awh = (float)(0.5 * b->aw);
 	P.ushift = (float)b->ushift;
+	P.ushl = (float)(b->ushift - (double)P.ushift);
 	PairArgs a;
 	sepdev_fill_args(b->d, a, &ps, b->dt, b->nh, 0.0, 0, 0, 0, parity);
 	a.flags = b->d->flags;
@@ -585,7 +670,8 @@ int batch_step_launch(sepb *b, int parity, const BatchDecide &dec)
 {
 	PairArgs a = batch_pair_args(b, parity);
 	CK(cudaGetLastError());
-	int rc = sepdev_batch_step(b->d, a, b->sys, b->wsys, b->nwarps, b->bs, b->run, b->slots, dec);
+	int rc = sepdev_batch_step(b->d, a, b->sys, b->wsys, b->nwarps, b->bs, b->run, b->slots, dec,
+				   b->ntypes > 1);
 	if (rc) return rc;
 	kb_decide<<<grid_for((long)b->nsys * 32, 256), 256, 0, b->d->st>>>(dec);
 	CKL(b->d);
@@ -710,6 +796,7 @@ int batch_initial_lists(sepb *b)
 	}
 	b->list_ok = 1;
 	b->h_run->last_any = 0;
+	for (int s = 0; s < b->nsys; s++) b->fresh[s] = 0;
 	return SEPDEV_OK;
 }
 

@@ -12,12 +12,15 @@
 #include "dev_decide.cuh"
 #include "dev_pair.cuh"
 
+#define SEPB_MAXTYPES 4     // particle types of a typed batch
+
 struct BatchSys {
 	int off, n, npad;      // slots and real particles
 	int coff, ncell;       // cell offset, real cells
 	int nc[3];             // cells per side
 	float fs;              // L / 2^32 (cubic box)
 	float shi, slo;        // dt * 2^64 / L as a float pair
+	LjScale sc;            // the single-LJ constants in this box's units
 	double L;
 	double T0;             // thermostat target
 };
@@ -63,7 +66,8 @@ struct BatchDecide {
 
 // launchers implemented next to the single-system kernels they share code with
 int sepdev_batch_step(sepdev *d, const PairArgs &a, const BatchSys *sys, const int *wsys, int nwarps,
-		      const BatchState *bs, const BatchRun *run, long long *slots, const BatchDecide &dec);
+		      const BatchState *bs, const BatchRun *run, long long *slots, const BatchDecide &dec,
+		      int typed);
 int sepdev_batch_build(sepdev *d, int parity, const int *cellstart, const BatchSys *sys,
 		       const int *wsys, int nwarps, const unsigned *flag, float rl2);
 
@@ -77,6 +81,11 @@ struct sepb {
 	double rc, skin, dt, tau;
 	int nh;
 	double cf, eps, sigma, aw, ushift;
+	// typed batch (ntypes > 1): {cf, eps, sigma, aw} per ordered type pair
+	// (symmetric), type ids in pos.w
+	int ntypes;
+	double tparam[SEPB_MAXTYPES * SEPB_MAXTYPES][4];
+	std::vector<char> fresh;       // state set and not yet run (types may be set)
 	std::vector<BatchSys> hsys;
 	BatchSys *sys;             // device
 	int *wsys, *csys;

@@ -9,8 +9,9 @@
 //    more than FP64 resolution (L / 2^64) without a single FP64 instruction.
 //  * velocity: float-float (hi + lo, ~48-bit mantissa).
 //  * per-pair force, energy and virial: FP32.
-//  * sums over particles: FP32 within a warp (<= 32 particles), then exact
-//    64-bit fixed point (scale 2^32) through integer atomics, so every total is
+//  * sums over particles: every particle's term is converted exactly to 64-bit
+//    fixed point (scale 2^32) and summed with integer warp reductions and
+//    integer atomics, so every total is exact to 2^-32 per term and
 //    independent of scheduling order.
 #pragma once
 
@@ -137,9 +138,7 @@ struct sepdev {
 	void *hio_scr;
 	size_t hio_bytes;
 
-	// kernel variants chosen by the tuner (SEPLIB_LJ_VARIANT overrides)
-	int lj_variant;
-	int nsm;
+	int nsm;                // streaming multiprocessors of the device
 
 	long launches;
 };
@@ -174,106 +173,105 @@ __device__ __forceinline__ float sep_hi(int a, int b, float s)
 // float-float: (hi, lo) + q, returns renormalised pair
 __device__ __forceinline__ void ff_add(float &hi, float &lo, float q)
 {
-	float s = hi + q;
-	float bp = s - hi;
-	float e = (hi - (s - bp)) + (q - bp);   // two-sum error
-	e += lo;
-	float h2 = s + e;
-	lo = e - (h2 - s);
+	const float s = __fadd_rn(hi, q);
+	const float bp = __fsub_rn(s, hi);
+	float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(q, bp));   // two-sum error
+	e = __fadd_rn(e, lo);
+	const float h2 = __fadd_rn(s, e);
+	lo = __fsub_rn(e, __fsub_rn(h2, s));
 	hi = h2;
 }
 
 // 64-bit fixed-point increment round((hi + lo) * (shi + slo)) with
 // |result| < 2^62; exact product of the high parts via FMA
+// (explicit roundings throughout, so every kernel that inlines it computes
+// the same bits whatever the compiler contracts around it)
 __device__ __forceinline__ long long ff_mul_fix(float hi, float lo, float shi, float slo)
 {
-	float p = hi * shi;
-	float e = fmaf(hi, shi, -p);
-	float r = e + (hi * slo + lo * shi);
+	const float p = __fmul_rn(hi, shi);
+	const float e = __fmaf_rn(hi, shi, -p);
+	const float r = __fadd_rn(e, __fmaf_rn(hi, slo, __fmul_rn(lo, shi)));
 	return __float2ll_rn(p) + __float2ll_rn(r);
-}
-
-// ---- packed FP32 pairs (f32x2 instructions of sm_100-family GPUs) --------
-// Two floats in one 64-bit register; one instruction operates on both.
-typedef unsigned long long f2_t;
-__device__ __forceinline__ f2_t f2_pack(float a, float b)
-{
-	f2_t r;
-	asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-	return r;
-}
-__device__ __forceinline__ void f2_unpack(f2_t r, float &a, float &b)
-{
-	asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
-}
-__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c)
-{
-	f2_t d;
-	asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-	return d;
-}
-__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b)
-{
-	f2_t d;
-	asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-	return d;
-}
-__device__ __forceinline__ f2_t f2_add(f2_t a, f2_t b)
-{
-	f2_t d;
-	asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-	return d;
-}
-__device__ __forceinline__ f2_t f2_sub(f2_t a, f2_t b)
-{
-	f2_t d;
-	asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-	return d;
-}
-__device__ __forceinline__ float f2_sum(f2_t r)
-{
-	float a, b;
-	f2_unpack(r, a, b);
-	return a + b;
 }
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31; }
 
-// Warp sum of NV floats, result valid in lane 0.
-template <int NV>
-__device__ __forceinline__ void warp_sum(float (&v)[NV])
+// Fixed-point value (units of 2^-32, rounded to the nearest unit) of a
+// float.  The 64-bit float-to-integer conversion runs at a small fraction of
+// the 32-bit rates, so for |v| < 2^22 the value is split exactly: n =
+// round(v) by the 1.5 * 2^23 addition (full-rate FP32), f = v - n exactly
+// (|f| <= 1/2, Sterbenz), and f * 2^32 converted with one 32-bit conversion.
+// Larger values (or NaN) take the 64-bit conversion.
+__device__ __forceinline__ long long to_fx(float v)
 {
-#pragma unroll
-	for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-		for (int k = 0; k < NV; k++) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+	if (!(fabsf(v) < 4194304.0f)) return __float2ll_rn(v * FX_SCALE);
+	const float M = 12582912.0f;
+	const float t = __fadd_rn(v, M);
+	const int n = __float_as_int(t) - 0x4B400000;
+	const float f = __fsub_rn(v, __fsub_rn(t, M));
+	// |f 2^32| <= 2^31: the one value that does not fit (f = 1/2) saturates,
+	// an error of one unit
+	const int lo = __float2int_rn(__fmul_rn(f, FX_SCALE));
+	return (long long)n * 4294967296ll + (long long)lo;
 }
 
-// Block reduction of NV floats: base[fld[k]] += sum v[k] through 64-bit
-// fixed-point atomics (FP32 inside each warp, exact integer sums above), plus
-// an optional max of a non-negative float into base[maxfld] (maxfld < 0: none).
-// Must be called by all threads of the block, once per kernel.
+// the same for a float-float (h + l, |l| <= ulp(h)/2, |h| < 2^23)
+__device__ __forceinline__ long long to_fx2(float h, float l)
+{
+	return to_fx(h) + (long long)__float2int_rn(__fmul_rn(l, FX_SCALE));
+}
+
+// m * a * b for float-float a and b, as a float-float (hi, lo): the product
+// of the high parts is split exactly with an FMA; the cross terms and the
+// mass factor carry the rest (relative error ~2^-44).  Every product and
+// sum is an explicit rounding, so no compiler contraction changes the bits.
+__device__ __forceinline__ void ff_mprod(float m, float ah, float al, float bh, float bl, float &hi,
+					 float &lo)
+{
+	const float p = __fmul_rn(ah, bh);
+	const float e = __fadd_rn(__fmaf_rn(ah, bh, -p), __fmaf_rn(ah, bl, __fmul_rn(al, bh)));
+	hi = __fmul_rn(m, p);
+	lo = __fadd_rn(__fmaf_rn(m, p, -hi), __fmul_rn(m, e));
+}
+
+// Exact warp sum of 64-bit fixed-point values (result in every lane): the
+// high words and the two 16-bit halves of the low words are summed
+// separately with integer warp reductions, so no carry is lost.  The high
+// words' sum must fit in 32 bits (|sum| < 2^31 units of 1).
+__device__ __forceinline__ long long warp_sum_fx(long long q)
+{
+	const unsigned FULL = 0xffffffffu;
+	const unsigned lo = (unsigned)q;
+	const int shi = __reduce_add_sync(FULL, (int)(q >> 32));
+	const unsigned smid = __reduce_add_sync(FULL, lo >> 16);
+	const unsigned slo = __reduce_add_sync(FULL, lo & 0xffffu);
+	return ((long long)shi << 32) + ((long long)smid << 16) + (long long)slo;
+}
+
+// Block reduction of NV fixed-point values: base[fld[k]] += sum q[k] through
+// 64-bit integer atomics, exact at every level (so totals do not depend on
+// the order of anything), plus an optional max of a non-negative float into
+// base[maxfld] (maxfld < 0: none).  Must be called by all threads of the
+// block, once per kernel.
 template <int NV>
-__device__ __forceinline__ void block_to_slot(float (&v)[NV], const int (&fld)[NV],
-					      long long *base, float maxval, int maxfld)
+__device__ __forceinline__ void block_to_slot_fx(const long long (&q)[NV], const int (&fld)[NV],
+						 long long *base, float maxval, int maxfld)
 {
 	__shared__ long long red[32][NV];
 	__shared__ unsigned redm[32];
-	warp_sum<NV>(v);
 	const unsigned mx = __reduce_max_sync(0xffffffffu, __float_as_uint(maxval));
 	const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-	if (lane_id() == 0) {
 #pragma unroll
-		for (int k = 0; k < NV; k++) red[w][k] = __float2ll_rn(v[k] * FX_SCALE);
-		redm[w] = mx;
+	for (int k = 0; k < NV; k++) {
+		const long long s = warp_sum_fx(q[k]);
+		if (lane_id() == 0) red[w][k] = s;
 	}
+	if (lane_id() == 0) redm[w] = mx;
 	__syncthreads();
 	if (w == 0) {
 #pragma unroll
 		for (int k = 0; k < NV; k++) {
-			long long s = (int)lane_id() < nw ? red[lane_id()][k] : 0ll;
-#pragma unroll
-			for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+			const long long s = warp_sum_fx((int)lane_id() < nw ? red[lane_id()][k] : 0ll);
 			if (lane_id() == 0 && s != 0)
 				atomicAdd((unsigned long long *)&base[fld[k]], (unsigned long long)s);
 		}
@@ -284,6 +282,18 @@ __device__ __forceinline__ void block_to_slot(float (&v)[NV], const int (&fld)[N
 				atomicMax((unsigned long long *)&base[maxfld], (unsigned long long)m);
 		}
 	}
+}
+
+// Block reduction of NV per-thread floats (each converted exactly to fixed
+// point first), as block_to_slot_fx.
+template <int NV>
+__device__ __forceinline__ void block_to_slot(const float (&v)[NV], const int (&fld)[NV],
+					      long long *base, float maxval, int maxfld)
+{
+	long long q[NV];
+#pragma unroll
+	for (int k = 0; k < NV; k++) q[k] = to_fx(v[k]);
+	block_to_slot_fx<NV>(q, fld, base, maxval, maxfld);
 }
 
 // host to_fixed (dev_state.cu) with the same operations and roundings

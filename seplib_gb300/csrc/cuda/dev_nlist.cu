@@ -9,8 +9,10 @@
 //                 share a cell, one atomic per group);
 //   2. k_scan     exclusive scan of the counts (one block);
 //   3. k_scatter  destination slot = cell start + rank in the cell;
-//   4. k_cellsort particles of a cell ordered by user index, so the order and
-//                 every floating-point sum after it are run-to-run identical;
+//   4. k_cellsort particles of a cell ordered by x (ties by user index), so
+//                 a run of particles is a compact slab along the cell row and
+//                 the order, and every floating-point sum after it, are
+//                 run-to-run identical;
 //   5. k_gather   all per-particle arrays permuted into cell order;
 //   6. k_build    FULL list (both i->j and j->i, so the force pass needs no
 //                 atomics), cut-off r^2 < rlist^2 on FP32 minimum-image
@@ -231,10 +233,6 @@ __device__ __forceinline__ float warp_max_f(float v, unsigned mask)
 // MOLX (same-molecule exclusions): the candidates' molecule indices are
 // staged in spm beside their positions, and in-box runs take a branch-free
 // loop that tests them from shared memory.
-// NSPLIT > 1: NSPLIT warps share the tile, warp `half` taking its runs
-// half, half + NSPLIT, ...  A tile that spans two cell rows stages two
-// neighbourhoods; split, no warp carries both.  Each particle is built by
-// one warp in the same order, so the lists do not change.
 template <bool WRAPFAST, bool MOLX = false>
 __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, float4 *sp, int *ring,
 					   int *spm = nullptr)
@@ -273,9 +271,13 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 		const int gmax = __reduce_max_sync(FULL, act ? g1 : 0);
 		for (int g = gmin; g < gmax; g++) {
 			if (act && g >= g0 && g < g1) {
-				const int r = (4 * g) & (BT_RING - 1);
-				gbase[g * 32] = make_int4(ring[r * 32 + lane], ring[(r + 1) * 32 + lane],
-							  ring[(r + 2) * 32 + lane], ring[(r + 3) * 32 + lane]);
+				const int r = (4 * g) & (BT_RING - 1), b0 = 4 * g;
+				// a group past the count is padded with the particle itself
+				// (separation zero), so readers take whole groups of four
+				gbase[g * 32] = make_int4(ring[r * 32 + lane],
+							  b0 + 1 < top ? ring[(r + 1) * 32 + lane] : (int)i,
+							  b0 + 2 < top ? ring[(r + 2) * 32 + lane] : (int)i,
+							  b0 + 3 < top ? ring[(r + 3) * 32 + lane] : (int)i);
 			}
 		}
 		flushed = top & ~3;
@@ -558,7 +560,7 @@ static int grow(sepdev *d, void **p, size_t bytes, size_t *cap)
 static int launch_build(sepdev *d, const BuildArgs &a)
 {
 	const int grid = grid_for((d->n + 31) / 32, BT_WARPS);
-	if (a.excl == SEPDEV_EXCL_SAMEMOL)      // two warps per tile
+	if (a.excl == SEPDEV_EXCL_SAMEMOL)
 		k_build_tiles_mol<<<grid, BT_WARPS * 32, 0, d->st>>>(d->n, a);
 	else
 		k_build_tiles<<<grid, BT_WARPS * 32, 0, d->st>>>(d->n, a);

@@ -20,9 +20,20 @@
 //  * all calls share the one array, which keeps the previous call's contents:
 //    each call clears what must start at zero itself, and calls that overlap
 //    on the GPU (concurrent streams, or host threads) race on it;
+//  * the cut-off may be at most half the shortest box side (the minimum
+//    image of every pair within it is then unique); shorter boxes are
+//    rejected;
 //  * the first call on each device looks up the array's device address
-//    (cudaGetSymbolAddress, with that device current) and caches it; make
-//    that first call before any stream capture.
+//    (cudaGetSymbolAddress, with that device current) and caches it.  With
+//    CUDA's lazy module loading (the default) that lookup is also what loads
+//    this file's module onto the device, array included: the first call
+//    takes the array's ~5 MB (plus the module's code) from the device, the
+//    later calls take nothing.  Make that first call before the caller's
+//    pool takes its memory and before any stream capture;
+//  * particles join their cell through atomics, so the order in which a
+//    particle's FP32 pair terms are summed varies from call to call: results
+//    can differ between calls in the last bits (well inside FP32 rounding of
+//    the pair maths).
 #include <math.h>
 #include <stdio.h>
 #include "dev_common.cuh"
@@ -120,7 +131,8 @@ __global__ void __launch_bounds__(256) k_na_force(NaForceArgs a)
 		const int cx = (int)__umulhi((unsigned)pi.x, (unsigned)a.nc[0]);
 		const int cy = (int)__umulhi((unsigned)pi.y, (unsigned)a.nc[1]);
 		const int cz = (int)__umulhi((unsigned)pi.z, (unsigned)a.nc[2]);
-		// offsets -1..1, fewer when a side has under three cells (no cell twice)
+		// offsets -1..1, fewer when a side has two cells (no cell twice);
+		// every side has at least two, since the cut-off is at most L/2
 		const int lx = a.nc[0] >= 3 ? -1 : 0, hx = a.nc[0] >= 2 ? 1 : 0;
 		const int ly = a.nc[1] >= 3 ? -1 : 0, hy = a.nc[1] >= 2 ? 1 : 0;
 		const int lz = a.nc[2] >= 3 ? -1 : 0, hz = a.nc[2] >= 2 ? 1 : 0;
@@ -192,6 +204,11 @@ extern "C" int sep_gpu_lj_forces_noalloc(const double *x, long n, const double *
 	}
 	if (!L || !param || !(L[0] > 0) || !(L[1] > 0) || !(L[2] > 0) || !(param[0] > 0)) {
 		sepdev_set_error("sep_gpu_lj_forces_noalloc: box lengths and cut-off must be positive",
+				 cudaErrorInvalidValue);
+		return SEPDEV_EINVAL;
+	}
+	if (2.0 * param[0] > L[0] || 2.0 * param[0] > L[1] || 2.0 * param[0] > L[2]) {
+		sepdev_set_error("sep_gpu_lj_forces_noalloc: the cut-off exceeds half a box side",
 				 cudaErrorInvalidValue);
 		return SEPDEV_EINVAL;
 	}

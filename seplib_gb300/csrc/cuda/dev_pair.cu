@@ -50,35 +50,78 @@ __device__ __forceinline__ void tab_eval(const float2 *__restrict__ t, int nt, f
 	u = a.y + w * (b.y - a.y);
 }
 
+// The eight kinetic fields of integrate_s into positions at..at+7 of a
+// reduction (slot fields relative to the reduction's base slot by off).
+template <int NQ>
+__device__ __forceinline__ void kin_fields(const long long (&kq)[8], int off, int at,
+					   long long (&q)[NQ], int (&fld)[NQ])
+{
+	q[at] = kq[0]; fld[at] = off + SLOT_EKIN;
+#pragma unroll
+	for (int k = 0; k < 6; k++) { q[at + 1 + k] = kq[1 + k]; fld[at + 1 + k] = off + SLOT_KINP + k; }
+	q[at + 7] = kq[7]; fld[at + 7] = off + SLOT_SUMV2;
+}
+
 // Integrate particle i (leap-frog, optional friction) and return its kinetic
 // contributions; F is the total force before friction.  fs, shi, slo: the
 // box-dependent scales (L/2^32 and dt*2^64/L split in two floats).
+// The velocity increment a dt and the half-step velocity v(t) = v - a dt/2
+// are float-float, and the kinetic terms leave as exact fixed point:
+// kq = {sum_k m v_k^2, m v_x v_x, m v_x v_y, m v_x v_z, m v_y v_y, m v_y v_z,
+// m v_z v_z} at v(t), and kq[7] = m |v(t + dt/2)|^2 (the next thermostat
+// update's sum).
 __device__ __forceinline__ void integrate_s(long i, float fx, float fy, float fz, float ei,
 					    const int4 pi, const PairArgs &a, const float (&fs)[3],
 					    const float (&shi)[3], const float (&slo)[3], float alpha,
-					    int4 *pos_out, float &ek, float (&kp)[6], float &sv2, float &d2)
+					    int4 *pos_out, long long (&kq)[8], float &d2)
 {
 	float4 vh = a.vhi[i], vl = a.vlo[i];
 	const uint4 lo = a.xlo[i];
 	const float m = vh.w, im = vl.w;
+	// every product and sum below is an explicit rounding, so the compiler
+	// cannot contract differently in the kernels that share this code
 	if (a.nh) {
-		const float am = alpha * m;
-		fx -= am * vh.x; fy -= am * vh.y; fz -= am * vh.z;
+		const float am = __fmul_rn(alpha, m);
+		fx = __fmaf_rn(-am, vh.x, fx); fy = __fmaf_rn(-am, vh.y, fy); fz = __fmaf_rn(-am, vh.z, fz);
 	}
 	a.frc[i] = make_float4(fx, fy, fz, ei);
-	// a dt with dt carried to ~48 bits, so the velocity and position updates
-	// use the same time step
-	const float ax = fx * im, ay = fy * im, az = fz * im;
-	const float qx = fmaf(ax, a.dt, ax * a.dt_lo), qy = fmaf(ay, a.dt, ay * a.dt_lo),
-		    qz = fmaf(az, a.dt, az * a.dt_lo);
-	ff_add(vh.x, vl.x, qx);
-	ff_add(vh.y, vl.y, qy);
-	ff_add(vh.z, vl.z, qz);
-	const float tx = vh.x - 0.5f * qx, ty = vh.y - 0.5f * qy, tz = vh.z - 0.5f * qz;
-	ek = m * (tx * tx + ty * ty + tz * tz);
-	kp[0] = m * tx * tx; kp[1] = m * tx * ty; kp[2] = m * tx * tz;
-	kp[3] = m * ty * ty; kp[4] = m * ty * tz; kp[5] = m * tz * tz;
-	sv2 = m * (vh.x * vh.x + vh.y * vh.y + vh.z * vh.z);
+	// a dt with dt carried to ~48 bits, as a float-float (qh, ql)
+	const float ax = __fmul_rn(fx, im), ay = __fmul_rn(fy, im), az = __fmul_rn(fz, im);
+	const float qhx = __fmul_rn(ax, a.dt), qhy = __fmul_rn(ay, a.dt), qhz = __fmul_rn(az, a.dt);
+	const float qlx = __fadd_rn(__fmaf_rn(ax, a.dt, -qhx), __fmul_rn(ax, a.dt_lo));
+	const float qly = __fadd_rn(__fmaf_rn(ay, a.dt, -qhy), __fmul_rn(ay, a.dt_lo));
+	const float qlz = __fadd_rn(__fmaf_rn(az, a.dt, -qhz), __fmul_rn(az, a.dt_lo));
+	ff_add(vh.x, vl.x, qhx); vl.x += qlx;
+	ff_add(vh.y, vl.y, qhy); vl.y += qly;
+	ff_add(vh.z, vl.z, qhz); vl.z += qlz;
+	// v(t) = v(t + dt/2) - q/2 (halving is exact)
+	float th[3], tl[3];
+	{
+		const float vv[3][2] = {{vh.x, vl.x}, {vh.y, vl.y}, {vh.z, vl.z}};
+		const float qq[3][2] = {{qhx, qlx}, {qhy, qly}, {qhz, qlz}};
+#pragma unroll
+		for (int k = 0; k < 3; k++) {
+			th[k] = vv[k][0];
+			tl[k] = vv[k][1];
+			ff_add(th[k], tl[k], -0.5f * qq[k][0]);
+			tl[k] = __fadd_rn(tl[k], -0.5f * qq[k][1]);
+		}
+	}
+	{
+		const int ka[6] = {0, 0, 0, 1, 1, 2}, kb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+		for (int c = 0; c < 6; c++) {
+			float h, l;
+			ff_mprod(m, th[ka[c]], tl[ka[c]], th[kb[c]], tl[kb[c]], h, l);
+			kq[1 + c] = to_fx2(h, l);
+		}
+		kq[0] = kq[1] + kq[4] + kq[6];
+		float h0, l0, h1, l1, h2, l2;
+		ff_mprod(m, vh.x, vl.x, vh.x, vl.x, h0, l0);
+		ff_mprod(m, vh.y, vl.y, vh.y, vl.y, h1, l1);
+		ff_mprod(m, vh.z, vl.z, vh.z, vl.z, h2, l2);
+		kq[7] = to_fx(h0) + to_fx(h1) + to_fx(h2) + to_fx(__fadd_rn(__fadd_rn(l0, l1), l2));
+	}
 	const long long ix = ff_mul_fix(vh.x, vl.x, shi[0], slo[0]);
 	const long long iy = ff_mul_fix(vh.y, vl.y, shi[1], slo[1]);
 	const long long iz = ff_mul_fix(vh.z, vl.z, shi[2], slo[2]);
@@ -111,9 +154,9 @@ __device__ __forceinline__ void integrate_s(long i, float fx, float fy, float fz
 
 __device__ __forceinline__ void integrate(long i, float fx, float fy, float fz, float ei,
 					  const int4 pi, const PairArgs &a, float alpha, int4 *pos_out,
-					  float &ek, float (&kp)[6], float &sv2, float &d2)
+					  long long (&kq)[8], float &d2)
 {
-	integrate_s(i, fx, fy, fz, ei, pi, a, a.fs, a.shi, a.slo, alpha, pos_out, ek, kp, sv2, d2);
+	integrate_s(i, fx, fy, fz, ei, pi, a, a.fs, a.shi, a.slo, alpha, pos_out, kq, d2);
 }
 
 // MOLV: also the molecular virial of the pass.  For each pair of atoms in
@@ -241,7 +284,8 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 	float etot = ec;
 #pragma unroll
 	for (int c = 0; c < NCH; c++) etot += e[c];
-	float ek = 0.f, kp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, sv2 = 0.f, d2 = 0.f;
+	long long kq[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+	float d2 = 0.f;
 	if (act) {
 		if (a.accumulate) {
 			const float4 fo = a.frc[i];
@@ -249,7 +293,7 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 		}
 		if (FUSED) {
 			const float alpha = a.alpha_dev ? (float)*a.alpha_dev : a.alpha;
-			integrate(i, fx, fy, fz, 0.5f * etot, pi, a, alpha, a.pos_out, ek, kp, sv2, d2);
+			integrate(i, fx, fy, fz, 0.5f * etot, pi, a, alpha, a.pos_out, kq, d2);
 		} else {
 			a.frc[i] = make_float4(fx, fy, fz, 0.5f * etot);
 		}
@@ -274,24 +318,32 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 	} else {
 		long long *ls = a.slots + (long)a.lslot * SLOT_FIELDS;
 		const long long off = ls - ps;
-		float v[NCH + 15 + NM];
+		long long q[NCH + 15 + NM];
 		int fld[NCH + 15 + NM];
 #pragma unroll
-		for (int c = 0; c < NCH; c++) { v[c] = 0.5f * e[c]; fld[c] = SLOT_EPOT0 + c; }
-		v[NCH] = 0.5f * ec; fld[NCH] = SLOT_ECOUL;
-		v[NCH + 1] = 0.5f * w0; v[NCH + 2] = 0.5f * w1; v[NCH + 3] = 0.5f * w2;
-		v[NCH + 4] = 0.5f * w3; v[NCH + 5] = 0.5f * w4; v[NCH + 6] = 0.5f * w5;
+		for (int c = 0; c < NCH; c++) { q[c] = to_fx(0.5f * e[c]); fld[c] = SLOT_EPOT0 + c; }
+		q[NCH] = to_fx(0.5f * ec); fld[NCH] = SLOT_ECOUL;
+		q[NCH + 1] = to_fx(0.5f * w0); q[NCH + 2] = to_fx(0.5f * w1); q[NCH + 3] = to_fx(0.5f * w2);
+		q[NCH + 4] = to_fx(0.5f * w3); q[NCH + 5] = to_fx(0.5f * w4); q[NCH + 6] = to_fx(0.5f * w5);
 #pragma unroll
 		for (int k = 0; k < 6; k++) fld[NCH + 1 + k] = SLOT_POTP + k;
-		v[NCH + 7] = ek; fld[NCH + 7] = (int)off + SLOT_EKIN;
+		kin_fields<NCH + 15 + NM>(kq, (int)off, NCH + 7, q, fld);
 #pragma unroll
-		for (int k = 0; k < 6; k++) { v[NCH + 8 + k] = kp[k]; fld[NCH + 8 + k] = (int)off + SLOT_KINP + k; }
-		v[NCH + 14] = sv2; fld[NCH + 14] = (int)off + SLOT_SUMV2;
-#pragma unroll
-		for (int k = 0; k < NM; k++) { v[NCH + 15 + k] = 0.5f * wm[k]; fld[NCH + 15 + k] = moff + k; }
-		block_to_slot<NCH + 15 + NM>(v, fld, ps, d2, (int)off + SLOT_MAXD2);
+		for (int k = 0; k < NM; k++) { q[NCH + 15 + k] = to_fx(0.5f * wm[k]); fld[NCH + 15 + k] = moff + k; }
+		block_to_slot_fx<NCH + 15 + NM>(q, fld, ps, d2, (int)off + SLOT_MAXD2);
 		step_decide_exit(a.dec);
 	}
+}
+
+// Sums of a cubic box's pair loop back to real units: forces times u,
+// virial times u^2, each with both halves of the float pair.
+__device__ __forceinline__ void lj_rescale(const LjScale &c, float &fx, float &fy, float &fz, float (&w)[6])
+{
+	fx = __fmaf_rn(fx, c.ul, __fmul_rn(fx, c.uh));
+	fy = __fmaf_rn(fy, c.ul, __fmul_rn(fy, c.uh));
+	fz = __fmaf_rn(fz, c.ul, __fmul_rn(fz, c.uh));
+#pragma unroll
+	for (int k = 0; k < 6; k++) w[k] = __fmaf_rn(w[k], c.u2l, __fmul_rn(w[k], c.u2h));
 }
 
 // Fast path for one Lennard-Jones potential on all pairs (the plain-LJ
@@ -302,52 +354,38 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 // the cut-off as a mask.  For a cubic box the box scale is folded out of the
 // pair loop: separations stay in fixed-point units (L/2^32) and the
 // per-particle sums are rescaled once.
-// PF (list staging): 0 - the next batch of indices is loaded while the
-// current one is computed; 1 - in addition, lane 0 asks L2 for the warp's
-// whole list tile at entry (one bulk prefetch, so the list stream does not
-// wait on DRAM batch by batch); 2 - as 1, and the position gathers of the
-// next batch are issued before the current batch is computed.
-template <int PF>
-__device__ __forceinline__ void lj_prefetch_tile(const PairArgs &a, long i, int cnt)
-{
-	if (PF == 0) return;
-	const int mx = __reduce_max_sync(0xffffffffu, cnt);
-	if ((threadIdx.x & 31) == 0 && mx > 0) {
-		const int *base = a.nl + nl_index(i, 0, a.maxnb);      // lane 0 starts the tile
-		const unsigned bytes = (unsigned)((mx + 3) >> 2) * 512u;   // groups of 4 entries x 32 lanes
-		asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(base), "r"(bytes) : "memory");
-	}
-}
-
-// The neighbour loop of k_lj.  OBS: accumulate energy, hit count and
-// virial (skipped on steps whose sepret nobody reads).
-template <bool OBS, bool CUBIC, int PF>
+// OBS: accumulate energy, hit count and virial (skipped on steps whose
+// sepret nobody reads).
+// sig2 = s2h + s2l as a float pair (s2l = 0 where the scale is exact).
+template <bool OBS, bool CUBIC>
 __device__ __forceinline__ void lj_pairs(const PairArgs &a, long i, int cnt, const int4 &pi,
-					 float sx, float sy, float sz, float rc2, float sig2,
+					 float sx, float sy, float sz, float rc2, float s2h, float s2l,
 					 float &fx, float &fy, float &fz, float &e, float &nin,
 					 float (&w)[6])
 {
-	const float eps48 = a.eps48, eps4 = a.eps4, awh = a.awh, aw = a.aw;
-	auto pair4 = [&](const int4 (&pj)[4], int rem) {
+	const float eps48 = a.eps48, eps4 = a.eps4, aw = a.aw, nb48 = -a.eps48 * a.awh;
+	auto pair4 = [&](const int4 (&pj)[4]) {
 #pragma unroll
 		for (int b = 0; b < 4; b++) {
 			const float dx = (float)(pi.x - pj[b].x) * sx;
 			const float dy = (float)(pi.y - pj[b].y) * sy;
 			const float dz = (float)(pi.z - pj[b].z) * sz;
 			const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-			const bool in = (b < rem) && (r2 < rc2);
+			const bool in = (r2 < rc2) & (r2 > 0.f);
 			// pairs outside the cut-off get s2 = 0, which zeroes their
 			// force and energy; the shift is added per hit at the end
-			const float s2 = in ? sig2 * fast_rcp(r2) : 0.f;
+			const float rr = fast_rcp(r2);
+			const float s2 = in ? __fmaf_rn(s2l, rr, __fmul_rn(s2h, rr)) : 0.f;
 			const float s6 = s2 * s2 * s2;
-			const float ft = eps48 * s6 * (s6 - awh) * s2;
-			// the force terms are rounded products (never contracted into
-			// the sums), so observed and unobserved steps give the same bits
-			const float gx = __fmul_rn(ft, dx), gy = __fmul_rn(ft, dy), gz = __fmul_rn(ft, dz);
-			fx += gx; fy += gy; fz += gz;
+			// 48 eps s6 (s6 - aw/2) s2, the reference's force factor
+			const float ft = __fmul_rn(__fmul_rn(s2, s6), __fmaf_rn(eps48, s6, nb48));
+			// explicit fused forms: observed and unobserved steps give the
+			// same force bits whatever the compiler does with the rest
+			fx = __fmaf_rn(ft, dx, fx); fy = __fmaf_rn(ft, dy, fy); fz = __fmaf_rn(ft, dz, fz);
 			if (OBS) {
 				e = fmaf(eps4 * s6, s6 - aw, e);
 				nin += in ? 1.f : 0.f;
+				const float gx = ft * dx, gy = ft * dy, gz = ft * dz;
 				w[0] = fmaf(gx, dx, w[0]); w[1] = fmaf(gx, dy, w[1]); w[2] = fmaf(gx, dz, w[2]);
 				w[3] = fmaf(gy, dy, w[3]); w[4] = fmaf(gy, dz, w[4]); w[5] = fmaf(gz, dz, w[5]);
 			}
@@ -355,51 +393,23 @@ __device__ __forceinline__ void lj_pairs(const PairArgs &a, long i, int cnt, con
 	};
 	const int4 *lp = (const int4 *)(a.nl + nl_index(i, 0, a.maxnb));
 	const int nb = (cnt + 3) >> 2;
-	// indices past the count point at the particle itself (masked)
-	auto idx = [&](const int4 &jc, int rem, int (&j)[4]) {
-		j[0] = jc.x; j[1] = rem > 1 ? jc.y : (int)i;
-		j[2] = rem > 2 ? jc.z : (int)i; j[3] = rem > 3 ? jc.w : (int)i;
-	};
-	if (PF < 2) {
-		int4 jn = nb > 0 ? __ldg(lp) : make_int4(0, 0, 0, 0);
-		for (int s0 = 0; s0 < nb; s0++) {
-			const int4 jc = jn;
-			if (s0 + 1 < nb) jn = __ldg(lp + (s0 + 1) * 32);
-			const int rem = cnt - 4 * s0;
-			int j[4];
-			idx(jc, rem, j);
-			int4 pj[4];
-#pragma unroll
-			for (int b = 0; b < 4; b++) pj[b] = __ldg(&a.pos[j[b]]);
-			pair4(pj, rem);
-		}
-	} else if (nb > 0) {
-		int4 jn = nb > 1 ? __ldg(lp + 32) : make_int4(0, 0, 0, 0);
-		int4 pn[4];
-		{
-			int j[4];
-			idx(__ldg(lp), cnt, j);
-#pragma unroll
-			for (int b = 0; b < 4; b++) pn[b] = __ldg(&a.pos[j[b]]);
-		}
-		for (int s0 = 0; s0 < nb; s0++) {
-			int4 pc[4];
-#pragma unroll
-			for (int b = 0; b < 4; b++) pc[b] = pn[b];
-			if (s0 + 1 < nb) {
-				int j[4];
-				idx(jn, cnt - 4 * (s0 + 1), j);
-#pragma unroll
-				for (int b = 0; b < 4; b++) pn[b] = __ldg(&a.pos[j[b]]);
-				if (s0 + 2 < nb) jn = __ldg(lp + (s0 + 2) * 32);
-			}
-			pair4(pc, cnt - 4 * s0);
-		}
+	int4 jn = nb > 0 ? __ldg(lp) : make_int4(0, 0, 0, 0);
+	for (int s0 = 0; s0 < nb; s0++) {
+		// the last group is padded with i itself, which the zero
+		// separation masks
+		const int4 jc = jn;
+		if (s0 + 1 < nb) jn = __ldg(lp + (s0 + 1) * 32);
+		int4 pj[4];
+		pj[0] = __ldg(&a.pos[jc.x]);
+		pj[1] = __ldg(&a.pos[jc.y]);
+		pj[2] = __ldg(&a.pos[jc.z]);
+		pj[3] = __ldg(&a.pos[jc.w]);
+		pair4(pj);
 	}
 }
 
-template <bool FUSED, bool CUBIC, int MINB, int PF>
-__global__ void __launch_bounds__(256, MINB) k_lj(long n, PairArgs a)
+template <bool FUSED, bool CUBIC>
+__global__ void __launch_bounds__(256, 4) k_lj(long n, PairArgs a)
 {
 	if (FUSED) step_decide_entry(a.dec);
 	if (a.flags && (a.flags[0] & 1u)) {
@@ -408,30 +418,24 @@ __global__ void __launch_bounds__(256, MINB) k_lj(long n, PairArgs a)
 	}
 	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
 	const bool act = i < n;
-	const float u = a.fs[0];
 	const float sx = CUBIC ? 1.f : a.fs[0], sy = CUBIC ? 1.f : a.fs[1], sz = CUBIC ? 1.f : a.fs[2];
-	const float rc2 = CUBIC ? a.rc2 / (u * u) : a.rc2;
-	const float sig2 = CUBIC ? a.sig2 / (u * u) : a.sig2;
+	const float rc2 = CUBIC ? a.sc.rc2s : a.rc2;
+	const float s2h = CUBIC ? a.sc.s2h : a.sig2, s2l = CUBIC ? a.sc.s2l : 0.f;
 	float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f, nin = 0.f;
 	float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 	int4 pi = make_int4(0, 0, 0, 0);
 	const int cnt = act ? a.ncnt[i] : 0;
-	lj_prefetch_tile<PF>(a, i, cnt);
 	const bool obs = !FUSED || (!a.skip_obs && step_observed(a.dec));
 	if (act) {
 		pi = a.pos[i];
-		if (obs) lj_pairs<true, CUBIC, PF>(a, i, cnt, pi, sx, sy, sz, rc2, sig2, fx, fy, fz, e, nin, w);
-		else lj_pairs<false, CUBIC, PF>(a, i, cnt, pi, sx, sy, sz, rc2, sig2, fx, fy, fz, e, nin, w);
+		if (obs) lj_pairs<true, CUBIC>(a, i, cnt, pi, sx, sy, sz, rc2, s2h, s2l, fx, fy, fz, e, nin, w);
+		else lj_pairs<false, CUBIC>(a, i, cnt, pi, sx, sy, sz, rc2, s2h, s2l, fx, fy, fz, e, nin, w);
 	}
-	float w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3], w4 = w[4], w5 = w[5];
 	e = fmaf(nin, a.ushift, e);
-	if (CUBIC) {
-		fx *= u; fy *= u; fz *= u;
-		const float u2 = u * u;
-		w0 *= u2; w1 *= u2; w2 *= u2; w3 *= u2; w4 *= u2; w5 *= u2;
-	}
-	const float etot = e;
-	float ek = 0.f, kp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, sv2 = 0.f, d2 = 0.f;
+	if (CUBIC) lj_rescale(a.sc, fx, fy, fz, w);
+	const float w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3], w4 = w[4], w5 = w[5];
+	long long kq[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+	float d2 = 0.f;
 	if (act) {
 		if (a.accumulate) {
 			const float4 fo = a.frc[i];
@@ -439,26 +443,26 @@ __global__ void __launch_bounds__(256, MINB) k_lj(long n, PairArgs a)
 		}
 		if (FUSED) {
 			const float alpha = a.alpha_dev ? (float)*a.alpha_dev : a.alpha;
-			integrate(i, fx, fy, fz, 0.5f * etot, pi, a, alpha, a.pos_out, ek, kp, sv2, d2);
+			integrate(i, fx, fy, fz, 0.5f * e, pi, a, alpha, a.pos_out, kq, d2);
 		} else {
-			a.frc[i] = make_float4(fx, fy, fz, 0.5f * etot);
+			a.frc[i] = make_float4(fx, fy, fz, 0.5f * e);
 		}
 	}
 	long long *ps = a.slots + (long)a.pslot * SLOT_FIELDS;
 	if (!FUSED) {
-		float v[7] = {0.5f * e, 0.5f * w0, 0.5f * w1, 0.5f * w2, 0.5f * w3, 0.5f * w4, 0.5f * w5};
+		const long long q[7] = {to_fx2(0.5f * e, 0.5f * nin * a.ushl), to_fx(0.5f * w0), to_fx(0.5f * w1),
+					to_fx(0.5f * w2), to_fx(0.5f * w3), to_fx(0.5f * w4), to_fx(0.5f * w5)};
 		const int fld[7] = {SLOT_EPOT0, SLOT_POTP, SLOT_POTP + 1, SLOT_POTP + 2, SLOT_POTP + 3,
 				    SLOT_POTP + 4, SLOT_POTP + 5};
-		block_to_slot<7>(v, fld, ps, 0.f, -1);
+		block_to_slot_fx<7>(q, fld, ps, 0.f, -1);
 	} else {
 		const int off = (int)((long)(a.lslot - a.pslot) * SLOT_FIELDS);
-		float v[15] = {0.5f * e, 0.5f * w0, 0.5f * w1, 0.5f * w2, 0.5f * w3, 0.5f * w4, 0.5f * w5,
-			       ek, kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], sv2};
-		const int fld[15] = {SLOT_EPOT0, SLOT_POTP, SLOT_POTP + 1, SLOT_POTP + 2, SLOT_POTP + 3,
-				     SLOT_POTP + 4, SLOT_POTP + 5, off + SLOT_EKIN, off + SLOT_KINP,
-				     off + SLOT_KINP + 1, off + SLOT_KINP + 2, off + SLOT_KINP + 3,
-				     off + SLOT_KINP + 4, off + SLOT_KINP + 5, off + SLOT_SUMV2};
-		block_to_slot<15>(v, fld, ps, d2, off + SLOT_MAXD2);
+		long long q[15] = {to_fx2(0.5f * e, 0.5f * nin * a.ushl), to_fx(0.5f * w0), to_fx(0.5f * w1),
+				   to_fx(0.5f * w2), to_fx(0.5f * w3), to_fx(0.5f * w4), to_fx(0.5f * w5)};
+		int fld[15] = {SLOT_EPOT0, SLOT_POTP, SLOT_POTP + 1, SLOT_POTP + 2, SLOT_POTP + 3,
+			       SLOT_POTP + 4, SLOT_POTP + 5};
+		kin_fields<15>(kq, off, 7, q, fld);
+		block_to_slot_fx<15>(q, fld, ps, d2, off + SLOT_MAXD2);
 		step_decide_exit(a.dec);
 	}
 }
@@ -467,16 +471,17 @@ __global__ void __launch_bounds__(256, MINB) k_lj(long n, PairArgs a)
 __global__ void __launch_bounds__(256) k_leapfrog(long n, PairArgs a)
 {
 	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-	float ek = 0.f, kp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, sv2 = 0.f, d2 = 0.f;
+	long long kq[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+	float d2 = 0.f;
 	if (i < n) {
 		const float4 f = a.frc[i];
 		const float alpha = a.alpha_dev ? (float)*a.alpha_dev : a.alpha;
-		integrate(i, f.x, f.y, f.z, f.w, a.pos[i], a, alpha, (int4 *)a.pos, ek, kp, sv2, d2);
+		integrate(i, f.x, f.y, f.z, f.w, a.pos[i], a, alpha, (int4 *)a.pos, kq, d2);
 	}
-	float v[8] = {ek, kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], sv2};
-	const int fld[8] = {SLOT_EKIN, SLOT_KINP, SLOT_KINP + 1, SLOT_KINP + 2, SLOT_KINP + 3,
-			    SLOT_KINP + 4, SLOT_KINP + 5, SLOT_SUMV2};
-	block_to_slot<8>(v, fld, a.slots + (long)a.lslot * SLOT_FIELDS, d2, SLOT_MAXD2);
+	long long q[8];
+	int fld[8];
+	kin_fields<8>(kq, 0, 0, q, fld);
+	block_to_slot_fx<8>(q, fld, a.slots + (long)a.lslot * SLOT_FIELDS, d2, SLOT_MAXD2);
 }
 
 __global__ void k_friction(long n, float alpha, const float4 *__restrict__ vhi, float4 *frc)
@@ -518,7 +523,8 @@ void sepdev_fill_args(sepdev *d, PairArgs &a, const sepdev_pairset *ps, double d
 	if (ps) {
 		const sepdev_pot &p0 = ps->pot[0];
 		a.rc2 = p0.rc2; a.eps48 = p0.eps48; a.eps4 = p0.eps4; a.sig2 = p0.sig2;
-		a.aw = p0.aw; a.awh = p0.awh; a.ushift = p0.ushift;
+		a.aw = p0.aw; a.awh = p0.awh; a.ushift = p0.ushift; a.ushl = p0.ushl;
+		a.sc = lj_scale(d->L[0], (double)p0.sig2, (double)p0.rc2);
 	}
 	for (int t = 0; t < SEPDEV_MAXTAB; t++) {
 		a.tab[t] = d->tab[t]; a.tab_n[t] = d->tab_n[t];
@@ -557,9 +563,6 @@ __global__ void __launch_bounds__(256, 4) k_lj_batch(PairArgs a, const BatchSys 
 	const int s = wsys[wg];
 	const BatchSys S = sys[s];
 	const bool act = i - S.off < S.n;
-	const float u = S.fs;
-	const float rc2 = a.rc2 / (u * u);
-	const float sig2 = a.sig2 / (u * u);
 	float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f, nin = 0.f;
 	float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 	int4 pi = make_int4(0, 0, 0, 0);
@@ -567,40 +570,146 @@ __global__ void __launch_bounds__(256, 4) k_lj_batch(PairArgs a, const BatchSys 
 	const bool obs = run->done + 1 >= run->total;
 	if (act) {
 		pi = a.pos[i];
-		if (obs) lj_pairs<true, true, 0>(a, i, cnt, pi, 1.f, 1.f, 1.f, rc2, sig2, fx, fy, fz, e, nin, w);
-		else lj_pairs<false, true, 0>(a, i, cnt, pi, 1.f, 1.f, 1.f, rc2, sig2, fx, fy, fz, e, nin, w);
+		if (obs)
+			lj_pairs<true, true>(a, i, cnt, pi, 1.f, 1.f, 1.f, S.sc.rc2s, S.sc.s2h, S.sc.s2l, fx, fy, fz, e, nin, w);
+		else
+			lj_pairs<false, true>(a, i, cnt, pi, 1.f, 1.f, 1.f, S.sc.rc2s, S.sc.s2h, S.sc.s2l, fx, fy, fz, e, nin, w);
 	}
 	e = fmaf(nin, a.ushift, e);
-	fx *= u; fy *= u; fz *= u;
-	const float u2 = u * u;
-	for (int k = 0; k < 6; k++) w[k] *= u2;
-	float ek = 0.f, kp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, sv2 = 0.f, d2 = 0.f;
+	lj_rescale(S.sc, fx, fy, fz, w);
+	long long kq[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+	float d2 = 0.f;
 	if (act) {
 		const float fsv[3] = {S.fs, S.fs, S.fs}, shv[3] = {S.shi, S.shi, S.shi}, slv[3] = {S.slo, S.slo, S.slo};
 		const float alpha = (float)bs[s].alpha;
-		integrate_s(i, fx, fy, fz, 0.5f * e, pi, a, fsv, shv, slv, alpha, a.pos_out, ek, kp, sv2, d2);
+		integrate_s(i, fx, fy, fz, 0.5f * e, pi, a, fsv, shv, slv, alpha, a.pos_out, kq, d2);
 	}
-	float v[15] = {0.5f * e, 0.5f * w[0], 0.5f * w[1], 0.5f * w[2], 0.5f * w[3], 0.5f * w[4], 0.5f * w[5],
-		       ek, kp[0], kp[1], kp[2], kp[3], kp[4], kp[5], sv2};
-	const int fld[15] = {SLOT_EPOT0, SLOT_POTP, SLOT_POTP + 1, SLOT_POTP + 2, SLOT_POTP + 3,
-			     SLOT_POTP + 4, SLOT_POTP + 5, SLOT_EKIN, SLOT_KINP, SLOT_KINP + 1,
-			     SLOT_KINP + 2, SLOT_KINP + 3, SLOT_KINP + 4, SLOT_KINP + 5, SLOT_SUMV2};
-	warp_sum<15>(v);
+	long long q[15] = {to_fx2(0.5f * e, 0.5f * nin * a.ushl), to_fx(0.5f * w[0]), to_fx(0.5f * w[1]),
+			   to_fx(0.5f * w[2]), to_fx(0.5f * w[3]), to_fx(0.5f * w[4]), to_fx(0.5f * w[5])};
+	int fld[15] = {SLOT_EPOT0, SLOT_POTP, SLOT_POTP + 1, SLOT_POTP + 2, SLOT_POTP + 3,
+		       SLOT_POTP + 4, SLOT_POTP + 5};
+	kin_fields<15>(kq, 0, 7, q, fld);
+#pragma unroll
+	for (int k = 0; k < 15; k++) q[k] = warp_sum_fx(q[k]);
 	const unsigned mx = __reduce_max_sync(FULL, __float_as_uint(d2));
 	if ((threadIdx.x & 31) == 0) {
 		long long *sl = slots + (long)s * SLOT_FIELDS;
-		for (int k = 0; k < 15; k++) {
-			const long long q = __float2ll_rn(v[k] * FX_SCALE);
-			if (q != 0) atomicAdd((unsigned long long *)&sl[fld[k]], (unsigned long long)q);
+		for (int k = 0; k < 15; k++)
+			if (q[k] != 0) atomicAdd((unsigned long long *)&sl[fld[k]], (unsigned long long)q[k]);
+		if (mx) atomicMax((unsigned long long *)&sl[SLOT_MAXD2], (unsigned long long)mx);
+	}
+}
+
+// Batched systems with one Lennard-Jones parameter set per type pair (the
+// reference's one sep_force_lj call per type pair, source/sepprfrc.c:743-1000:
+// the term of types "ab" acts on pairs of types a and b in either order; the
+// energies of the calls add).  Type ids are in pos.w; the parameter sets
+// come from a.ps (unscaled) and are scaled to each system's fixed-point
+// units per pair.  A type pair without a term has rc2 = 0 and eps = 0.
+template <bool OBS>
+__device__ __forceinline__ void ljt_pairs(const PairArgs &a, long i, int cnt, const int4 &pi, float iu2,
+					  const sepdev_pot *sp, int nt, float &fx, float &fy, float &fz,
+					  float &e, float (&w)[6])
+{
+	const int4 *lp = (const int4 *)(a.nl + nl_index(i, 0, a.maxnb));
+	const int nb = (cnt + 3) >> 2;
+	const int row = pi.w * nt;
+	int4 jn = nb > 0 ? __ldg(lp) : make_int4(0, 0, 0, 0);
+	for (int s0 = 0; s0 < nb; s0++) {
+		const int4 jc = jn;
+		if (s0 + 1 < nb) jn = __ldg(lp + (s0 + 1) * 32);
+		const int rem = cnt - 4 * s0;
+		const int j[4] = {jc.x, rem > 1 ? jc.y : (int)i, rem > 2 ? jc.z : (int)i,
+				  rem > 3 ? jc.w : (int)i};
+		int4 pj[4];
+#pragma unroll
+		for (int b = 0; b < 4; b++) pj[b] = __ldg(&a.pos[j[b]]);
+#pragma unroll
+		for (int b = 0; b < 4; b++) {
+			const sepdev_pot &pp = sp[row + pj[b].w];
+			const float dx = (float)(pi.x - pj[b].x), dy = (float)(pi.y - pj[b].y),
+				    dz = (float)(pi.z - pj[b].z);
+			const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+			const bool in = (b < rem) && (r2 < pp.rc2 * iu2);
+			const float s2 = in ? pp.sig2 * iu2 * fast_rcp(r2) : 0.f;
+			const float s6 = s2 * s2 * s2;
+			const float ft = __fmul_rn(__fmul_rn(s2, s6), __fmaf_rn(pp.eps48, s6, -pp.eps48 * pp.awh));
+			fx = __fmaf_rn(ft, dx, fx); fy = __fmaf_rn(ft, dy, fy); fz = __fmaf_rn(ft, dz, fz);
+			if (OBS) {
+				const float gx = ft * dx, gy = ft * dy, gz = ft * dz;
+				e += in ? fmaf(pp.eps4 * s6, s6 - pp.aw, pp.ushift) : 0.f;
+				w[0] = fmaf(gx, dx, w[0]); w[1] = fmaf(gx, dy, w[1]); w[2] = fmaf(gx, dz, w[2]);
+				w[3] = fmaf(gy, dy, w[3]); w[4] = fmaf(gy, dz, w[4]); w[5] = fmaf(gz, dz, w[5]);
+			}
 		}
+	}
+}
+
+__global__ void __launch_bounds__(256, 4) k_lj_batch_typed(PairArgs a, const BatchSys *sys,
+							  const int *wsys, int nwarps,
+							  const BatchState *bs, const BatchRun *run,
+							  long long *slots, BatchDecide dec)
+{
+	const unsigned FULL = 0xffffffffu;
+	__shared__ sepdev_pot sp[SEPB_MAXTYPES * SEPB_MAXTYPES];
+	const int nt = a.ps->ntypes;
+	for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) sp[k] = a.ps->pot[k];
+	__syncthreads();
+	if (dec.reset_while && blockIdx.x == 0 && threadIdx.x == 0)
+		cudaGraphSetConditional(dec.h_while, 0);
+	if (a.flags && (a.flags[0] & 1u)) return;      // list overflow: the decision stops the loop
+	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	const long wg = i >> 5;
+	if (wg >= nwarps) return;                      // whole warps
+	const int s = wsys[wg];
+	const BatchSys S = sys[s];
+	const bool act = i - S.off < S.n;
+	const float u = S.fs, iu2 = 1.f / (u * u);
+	float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
+	float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+	int4 pi = make_int4(0, 0, 0, 0);
+	const int cnt = act ? a.ncnt[i] : 0;
+	const bool obs = run->done + 1 >= run->total;
+	if (act) {
+		pi = a.pos[i];
+		if (obs) ljt_pairs<true>(a, i, cnt, pi, iu2, sp, nt, fx, fy, fz, e, w);
+		else ljt_pairs<false>(a, i, cnt, pi, iu2, sp, nt, fx, fy, fz, e, w);
+	}
+	fx *= u; fy *= u; fz *= u;
+	const float u2 = u * u;
+	for (int k = 0; k < 6; k++) w[k] *= u2;
+	long long kq[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+	float d2 = 0.f;
+	if (act) {
+		const float fsv[3] = {S.fs, S.fs, S.fs}, shv[3] = {S.shi, S.shi, S.shi}, slv[3] = {S.slo, S.slo, S.slo};
+		const float alpha = (float)bs[s].alpha;
+		integrate_s(i, fx, fy, fz, 0.5f * e, pi, a, fsv, shv, slv, alpha, a.pos_out, kq, d2);
+	}
+	long long q[15] = {to_fx(0.5f * e), to_fx(0.5f * w[0]), to_fx(0.5f * w[1]), to_fx(0.5f * w[2]),
+			   to_fx(0.5f * w[3]), to_fx(0.5f * w[4]), to_fx(0.5f * w[5])};
+	int fld[15] = {SLOT_EPOT0, SLOT_POTP, SLOT_POTP + 1, SLOT_POTP + 2, SLOT_POTP + 3,
+		       SLOT_POTP + 4, SLOT_POTP + 5};
+	kin_fields<15>(kq, 0, 7, q, fld);
+#pragma unroll
+	for (int k = 0; k < 15; k++) q[k] = warp_sum_fx(q[k]);
+	const unsigned mx = __reduce_max_sync(FULL, __float_as_uint(d2));
+	if ((threadIdx.x & 31) == 0) {
+		long long *sl = slots + (long)s * SLOT_FIELDS;
+		for (int k = 0; k < 15; k++)
+			if (q[k] != 0) atomicAdd((unsigned long long *)&sl[fld[k]], (unsigned long long)q[k]);
 		if (mx) atomicMax((unsigned long long *)&sl[SLOT_MAXD2], (unsigned long long)mx);
 	}
 }
 
 int sepdev_batch_step(sepdev *d, const PairArgs &a, const BatchSys *sys, const int *wsys, int nwarps,
-		      const BatchState *bs, const BatchRun *run, long long *slots, const BatchDecide &dec)
+		      const BatchState *bs, const BatchRun *run, long long *slots, const BatchDecide &dec,
+		      int typed)
 {
-	k_lj_batch<<<grid_for((long)nwarps * 32, 256), 256, 0, d->st>>>(a, sys, wsys, nwarps, bs, run, slots, dec);
+	if (typed)
+		k_lj_batch_typed<<<grid_for((long)nwarps * 32, 256), 256, 0, d->st>>>(a, sys, wsys, nwarps, bs, run,
+										   slots, dec);
+	else
+		k_lj_batch<<<grid_for((long)nwarps * 32, 256), 256, 0, d->st>>>(a, sys, wsys, nwarps, bs, run, slots, dec);
 	CKL(d);
 	return SEPDEV_OK;
 }
@@ -625,16 +734,10 @@ static void launch_fused(sepdev *d, int var, const PairArgs &a, size_t shm, bool
 			k_pair<VAR_GENERAL_COUL, FUSED, true><<<grid, B, shm, d->st>>>(d->n, a);
 		else
 			k_pair<VAR_GENERAL, FUSED, true><<<grid, B, shm, d->st>>>(d->n, a);
-	} else if (var == VAR_SINGLE && cubic) {
-		switch (d->lj_variant) {
-		case 1: k_lj<FUSED, true, 5, 0><<<grid, B, 0, d->st>>>(d->n, a); break;
-		case 2: k_lj<FUSED, true, 4, 1><<<grid, B, 0, d->st>>>(d->n, a); break;
-		case 3: k_lj<FUSED, true, 3, 2><<<grid, B, 0, d->st>>>(d->n, a); break;
-		case 4: k_lj<FUSED, true, 4, 2><<<grid, B, 0, d->st>>>(d->n, a); break;
-		default: k_lj<FUSED, true, 4, 0><<<grid, B, 0, d->st>>>(d->n, a); break;
-		}
-	} else if (var == VAR_SINGLE)
-		k_lj<FUSED, false, 4, 0><<<grid, B, 0, d->st>>>(d->n, a);
+	} else if (var == VAR_SINGLE && cubic)
+		k_lj<FUSED, true><<<grid, B, 0, d->st>>>(d->n, a);
+	else if (var == VAR_SINGLE)
+		k_lj<FUSED, false><<<grid, B, 0, d->st>>>(d->n, a);
 	else if (var == VAR_GENERAL)
 		k_pair<VAR_GENERAL, FUSED><<<grid, B, shm, d->st>>>(d->n, a);
 	else

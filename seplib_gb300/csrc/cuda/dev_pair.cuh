@@ -3,6 +3,26 @@
 #include "dev_common.cuh"
 #include "dev_decide.cuh"
 
+// A cubic box measured in fixed-point units u = L / 2^32: u and u^2 as float
+// pairs (hi + lo), sigma^2 / u^2 as a float pair and rc^2 / u^2, all rounded
+// once from FP64.  Pair terms computed in these units carry no systematic
+// error from a rounded scale: s^2 = (s2h + s2l) / r^2 and the rescaled
+// force and virial use both halves of u and u^2.
+struct LjScale {
+	float uh, ul, u2h, u2l, s2h, s2l, rc2s;
+};
+
+static inline LjScale lj_scale(double L, double sig2, double rc2)
+{
+	LjScale c;
+	const double u = L / 4294967296.0, u2 = u * u, s2 = sig2 / u2;
+	c.uh = (float)u; c.ul = (float)(u - (double)c.uh);
+	c.u2h = (float)u2; c.u2l = (float)(u2 - (double)c.u2h);
+	c.s2h = (float)s2; c.s2l = (float)(s2 - (double)c.s2h);
+	c.rc2s = (float)(rc2 / u2);
+	return c;
+}
+
 struct PairArgs {
 	const int4 *pos;
 	int4 *pos_out;
@@ -17,6 +37,8 @@ struct PairArgs {
 	const sepdev_pairset *ps;
 	// single-potential fast path
 	float rc2, eps48, eps4, sig2, aw, awh, ushift;
+	float ushl;                 // ushift - (float)ushift: the shift's remainder
+	LjScale sc;                 // cubic boxes: the fixed-point unit and scaled constants
 	// tables
 	const float2 *tab[SEPDEV_MAXTAB];
 	float tab_r2min[SEPDEV_MAXTAB], tab_idr2[SEPDEV_MAXTAB];
@@ -41,6 +63,9 @@ struct PairArgs {
 	int mslot;
 };
 
+
+// copy a pair set to the device (skipped when the device copy is current)
+int sepdev_upload_pairset(sepdev *d, const sepdev_pairset *ps);
 
 void sepdev_fill_args(sepdev *d, PairArgs &a, const sepdev_pairset *ps, double dt, int nh,
 		      double alpha, int accumulate, int pslot, int lslot, int parity);

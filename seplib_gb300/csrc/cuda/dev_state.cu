@@ -80,10 +80,6 @@ extern "C" int sepdev_create(sepdev **out, long n)
 		const char *hio = getenv("SEPLIB_HOSTIO");
 		d->hostio_direct = pma == 1 && !(hio && strcmp(hio, "staged") == 0);
 	}
-	{
-		const char *v = getenv("SEPLIB_LJ_VARIANT");
-		d->lj_variant = v ? atoi(v) : 0;
-	}
 	*out = d;
 	return SEPDEV_OK;
 }

@@ -8,35 +8,24 @@
 #include "sep_rt.h"
 
 /* Nose-Hoover (source/sepintgr.c:149-168).  The thermostat update itself is
- * scalar and done here in FP64 from the device's sum m v^2; the friction
- * f -= alpha m v is deferred to the next force materialisation, normally the
- * fused leap-frog kernel. */
+ * scalar and done here in FP64 from the device's exact sum m v^2 (made
+ * current first: a program that changed the particles on the host has them
+ * uploaded here); the friction f -= alpha m v is deferred to the next force
+ * materialisation, normally the fused leap-frog kernel. */
 void sep_nosehoover(seppart *ptr, double temp0, double *alpha, const double tau, sepsys *sys)
 {
 	rt_ctx *c = rt_get(ptr, __func__);
-	double sv2;
-	if (c->dev && c->dev_valid) {
-		if (!c->sumv2_valid) {
-			rt_check(sepdev_sumv2(c->dev, &c->sumv2), "kinetic sum");
-			c->sumv2_valid = 1;
-		}
-		sv2 = c->sumv2;
-	} else {
-		sv2 = 0.0;
-		for (long i = 0; i < sys->npart; i++)
-			for (int k = 0; k < 3; k++) sv2 += ptr[i].v[k] * ptr[i].v[k] * ptr[i].m;
+	rt_need_device(c, sys);
+	if (!c->sumv2_valid) {
+		rt_check(sepdev_sumv2(c->dev, &c->sumv2), "kinetic sum");
+		c->sumv2_valid = 1;
 	}
-	const double ekin = 0.5 * sv2 / sys->npart;
+	const double ekin = 0.5 * c->sumv2 / sys->npart;
 	const double temp = 0.666667 * ekin;
 	*alpha = *alpha + sys->dt / (tau * tau) * (temp / temp0 - 1.0);
-	if (c->dev && c->dev_valid) {
-		c->friction = 1;
-		c->friction_alpha += *alpha;
-		c->host_valid = 0;
-	} else {
-		for (long i = 0; i < sys->npart; i++)
-			for (int k = 0; k < 3; k++) ptr[i].f[k] -= *alpha * ptr[i].m * ptr[i].v[k];
-	}
+	c->friction = 1;
+	c->friction_alpha += *alpha;
+	c->host_valid = 0;
 }
 
 /* Leap-frog (source/sepintgr.c:42-88).  Pending pair terms, friction and the

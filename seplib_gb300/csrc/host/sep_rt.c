@@ -380,6 +380,7 @@ void rt_pairset(rt_ctx *c, sepdev_pairset *ps)
 				P->aw = (float)T->aw;
 				P->awh = (float)(0.5 * T->aw);
 				P->ushift = (float)T->ushift;
+				P->ushl = (float)(T->ushift - (double)P->ushift);
 				P->table = T->table;
 			}
 	}

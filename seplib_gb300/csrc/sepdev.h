@@ -72,6 +72,7 @@ typedef struct {
 	float rc2;
 	float eps48, eps4, sig2, aw, awh;
 	float ushift;
+	float ushl;            /* the shift's remainder: shift - (float)shift */
 	int table;             /* index of the table for SEPDEV_POT_TABLE */
 } sepdev_pot;
 
