@@ -74,9 +74,10 @@ def parse():
     ap.add_argument("--ncell", type=int, default=40, help="fcc cells per edge (40: N=256000)")
     ap.add_argument("--cpu-steps", type=int, default=0, help="oracle steps for cpu_baseline (0: auto)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="default kernel parameters instead of the autotuner's")
     ap.add_argument("--no-workloads", action="store_true",
                     help="skip the batched, adjoint and butane sub-objects of the headline line")
-    ap.add_argument("--tpp", type=int, default=0)
     ap.add_argument("--workload", default="plain", choices=["plain", "batched", "adjoint", "butane"],
                     help="plain: one N=4 ncell^3 system (the headline); batched: 512 independent "
                          "systems stepped together; adjoint: gradients of 64 replicas x 4000")
@@ -205,11 +206,32 @@ def write_state(path, s):
         fh.write(np.ascontiguousarray(s.types, "S1").tobytes())
 
 
+TUNING = {}          # the tuned table of this process (applied to the C driver too)
+
+
+def tuned(lib, args):
+    """Apply the autotuner's table (cached for this GPU and build, or timed
+    now: seplib_gb300/tune.py) and remember it for the C loop driver."""
+    from seplib_gb300 import tune
+    if not TUNING:
+        if args.no_tune:
+            rec = dict(classes=list(tune.CLASSES), chosen=[[1, 2, 1.0]] * (len(tune.CLASSES) + 1),
+                       source="default")
+            tune.apply(lib, rec["classes"], [tuple(c) for c in rec["chosen"]])
+        else:
+            rec = tune.load_or_tune(lib)
+        TUNING.update(classes=rec["classes"], chosen=rec["chosen"], source=rec["source"],
+                      seconds=rec.get("seconds"))
+    return TUNING
+
+
 def run_driver(state, steps, warmup, rc, dt, skin, t0, tau, top=None):
     """time the prgs-style loop in C (seplib_gb300/csrc/driver/e2e_loop.c)"""
-    from seplib_gb300 import build as sbuild
+    from seplib_gb300 import build as sbuild, tune
     cmd = [sbuild.E2E, state, str(steps), str(warmup), str(FLUSH_BYTES), repr(rc), repr(dt), repr(skin),
            repr(t0), repr(tau)] + ([top] if top else [])
+    if TUNING:
+        cmd += ["--tune"] + tune.as_args(TUNING["classes"], TUNING["chosen"])
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise SystemExit("loop driver failed: %s" % (r.stderr or r.stdout))
@@ -259,6 +281,7 @@ def run_batched(args, rank, world, steps=None, single_every=1, emit=True):
     from seplib_gb300.batch import Batch
     build.build()
     lib = load()
+    tuned(lib, args)
     systems, rhos, temps = configs.replica_sweep(nsys=args.nsys, seed=4 + rank)
     ntot = int(sum(s.n for s in systems))
     b = Batch(lib, systems, rc=RC, skin=SKIN, dt=DT, T0=temps, tau=TAU)
@@ -336,6 +359,7 @@ def run_adjoint(args, rank, world, steps=None, emit=True):
     from seplib_gb300.adjoint import Adjoint
     build.build()
     lib = load()
+    tuned(lib, args)
     nrep, steps = 64, steps or args.steps
     systems = [configs.plain_lj_large(10, seed=100 + 64 * rank + k, temp=1.0) for k in range(nrep)]
     param = (RC, 1.0, 1.0, 1.0)
@@ -381,8 +405,9 @@ def run_butane(args, rank, world, steps=None, emit=True):
     sep C API from host seppart arrays, run by the C loop driver.  The L2 is
     flushed before every step, outside the per-step wall-clock spans (each
     step ends in a synchronous read-back of its sepret)."""
-    from seplib_gb300 import build, configs
+    from seplib_gb300 import build, configs, load
     build.build()
+    tuned(load(), args)
     steps = steps or args.steps
     s = configs.butane(nmol=8000, rho=0.6, temp=4.0, seed=3 + rank)
     n = s.n
@@ -465,6 +490,7 @@ def main():
     lib = load()
     if not lib.sep_gpu_available():
         raise SystemExit("no CUDA device visible")
+    tuning = tuned(lib, args)
     s = configs.plain_lj_large(args.ncell, seed=2 + rank)
     n = s.n
     fun = A.fun_ptr(lib, "sep_lj_shift")
@@ -477,8 +503,6 @@ def main():
     # warm-up steps (the loops are bitwise identical, so are the segments).
     def segment(mode):
         atoms, sys_ = new_system(lib, s)
-        if args.tpp:
-            lib.sep_gpu_set_tpp(atoms, args.tpp)
         ret = A.SepRet()
         alpha = C.c_double(0.0)
         args_run = (atoms, C.byref(sys_), C.byref(ret), b"AA", fun, None, RC, A.SEP_ALL, 1, T0,
@@ -569,7 +593,12 @@ def main():
         cfgd["graph_loop_no_flush"] = {
             "value": graph_loop_pss, "unit": "particle-steps/s", "list_rebuilds": segg["rebuilds"],
             "what": "sep_gpu_run, one CUDA graph with a WHILE node, L2 not flushed (production loop)"}
-        cfgd["tpp"] = info.tpp
+        cfgd["kernel_params"] = {"team": info.team, "groups": info.groups, "cellf": info.cellf}
+        cfgd["tuning"] = {"what": "kernel parameters by system size (n <= classes[k]; the last "
+                                  "entry: larger), each [team, groups, cellf], from the autotuner "
+                                  "(seplib_gb300/tune.py)",
+                          "classes": tuning["classes"], "chosen": tuning["chosen"],
+                          "source": tuning["source"], "tune_seconds": tuning.get("seconds")}
         cfgd["list_mean_full"] = round(info.list_mean, 2)
         cfgd["list_rebuilds_in_timed_steps"] = rebuilds
         cfgd["final_state"] = {"epot_per_particle": epot_pp, "temperature": temp}

@@ -59,8 +59,33 @@ int sep_gpu_run(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
 		double (*fun)(double, char), const double *ljparam, double cf,
 		unsigned opt, int nh, double T0, double *alpha, double tau, long nsteps);
 
-/* Lanes per particle in the pair kernels: 1, 2 or 4 (default chosen by size). */
-int sep_gpu_set_tpp(seppart *ptr, int tpp);
+/*
+ * Kernel parameters by system size, chosen by the autotuner
+ * (seplib_gb300/tune.py: short timed trials on the GPU, cached as JSON) or
+ * set by hand.  A system of n particles takes the first class with
+ * n <= nmax[k]; the last class takes every larger system.
+ *   team    lanes per particle in the Lennard-Jones step kernels, 1 or 2;
+ *   groups  groups of four neighbours a lane gathers per iteration, 1 or 2
+ *           (a speed choice only: the sums keep their order);
+ *   cellf   cell edge of the neighbour-list build over the list cut-off,
+ *           1.0 to 2.0.
+ * team and cellf change the order of floating-point sums: a system gives
+ * the same bits alone (sep_gpu_run, the C API loop) and in a batch
+ * (sepbatch.h) under the same table.  A single system takes its class at
+ * every neighbour-list build, a batch at sepb_create.  Default: one class,
+ * team 1, groups 2, cellf 1.0.  Returns 0, or -1 for values out of range.
+ */
+#define SEP_GPU_NCLASS 8
+typedef struct {
+	int nclass;
+	long nmax[SEP_GPU_NCLASS];
+	int team[SEP_GPU_NCLASS];
+	int groups[SEP_GPU_NCLASS];
+	double cellf[SEP_GPU_NCLASS];
+} sep_gpu_tuning;
+
+int sep_gpu_set_tuning(const sep_gpu_tuning *t);
+int sep_gpu_get_tuning(sep_gpu_tuning *t);
 
 /* Diagnostics. */
 typedef struct {
@@ -69,7 +94,8 @@ typedef struct {
 	int list_capacity;    /* neighbour slots per particle */
 	int list_max;         /* largest neighbour count of the current list */
 	double list_mean;     /* mean neighbour count (full list) */
-	int tpp;
+	int team, groups;     /* kernel parameters taken at the last list build */
+	double cellf;
 	int direct_io;        /* 1: uploads/downloads read and write the seppart array from
 	                       * device code (GPU access to pageable host memory) */
 } sep_gpu_info;

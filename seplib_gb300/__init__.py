@@ -21,8 +21,17 @@ _lib = None
 class GpuInfo(C.Structure):
     """``sep_gpu_info`` (include/sepgpu.h)."""
     _fields_ = [("launches", C.c_long), ("list_builds", C.c_long), ("list_capacity", C.c_int),
-                ("list_max", C.c_int), ("list_mean", C.c_double), ("tpp", C.c_int),
-                ("direct_io", C.c_int)]
+                ("list_max", C.c_int), ("list_mean", C.c_double), ("team", C.c_int),
+                ("groups", C.c_int), ("cellf", C.c_double), ("direct_io", C.c_int)]
+
+
+NCLASS = 8
+
+
+class Tuning(C.Structure):
+    """``sep_gpu_tuning`` (include/sepgpu.h): kernel parameters by system size."""
+    _fields_ = [("nclass", C.c_int), ("nmax", C.c_long * NCLASS), ("team", C.c_int * NCLASS),
+                ("groups", C.c_int * NCLASS), ("cellf", C.c_double * NCLASS)]
 
 
 class GpuTiming(C.Structure):
@@ -46,7 +55,8 @@ _GPU_SIGNATURES = {
     "sep_gpu_run": (C.c_int, [sepapi.PART_P, sepapi.SYS_P, sepapi.RET_P, C.c_char_p, C.c_void_p,
                              sepapi.D_P, C.c_double, C.c_uint, C.c_int, C.c_double, sepapi.D_P,
                              C.c_double, C.c_long]),
-    "sep_gpu_set_tpp": (C.c_int, [sepapi.PART_P, C.c_int]),
+    "sep_gpu_set_tuning": (C.c_int, [C.c_void_p]),
+    "sep_gpu_get_tuning": (C.c_int, [C.c_void_p]),
     "sep_gpu_info_get": (C.c_int, [sepapi.PART_P, C.POINTER(GpuInfo)]),
     "sep_gpu_list_pairs": (C.c_long, [sepapi.PART_P, C.POINTER(C.c_int), C.c_long]),
     "sep_gpu_event_record": (C.c_int, [sepapi.PART_P, C.c_int]),
@@ -61,6 +71,9 @@ _GPU_SIGNATURES = {
     "sep_gpu_flush_l2": (C.c_int, [sepapi.PART_P, C.c_long]),
     "sepb_create": (C.c_void_p, [C.c_int, C.POINTER(C.c_int), sepapi.D_P, C.c_double, C.c_double,
                                  C.c_double, sepapi.D_P]),
+    "sepb_create_typed": (C.c_void_p, [C.c_int, C.POINTER(C.c_int), sepapi.D_P, C.c_double, C.c_double,
+                                       C.c_int, sepapi.D_P]),
+    "sepb_set_types": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "sepb_set_state": (C.c_int, [C.c_void_p, C.c_int, sepapi.D_P, sepapi.D_P, sepapi.D_P]),
     "sepb_set_thermostat": (C.c_int, [C.c_void_p, sepapi.D_P, C.c_double, sepapi.D_P]),
     "sepb_run": (C.c_int, [C.c_void_p, C.c_long]),

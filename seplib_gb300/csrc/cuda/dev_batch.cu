@@ -304,7 +304,7 @@ extern "C" void sepb_destroy(sepb *b)
 	if (b->exec) cudaGraphExecDestroy(b->exec);
 	if (b->graph) cudaGraphDestroy(b->graph);
 	void *dv[] = {b->sys, b->wsys, b->csys, b->flag, b->cellcount, b->cellstart, b->slots, b->bs, b->run,
-		      b->flush_buf};
+		      b->flush_buf, b->wstep};
 	for (size_t k = 0; k < sizeof dv / sizeof dv[0]; k++)
 		if (dv[k]) cudaFree(dv[k]);
 	if (b->h_bs) cudaFreeHost(b->h_bs);
@@ -316,8 +316,9 @@ extern "C" void sepb_destroy(sepb *b)
 #define BCK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { sepdev_set_error(#call, e_); \
 	sepb_destroy(b); return NULL; } } while (0)
 
-extern "C" sepb *sepb_create(int nsys, const int *npart, const double *L, double rc, double skin,
-			     double dt, const double *ljparam)
+// typed: the per-type-pair kernel, which takes one lane per particle
+static sepb *batch_make(int nsys, const int *npart, const double *L, double rc, double skin, double dt,
+			const double *ljparam, int typed)
 {
 	if (nsys <= 0 || !npart || !L || !(rc > 0) || !(skin >= 0) || !(dt > 0)) {
 		batch_fail("sepb_create: invalid arguments", SEPDEV_EINVAL);
@@ -343,6 +344,7 @@ extern "C" sepb *sepb_create(int nsys, const int *npart, const double *L, double
 	b->alpha0.assign(nsys, 0.0);
 	long off = 0, coff = 0;
 	std::vector<int> hw, hc;
+	std::vector<int4> hstep;
 	for (int s = 0; s < nsys; s++) {
 		BatchSys &S = b->hsys[s];
 		if (npart[s] <= 0 || !(L[s] > 0)) { batch_fail("sepb_create: empty system or box", SEPDEV_EINVAL); delete b; return NULL; }
@@ -357,7 +359,10 @@ extern "C" sepb *sepb_create(int nsys, const int *npart, const double *L, double
 		const double sc = dt * 18446744073709551616.0 / L[s];
 		S.shi = (float)sc;
 		S.slo = (float)(sc - (double)S.shi);
-		int nc = (int)floor(L[s] / rlist);
+		// the kernel parameters of the system's size class
+		sepdev_tuning_for(S.n, &S.team, &S.groups, &S.cellf);
+		if (typed) S.team = 1;
+		int nc = (int)floor(L[s] / (rlist * S.cellf));
 		if (nc < 1) nc = 1;
 		// the single-system grid bound: at most 2n + 64 cells
 		int ncs[3] = {nc, nc, nc};
@@ -371,6 +376,8 @@ extern "C" sepb *sepb_create(int nsys, const int *npart, const double *L, double
 		S.coff = (int)coff;
 		S.T0 = 1.0;
 		for (int w = 0; w < S.npad / 32; w++) hw.push_back(s);
+		for (int k = 0; k < S.npad; k += 32 / S.team)
+			hstep.push_back(make_int4(s, (int)off + k, S.team, S.groups));
 		for (int c = 0; c < S.ncell + 1; c++) hc.push_back(s);
 		hc.push_back(-1);                       // the end entry
 		off += S.npad;
@@ -386,6 +393,9 @@ extern "C" sepb *sepb_create(int nsys, const int *npart, const double *L, double
 	for (int k = 0; k < 3; k++) { d->L[k] = 1.0; d->fscale[k] = (float)(1.0 / 4294967296.0); }
 	BCK(cudaMalloc((void **)&b->sys, sizeof(BatchSys) * nsys));
 	BCK(cudaMalloc((void **)&b->wsys, sizeof(int) * b->nwarps));
+	b->nstepw = (int)hstep.size();
+	BCK(cudaMalloc((void **)&b->wstep, sizeof(int4) * b->nstepw));
+	BCK(cudaMemcpy(b->wstep, hstep.data(), sizeof(int4) * b->nstepw, cudaMemcpyHostToDevice));
 	BCK(cudaMalloc((void **)&b->csys, sizeof(int) * b->ncells));
 	BCK(cudaMalloc((void **)&b->flag, sizeof(unsigned) * nsys));
 	BCK(cudaMalloc((void **)&b->cellcount, sizeof(int) * b->ncells));
@@ -413,6 +423,12 @@ extern "C" sepb *sepb_create(int nsys, const int *npart, const double *L, double
 	if (maxnb > 1024) maxnb = 1024;
 	if (sepdev_grow_list_to(d, maxnb)) { sepb_destroy(b); return NULL; }
 	return b;
+}
+
+extern "C" sepb *sepb_create(int nsys, const int *npart, const double *L, double rc, double skin,
+			     double dt, const double *ljparam)
+{
+	return batch_make(nsys, npart, L, rc, skin, dt, ljparam, 0);
 }
 
 extern "C" int sepb_set_state(sepb *b, int s, const double *x, const double *v, const double *m)
@@ -502,7 +518,7 @@ extern "C" sepb *sepb_create_typed(int nsys, const int *npart, const double *L, 
 		batch_fail("sepb_create_typed: no type pair interacts", SEPDEV_EINVAL);
 		return NULL;
 	}
-	sepb *b = sepb_create(nsys, npart, L, rc, skin, dt, p0);
+	sepb *b = batch_make(nsys, npart, L, rc, skin, dt, p0, 1);
 	if (!b) return NULL;
 	b->ntypes = ntypes;
 	memcpy(b->tparam, ljparams, sizeof(double) * 4 * ntypes * ntypes);
@@ -670,7 +686,7 @@ int batch_step_launch(sepb *b, int parity, const BatchDecide &dec)
 {
 	PairArgs a = batch_pair_args(b, parity);
 	CK(cudaGetLastError());
-	int rc = sepdev_batch_step(b->d, a, b->sys, b->wsys, b->nwarps, b->bs, b->run, b->slots, dec,
+	int rc = sepdev_batch_step(b->d, a, b->sys, b->wstep, b->nstepw, b->bs, b->run, b->slots, dec,
 				   b->ntypes > 1);
 	if (rc) return rc;
 	kb_decide<<<grid_for((long)b->nsys * 32, 256), 256, 0, b->d->st>>>(dec);

@@ -21,6 +21,8 @@ struct BatchSys {
 	float fs;              // L / 2^32 (cubic box)
 	float shi, slo;        // dt * 2^64 / L as a float pair
 	LjScale sc;            // the single-LJ constants in this box's units
+	int team, groups;      // kernel parameters of the system's size class
+	double cellf;          // cell edge over the list cut-off
 	double L;
 	double T0;             // thermostat target
 };
@@ -65,7 +67,7 @@ struct BatchDecide {
 };
 
 // launchers implemented next to the single-system kernels they share code with
-int sepdev_batch_step(sepdev *d, const PairArgs &a, const BatchSys *sys, const int *wsys, int nwarps,
+int sepdev_batch_step(sepdev *d, const PairArgs &a, const BatchSys *sys, const int4 *wstep, int nwarps,
 		      const BatchState *bs, const BatchRun *run, long long *slots, const BatchDecide &dec,
 		      int typed);
 int sepdev_batch_build(sepdev *d, int parity, const int *cellstart, const BatchSys *sys,
@@ -89,6 +91,8 @@ struct sepb {
 	std::vector<BatchSys> hsys;
 	BatchSys *sys;             // device
 	int *wsys, *csys;
+	int4 *wstep;               // per warp of the step kernel: system, first slot, team, groups
+	int nstepw;
 	unsigned *flag;
 	int *cellcount, *cellstart;
 	long long *slots;

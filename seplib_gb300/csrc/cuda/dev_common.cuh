@@ -81,10 +81,15 @@ struct sepdev {
 	int *cellstart;         // ncells + 1
 	int *perm;              // new slot -> old slot
 
-	// neighbour list: tiles of 32/tpp particles, each tile maxnb*(32/tpp) ints
+	// neighbour list: tiles of 32 particles, each tile maxnb * 32 ints (nl_index)
 	int *nl;
 	int *ncnt;
-	int maxnb, tpp;
+	int maxnb;
+	// kernel parameters of the system's size class (the tuning table),
+	// taken at every list build: lanes per particle, neighbour groups per
+	// iteration, cell edge over the list cut-off
+	int team, groups;
+	double cellf;
 	size_t cap_nl;
 	double rlist;
 	int excl;

@@ -282,6 +282,11 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 		}
 		flushed = top & ~3;
 	};
+	// 0 < r^2 < rlist^2 as one unsigned comparison of the bit patterns
+	// (r^2 >= 0): the zero separation of a particle with itself fails it,
+	// so the fast loops need no index test
+	const unsigned rl2m1 = __float_as_uint(a.rl2) - 1u;
+	auto inlist = [&](float r2) { return (__float_as_uint(r2) - 1u) < rl2m1; };
 	auto test = [&](int fill) {
 		__syncwarp();
 		// entries not yet written out must stay in the ring through this chunk
@@ -295,7 +300,7 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 					const float dx = mx - q.x, dy = my - q.y, dz = mz - q.z;
 					const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 					const int j = __float_as_int(q.w);
-					const bool hit = (r2 < a.rl2) & (j != (int)i) & !((mi != -1) & (mi == spm[c]));
+					const bool hit = inlist(r2) & !((mi != -1) & (mi == spm[c]));
 					ring[(cnt & (BT_RING - 1)) * 32 + lane] = j;
 					cnt += hit ? 1 : 0;
 				}
@@ -306,7 +311,7 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 					const float dx = mx - q.x, dy = my - q.y, dz = mz - q.z;
 					const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 					const int j = __float_as_int(q.w);
-					const bool hit = (r2 < a.rl2) & (j != (int)i);
+					const bool hit = inlist(r2);
 					ring[(cnt & (BT_RING - 1)) * 32 + lane] = j;
 					cnt += hit ? 1 : 0;
 				}
@@ -320,7 +325,7 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 					const float dy = sep_hi(pi.y, __float_as_int(q.y), a.fs[1]);
 					const float dz = sep_hi(pi.z, __float_as_int(q.z), a.fs[2]);
 					const int j = __float_as_int(q.w);
-					const bool hit = (dx * dx + dy * dy + dz * dz < a.rl2) & (j != (int)i);
+					const bool hit = inlist(dx * dx + dy * dy + dz * dz);
 					ring[(cnt & (BT_RING - 1)) * 32 + lane] = j;
 					cnt += hit ? 1 : 0;
 				}
@@ -568,11 +573,12 @@ static int launch_build(sepdev *d, const BuildArgs &a)
 	return SEPDEV_OK;
 }
 
-// Cell grid for cut-off rlist: edge >= rlist, total cells bounded by 2n + 64.
+// Cell grid for cut-off rlist: edge >= cellf * rlist (cellf >= 1, from the
+// tuning table), total cells bounded by 2n + 64.
 static int cell_grid(sepdev *d, double rlist)
 {
 	for (int k = 0; k < 3; k++) {
-		int c = (int)floor(d->L[k] / rlist);
+		int c = (int)floor(d->L[k] / (rlist * d->cellf));
 		d->ncell[k] = c < 1 ? 1 : c;
 	}
 	while ((long)d->ncell[0] * d->ncell[1] * d->ncell[2] > 2 * d->n + 64) {
@@ -718,6 +724,8 @@ extern "C" int sepdev_build_list(sepdev *d, double rlist, int excl, int trigger)
 		excl = SEPDEV_EXCL_NONE;
 	d->rlist = rlist;
 	d->excl = excl;
+	// the kernel parameters of the system's size class, as tuned
+	sepdev_tuning_for(d->n, &d->team, &d->groups, &d->cellf);
 	int rc;
 	if ((rc = cell_grid(d, rlist))) return rc;
 	if ((rc = sepdev_sort_async(d, d->cur, trigger))) return rc;
@@ -796,9 +804,9 @@ extern "C" long sepdev_list_pairs(sepdev *d, int *pairs, long cap)
 	return np;
 }
 
-extern "C" int sepdev_set_tpp(sepdev *d, int tpp)
+extern "C" void sepdev_params(sepdev *d, int *team, int *groups, double *cellf)
 {
-	return tpp == 1 ? SEPDEV_OK : SEPDEV_EINVAL;
+	if (team) *team = d->team;
+	if (groups) *groups = d->groups;
+	if (cellf) *cellf = d->cellf;
 }
-
-extern "C" int sepdev_get_tpp(sepdev *d) { (void)d; return 1; }

@@ -10,9 +10,9 @@
 // GB300 design:
 //   * FULL neighbour list: each particle sums all its pair forces itself, so
 //     no atomics touch the force array; energies and virials are halved.
-//   * TPP lanes per particle (1, 2 or 4) walk its list in warp tiles: lane
-//     (p, q) of a warp reads entry s*32 + p*TPP + q, so each list load of a
-//     warp is one coalesced 128-byte line.
+//   * one lane per particle walks its list in warp tiles: the lanes of a
+//     warp read the same group of four entries of their 32 lists with one
+//     coalesced 512-byte load (the layout is nl_index, dev_common.cuh).
 //   * j positions are 16-byte int4 gathers through the read-only path;
 //     separations are int32 differences of fixed-point high words
 //     (minimum image by wrap-around) converted to FP32.
@@ -75,8 +75,10 @@ __device__ __forceinline__ void integrate_s(long i, float fx, float fy, float fz
 					    const float (&shi)[3], const float (&slo)[3], float alpha,
 					    int4 *pos_out, long long (&kq)[8], float &d2)
 {
-	float4 vh = a.vhi[i], vl = a.vlo[i];
-	const uint4 lo = a.xlo[i];
+	// the per-particle state is read and written once per step: streaming
+	// accesses keep it from displacing the neighbours' positions in L1
+	float4 vh = __ldcs(&a.vhi[i]), vl = __ldcs(&a.vlo[i]);
+	const uint4 lo = __ldcs(&a.xlo[i]);
 	const float m = vh.w, im = vl.w;
 	// every product and sum below is an explicit rounding, so the compiler
 	// cannot contract differently in the kernels that share this code
@@ -84,7 +86,7 @@ __device__ __forceinline__ void integrate_s(long i, float fx, float fy, float fz
 		const float am = __fmul_rn(alpha, m);
 		fx = __fmaf_rn(-am, vh.x, fx); fy = __fmaf_rn(-am, vh.y, fy); fz = __fmaf_rn(-am, vh.z, fz);
 	}
-	a.frc[i] = make_float4(fx, fy, fz, ei);
+	__stcs(&a.frc[i], make_float4(fx, fy, fz, ei));
 	// a dt with dt carried to ~48 bits, as a float-float (qh, ql)
 	const float ax = __fmul_rn(fx, im), ay = __fmul_rn(fy, im), az = __fmul_rn(fz, im);
 	const float qhx = __fmul_rn(ax, a.dt), qhy = __fmul_rn(ay, a.dt), qhz = __fmul_rn(az, a.dt);
@@ -142,10 +144,10 @@ __device__ __forceinline__ void integrate_s(long i, float fx, float fy, float fz
 	const int4 po = make_int4((int)(unsigned)(X1 >> 32), (int)(unsigned)(Y1 >> 32),
 				  (int)(unsigned)(Z1 >> 32), pi.w);
 	pos_out[i] = po;
-	a.xlo[i] = make_uint4((unsigned)X1, (unsigned)Y1, (unsigned)Z1, 0u);
-	a.vhi[i] = vh;
-	a.vlo[i] = vl;
-	const int4 xn = a.xn[i];
+	__stcs(&a.xlo[i], make_uint4((unsigned)X1, (unsigned)Y1, (unsigned)Z1, 0u));
+	__stcs(&a.vhi[i], vh);
+	__stcs(&a.vlo[i], vl);
+	const int4 xn = __ldcs(&a.xn[i]);
 	const float dx = sep_hi(po.x, xn.x, fs[0]);
 	const float dy = sep_hi(po.y, xn.y, fs[1]);
 	const float dz = sep_hi(po.z, xn.z, fs[2]);
@@ -348,17 +350,31 @@ __device__ __forceinline__ void lj_rescale(const LjScale &c, float &fx, float &f
 
 // Fast path for one Lennard-Jones potential on all pairs (the plain-LJ
 // workload).  A lane owns one particle and consumes its neighbour list in
-// batches of four: one 16-byte load brings the next four indices (the
+// batches of eight: two 16-byte loads bring the next eight indices (the
 // following batch is already in flight while the current one is computed),
-// then four independent position gathers, then branch-free pair maths with
+// then eight independent position gathers, then branch-free pair maths with
 // the cut-off as a mask.  For a cubic box the box scale is folded out of the
 // pair loop: separations stay in fixed-point units (L/2^32) and the
 // per-particle sums are rescaled once.
 // OBS: accumulate energy, hit count and virial (skipped on steps whose
 // sepret nobody reads).
 // sig2 = s2h + s2l as a float pair (s2l = 0 where the scale is exact).
-template <bool OBS, bool CUBIC>
-__device__ __forceinline__ void lj_pairs(const PairArgs &a, long i, int cnt, const int4 &pi,
+// A group of four list entries: read once, so it is not kept in L1, where
+// the neighbours' positions need the room.
+__device__ __forceinline__ int4 ld_list(const int4 *p)
+{
+	int4 r;
+	asm volatile("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
+		     : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
+	return r;
+}
+
+// TEAM lanes share a particle: lane h of the team takes the list's groups
+// of four h, h + TEAM, h + 2 TEAM, ...; each lane gathers G groups per
+// iteration.  G only changes how many loads are in flight, not the order of
+// the sums; TEAM does change it (the partial sums are added afterwards).
+template <bool OBS, bool CUBIC, int TEAM, int G>
+__device__ __forceinline__ void lj_pairs(const PairArgs &a, long i, int h, int cnt, const int4 &pi,
 					 float sx, float sy, float sz, float rc2, float s2h, float s2l,
 					 float &fx, float &fy, float &fz, float &e, float &nin,
 					 float (&w)[6])
@@ -393,22 +409,51 @@ __device__ __forceinline__ void lj_pairs(const PairArgs &a, long i, int cnt, con
 	};
 	const int4 *lp = (const int4 *)(a.nl + nl_index(i, 0, a.maxnb));
 	const int nb = (cnt + 3) >> 2;
-	int4 jn = nb > 0 ? __ldg(lp) : make_int4(0, 0, 0, 0);
-	for (int s0 = 0; s0 < nb; s0++) {
-		// the last group is padded with i itself, which the zero
-		// separation masks
-		const int4 jc = jn;
-		if (s0 + 1 < nb) jn = __ldg(lp + (s0 + 1) * 32);
-		int4 pj[4];
-		pj[0] = __ldg(&a.pos[jc.x]);
-		pj[1] = __ldg(&a.pos[jc.y]);
-		pj[2] = __ldg(&a.pos[jc.z]);
-		pj[3] = __ldg(&a.pos[jc.w]);
-		pair4(pj);
+	// G groups per iteration, the next G groups of indices in flight; the
+	// last group is padded with i itself, and a group past the end is i
+	// four times: the zero separation masks both
+	constexpr int STEP = TEAM * G;
+	const int4 self4 = make_int4((int)i, (int)i, (int)i, (int)i);
+	int4 jn[G];
+#pragma unroll
+	for (int q = 0; q < G; q++) jn[q] = h + q * TEAM < nb ? ld_list(lp + (h + q * TEAM) * 32) : self4;
+	for (int g0 = h; g0 < nb; g0 += STEP) {
+		int4 jc[G];
+#pragma unroll
+		for (int q = 0; q < G; q++) {
+			jc[q] = jn[q];
+			const int g = g0 + STEP + q * TEAM;
+			jn[q] = g < nb ? ld_list(lp + g * 32) : self4;
+		}
+		int4 pj[G][4];
+#pragma unroll
+		for (int q = 0; q < G; q++) {
+			pj[q][0] = __ldg(&a.pos[jc[q].x]); pj[q][1] = __ldg(&a.pos[jc[q].y]);
+			pj[q][2] = __ldg(&a.pos[jc[q].z]); pj[q][3] = __ldg(&a.pos[jc[q].w]);
+		}
+#pragma unroll
+		for (int q = 0; q < G; q++) pair4(pj[q]);
 	}
 }
 
-template <bool FUSED, bool CUBIC>
+// the partial sums of a team's second lane onto its first (lanes 0-15 of
+// the warp hold the particles, lanes 16-31 their second halves)
+template <int TEAM>
+__device__ __forceinline__ void team_sum(float &fx, float &fy, float &fz, float &e, float &nin,
+					 float (&w)[6])
+{
+	if (TEAM == 1) return;
+	const unsigned FULL = 0xffffffffu;
+	fx += __shfl_down_sync(FULL, fx, 16); fy += __shfl_down_sync(FULL, fy, 16);
+	fz += __shfl_down_sync(FULL, fz, 16); e += __shfl_down_sync(FULL, e, 16);
+	nin += __shfl_down_sync(FULL, nin, 16);
+#pragma unroll
+	for (int k = 0; k < 6; k++) w[k] += __shfl_down_sync(FULL, w[k], 16);
+}
+
+// TEAM lanes per particle: a warp holds 32 / TEAM particles; after the
+// pair loop the first lane of each team carries the particle on alone.
+template <bool FUSED, bool CUBIC, int TEAM, int G>
 __global__ void __launch_bounds__(256, 4) k_lj(long n, PairArgs a)
 {
 	if (FUSED) step_decide_entry(a.dec);
@@ -416,20 +461,31 @@ __global__ void __launch_bounds__(256, 4) k_lj(long n, PairArgs a)
 		if (FUSED) step_decide_skip(a.dec);
 		return;
 	}
-	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-	const bool act = i < n;
+	constexpr int PPW = 32 / TEAM;
+	const int lane = threadIdx.x & 31, h = lane / PPW;
+	const long i = (blockIdx.x * (long)blockDim.x + threadIdx.x) / 32 * PPW + lane % PPW;
+	const bool inrange = i < n;
 	const float sx = CUBIC ? 1.f : a.fs[0], sy = CUBIC ? 1.f : a.fs[1], sz = CUBIC ? 1.f : a.fs[2];
 	const float rc2 = CUBIC ? a.sc.rc2s : a.rc2;
 	const float s2h = CUBIC ? a.sc.s2h : a.sig2, s2l = CUBIC ? a.sc.s2l : 0.f;
 	float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f, nin = 0.f;
 	float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 	int4 pi = make_int4(0, 0, 0, 0);
-	const int cnt = act ? a.ncnt[i] : 0;
+	const int cnt = inrange ? a.ncnt[i] : 0;
 	const bool obs = !FUSED || (!a.skip_obs && step_observed(a.dec));
-	if (act) {
+	if (inrange) {
 		pi = a.pos[i];
-		if (obs) lj_pairs<true, CUBIC>(a, i, cnt, pi, sx, sy, sz, rc2, s2h, s2l, fx, fy, fz, e, nin, w);
-		else lj_pairs<false, CUBIC>(a, i, cnt, pi, sx, sy, sz, rc2, s2h, s2l, fx, fy, fz, e, nin, w);
+		if (obs)
+			lj_pairs<true, CUBIC, TEAM, G>(a, i, h, cnt, pi, sx, sy, sz, rc2, s2h, s2l, fx, fy, fz, e, nin, w);
+		else
+			lj_pairs<false, CUBIC, TEAM, G>(a, i, h, cnt, pi, sx, sy, sz, rc2, s2h, s2l, fx, fy, fz, e, nin, w);
+	}
+	team_sum<TEAM>(fx, fy, fz, e, nin, w);
+	const bool act = inrange && h == 0;
+	if (!act) {
+		fx = fy = fz = e = nin = 0.f;
+#pragma unroll
+		for (int k = 0; k < 6; k++) w[k] = 0.f;
 	}
 	e = fmaf(nin, a.ushift, e);
 	if (CUBIC) lj_rescale(a.sc, fx, fy, fz, w);
@@ -545,11 +601,32 @@ void sepdev_fill_args(sepdev *d, PairArgs &a, const sepdev_pairset *ps, double d
 
 // Batched systems: one fused step (LJ forces, Nose-Hoover friction,
 // leap-frog) over every system at once.  A warp belongs to one system and
-// takes that system's box scales and thermostat; the arithmetic per particle
-// is the single-system k_lj's (cubic form), and each warp adds its sums to
-// its system's accumulator slot with the same fixed-point conversion as the
-// block reduction there, so a system's results do not depend on the batch.
-__global__ void __launch_bounds__(256, 4) k_lj_batch(PairArgs a, const BatchSys *sys, const int *wsys,
+// takes that system's box scales, thermostat and kernel parameters (its
+// entry of wstep: system, first slot, team size, neighbour groups per
+// iteration); the arithmetic per particle is the single-system k_lj's
+// (cubic form) under the same parameters, and each warp adds its sums to
+// its system's accumulator slot with the same exact fixed-point conversion
+// as the block reduction there, so a system's results do not depend on the
+// batch.
+template <bool OBS>
+__device__ __forceinline__ void lj_pairs_any(int team, int groups, const PairArgs &a, long i, int h,
+					     int cnt, const int4 &pi, const LjScale &sc, float &fx, float &fy,
+					     float &fz, float &e, float &nin, float (&w)[6])
+{
+	if (team == 1) {
+		if (groups == 2)
+			lj_pairs<OBS, true, 1, 2>(a, i, h, cnt, pi, 1.f, 1.f, 1.f, sc.rc2s, sc.s2h, sc.s2l, fx, fy, fz, e, nin, w);
+		else
+			lj_pairs<OBS, true, 1, 1>(a, i, h, cnt, pi, 1.f, 1.f, 1.f, sc.rc2s, sc.s2h, sc.s2l, fx, fy, fz, e, nin, w);
+	} else {
+		if (groups == 2)
+			lj_pairs<OBS, true, 2, 2>(a, i, h, cnt, pi, 1.f, 1.f, 1.f, sc.rc2s, sc.s2h, sc.s2l, fx, fy, fz, e, nin, w);
+		else
+			lj_pairs<OBS, true, 2, 1>(a, i, h, cnt, pi, 1.f, 1.f, 1.f, sc.rc2s, sc.s2h, sc.s2l, fx, fy, fz, e, nin, w);
+	}
+}
+
+__global__ void __launch_bounds__(256, 4) k_lj_batch(PairArgs a, const BatchSys *sys, const int4 *wstep,
 						    int nwarps, const BatchState *bs, const BatchRun *run,
 						    long long *slots, BatchDecide dec)
 {
@@ -557,23 +634,29 @@ __global__ void __launch_bounds__(256, 4) k_lj_batch(PairArgs a, const BatchSys 
 	if (dec.reset_while && blockIdx.x == 0 && threadIdx.x == 0)
 		cudaGraphSetConditional(dec.h_while, 0);
 	if (a.flags && (a.flags[0] & 1u)) return;      // list overflow: the decision stops the loop
-	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-	const long wg = i >> 5;
+	const long wg = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
 	if (wg >= nwarps) return;                      // whole warps
-	const int s = wsys[wg];
+	const int4 W = wstep[wg];
+	const int s = W.x, team = W.z, ppw = 32 / team, lane = threadIdx.x & 31, h = lane / ppw;
+	const long i = W.y + lane % ppw;
 	const BatchSys S = sys[s];
-	const bool act = i - S.off < S.n;
+	const bool inrange = i - S.off < S.n;
 	float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f, nin = 0.f;
 	float w[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 	int4 pi = make_int4(0, 0, 0, 0);
-	const int cnt = act ? a.ncnt[i] : 0;
+	const int cnt = inrange ? a.ncnt[i] : 0;
 	const bool obs = run->done + 1 >= run->total;
-	if (act) {
+	if (inrange) {
 		pi = a.pos[i];
-		if (obs)
-			lj_pairs<true, true>(a, i, cnt, pi, 1.f, 1.f, 1.f, S.sc.rc2s, S.sc.s2h, S.sc.s2l, fx, fy, fz, e, nin, w);
-		else
-			lj_pairs<false, true>(a, i, cnt, pi, 1.f, 1.f, 1.f, S.sc.rc2s, S.sc.s2h, S.sc.s2l, fx, fy, fz, e, nin, w);
+		if (obs) lj_pairs_any<true>(team, W.w, a, i, h, cnt, pi, S.sc, fx, fy, fz, e, nin, w);
+		else lj_pairs_any<false>(team, W.w, a, i, h, cnt, pi, S.sc, fx, fy, fz, e, nin, w);
+	}
+	if (team == 2) team_sum<2>(fx, fy, fz, e, nin, w);
+	const bool act = inrange && h == 0;
+	if (!act) {
+		fx = fy = fz = e = nin = 0.f;
+#pragma unroll
+		for (int k = 0; k < 6; k++) w[k] = 0.f;
 	}
 	e = fmaf(nin, a.ushift, e);
 	lj_rescale(S.sc, fx, fy, fz, w);
@@ -646,7 +729,7 @@ __device__ __forceinline__ void ljt_pairs(const PairArgs &a, long i, int cnt, co
 }
 
 __global__ void __launch_bounds__(256, 4) k_lj_batch_typed(PairArgs a, const BatchSys *sys,
-							  const int *wsys, int nwarps,
+							  const int4 *wstep, int nwarps,
 							  const BatchState *bs, const BatchRun *run,
 							  long long *slots, BatchDecide dec)
 {
@@ -658,10 +741,11 @@ __global__ void __launch_bounds__(256, 4) k_lj_batch_typed(PairArgs a, const Bat
 	if (dec.reset_while && blockIdx.x == 0 && threadIdx.x == 0)
 		cudaGraphSetConditional(dec.h_while, 0);
 	if (a.flags && (a.flags[0] & 1u)) return;      // list overflow: the decision stops the loop
-	const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-	const long wg = i >> 5;
-	if (wg >= nwarps) return;                      // whole warps
-	const int s = wsys[wg];
+	const long wg = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+	if (wg >= nwarps) return;                      // whole warps (one lane per particle)
+	const int4 W = wstep[wg];
+	const int s = W.x;
+	const long i = W.y + (threadIdx.x & 31);
 	const BatchSys S = sys[s];
 	const bool act = i - S.off < S.n;
 	const float u = S.fs, iu2 = 1.f / (u * u);
@@ -701,15 +785,16 @@ __global__ void __launch_bounds__(256, 4) k_lj_batch_typed(PairArgs a, const Bat
 	}
 }
 
-int sepdev_batch_step(sepdev *d, const PairArgs &a, const BatchSys *sys, const int *wsys, int nwarps,
+int sepdev_batch_step(sepdev *d, const PairArgs &a, const BatchSys *sys, const int4 *wstep, int nwarps,
 		      const BatchState *bs, const BatchRun *run, long long *slots, const BatchDecide &dec,
 		      int typed)
 {
 	if (typed)
-		k_lj_batch_typed<<<grid_for((long)nwarps * 32, 256), 256, 0, d->st>>>(a, sys, wsys, nwarps, bs, run,
+		k_lj_batch_typed<<<grid_for((long)nwarps * 32, 256), 256, 0, d->st>>>(a, sys, wstep, nwarps, bs, run,
 										   slots, dec);
 	else
-		k_lj_batch<<<grid_for((long)nwarps * 32, 256), 256, 0, d->st>>>(a, sys, wsys, nwarps, bs, run, slots, dec);
+		k_lj_batch<<<grid_for((long)nwarps * 32, 256), 256, 0, d->st>>>(a, sys, wstep, nwarps, bs, run, slots,
+									       dec);
 	CKL(d);
 	return SEPDEV_OK;
 }
@@ -734,10 +819,18 @@ static void launch_fused(sepdev *d, int var, const PairArgs &a, size_t shm, bool
 			k_pair<VAR_GENERAL_COUL, FUSED, true><<<grid, B, shm, d->st>>>(d->n, a);
 		else
 			k_pair<VAR_GENERAL, FUSED, true><<<grid, B, shm, d->st>>>(d->n, a);
-	} else if (var == VAR_SINGLE && cubic)
-		k_lj<FUSED, true><<<grid, B, 0, d->st>>>(d->n, a);
-	else if (var == VAR_SINGLE)
-		k_lj<FUSED, false><<<grid, B, 0, d->st>>>(d->n, a);
+	} else if (var == VAR_SINGLE && cubic) {
+		// the team size and neighbour groups of the system's size class
+		const int g2 = grid_for(d->n * d->team, B);
+		if (d->team == 2) {
+			if (d->groups == 2) k_lj<FUSED, true, 2, 2><<<g2, B, 0, d->st>>>(d->n, a);
+			else k_lj<FUSED, true, 2, 1><<<g2, B, 0, d->st>>>(d->n, a);
+		} else {
+			if (d->groups == 2) k_lj<FUSED, true, 1, 2><<<g2, B, 0, d->st>>>(d->n, a);
+			else k_lj<FUSED, true, 1, 1><<<g2, B, 0, d->st>>>(d->n, a);
+		}
+	} else if (var == VAR_SINGLE)
+		k_lj<FUSED, false, 1, 2><<<grid, B, 0, d->st>>>(d->n, a);
 	else if (var == VAR_GENERAL)
 		k_pair<VAR_GENERAL, FUSED><<<grid, B, shm, d->st>>>(d->n, a);
 	else

@@ -43,7 +43,7 @@ struct Runner {
 	// key of the captured graph
 	sepdev_pairset ps;
 	double dt, T0, tau, skin;
-	int nh, parity, maxnb, tpp;
+	int nh, parity, maxnb, team, groups;
 	const int *nl;
 	long ncells;
 	int valid;
@@ -197,7 +197,7 @@ static int build_graph(sepdev *d, Runner *r, const sepdev_pairset *ps, const sep
 	CK(cudaGraphInstantiate(&r->exec, r->graph, 0));
 	r->ps = *ps;
 	r->dt = cfg->dt; r->T0 = cfg->T0; r->tau = cfg->tau; r->skin = cfg->skin; r->nh = cfg->nh;
-	r->parity = parity; r->maxnb = d->maxnb; r->tpp = d->tpp; r->nl = d->nl;
+	r->parity = parity; r->maxnb = d->maxnb; r->team = d->team; r->groups = d->groups; r->nl = d->nl;
 	r->ncells = d->ncells;
 	r->valid = 1;
 	return SEPDEV_OK;
@@ -206,7 +206,8 @@ static int build_graph(sepdev *d, Runner *r, const sepdev_pairset *ps, const sep
 static bool graph_matches(const sepdev *d, const Runner *r, const sepdev_pairset *ps,
 			  const sepdev_runcfg *cfg, int parity)
 {
-	return r->valid && r->parity == parity && r->maxnb == d->maxnb && r->tpp == d->tpp &&
+	return r->valid && r->parity == parity && r->maxnb == d->maxnb && r->team == d->team &&
+	       r->groups == d->groups &&
 	       r->nl == d->nl && r->ncells == d->ncells && r->dt == cfg->dt && r->T0 == cfg->T0 &&
 	       r->tau == cfg->tau && r->skin == cfg->skin && r->nh == cfg->nh &&
 	       memcmp(&r->ps, ps, sizeof *ps) == 0;

@@ -69,7 +69,9 @@ extern "C" int sepdev_create(sepdev **out, long n)
 	CK(cudaMemsetAsync(d->slots, 0, sizeof(long long) * d->nslots * SLOT_FIELDS, d->st));
 	CK(cudaMemsetAsync(d->flags, 0, sizeof(unsigned) * 4, d->st));
 	CK(cudaMemsetAsync(d->frc, 0, sizeof(float4) * n, d->st));
-	d->tpp = 1;
+	d->team = 1;
+	d->groups = 2;
+	d->cellf = 1.0;
 	CK(cudaDeviceGetAttribute(&d->nsm, cudaDevAttrMultiProcessorCount, d->device));
 	{
 		// in-place transfers need device access to pageable host memory

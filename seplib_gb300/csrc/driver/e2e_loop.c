@@ -17,6 +17,10 @@
  * sepret values back; the final sep_gpu_sync (timed) downloads x, v and f.
  *
  *   sep_e2e_loop STATE STEPS WARMUP FLUSH_BYTES RC DT SKIN T0 TAU [TOPOLOGY]
+ *                [--tune NCLASS (NMAX TEAM GROUPS CELLF) x NCLASS]
+ *
+ * --tune applies a table of kernel parameters by system size
+ * (sep_gpu_set_tuning) before the run, as the autotuner chose it.
  *
  * STATE is a binary file: int64 n, double L[3], double x[3n], double v[3n],
  * double m[n], char type[n].  Before every timed step FLUSH_BYTES are
@@ -27,6 +31,7 @@
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
+#include <string.h>
 #include <time.h>
 #include "sep.h"
 
@@ -39,6 +44,28 @@ static double now(void)
 
 int main(int argc, char **argv)
 {
+	for (int k = 10; k < argc; k++) {
+		if (strcmp(argv[k], "--tune") != 0) continue;
+		sep_gpu_tuning t;
+		memset(&t, 0, sizeof t);
+		t.nclass = k + 1 < argc ? atoi(argv[k + 1]) : 0;
+		if (t.nclass < 1 || t.nclass > SEP_GPU_NCLASS || k + 2 + 4 * t.nclass != argc) {
+			fprintf(stderr, "bad --tune table\n");
+			return 2;
+		}
+		for (int c = 0; c < t.nclass; c++) {
+			t.nmax[c] = atol(argv[k + 2 + 4 * c]);
+			t.team[c] = atoi(argv[k + 3 + 4 * c]);
+			t.groups[c] = atoi(argv[k + 4 + 4 * c]);
+			t.cellf[c] = atof(argv[k + 5 + 4 * c]);
+		}
+		if (sep_gpu_set_tuning(&t) != 0) {
+			fprintf(stderr, "sep_gpu_set_tuning rejected the table\n");
+			return 2;
+		}
+		argc = k;
+		break;
+	}
 	if (argc != 10 && argc != 11) {
 		fprintf(stderr, "usage: %s STATE STEPS WARMUP FLUSH_BYTES RC DT SKIN T0 TAU [TOPOLOGY]\n", argv[0]);
 		return 2;

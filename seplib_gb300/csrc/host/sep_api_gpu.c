@@ -37,16 +37,33 @@ int sep_gpu_invalidate(seppart *ptr)
 	return 0;
 }
 
-int sep_gpu_set_tpp(seppart *ptr, int tpp)
+int sep_gpu_set_tuning(const sep_gpu_tuning *t)
 {
-	rt_ctx *c = rt_get(ptr, __func__);
-	if (tpp != 1 && tpp != 2 && tpp != 4) return -1;
-	c->tpp = tpp;
-	if (c->dev) {
-		rt_flush(c);
-		extern int sepdev_set_tpp(sepdev *d, int tpp);
-		sepdev_set_tpp(c->dev, tpp);
-		c->list_stale = 1;
+	if (!t || t->nclass < 1 || t->nclass > SEP_GPU_NCLASS) return -1;
+	sepdev_tuning d;
+	memset(&d, 0, sizeof d);
+	d.nclass = t->nclass;
+	for (int k = 0; k < t->nclass; k++) {
+		d.nmax[k] = t->nmax[k];
+		d.team[k] = t->team[k];
+		d.groups[k] = t->groups[k];
+		d.cellf[k] = t->cellf[k];
+	}
+	return sepdev_tuning_set(&d) == SEPDEV_OK ? 0 : -1;
+}
+
+int sep_gpu_get_tuning(sep_gpu_tuning *t)
+{
+	if (!t) return -1;
+	sepdev_tuning d;
+	sepdev_tuning_get(&d);
+	memset(t, 0, sizeof *t);
+	t->nclass = d.nclass;
+	for (int k = 0; k < d.nclass; k++) {
+		t->nmax[k] = d.nmax[k];
+		t->team[k] = d.team[k];
+		t->groups[k] = d.groups[k];
+		t->cellf[k] = d.cellf[k];
 	}
 	return 0;
 }
@@ -64,8 +81,7 @@ int sep_gpu_info_get(seppart *ptr, sep_gpu_info *info)
 	info->list_capacity = cap;
 	info->list_max = mx;
 	info->list_mean = mean;
-	extern int sepdev_get_tpp(sepdev *d);
-	info->tpp = sepdev_get_tpp(c->dev);
+	sepdev_params(c->dev, &info->team, &info->groups, &info->cellf);
 	info->direct_io = sepdev_direct_io(c->dev);
 	return 0;
 }

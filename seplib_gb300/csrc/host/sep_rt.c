@@ -182,7 +182,6 @@ void rt_need_device(rt_ctx *c, const sepsys *sys)
 		if (sepdev_device_count() < 1)
 			sep_error("no CUDA device is available; this sep library runs on the GPU only");
 		rt_check(sepdev_create(&c->dev, c->n), "device context");
-		if (c->tpp) sepdev_set_tpp(c->dev, c->tpp);
 	}
 	if (c->dev_valid && !c->topo_dirty) return;
 	const int uploading = !c->dev_valid;

@@ -137,7 +137,6 @@ typedef struct rt_ctx {
 
 	/* statistics */
 	long nbuild;
-	int tpp;
 } rt_ctx;
 
 #define RT_SEED_DEFAULT 0x5eb15eedULL

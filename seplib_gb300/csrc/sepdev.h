@@ -402,9 +402,31 @@ void sepdev_molvir_disable(sepdev *d);
 int sepdev_mol_state(sepdev *d, double *kin, double *corr, double *cm, double *vcm, double *L0,
 		     double *L1);
 
-/* lanes per particle in the pair kernels (1, 2, 4); invalidates the list */
-int sepdev_set_tpp(sepdev *d, int tpp);
-int sepdev_get_tpp(sepdev *d);
+/*
+ * Kernel parameters by system size, the table the autotuner fills (one per
+ * process).  A system of n particles takes the first class with n <=
+ * nmax[k] (the last class takes every larger system):
+ *   team    lanes per particle in the LJ step kernels (1 or 2);
+ *   groups  groups of four neighbours each lane gathers per iteration
+ *           (1 or 2; only a speed choice, the sums keep their order);
+ *   cellf   cell edge of the list build over the list cut-off (1 to 2).
+ * team and cellf change the order of floating-point sums, so one system
+ * gives the same bits alone and in a batch only under the same table.  A
+ * single system takes its class at every list build; a batch at creation.
+ */
+#define SEPDEV_NCLASS 8
+typedef struct {
+	int nclass;
+	long nmax[SEPDEV_NCLASS];
+	int team[SEPDEV_NCLASS];
+	int groups[SEPDEV_NCLASS];
+	double cellf[SEPDEV_NCLASS];
+} sepdev_tuning;
+int sepdev_tuning_set(const sepdev_tuning *t);      /* SEPDEV_EINVAL if out of range */
+void sepdev_tuning_get(sepdev_tuning *t);
+void sepdev_tuning_for(long n, int *team, int *groups, double *cellf);
+/* the parameters a context took at its last list build */
+void sepdev_params(sepdev *d, int *team, int *groups, double *cellf);
 
 /* kernel launches issued by this context so far (all kinds) */
 long sepdev_launch_count(sepdev *d);
