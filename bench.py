@@ -46,6 +46,7 @@ sys.path.insert(0, HERE)
 RHO, TEMP, RC, SKIN, DT, T0, TAU = 0.8442, 1.0, 2.5, 0.3, 0.005, 1.0, 10.0
 L2_BYTES = 129 * 2 ** 20
 FLUSH_BYTES = 256 * 2 ** 20     # written between timed steps: about twice the L2
+EXTRA_STEPS = 2000              # minimum steps of the e2e and production-loop figures
 # DRAM bytes (read + write) per launch of the step kernels, measured by ncu:
 # one line per kernel and workload in profiles/traffic.txt, with the command
 # that measured it
@@ -501,7 +502,7 @@ def main():
     # CUDA event pair per step.  Each measurement runs on a fresh copy of the
     # system over the same trajectory segment: steps [W, W + K) after W
     # warm-up steps (the loops are bitwise identical, so are the segments).
-    def segment(mode):
+    def segment(mode, nsteps):
         atoms, sys_ = new_system(lib, s)
         ret = A.SepRet()
         alpha = C.c_double(0.0)
@@ -514,14 +515,22 @@ def main():
         if mode == "graph":
             # the production loop: one graph with a WHILE node, no flush
             lib.sep_gpu_event_record(atoms, 2)
-            assert lib.sep_gpu_run(*args_run, args.steps) == 0
+            assert lib.sep_gpu_run(*args_run, nsteps) == 0
             lib.sep_gpu_event_record(atoms, 3)
             msf = C.c_float()
             lib.sep_gpu_event_elapsed(atoms, 2, 3, C.byref(msf))
             ms = msf.value
         else:
-            tm = GpuTiming(flush_bytes=FLUSH_BYTES, kernel_spans=1 if mode == "kernel" else 0)
-            rc = lib.sep_gpu_run_timed(*args_run, args.steps, C.byref(tm))
+            # every step sums its energy and virial, as the reference's
+            # loop of API calls does
+            # "whole": no flush (the per-step working set is larger than
+            # L2) and one event pair per launched graph of up to 64 steps;
+            # "steps": L2 flushed before every step, one event pair per step;
+            # "kernel": flushed, one event pair per fused step kernel
+            spans = {"whole": 2, "steps": 0, "kernel": 1}[mode]
+            tm = GpuTiming(flush_bytes=0 if mode == "whole" else FLUSH_BYTES, kernel_spans=spans,
+                           observe=1)
+            rc = lib.sep_gpu_run_timed(*args_run, nsteps, C.byref(tm))
             assert rc == 0, lib.sep_gpu_error()
             ms = tm.ms_kernel if mode == "kernel" else tm.ms_steps
         lib.sep_gpu_stream_sync(atoms)
@@ -534,17 +543,22 @@ def main():
 
     clocks = Clocks()
     clocks.start()
-    seg = segment("steps")
-    segk = segment("kernel")
+    seg = segment("whole", args.steps)
     clk = clocks.stop()
-    segg = segment("graph")
+    segf = segment("steps", args.steps)
+    segk = segment("kernel", args.steps)
+    # the production loop's figure over at least EXTRA_STEPS steps, so that
+    # a short timed run does not report launch latency
+    g_steps = max(args.steps, EXTRA_STEPS)
+    segg = segment("graph", g_steps)
     t_dev = allmax(world, seg["ms"] / 1e3)
     t_kernel = allmax(world, segk["ms"] / 1e3)
+    t_flushed = allmax(world, segf["ms"] / 1e3)
     rebuilds = seg["rebuilds"]
     epot_pp = seg["epot"] / n
     temp = 2.0 * seg["ekin"] / (3.0 * n)
     value = world * n * args.steps / t_dev
-    graph_loop_pss = n * args.steps / (segg["ms"] / 1e3)
+    graph_loop_pss = n * g_steps / (segg["ms"] / 1e3)
     info = seg["info"]
 
     # ---- roofline of the fused step kernel (its own timed pass, same segment) ----
@@ -561,7 +575,9 @@ def main():
     # state goes to it through a file.  Per timed step: the five API calls,
     # each step's sepret read-back; the first step uploads the host arrays,
     # the final sep_gpu_sync (timed) downloads them.
-    e_steps = args.steps
+    # at least EXTRA_STEPS steps: the first step's upload and the final
+    # download are one-off costs that a short run would let dominate
+    e_steps = max(args.steps, EXTRA_STEPS)
     e2e_warm = max(3, args.warmup // 10)
     with tempfile.TemporaryDirectory() as tmp:
         state = os.path.join(tmp, "state.bin")
@@ -587,12 +603,25 @@ def main():
     wset = n * (16 * 2 + 16 * 4 + 16 + 4) + n * info.list_capacity * 4
     if rank == 0:
         cfgd = workload_config(args, n)
-        cfgd["l2"] = ("flushed: %d MiB written before every timed step, outside the timed spans "
-                      "(per-step working set %.0f MiB, L2 %d MiB)" % (FLUSH_BYTES >> 20, wset / 2 ** 20,
-                                                                  L2_BYTES >> 20))
+        cfgd["l2"] = ("value: not flushed, the inputs are larger than L2 (per-step working set "
+                      "%.0f MiB, L2 %d MiB); roofline kernel spans and flushed_steps: %d MiB "
+                      "written before every step, outside the spans" % (wset / 2 ** 20, L2_BYTES >> 20,
+                                                                     FLUSH_BYTES >> 20))
+        cfgd["timing"] = ("value: sep_gpu_run_timed, graphs of 64 unrolled steps (list rebuild when "
+                          "due, fused step, decision), one CUDA event pair around each graph launch, "
+                          "summed")
+        cfgd["flushed_steps"] = {
+            "value": world * n * args.steps / t_flushed, "unit": "particle-steps/s",
+            "list_rebuilds": segf["rebuilds"],
+            "what": "the same steps with L2 flushed before each and one event pair per step (the "
+                    "events' own cost is inside the spans)"}
         cfgd["graph_loop_no_flush"] = {
             "value": graph_loop_pss, "unit": "particle-steps/s", "list_rebuilds": segg["rebuilds"],
-            "what": "sep_gpu_run, one CUDA graph with a WHILE node, L2 not flushed (production loop)"}
+            "steps": g_steps,
+            "what": "sep_gpu_run, one CUDA graph with a WHILE node, L2 not flushed (production loop; "
+                    "energy and virial summed on the last step only, as sep_gpu_run returns)"}
+        cfgd["observed"] = ("value and roofline: every timed step sums its energy and virial, as a "
+                            "loop of sep_force_pairs / sep_leapfrog calls does")
         cfgd["kernel_params"] = {"team": info.team, "groups": info.groups, "cellf": info.cellf}
         cfgd["tuning"] = {"what": "kernel parameters by system size (n <= classes[k]; the last "
                                   "entry: larger), each [team, groups, cellf], from the autotuner "

@@ -130,16 +130,23 @@ int sep_gpu_time_step_kernel(seppart *ptr, sepsys *sys, sepret *ret, const char 
  * a buffer of its own (on its stream, outside the timed spans) so that no
  * step finds the previous step's data in L2.  One pair of CUDA events per
  * step brackets either the whole step (list rebuild when due, fused
- * force + integration kernel, loop decision) or, with kernel_spans set, the
- * fused kernel alone; the summed device times come back in tm.
+ * force + integration kernel, loop decision) or, with kernel_spans 1, the
+ * fused kernel alone; the summed device times come back in tm.  With
+ * kernel_spans 2 nothing is flushed and the events bracket whole launches of
+ * up to 64 steps (for working sets larger than L2, where a flush adds
+ * nothing but the events' own cost).
  */
 typedef struct {
 	long flush_bytes;      /* in: bytes written between steps (0: no flush) */
-	int kernel_spans;      /* in: 0: time each step; 1: time each fused step kernel */
+	int kernel_spans;      /* in: 0: time each step; 1: time each fused step kernel;
+				* 2: time whole launches of up to 64 steps, with no event
+				* inside them (flush_bytes must be 0) */
 	double ms_steps;       /* out: summed device time of the steps (kernel_spans == 0) */
 	double ms_kernel;      /* out: summed device time of the kernels (kernel_spans == 1) */
 	long launches;         /* out: steps launched */
 	long overflows;        /* out: neighbour-list regrowths (outside the spans) */
+	int observe;           /* in: 1: every step sums its energy and virial, as a loop of
+				* API calls does; 0: only the last step, as sep_gpu_run */
 } sep_gpu_timing;
 
 int sep_gpu_run_timed(seppart *ptr, sepsys *sys, sepret *ret, const char *types,

@@ -37,7 +37,8 @@ class Tuning(C.Structure):
 class GpuTiming(C.Structure):
     """``sep_gpu_timing`` (include/sepgpu.h)."""
     _fields_ = [("flush_bytes", C.c_long), ("kernel_spans", C.c_int), ("ms_steps", C.c_double),
-                ("ms_kernel", C.c_double), ("launches", C.c_long), ("overflows", C.c_long)]
+                ("ms_kernel", C.c_double), ("launches", C.c_long), ("overflows", C.c_long),
+                ("observe", C.c_int)]
 
 
 class SepbResult(C.Structure):

@@ -191,38 +191,12 @@ __device__ __forceinline__ void ff_add(float &hi, float &lo, float q)
 // |result| < 2^62; exact product of the high parts via FMA
 // (explicit roundings throughout, so every kernel that inlines it computes
 // the same bits whatever the compiler contracts around it)
-// Round-to-nearest-even of a float to a 64-bit integer from FP32 and
-// integer instructions (the 64-bit conversion runs at a small fraction of
-// their rates), the same value as __float2ll_rn for |v| < 2^63:
-//   |v| < 2^22          the 1.5 * 2^23 addition rounds v to an integer;
-//   2^22 <= |v| < 2^23  v = m / 2 (m the 24-bit significand), the half
-//                       rounded to even;
-//   2^23 <= |v| < 2^63  v = m 2^k, an integer: a 64-bit shift.
-// Larger values, infinities and NaN take the conversion itself.
-__device__ __forceinline__ long long f2ll_rn(float v)
-{
-	if (fabsf(v) < 4194304.0f)
-		return (long long)(__float_as_int(__fadd_rn(v, 12582912.0f)) - 0x4B400000);
-	const unsigned b = __float_as_uint(v);
-	const int k = (int)((b >> 23) & 0xffu) - 150;
-	if (k > 39) return __float2ll_rn(v);
-	const unsigned m = (b & 0x7fffffu) | 0x800000u;
-	long long q;
-	if (k < 0) {
-		const unsigned h = m >> 1;
-		q = (long long)(h + (m & h & 1u));
-	} else {
-		q = (long long)m << k;
-	}
-	return (b >> 31) ? -q : q;
-}
-
 __device__ __forceinline__ long long ff_mul_fix(float hi, float lo, float shi, float slo)
 {
 	const float p = __fmul_rn(hi, shi);
 	const float e = __fmaf_rn(hi, shi, -p);
 	const float r = __fadd_rn(e, __fmaf_rn(hi, slo, __fmul_rn(lo, shi)));
-	return f2ll_rn(p) + f2ll_rn(r);
+	return __float2ll_rn(p) + __float2ll_rn(r);
 }
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31; }
@@ -235,7 +209,7 @@ __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31; }
 // Larger values (or NaN) take the 64-bit conversion.
 __device__ __forceinline__ long long to_fx(float v)
 {
-	if (!(fabsf(v) < 4194304.0f)) return f2ll_rn(v * FX_SCALE);
+	if (!(fabsf(v) < 4194304.0f)) return __float2ll_rn(v * FX_SCALE);
 	const float M = 12582912.0f;
 	const float t = __fadd_rn(v, M);
 	const int n = __float_as_int(t) - 0x4B400000;

@@ -35,6 +35,7 @@ struct DecideArgs {
 	int pair_end;          // last step of a loop iteration: count down, set the loop handle
 	int use_handles;
 	int reset_while;       // first step of an iteration: clear the loop handle on entry
+	int obs_all;           // every step is observed (measurement of the API loop's work)
 	cudaGraphConditionalHandle h_next, h_while;
 };
 
@@ -93,10 +94,11 @@ __device__ __forceinline__ void decide_warp(const DecideArgs &a)
 // Whether this step's energy and virial are observed: in the device loop
 // only the last step of a call reports them (sep_gpu_run returns the last
 // step's sepret); every other step needs forces, the kinetic sum and the
-// displacement only.  Without a decision (API path) every step reports.
+// displacement only.  Without a decision (API path), or when asked to
+// (obs_all), every step reports.
 __device__ __forceinline__ bool step_observed(const DecideArgs &a)
 {
-	return !a.rs || a.rs->done + 1 >= a.rs->total;
+	return a.obs_all || !a.rs || a.rs->done + 1 >= a.rs->total;
 }
 
 // In a step kernel with a decision attached: on entry (before anything can

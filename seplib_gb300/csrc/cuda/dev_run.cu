@@ -86,6 +86,7 @@ static DecideArgs decide_args(sepdev *d, Runner *r, const sepdev_runcfg *cfg)
 	a.T0 = cfg->T0;
 	a.n = (double)d->n;
 	a.nh = cfg->nh;
+	a.obs_all = cfg->observe_all;
 	return a;
 }
 
@@ -318,9 +319,11 @@ extern "C" int sepdev_run(sepdev *d, const sepdev_pairset *ps, const sepdev_runc
 //
 // The flush writes flush_bytes to a context-owned buffer so that no step
 // finds the previous step's data in L2; it lies outside the [e0, e1] span.
-// With kernel_spans set the events bracket the fused step kernel instead of
-// the whole step.  The host launches one graph per TM_RING steps and reads
-// the events between launches.
+// With kernel_spans 1 the events bracket the fused step kernel instead of
+// the whole step; with kernel_spans 2 there are no events inside the graph
+// and no flush: one pair of stream events brackets each graph launch.  The
+// host launches one graph per TM_RING steps and reads the events between
+// launches.
 
 #define TM_RING 64
 
@@ -425,7 +428,7 @@ static int build_timed_graph(sepdev *d, Runner *r, const sepdev_pairset *ps, con
 		const int p = parity ^ (k & 1);
 		CK(cudaStreamBeginCaptureToGraph(d->st, t->g, &tail, NULL, 1, cudaStreamCaptureModeRelaxed));
 		if (flush) flush_launch(d, flush, 0x9e3779b9u * (unsigned)(k + 1));
-		if (!kernel_spans) e = cudaEventRecordWithFlags(ev->e0[k], d->st, cudaEventRecordExternal);
+		if (kernel_spans == 0) e = cudaEventRecordWithFlags(ev->e0[k], d->st, cudaEventRecordExternal);
 		if (e == cudaSuccess) rc = capture_tail(d, &tail);
 		if ((rc = end_capture(d, rc, e, "capture(flush)"))) return rc;
 		cudaGraphNode_t nif;
@@ -436,9 +439,10 @@ static int build_timed_graph(sepdev *d, Runner *r, const sepdev_pairset *ps, con
 			dec.use_handles = 1;
 			dec.h_next = h[k + 1];
 		}
-		if (kernel_spans) e = cudaEventRecordWithFlags(ev->e0[k], d->st, cudaEventRecordExternal);
+		if (kernel_spans == 1) e = cudaEventRecordWithFlags(ev->e0[k], d->st, cudaEventRecordExternal);
 		if (e == cudaSuccess) rc = step_launch(d, r, ps, cfg, p, dec);
-		if (e == cudaSuccess && !rc) e = cudaEventRecordWithFlags(ev->e1[k], d->st, cudaEventRecordExternal);
+		if (e == cudaSuccess && !rc && kernel_spans != 2)
+			e = cudaEventRecordWithFlags(ev->e1[k], d->st, cudaEventRecordExternal);
 		if (e == cudaSuccess && !rc) rc = capture_tail(d, &tail);
 		if ((rc = end_capture(d, rc, e, "capture(timed step)"))) return rc;
 	}
@@ -451,6 +455,9 @@ static int run_timed_inner(sepdev *d, Runner *r, const sepdev_pairset *ps, const
 {
 	RunState *h = r->h_rs;
 	const size_t flush = (size_t)(tm->flush_bytes > 0 ? tm->flush_bytes : 0) & ~(size_t)15;
+	// kernel_spans 2: one span per graph launch, so no flush may sit inside it
+	const bool whole = tm->kernel_spans == 2;
+	if (whole && flush) return SEPDEV_EINVAL;
 	int rc;
 	if (flush && (rc = flush_reserve(d, flush))) return rc;
 	CK(cudaMemcpyAsync(r->rs, h, sizeof *h, cudaMemcpyHostToDevice, d->st));
@@ -464,17 +471,19 @@ static int run_timed_inner(sepdev *d, Runner *r, const sepdev_pairset *ps, const
 		    (rc = build_timed_graph(d, r, ps, cfg, d->cur, m, flush, tm->kernel_spans, ev, t)))
 			return rc;
 		const long done0 = h->done;
+		if (whole) CK(cudaEventRecord(ev->e0[0], d->st));
 		CK(cudaGraphLaunch(t->exec, d->st));
+		if (whole) CK(cudaEventRecord(ev->e1[0], d->st));
 		d->launches += 1;
 		CK(cudaMemcpyAsync(h, r->rs, sizeof *h, cudaMemcpyDeviceToHost, d->st));
 		CK(cudaStreamSynchronize(d->st));
 		double sum = 0.0;
-		for (int j = 0; j < m; j++) {
+		for (int j = 0; j < (whole ? 1 : m); j++) {
 			float a = 0.f;
 			CK(cudaEventElapsedTime(&a, ev->e0[j], ev->e1[j]));
 			sum += a;
 		}
-		if (tm->kernel_spans) tm->ms_kernel += sum;
+		if (tm->kernel_spans == 1) tm->ms_kernel += sum;
 		else tm->ms_steps += sum;
 		tm->launches += m;
 		// every completed step flipped the position buffer

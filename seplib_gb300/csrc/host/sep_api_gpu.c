@@ -217,7 +217,7 @@ int sep_gpu_run(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
 static double time_kernel_loop(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
 			       double (*fun)(double, char), const double *ljparam, double cf,
 			       unsigned opt, int nh, double T0, double *alpha, double tau,
-			       long nsteps, long flush);
+			       long nsteps, long flush, int observe);
 
 int sep_gpu_run_timed(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
 		      double (*fun)(double, char), const double *ljparam, double cf, unsigned opt,
@@ -233,12 +233,13 @@ int sep_gpu_run_timed(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
 		tm->launches = tm->overflows = 0;
 		return 0;
 	}
-	if (tm->kernel_spans) {
+	if (tm->kernel_spans == 2 && tm->flush_bytes > 0) return -1;
+	if (tm->kernel_spans == 1) {
 		/* stream events around host-launched steps: an event node inside
 		 * a graph costs several microseconds, a stream event much less */
 		double a0 = alpha ? *alpha : 0.0;
 		tm->ms_kernel = time_kernel_loop(ptr, sys, ret, types, fun, ljparam, cf, opt, nh, T0,
-						 &a0, tau, nsteps, tm->flush_bytes);
+						 &a0, tau, nsteps, tm->flush_bytes, tm->observe);
 		if (alpha && nh) *alpha = a0;
 		tm->ms_steps = 0.0;
 		tm->launches = nsteps;
@@ -255,6 +256,7 @@ int sep_gpu_run_timed(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
 	cfg.T0 = T0;
 	cfg.tau = tau;
 	cfg.force_trigger = c->pending_trigger;
+	cfg.observe_all = tm->observe ? 1 : 0;
 	if (!c->sumv2_valid) {
 		rt_check(sepdev_sumv2(c->dev, &c->sumv2), "kinetic sum");
 		c->sumv2_valid = 1;
@@ -294,7 +296,7 @@ int sep_gpu_flush_l2(seppart *ptr, long bytes)
 static double time_kernel_loop(seppart *ptr, sepsys *sys, sepret *ret, const char *types,
 			       double (*fun)(double, char), const double *ljparam, double cf,
 			       unsigned opt, int nh, double T0, double *alpha, double tau,
-			       long nsteps, long flush)
+			       long nsteps, long flush, int observe)
 {
 	double total = 0.0;
 	for (long s = 0; s < nsteps; s++) {
@@ -308,9 +310,10 @@ static double time_kernel_loop(seppart *ptr, sepsys *sys, sepret *ret, const cha
 		const int slot = rt_new_slot(c), lf = rt_new_slot(c);
 		if (flush > 0) rt_check(sepdev_flush_l2(c->dev, (size_t)flush, (unsigned)s), "L2 flush");
 		rt_check(sepdev_event_record(c->dev, 0), "event");
-		/* as in the device loop, only the last step reports energy and virial */
+		/* as in the device loop, only the last step reports energy and
+		 * virial, unless every step is to be observed */
 		rt_check(sepdev_step_obs(c->dev, &ps, 0, sys->dt, nh, nh ? *alpha : 0.0, slot, lf,
-					 s + 1 == nsteps), "step");
+					 observe || s + 1 == nsteps), "step");
 		rt_check(sepdev_event_record(c->dev, 1), "event");
 		float ms = 0.f;
 		rt_check(sepdev_event_elapsed(c->dev, 0, 1, &ms), "event");
@@ -341,7 +344,7 @@ int sep_gpu_time_step_kernel(seppart *ptr, sepsys *sys, sepret *ret, const char 
 			     long nsteps, double *ms_per_launch)
 {
 	const double total = time_kernel_loop(ptr, sys, ret, types, fun, ljparam, cf, opt, nh, T0,
-					       alpha, tau, nsteps, 0);
+					       alpha, tau, nsteps, 0, 0);
 	if (ms_per_launch) *ms_per_launch = nsteps > 0 ? total / nsteps : 0.0;
 	return 0;
 }

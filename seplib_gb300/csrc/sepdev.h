@@ -221,6 +221,7 @@ typedef struct {
 	int nh;
 	double T0, tau;
 	int force_trigger;     /* report an update after the first step */
+	int observe_all;       /* every step sums its energy and virial (else only the last) */
 } sepdev_runcfg;
 
 int sepdev_run(sepdev *d, const sepdev_pairset *ps, const sepdev_runcfg *cfg, long nsteps,
@@ -234,7 +235,8 @@ int sepdev_run(sepdev *d, const sepdev_pairset *ps, const sepdev_runcfg *cfg, lo
  */
 typedef struct {
 	long flush_bytes;      /* in: bytes written between steps (0: no flush) */
-	int kernel_spans;      /* in: 0: events around each step; 1: around each fused step kernel */
+	int kernel_spans;      /* in: 0: events around each step; 1: around each fused step kernel;
+				* 2: around each graph launch of up to 64 steps (no flush) */
 	double ms_steps;       /* out: summed device time of the steps (kernel_spans == 0) */
 	double ms_kernel;      /* out: summed device time of the fused step kernel (kernel_spans == 1) */
 	long launches;         /* out: steps launched (skipped ones included) */

@@ -180,6 +180,43 @@ def test_timed_loop_equals_graph_loop(gpu_lib):
     a.close(); b.close()
 
 
+def test_observed_timed_loop_equals_graph_loop(gpu_lib):
+    """The timed loop with every step observed (energy and virial summed each
+    step, as a loop of API calls does) takes the same trajectory and leaves
+    the same sepret as sep_gpu_run, which observes only its last step."""
+    from seplib_gb300 import GpuTiming
+    s = small()
+    a = Handle(gpu_lib, s, skin=0.5)
+    b = Handle(gpu_lib, s, skin=0.5)
+    nsteps = 120
+    for h in (a, b):
+        h.step(nh=(1.0, 10.0))
+    assert gpu_lib.sep_gpu_run(a.atoms, C.byref(a.sys), C.byref(a.ret), b"AA", a.fun(), None, 2.5,
+                               A.SEP_ALL, 1, 1.0, C.byref(a.alpha), 10.0, nsteps) == 0
+    # per-step spans, kernel spans, whole-launch spans (the last with no
+    # flush: a flush inside a whole-launch span is refused)
+    for k, part in ((0, 40), (1, 40), (2, nsteps - 80)):
+        if k == 2:
+            bad = GpuTiming(flush_bytes=1 << 20, kernel_spans=2, observe=1)
+            assert gpu_lib.sep_gpu_run_timed(b.atoms, C.byref(b.sys), C.byref(b.ret), b"AA", b.fun(),
+                                             None, 2.5, A.SEP_ALL, 1, 1.0, C.byref(b.alpha), 10.0,
+                                             part, C.byref(bad)) == -1
+        tm = GpuTiming(flush_bytes=64 << 20 if k < 2 else 0, kernel_spans=k, observe=1)
+        rc = gpu_lib.sep_gpu_run_timed(b.atoms, C.byref(b.sys), C.byref(b.ret), b"AA", b.fun(), None,
+                                       2.5, A.SEP_ALL, 1, 1.0, C.byref(b.alpha), 10.0, part,
+                                       C.byref(tm))
+        assert rc == 0, gpu_lib.sep_gpu_error()
+        assert (tm.ms_kernel if k == 1 else tm.ms_steps) > 0
+    a.sync(); b.sync()
+    assert a.sys.nupdate_neighb == b.sys.nupdate_neighb and a.sys.nupdate_neighb > 1
+    assert np.array_equal(a.view["x"], b.view["x"])
+    assert np.array_equal(a.view["v"], b.view["v"])
+    assert a.alpha.value == b.alpha.value
+    assert a.ret.epot == b.ret.epot and a.ret.ekin == b.ret.ekin
+    assert np.array_equal(np.array(a.ret.pot_P), np.array(b.ret.pot_P))
+    a.close(); b.close()
+
+
 def test_nve_drift(gpu_lib, ora):
     """Energy drift over 1e4 NVE steps of the N=1000 workload.  Truncation at
     rc makes the total energy a random walk whose drift varies by a factor of
