@@ -311,12 +311,7 @@ extern "C" int sepdev_bonded(sepdev *d, const sepdev_bterm *t, int nt, int accum
 	}
 	a.accumulate = accumulate;
 	a.slots = d->slots;
-	// small systems (32000 beads: 125 blocks of 256 for 152 SMs) take
-	// smaller blocks so that every SM gets work; the sums are exact, so
-	// the block size does not change any result
-	const long nt_ = d->n * BOND_LPA;
-	const int bs = nt_ >= 512L * d->nsm ? 256 : (nt_ >= 256L * d->nsm ? 128 : 64);
-	k_bonded<<<grid_for(nt_, bs), bs, 0, d->st>>>(d->n, a);
+	k_bonded<<<grid_for(d->n * BOND_LPA, 256), 256, 0, d->st>>>(d->n, a);
 	CKL(d);
 	return SEPDEV_OK;
 }

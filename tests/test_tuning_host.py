@@ -54,3 +54,34 @@ def test_rejected_tables(saved, bad):
 def test_driver_words():
     words = tune.as_args([1024, 8192], [(1, 2, 1.0), (2, 1, 1.2), (2, 2, 1.0)])
     assert words == ["3", "1024", "1", "2", "1.0", "8192", "2", "1", "1.2", "0", "2", "2", "1.0"]
+
+
+def test_cache_roundtrip(saved, tmp_path, monkeypatch):
+    """load_or_tune times once, writes the table next to the library (here a
+    temporary path) and later calls load it for the same GPU and build."""
+    calls = []
+
+    def fake_tune(lib, **kw):
+        calls.append(kw)
+        chosen = [(2, 2, 1.0), (1, 2, 1.2), (1, 1, 1.0)]
+        tune.apply(lib, list(tune.CLASSES), chosen)
+        return dict(classes=list(tune.CLASSES), chosen=[list(c) for c in chosen], trials=[], seconds=0.0)
+
+    monkeypatch.setattr(tune, "tune", fake_tune)
+    path = str(tmp_path / "tuning.json")
+    rec = tune.load_or_tune(saved, path=path)
+    assert rec["source"] == "tuned" and len(calls) == 1
+    tune.apply(saved, [], [(1, 2, 1.0)])                     # something else in between
+    rec2 = tune.load_or_tune(saved, path=path)
+    assert rec2["source"] == "cache" and len(calls) == 1
+    cur = tune.current(saved)
+    assert [(c["team"], c["groups"], c["cellf"]) for c in cur] == [(2, 2, 1.0), (1, 2, 1.2), (1, 1, 1.0)]
+    # a different build (key) is timed again
+    import json
+    with open(path) as fh:
+        d = json.load(fh)
+    d["key"] = "another|0|0"
+    with open(path, "w") as fh:
+        json.dump(d, fh)
+    rec3 = tune.load_or_tune(saved, path=path)
+    assert rec3["source"] == "tuned" and len(calls) == 2
