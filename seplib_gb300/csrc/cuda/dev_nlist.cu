@@ -253,9 +253,9 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 	const int lo1 = nc1 >= 3 ? -1 : 0, hi1 = nc1 >= 2 ? 1 : 0;
 	const int lo2 = nc2 >= 3 ? -1 : 0, hi2 = nc2 >= 2 ? 1 : 0;
 	const int cap = a.maxnb;
-	const float rl = sqrtf(a.rl2);
+	const float rl = sqrtf(a.rl2), rlm = rl * 1.0001f;
 	int cnt = 0, flushed = 0;     // entries found / entries written out (multiple of 4)
-	bool me = false, local = false;
+	bool me = false, local = false, filt = false;
 	float mx = 0.f, my = 0.f, mz = 0.f;
 	float bx0 = 0.f, bx1 = 0.f, by0 = 0.f, by1 = 0.f, bz0 = 0.f, bz1 = 0.f;
 	int4 ref = pi;
@@ -372,6 +372,17 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 		bx0 = warp_min_f(me ? mx : 3.0e38f, FULL); bx1 = warp_max_f(me ? mx : -3.0e38f, FULL);
 		by0 = warp_min_f(me ? my : 3.0e38f, FULL); by1 = warp_max_f(me ? my : -3.0e38f, FULL);
 		bz0 = warp_min_f(me ? mz : 3.0e38f, FULL); bz1 = warp_max_f(me ? mz : -3.0e38f, FULL);
+		// A wrapped region (small boxes) can still drop candidates farther
+		// than rlist from the run's bounding box, taken in the frame of the
+		// run's first particle, when no lane can meet a candidate's other
+		// image within rlist: half the box minus the run's reach from that
+		// particle exceeds rlist on every axis.  rlm carries a margin for
+		// the roundings, so the filter only removes candidates the test
+		// would reject, and the list is the same with or without it.
+		filt = WRAPFAST && !local &&
+		       0.5f * a.fs[0] * 4294967296.f - fmaxf(-bx0, bx1) > rlm &&
+		       0.5f * a.fs[1] * 4294967296.f - fmaxf(-by0, by1) > rlm &&
+		       0.5f * a.fs[2] * 4294967296.f - fmaxf(-bz0, bz1) > rlm;
 		int sA0, sA1, sB0 = 0, sB1 = 0;
 		if (xhi - xlo + 3 >= nc0) { sA0 = 0; sA1 = nc0; }
 		else {
@@ -439,6 +450,16 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 				} else {
 					q = make_float4(__int_as_float(pj.x), __int_as_float(pj.y), __int_as_float(pj.z),
 							__int_as_float(jc + lane));
+					if (filt) {
+						const float ox = sep_hi(pj.x, ref.x, a.fs[0]);
+						const float oy = sep_hi(pj.y, ref.y, a.fs[1]);
+						const float oz = sep_hi(pj.z, ref.z, a.fs[2]);
+						const float ex = fmaxf(fmaxf(bx0 - ox, ox - bx1), 0.f);
+						const float ey = fmaxf(fmaxf(by0 - oy, oy - by1), 0.f);
+						const float ez = fmaxf(fmaxf(bz0 - oz, oz - bz1), 0.f);
+						keep = ex < rlm && ey < rlm && ez < rlm &&
+						       fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < rlm * rlm;
+					}
 				}
 			}
 			const unsigned kb = __ballot_sync(FULL, keep);
