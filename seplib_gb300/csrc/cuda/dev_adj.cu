@@ -61,9 +61,9 @@ __global__ void ka_build(const BatchSys *sys, const int *wsys, int nwarps, const
 			for (int ox = lx; ox <= hx; ox++) {
 				const int xx = (cx + ox + nc0) % nc0;
 				const int c = S.coff + xx + nc0 * (yy + nc1 * zz);
-				// four members at a time: their indices and positions are
-				// loaded before any is tested (independent loads in
-				// flight), then tested and appended in member order
+				// eight, then four members at a time: their indices and
+				// positions are loaded before any is tested (independent
+				// loads in flight), then tested and appended in member order
 				auto test = [&](int j, const int4 &pj) {
 					if (j == (int)t) return;
 					const float dx = sep_hi(pi.x, pj.x, S.fs);
@@ -76,6 +76,16 @@ __global__ void ka_build(const BatchSys *sys, const int *wsys, int nwarps, const
 				};
 				int k = cellstart[c];
 				const int ke = cellstart[c + 1];
+				for (; k + 8 <= ke; k += 8) {
+					int jq[8];
+					int4 pq[8];
+#pragma unroll
+					for (int q = 0; q < 8; q++) jq[q] = perm[k + q];
+#pragma unroll
+					for (int q = 0; q < 8; q++) pq[q] = pos[jq[q]];
+#pragma unroll
+					for (int q = 0; q < 8; q++) test(jq[q], pq[q]);
+				}
 				for (; k + 4 <= ke; k += 4) {
 					int jq[4];
 					int4 pq[4];
@@ -202,13 +212,13 @@ __global__ void __launch_bounds__(256) ka_pair(AdjPair a)
 		const int4 pi = a.pos[i];
 		const float4 hi = a.h[i];
 		const int row = NT > 1 ? pi.w * NT : 0;
-		// the list in groups of four indices (one 16-byte load), the four
-		// positions loaded before any pair is evaluated, pairs in list order
-		auto pair = [&](int j, const int4 &pj) {
+		for (int k = 0; k < cnt; k++) {
+			const int j = lp[nl_index(li, k, a.maxnb)];
+			const int4 pj = a.pos[j];
 			const AdjPot &pp = sp[NT > 1 ? row + pj.w : 0];
 			const float dx = sep_hi(pi.x, pj.x, fs), dy = sep_hi(pi.y, pj.y, fs), dz = sep_hi(pi.z, pj.z, fs);
 			const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-			if (s >= pp.rc2) return;
+			if (s >= pp.rc2) continue;
 			const float is = 1.0f / s;
 			const float q = pp.sig2 * is;
 			const float s6 = q * q * q;
@@ -236,17 +246,6 @@ __global__ void __launch_bounds__(256) ka_pair(AdjPair a)
 				ge[t] += mine ? te : 0.f;
 				gs[t] += mine ? ts : 0.f;
 			}
-		};
-		const int4 *lp4 = (const int4 *)(lp + nl_index(li, 0, a.maxnb));
-		const int ng = cnt >> 2;
-		for (int g = 0; g < ng; g++) {
-			const int4 jg = lp4[g * 32];
-			const int4 p0 = a.pos[jg.x], p1 = a.pos[jg.y], p2 = a.pos[jg.z], p3 = a.pos[jg.w];
-			pair(jg.x, p0); pair(jg.y, p1); pair(jg.z, p2); pair(jg.w, p3);
-		}
-		for (int k = ng * 4; k < cnt; k++) {
-			const int j = lp[nl_index(li, k, a.maxnb)];
-			pair(j, a.pos[j]);
 		}
 		a.lx[3 * i] += (double)lxx;
 		a.lx[3 * i + 1] += (double)lxy;
