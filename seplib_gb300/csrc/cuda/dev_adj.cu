@@ -15,9 +15,9 @@
 // virial phi s; primes are d/ds.  The parameter gradients add, per pair and
 // side, phi_theta d.h_i + (1/2K)(u_theta + phi_theta s / 3V).
 //
-// Slot order never changes after the initial sort: list rebuilds use a
-// per-particle scan of index-only cell lists, so no permutation has to be
-// undone in reverse.  Checkpoints every C steps hold the full replica state
+// Slot order never changes after the initial sort: list rebuilds read the
+// cells' members through index-only cell lists (the tile-staged build with
+// an index indirection), so no permutation has to be undone in reverse.  Checkpoints every C steps hold the full replica state
 // and list; the backward pass recomputes a segment from its checkpoint,
 // keeping the states and the lists of every rebuilt replica, and sweeps it.
 #include <math.h>
@@ -30,85 +30,6 @@
 #include "sepbatch.h"
 
 // ---- list rebuild without moving particles ----------------------------------
-
-// one thread per particle of a flagged system: scan the (deduplicated) 27
-// neighbouring cells of the index-only cell list, append every j with
-// r^2 < rl2 in cell order (members ordered by user index)
-__global__ void ka_build(const BatchSys *sys, const int *wsys, int nwarps, const unsigned *flag,
-			 const int4 *pos, const int *cellstart, const int *perm, int *nl, int *ncnt,
-			 int maxnb, float rl2, unsigned *oflow)
-{
-	const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-	const long wg = t >> 5;
-	if (wg >= nwarps) return;
-	const int s = wsys[wg];
-	if (!flag[s]) return;
-	const BatchSys S = sys[s];
-	if (t - S.off >= S.n) return;
-	const int4 pi = pos[t];
-	const int nc0 = S.nc[0], nc1 = S.nc[1], nc2 = S.nc[2];
-	const int cx = (int)__umulhi((unsigned)pi.x, (unsigned)nc0);
-	const int cy = (int)__umulhi((unsigned)pi.y, (unsigned)nc1);
-	const int cz = (int)__umulhi((unsigned)pi.z, (unsigned)nc2);
-	const int lx = nc0 >= 3 ? -1 : 0, hx = nc0 >= 2 ? 1 : 0;
-	const int ly = nc1 >= 3 ? -1 : 0, hy = nc1 >= 2 ? 1 : 0;
-	const int lz = nc2 >= 3 ? -1 : 0, hz = nc2 >= 2 ? 1 : 0;
-	int cnt = 0;
-	for (int oz = lz; oz <= hz; oz++) {
-		const int zz = (cz + oz + nc2) % nc2;
-		for (int oy = ly; oy <= hy; oy++) {
-			const int yy = (cy + oy + nc1) % nc1;
-			for (int ox = lx; ox <= hx; ox++) {
-				const int xx = (cx + ox + nc0) % nc0;
-				const int c = S.coff + xx + nc0 * (yy + nc1 * zz);
-				// eight, then four members at a time: their indices and
-				// positions are loaded before any is tested (independent
-				// loads in flight), then tested and appended in member order
-				auto test = [&](int j, const int4 &pj) {
-					if (j == (int)t) return;
-					const float dx = sep_hi(pi.x, pj.x, S.fs);
-					const float dy = sep_hi(pi.y, pj.y, S.fs);
-					const float dz = sep_hi(pi.z, pj.z, S.fs);
-					if (dx * dx + dy * dy + dz * dz < rl2) {
-						if (cnt < maxnb) nl[nl_index(t, cnt, maxnb)] = j;
-						cnt++;
-					}
-				};
-				int k = cellstart[c];
-				const int ke = cellstart[c + 1];
-				for (; k + 8 <= ke; k += 8) {
-					int jq[8];
-					int4 pq[8];
-#pragma unroll
-					for (int q = 0; q < 8; q++) jq[q] = perm[k + q];
-#pragma unroll
-					for (int q = 0; q < 8; q++) pq[q] = pos[jq[q]];
-#pragma unroll
-					for (int q = 0; q < 8; q++) test(jq[q], pq[q]);
-				}
-				for (; k + 4 <= ke; k += 4) {
-					int jq[4];
-					int4 pq[4];
-#pragma unroll
-					for (int q = 0; q < 4; q++) jq[q] = perm[k + q];
-#pragma unroll
-					for (int q = 0; q < 4; q++) pq[q] = pos[jq[q]];
-#pragma unroll
-					for (int q = 0; q < 4; q++) test(jq[q], pq[q]);
-				}
-				for (; k < ke; k++) {
-					const int j = perm[k];
-					test(j, pos[j]);
-				}
-			}
-		}
-	}
-	ncnt[t] = cnt < maxnb ? cnt : maxnb;
-	if (cnt > maxnb) atomicOr(oflow, 1u);
-	// the last group of four is padded with the particle itself, as the
-	// list builder pads it (the step kernel reads whole groups)
-	for (int k = cnt; k < ((cnt + 3) & ~3) && k < maxnb; k++) nl[nl_index(t, k, maxnb)] = (int)t;
-}
 
 // a rebuilt system measures displacements from here on (skin test)
 __global__ void ka_xn(const int *wsys, int nwarps, const unsigned *flag, const int4 *pos, int4 *xn,
@@ -440,10 +361,11 @@ static int adj_rebuild(sepadj *A, int parity)
 	int rc = batch_cells_launch(b, parity);
 	if (rc) return rc;
 	CK(cudaMemsetAsync(d->flags, 0, sizeof(unsigned) * 2, d->st));
-	const float rl = (float)(b->rc + b->skin);
-	ka_build<<<grid_for(b->ntot, 256), 256, 0, d->st>>>(b->sys, b->wsys, b->nwarps, b->flag, d->pos[parity],
-							   b->cellstart, d->perm, d->nl, d->ncnt, d->maxnb,
-							   rl * rl, d->flags);
+	// the tile-staged build of the batched systems, reading each cell's
+	// members through the index-only cell lists
+	if ((rc = sepdev_batch_build(d, parity, b->cellstart, b->sys, b->wsys, b->nwarps, b->flag,
+				     (float)((b->rc + b->skin) * (b->rc + b->skin)), d->perm)))
+		return rc;
 	ka_xn<<<grid_for(b->ntot, 256), 256, 0, d->st>>>(b->wsys, b->nwarps, b->flag, d->pos[parity], d->xn,
 							d->cross, d->cbase);
 	CKL(d);

@@ -679,7 +679,7 @@ int batch_rebuild_launch(sepb *b, int parity)
 	CKL(d);
 	CK(cudaMemsetAsync(d->flags, 0, sizeof(unsigned) * 2, d->st));
 	return sepdev_batch_build(d, parity, b->cellstart, b->sys, b->wsys, b->nwarps, b->flag,
-				  (float)((b->rc + b->skin) * (b->rc + b->skin)));
+				  (float)((b->rc + b->skin) * (b->rc + b->skin)), NULL);
 }
 
 int batch_step_launch(sepb *b, int parity, const BatchDecide &dec)

@@ -70,8 +70,9 @@ struct BatchDecide {
 int sepdev_batch_step(sepdev *d, const PairArgs &a, const BatchSys *sys, const int4 *wstep, int nwarps,
 		      const BatchState *bs, const BatchRun *run, long long *slots, const BatchDecide &dec,
 		      int typed);
+// perm != NULL: the cell lists hold slot indices (particles not moved)
 int sepdev_batch_build(sepdev *d, int parity, const int *cellstart, const BatchSys *sys,
-		       const int *wsys, int nwarps, const unsigned *flag, float rl2);
+		       const int *wsys, int nwarps, const unsigned *flag, float rl2, const int *perm);
 
 // host-side batch (dev_batch.cu); the adjoint (dev_adj.cu) builds on it
 struct sepb {

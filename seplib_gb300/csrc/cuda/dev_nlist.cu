@@ -188,6 +188,7 @@ struct BuildArgs {
 	int excl;
 	const int *gid, *mol;
 	const int *exs, *exi;   // CSR for the active exclusion mode
+	const int *perm;        // PERM builds: the cell lists hold slot indices (particles not moved)
 };
 
 // Tile-staged list build: one warp per tile of 32 consecutive particles (in
@@ -233,7 +234,9 @@ __device__ __forceinline__ float warp_max_f(float v, unsigned mask)
 // MOLX (same-molecule exclusions): the candidates' molecule indices are
 // staged in spm beside their positions, and in-box runs take a branch-free
 // loop that tests them from shared memory.
-template <bool WRAPFAST, bool MOLX = false>
+// PERM: the particles are not in cell order; a cell's members are the
+// slots perm[cellstart[c] .. cellstart[c + 1]) (the adjoint's fixed slots).
+template <bool WRAPFAST, bool MOLX = false, bool PERM = false>
 __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, float4 *sp, int *ring,
 					   int *spm = nullptr)
 {
@@ -356,8 +359,12 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 		const unsigned mine = __ballot_sync(FULL, act && row == rrow);
 		todo &= ~mine;
 		me = (mine >> lane) & 1u;
-		const int xlo = __shfl_sync(FULL, cx, __ffs(mine) - 1);
-		const int xhi = __shfl_sync(FULL, cx, 31 - __clz(mine));
+		// the run's cells along x: in cell order its first and last lanes;
+		// over index-only cell lists the lanes are in no order (min, max)
+		const int xlo = PERM ? (int)__reduce_min_sync(FULL, me ? (unsigned)cx : 0xffffffffu)
+				     : __shfl_sync(FULL, cx, __ffs(mine) - 1);
+		const int xhi = PERM ? (int)__reduce_max_sync(FULL, me ? (unsigned)cx : 0u)
+				     : __shfl_sync(FULL, cx, 31 - __clz(mine));
 		const int ry = rrow % nc1, rz = rrow / nc1;
 		// the staged region spans (xhi - xlo + 3) x 3 x 3 cells; when that is
 		// under half the box on every axis, separations need no wrapping
@@ -420,21 +427,23 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 		};
 		next_seg();
 		int4 pn = make_int4(0, 0, 0, 0);
-		int mn = 0;
+		int mn = 0, jn = 0;
 		if (sidx < nseg && lane < je - jj) {
-			pn = a.pos[jj + lane];
-			if (MOLX) mn = a.mol[jj + lane];
+			jn = PERM ? a.perm[jj + lane] : jj + lane;
+			pn = a.pos[jn];
+			if (MOLX) mn = a.mol[jn];
 		}
 		int fill = 0;
 		while (sidx < nseg) {
-			const int jc = jj, take = min(32, je - jj);
+			const int take = min(32, je - jj);
 			const int4 pj = pn;
-			const int mj = mn;
+			const int mj = mn, jcur = jn;
 			jj += 32;
 			if (jj >= je) { sidx++; next_seg(); }
 			if (sidx < nseg && lane < min(32, je - jj)) {
-				pn = a.pos[jj + lane];
-				if (MOLX) mn = a.mol[jj + lane];
+				jn = PERM ? a.perm[jj + lane] : jj + lane;
+				pn = a.pos[jn];
+				if (MOLX) mn = a.mol[jn];
 			}
 			if (fill + take > BT_CAP) { test(fill); fill = 0; }
 			bool keep = lane < take;
@@ -442,14 +451,14 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 			if (keep) {
 				if (local) {
 					q = make_float4(sep_hi(pj.x, ref.x, a.fs[0]), sep_hi(pj.y, ref.y, a.fs[1]),
-							sep_hi(pj.z, ref.z, a.fs[2]), __int_as_float(jc + lane));
+							sep_hi(pj.z, ref.z, a.fs[2]), __int_as_float(jcur));
 					const float ex = fmaxf(fmaxf(bx0 - q.x, q.x - bx1), 0.f);
 					const float ey = fmaxf(fmaxf(by0 - q.y, q.y - by1), 0.f);
 					const float ez = fmaxf(fmaxf(bz0 - q.z, q.z - bz1), 0.f);
 					keep = ex < rl && ey < rl && ez < rl && fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < a.rl2;
 				} else {
 					q = make_float4(__int_as_float(pj.x), __int_as_float(pj.y), __int_as_float(pj.z),
-							__int_as_float(jc + lane));
+							__int_as_float(jcur));
 					if (filt) {
 						const float ox = sep_hi(pj.x, ref.x, a.fs[0]);
 						const float oy = sep_hi(pj.y, ref.y, a.fs[1]);
@@ -519,6 +528,25 @@ __global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles_batch(BuildArgs a
 	b.cellstart = a.cellstart + S.coff;
 	for (int k = 0; k < 3; k++) { b.nc[k] = S.nc[k]; b.fs[k] = S.fs; }
 	build_tile<true>(S.off + S.n, b, wg * 32, sp_all[w], ring_all[w]);
+}
+
+// The same over index-only cell lists (particles not moved: the adjoint).
+__global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles_batch_perm(BuildArgs a, const BatchSys *sys,
+									 const int *wsys, int nwarps,
+									 const unsigned *flag)
+{
+	__shared__ float4 sp_all[BT_WARPS][BT_CAP];
+	__shared__ int ring_all[BT_WARPS][BT_RING * 32];
+	const int w = threadIdx.x >> 5;
+	const long wg = (long)blockIdx.x * BT_WARPS + w;
+	if (wg >= nwarps) return;
+	const int s = wsys[wg];
+	if (!flag[s]) return;
+	const BatchSys S = sys[s];
+	BuildArgs b = a;
+	b.cellstart = a.cellstart + S.coff;
+	for (int k = 0; k < 3; k++) { b.nc[k] = S.nc[k]; b.fs[k] = S.fs; }
+	build_tile<true, false, true>(S.off + S.n, b, wg * 32, sp_all[w], ring_all[w]);
 }
 
 // Deterministic order inside each cell: one warp per cell ranks its members
@@ -703,11 +731,12 @@ int sepdev_build_args(sepdev *d, BuildArgs *a, int parity)
 	a->mol = d->mol;
 	a->exs = d->excl == SEPDEV_EXCL_BONDS ? d->exb_start : d->exa_start;
 	a->exi = d->excl == SEPDEV_EXCL_BONDS ? d->exb_idx : d->exa_idx;
+	a->perm = NULL;
 	return SEPDEV_OK;
 }
 
 int sepdev_batch_build(sepdev *d, int parity, const int *cellstart, const BatchSys *sys,
-		       const int *wsys, int nwarps, const unsigned *flag, float rl2)
+		       const int *wsys, int nwarps, const unsigned *flag, float rl2, const int *perm)
 {
 	BuildArgs a;
 	memset(&a, 0, sizeof a);
@@ -721,7 +750,12 @@ int sepdev_batch_build(sepdev *d, int parity, const int *cellstart, const BatchS
 	a.excl = SEPDEV_EXCL_NONE;
 	a.gid = d->gid;
 	a.mol = d->mol;
-	k_build_tiles_batch<<<grid_for(nwarps, BT_WARPS), BT_WARPS * 32, 0, d->st>>>(a, sys, wsys, nwarps, flag);
+	a.perm = perm;
+	if (perm)
+		k_build_tiles_batch_perm<<<grid_for(nwarps, BT_WARPS), BT_WARPS * 32, 0, d->st>>>(a, sys, wsys, nwarps,
+												   flag);
+	else
+		k_build_tiles_batch<<<grid_for(nwarps, BT_WARPS), BT_WARPS * 32, 0, d->st>>>(a, sys, wsys, nwarps, flag);
 	CKL(d);
 	return SEPDEV_OK;
 }
