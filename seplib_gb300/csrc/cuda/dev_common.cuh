@@ -94,6 +94,7 @@ struct sepdev {
 	double rlist;
 	int excl;
 	int list_valid;
+	int list_unchecked;       // built without the capacity check: the next read of the flags decides
 
 	// exclusions (user indices, CSR)
 	int *exb_start, *exb_idx, *exa_start, *exa_idx;

@@ -770,9 +770,9 @@ int sepdev_build_async(sepdev *d, int parity)
 	return launch_build(d, a);
 }
 
-// Host-driven rebuild: sort, build, check the capacity and grow it when a
-// particle overflowed (synchronous).
-extern "C" int sepdev_build_list(sepdev *d, double rlist, int excl, int trigger)
+// The host-driven rebuild's first part: kernel parameters, cell grid, sort
+// (asynchronous), and a first list capacity from the mean density.
+static int list_prepare(sepdev *d, double rlist, int excl, int trigger)
 {
 	if (!(rlist > 0)) return SEPDEV_EINVAL;
 	if ((excl == SEPDEV_EXCL_BONDS || excl == SEPDEV_EXCL_ALLBONDED) && !d->has_excl)
@@ -789,15 +789,67 @@ extern "C" int sepdev_build_list(sepdev *d, double rlist, int excl, int trigger)
 		const double est = 4.18879020479 * rlist * rlist * rlist * (double)d->n / vol;
 		if ((rc = list_capacity(d, (int)(1.35 * est) + 32))) return rc;
 	}
+	return SEPDEV_OK;
+}
+
+// Build from the sorted order, check the capacity, grow it and build again
+// when a particle overflowed (synchronous).
+static int build_checked(sepdev *d)
+{
+	int rc;
 	for (int attempt = 0; attempt < 4; attempt++) {
 		if ((rc = sepdev_build_async(d, d->cur))) return rc;
 		unsigned fl[2];
 		CK(cudaMemcpyAsync(fl, d->flags, sizeof fl, cudaMemcpyDeviceToHost, d->st));
 		CK(cudaStreamSynchronize(d->st));
-		if (!(fl[0] & 1u)) { d->list_valid = 1; return SEPDEV_OK; }
+		if (!(fl[0] & 1u)) {
+			d->list_valid = 1;
+			d->list_unchecked = 0;
+			return SEPDEV_OK;
+		}
 		if ((rc = list_capacity(d, (int)(fl[1] * 1.25) + 16))) return rc;
 	}
 	return SEPDEV_EOVERFLOW;
+}
+
+// Host-driven rebuild: sort, build, check the capacity and grow it when a
+// particle overflowed (synchronous).
+extern "C" int sepdev_build_list(sepdev *d, double rlist, int excl, int trigger)
+{
+	int rc;
+	if ((rc = list_prepare(d, rlist, excl, trigger))) return rc;
+	return build_checked(d);
+}
+
+// The same without waiting: the list is marked unchecked.  A step kernel
+// skips its work when the build overflowed (flags[0]); the next read of
+// the flags with the step's sums (sepdev_slots_read) clears the mark, and
+// every other consumer confirms the list first (sepdev_list_confirm).
+extern "C" int sepdev_build_list_deferred(sepdev *d, double rlist, int excl, int trigger)
+{
+	int rc;
+	if ((rc = list_prepare(d, rlist, excl, trigger))) return rc;
+	if ((rc = sepdev_build_async(d, d->cur))) return rc;
+	d->list_valid = 1;
+	d->list_unchecked = 1;
+	return SEPDEV_OK;
+}
+
+// Settle an unchecked list: read the overflow flag, and on overflow grow the
+// capacity and build again from the same sorted order (synchronous).
+extern "C" int sepdev_list_confirm(sepdev *d)
+{
+	if (!d->list_unchecked) return SEPDEV_OK;
+	unsigned fl[2];
+	CK(cudaMemcpyAsync(fl, d->flags, sizeof fl, cudaMemcpyDeviceToHost, d->st));
+	CK(cudaStreamSynchronize(d->st));
+	if (!(fl[0] & 1u)) {
+		d->list_unchecked = 0;
+		return SEPDEV_OK;
+	}
+	int rc;
+	if ((rc = list_capacity(d, (int)(fl[1] * 1.25) + 16))) return rc;
+	return build_checked(d);
 }
 
 // Grow the list for a count the device reported (used after an in-graph overflow).
@@ -809,6 +861,8 @@ int sepdev_grow_list(sepdev *d, int needed)
 extern "C" int sepdev_list_stats(sepdev *d, int *maxcount, double *meancount, int *capacity)
 {
 	if (!d->list_valid || !d->ncnt) return SEPDEV_EINVAL;
+	int rc;
+	if ((rc = sepdev_list_confirm(d))) return rc;
 	int *h = (int *)malloc(sizeof(int) * d->n);
 	if (!h) return SEPDEV_ENOMEM;
 	cudaError_t e = cudaMemcpyAsync(h, d->ncnt, sizeof(int) * d->n, cudaMemcpyDeviceToHost, d->st);
@@ -833,7 +887,7 @@ static int cmp_pair(const void *a, const void *b)
 
 extern "C" long sepdev_list_pairs(sepdev *d, int *pairs, long cap)
 {
-	if (!d->list_valid) return -1;
+	if (!d->list_valid || sepdev_list_confirm(d)) return -1;
 	const long n = d->n;
 	const size_t len = (size_t)((n + 31) / 32) * 32 * (size_t)d->maxnb;
 	int *nl = (int *)malloc(sizeof(int) * len), *cnt = (int *)malloc(sizeof(int) * n);

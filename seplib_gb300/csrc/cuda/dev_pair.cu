@@ -862,14 +862,18 @@ extern "C" int sepdev_pair_forces(sepdev *d, const sepdev_pairset *ps, int accum
 {
 	if (!d->list_valid || slot < 0 || slot >= d->nslots) return SEPDEV_EINVAL;
 	int rc;
+	if ((rc = sepdev_list_confirm(d))) return rc;
 	if ((rc = sepdev_upload_pairset(d, ps))) return rc;
 	PairArgs a;
 	sepdev_fill_args(d, a, ps, 0.0, 0, 0.0, accumulate, slot, slot, d->cur);
 	return sepdev_launch_pair(d, ps, a, false);
 }
 
-extern "C" int sepdev_step_obs(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
-			       int nh, double alpha, int pair_slot, int lf_slot, int observe)
+// the fused step on a list that may still be unchecked: the kernel skips its
+// work (positions, velocities, forces and sums untouched) when the build
+// overflowed; the caller reads the flags with the step's sums
+static int step_launch_checked(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt, int nh,
+			       double alpha, int pair_slot, int lf_slot, int observe)
 {
 	if (!d->list_valid || pair_slot < 0 || pair_slot >= d->nslots || lf_slot < 0 ||
 	    lf_slot >= d->nslots)
@@ -879,9 +883,32 @@ extern "C" int sepdev_step_obs(sepdev *d, const sepdev_pairset *ps, int accumula
 	PairArgs a;
 	sepdev_fill_args(d, a, ps, dt, nh, alpha, accumulate, pair_slot, lf_slot, d->cur);
 	a.skip_obs = !observe;
+	if (d->list_unchecked) a.flags = d->flags;
 	if ((rc = sepdev_launch_pair(d, ps, a, true))) return rc;
 	d->cur ^= 1;
 	return SEPDEV_OK;
+}
+
+extern "C" int sepdev_step_deferred(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
+				    int nh, double alpha, int pair_slot, int lf_slot)
+{
+	return step_launch_checked(d, ps, accumulate, dt, nh, alpha, pair_slot, lf_slot, 1);
+}
+
+// a deferred step that found the list overflowed did nothing: its buffer
+// flip is undone before the step runs again
+extern "C" void sepdev_step_retract(sepdev *d)
+{
+	d->cur ^= 1;
+}
+
+extern "C" int sepdev_step_obs(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
+			       int nh, double alpha, int pair_slot, int lf_slot, int observe)
+{
+	if (!d->list_valid) return SEPDEV_EINVAL;
+	int rc;
+	if ((rc = sepdev_list_confirm(d))) return rc;
+	return step_launch_checked(d, ps, accumulate, dt, nh, alpha, pair_slot, lf_slot, observe);
 }
 
 extern "C" int sepdev_step(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,

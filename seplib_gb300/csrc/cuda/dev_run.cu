@@ -260,8 +260,10 @@ static int run_loop(sepdev *d, const sepdev_pairset *ps, const sepdev_runcfg *cf
 		    int *last_trig)
 {
 	if (!d->list_valid || nsteps < 0) return SEPDEV_EINVAL;
+	int rc;
+	if ((rc = sepdev_list_confirm(d))) return rc;
 	Runner *r;
-	int rc = runner_get(d, &r);
+	rc = runner_get(d, &r);
 	if (rc) return rc;
 	if ((rc = run_begin(d, r, ps, cfg, *alpha, *sumv2, nsteps))) return rc;
 	RunState *h = r->h_rs;
@@ -523,6 +525,7 @@ static int run_timed_loop(sepdev *d, const sepdev_pairset *ps, const sepdev_runc
 			  int *last_trig, sepdev_timing *tm)
 {
 	if (!d->list_valid || nsteps < 0 || !tm) return SEPDEV_EINVAL;
+	if (sepdev_list_confirm(d)) return SEPDEV_ECUDA;
 	tm->ms_steps = tm->ms_kernel = 0.0;
 	tm->launches = 0;
 	tm->overflows = 0;

@@ -316,6 +316,8 @@ extern "C" int sepdev_slots_read(sepdev *d, int nslots, double *out, unsigned *f
 				   cudaMemcpyDeviceToHost, d->st));
 	CK(cudaMemcpyAsync(d->h_flags, d->flags, sizeof(unsigned) * 4, cudaMemcpyDeviceToHost, d->st));
 	CK(cudaStreamSynchronize(d->st));
+	// an unchecked list that did not overflow is settled by this read
+	if (d->list_unchecked && !(d->h_flags[0] & 1u)) d->list_unchecked = 0;
 	for (int s = 0; s < nslots; s++)
 		for (int k = 0; k < SLOT_FIELDS; k++) {
 			long long v = d->h_slots[s * SLOT_FIELDS + k];

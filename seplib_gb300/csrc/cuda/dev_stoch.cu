@@ -478,6 +478,7 @@ extern "C" int sepdev_ext_download(sepdev *d, double *pv, double *pa, double *pr
 extern "C" int sepdev_dpd_forces(sepdev *d, const sepdev_dpd *p, int accumulate, int slot, int slot2)
 {
 	if (!d->ext[0] || !d->list_valid) return SEPDEV_EINVAL;
+	if (sepdev_list_confirm(d)) return SEPDEV_ECUDA;
 	if (slot < 0 || slot >= d->nslots || (p->virial && (slot2 < 0 || slot2 >= d->nslots)))
 		return SEPDEV_EINVAL;
 	const bool molv = p->virial && p->mslot >= 0 && d->molvir_on;

@@ -39,14 +39,20 @@ void sep_leapfrog(seppart *ptr, sepsys *sys, sepret *retval)
 	int lf;
 	/* pending bonded terms go first; the step adds the pair forces to them */
 	rt_launch_bonded(c);
+	sepdev_pairset ps;
+	int fused = 0, acc = 0, fr = 0, pslot = -1;
+	double fa = 0.0;
 	if (c->pass_slot >= 0) {
-		sepdev_pairset ps;
 		extern void rt_pairset(rt_ctx *c, sepdev_pairset *ps);
 		rt_pairset(c, &ps);
 		rt_pass_mol_slot(c);
 		lf = rt_new_slot(c);
-		rt_check(sepdev_step(c->dev, &ps, !c->forces_zero, sys->dt, c->friction,
-				     c->friction_alpha, c->pass_slot, lf), "fused step");
+		fused = 1;
+		acc = !c->forces_zero;
+		fr = c->friction;
+		fa = c->friction_alpha;
+		pslot = c->pass_slot;
+		rt_check(sepdev_step_deferred(c->dev, &ps, acc, sys->dt, fr, fa, pslot, lf), "fused step");
 		c->nterms = 0;
 		c->coul_on = 0;
 		c->pass_slot = -1;
@@ -60,7 +66,18 @@ void sep_leapfrog(seppart *ptr, sepsys *sys, sepret *retval)
 	c->friction_alpha = 0.0;
 	c->host_valid = 0;
 	rt_add_op(c, retval, OP_KIN, lf, 0);
-	rt_read_slots(c, sys, lf);
+	if (fused) {
+		/* the list built in this step's sep_force_pairs overflowed: the
+		 * step did nothing; grow the list and run it again */
+		while (rt_read_step_slots(c, sys, lf)) {
+			sepdev_step_retract(c->dev);
+			rt_check(sepdev_list_confirm(c->dev), "neighbour-list build");
+			rt_pass_mol_slot(c);
+			rt_check(sepdev_step_deferred(c->dev, &ps, acc, sys->dt, fr, fa, pslot, lf), "fused step");
+		}
+	} else {
+		rt_read_slots(c, sys, lf);
+	}
 	if (sqrt(sys->max_dist2) > sys->skin * 0.5 || c->pending_trigger) {
 		sys->neighb_flag = 1;
 		sys->nupdate_neighb++;

@@ -468,12 +468,15 @@ void rt_materialize_forces(rt_ctx *c)
 	}
 }
 
-void rt_read_slots(rt_ctx *c, sepsys *sys, int lf_slot)
+static int read_slots(rt_ctx *c, sepsys *sys, int lf_slot, int step_may_skip)
 {
-	if (!c->dev) return;
+	if (!c->dev) return 0;
 	double vals[16 * SLOT_FIELDS];
 	unsigned flags[4];
 	rt_check(sepdev_slots_read(c->dev, c->nslots, vals, flags), "slot read-back");
+	/* a deferred step on a list whose build overflowed did nothing: leave
+	 * the slots and the operations for its second run */
+	if (step_may_skip && (flags[0] & 1u)) return 1;
 	for (int k = 0; k < c->nops; k++) {
 		const rt_op *o = &c->ops[k];
 		const double *s = vals + o->slot * SLOT_FIELDS;
@@ -519,6 +522,17 @@ void rt_read_slots(rt_ctx *c, sepsys *sys, int lf_slot)
 	c->nops = 0;
 	c->nslots = 0;
 	rt_check(sepdev_slots_reset(c->dev), "slot reset");
+	return 0;
+}
+
+void rt_read_slots(rt_ctx *c, sepsys *sys, int lf_slot)
+{
+	read_slots(c, sys, lf_slot, 0);
+}
+
+int rt_read_step_slots(rt_ctx *c, sepsys *sys, int lf_slot)
+{
+	return read_slots(c, sys, lf_slot, 1);
 }
 
 void rt_flush(rt_ctx *c)
@@ -568,7 +582,10 @@ void rt_prepare_list(rt_ctx *c, sepsys *sys, unsigned opt, int brute_excl_bonds)
 	rt_launch_bonded(c);
 	if (want_excl != SEPDEV_EXCL_NONE && want_excl != SEPDEV_EXCL_SAMEMOL && c->topo_dirty)
 		rt_need_device(c, sys);
-	rt_check(sepdev_build_list(c->dev, rlist, want_excl, c->trigger_next), "neighbour-list build");
+	/* the capacity check is left to the step's read-back, or to the next
+	 * other consumer of the list (sepdev_build_list_deferred) */
+	rt_check(sepdev_build_list_deferred(c->dev, rlist, want_excl, c->trigger_next),
+		 "neighbour-list build");
 	c->list_excl = want_excl;
 	c->list_rlist = rlist;
 	c->list_stale = 0;

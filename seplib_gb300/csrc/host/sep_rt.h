@@ -162,6 +162,9 @@ void rt_queue_bonded(rt_ctx *c, const sepdev_bterm *t); /* defer a bonded term *
 void rt_launch_bonded(rt_ctx *c);        /* launch the pending bonded terms (one kernel) */
 void rt_materialize_forces(rt_ctx *c);   /* pending pass + friction + zeroing into stored forces */
 void rt_read_slots(rt_ctx *c, sepsys *sys, int leapfrog_slot);   /* sync, apply ops */
+/* the same after a deferred fused step: 1 (nothing applied, slots kept)
+ * when the step found its list overflowed and must run again */
+int rt_read_step_slots(rt_ctx *c, sepsys *sys, int leapfrog_slot);
 int rt_ret_pending(rt_ctx *c, const sepret *ret);
 void rt_flush(rt_ctx *c);                /* everything pending, then read slots */
 

@@ -141,6 +141,12 @@ int sepdev_slots_read(sepdev *d, int nslots, double *out, unsigned *flags);
 /* Rebuild the cell order and the full neighbour list with cut-off rlist.
  * trigger != 0 marks a skin-triggered rebuild (crossing base reset). */
 int sepdev_build_list(sepdev *d, double rlist, int excl, int trigger);
+/* The same without waiting for the capacity check: the list is marked
+ * unchecked.  sepdev_step_deferred runs on it (skipping its work if the
+ * build overflowed), sepdev_slots_read settles it when its flags show no
+ * overflow, every other consumer confirms it first (synchronous). */
+int sepdev_build_list_deferred(sepdev *d, double rlist, int excl, int trigger);
+int sepdev_list_confirm(sepdev *d);
 /* Pair set of the current list, user indices, i<j, unique: returns count,
  * fills up to cap pairs (2 ints each).  Test and diagnostics helper. */
 long sepdev_list_pairs(sepdev *d, int *pairs, long cap);
@@ -168,6 +174,13 @@ int sepdev_step(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
  * step of a loop whose sepret only reports its last step) */
 int sepdev_step_obs(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
 		    int nh, double alpha, int pair_slot, int lf_slot, int observe);
+
+/* sepdev_step on a list that may be unchecked (sepdev_build_list_deferred);
+ * if flags[0] & 1 at the following sepdev_slots_read, the step did nothing:
+ * sepdev_step_retract, sepdev_list_confirm, and run it again. */
+int sepdev_step_deferred(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
+			 int nh, double alpha, int pair_slot, int lf_slot);
+void sepdev_step_retract(sepdev *d);
 
 /* f -= alpha m v on the stored forces. */
 int sepdev_friction(sepdev *d, double alpha);

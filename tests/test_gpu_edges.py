@@ -66,6 +66,57 @@ def test_tiny_and_ragged_systems(gpu_lib, ora, n):
     h.close()
 
 
+def cluster_system(seed=17):
+    """a dense fcc cluster in a dilute fluid: the densest particles have far
+    more neighbours than the mean density predicts"""
+    rng = np.random.default_rng(seed)
+    L = np.array([16.0, 16.0, 16.0])
+    cl, _ = cfg.fcc(6, 1.6)
+    cl = cl - cl.mean(0) + 0.5 * L
+    def mind2(a, p):
+        d = a - p
+        d -= L * np.round(d / L)
+        return (d * d).sum(1).min()
+    dil = []
+    while len(dil) < 1000:
+        p = spread(1, L, rng)[0]
+        if mind2(cl, p) > 0.95 ** 2 and (not dil or mind2(np.asarray(dil), p) > 0.95 ** 2):
+            dil.append(p)
+    x = np.concatenate([cl, np.array(dil)])
+    n = len(x)
+    return cfg.System(x=x, v=np.zeros((n, 3)), L=L, types=np.full(n, b"A", "S1"), m=np.ones(n), z=np.zeros(n))
+
+
+def test_list_overflow_in_a_step(gpu_lib, ora):
+    """The list is built without waiting for its capacity check; a fused step
+    on a list that overflowed does nothing, and sep_leapfrog grows the list
+    and runs the step again: one step from the cluster system against the
+    FP64 oracle's step."""
+    s = cluster_system()
+    h = Handle(gpu_lib, s, skin=0.3)
+    h.step()
+    h.sync()
+    info = seplib_gb300.GpuInfo()
+    gpu_lib.sep_gpu_info_get(h.atoms, C.byref(info))
+    est = 1.35 * 4.18879020479 * 2.8 ** 3 * s.n / np.prod(s.L) + 32
+    assert info.list_max > est and info.list_capacity >= info.list_max
+    r = ora.run_lj(s.x, s.v, s.m, s.types, s.L, ora.POT_LJSHIFT, None, 2.5, 0.3, 0.005, 1)
+    assert rel_l2(h.view["v"], r["v"]) < 1e-5
+    dx = h.view["x"] - r["x"]
+    dx -= s.L * np.round(dx / s.L)
+    assert np.abs(dx).max() < 1e-6
+    # the energy cancels between the compressed cluster's repulsive pairs and
+    # the rest: the bar is relative to the sum of the pair energies' sizes
+    d = s.x[:, None, :] - s.x[None, :, :]
+    d -= s.L * np.round(d / s.L)
+    r2 = (d * d).sum(-1)
+    iu = np.triu_indices(s.n, 1)
+    r2 = r2[iu][r2[iu] < 2.5 ** 2]
+    sabs = np.abs(4.0 * (r2 ** -6 - r2 ** -3) - 4.0 * (2.5 ** -12 - 2.5 ** -6)).sum()
+    assert abs(h.ret.epot - r["epot"]) <= 1e-6 * sabs
+    h.close()
+
+
 def test_list_overflow_grows(gpu_lib, ora):
     rng = np.random.default_rng(17)
     L = np.array([16.0, 16.0, 16.0])
