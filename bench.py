@@ -543,9 +543,9 @@ def main():
 
     clocks = Clocks()
     clocks.start()
-    seg = segment("whole", args.steps)
+    seg = segment("steps", args.steps)
     clk = clocks.stop()
-    segf = segment("steps", args.steps)
+    segw = segment("whole", args.steps)
     segk = segment("kernel", args.steps)
     # the production loop's figure over at least EXTRA_STEPS steps, so that
     # a short timed run does not report launch latency
@@ -553,7 +553,7 @@ def main():
     segg = segment("graph", g_steps)
     t_dev = allmax(world, seg["ms"] / 1e3)
     t_kernel = allmax(world, segk["ms"] / 1e3)
-    t_flushed = allmax(world, segf["ms"] / 1e3)
+    t_whole = allmax(world, segw["ms"] / 1e3)
     rebuilds = seg["rebuilds"]
     epot_pp = seg["epot"] / n
     temp = 2.0 * seg["ekin"] / (3.0 * n)
@@ -600,21 +600,22 @@ def main():
                "sample": "%d MD steps of the full N=%d system (oracle port of the reference's "
                          "threaded linked-cell LJ path, FP64), %.1f s" % (steps, n, el)}
 
-    wset = n * (16 * 2 + 16 * 4 + 16 + 4) + n * info.list_capacity * 4
+    # bytes a step touches: the list entries in use (groups of four) and the
+    # per-particle state the fused step reads and writes
+    wset = n * (4 * 4 * math.ceil(info.list_mean / 4 + 0.5) + 164)
     if rank == 0:
         cfgd = workload_config(args, n)
-        cfgd["l2"] = ("value: not flushed, the inputs are larger than L2 (per-step working set "
-                      "%.0f MiB, L2 %d MiB); roofline kernel spans and flushed_steps: %d MiB "
-                      "written before every step, outside the spans" % (wset / 2 ** 20, L2_BYTES >> 20,
-                                                                     FLUSH_BYTES >> 20))
+        cfgd["l2"] = ("flushed: %d MiB written before every timed step, outside the timed spans "
+                      "(a step touches about %.0f MiB, L2 %d MiB)" % (FLUSH_BYTES >> 20, wset / 2 ** 20,
+                                                                     L2_BYTES >> 20))
         cfgd["timing"] = ("value: sep_gpu_run_timed, graphs of 64 unrolled steps (list rebuild when "
-                          "due, fused step, decision), one CUDA event pair around each graph launch, "
-                          "summed")
-        cfgd["flushed_steps"] = {
-            "value": world * n * args.steps / t_flushed, "unit": "particle-steps/s",
-            "list_rebuilds": segf["rebuilds"],
-            "what": "the same steps with L2 flushed before each and one event pair per step (the "
-                    "events' own cost is inside the spans)"}
+                          "due, fused step, decision), one CUDA event pair around each step, summed "
+                          "(the event nodes' own cost is inside the spans)")
+        cfgd["unflushed_graph_launches"] = {
+            "value": world * n * args.steps / t_whole, "unit": "particle-steps/s",
+            "list_rebuilds": segw["rebuilds"],
+            "what": "the same steps without the flush, one event pair around each launched graph of "
+                    "up to 64 steps (L2 keeps part of a step's data for the next)"}
         cfgd["graph_loop_no_flush"] = {
             "value": graph_loop_pss, "unit": "particle-steps/s", "list_rebuilds": segg["rebuilds"],
             "steps": g_steps,
