@@ -238,3 +238,57 @@ def test_butane_full_size_forces(gpu_lib, ora, tmp_path):
     eref = e + eb + ea + et
     assert abs(h.ret.epot - eref) < 1e-5 * (abs(e) + abs(eb) + abs(ea) + abs(et))
     h.close()
+
+
+def test_butane_full_size_nvt_trajectory(gpu_lib, ora, tmp_path):
+    """the molecular workload at full size (8000 butane chains, 32000 beads)
+    over 20 steps of the prgs/prg2.c loop, list rebuilds included, against
+    the same call sequence in FP64"""
+    s = cfg.butane(nmol=8000, rho=0.6, seed=3)
+    s.x = np.mod(s.x + np.random.default_rng(17).normal(0, 0.02, s.x.shape), s.L)
+    top = tmp_path / "b8000.top"
+    cfg.write_top(str(top), s)
+    h = Handle(gpu_lib, s, update=A.SEP_LLIST_NEIGHBLIST, dt=0.002)
+    lib = gpu_lib
+    lib.sep_read_topology_file(h.atoms, str(top).encode(), C.byref(h.sys), b"q")
+    mol = h.view["molindex"].copy()
+    rb = (C.c_double * 6)(*RB)
+    nsteps = 20
+    for _ in range(nsteps):
+        lib.sep_reset_retval(C.byref(h.ret))
+        lib.sep_reset_force(h.atoms, C.byref(h.sys))
+        lib.sep_force_pairs(h.atoms, b"CC", 2.5, h.fun(), C.byref(h.sys), C.byref(h.ret),
+                            A.SEP_EXCL_SAME_MOL)
+        lib.sep_stretch_harmonic(h.atoms, 0, 0.4, 33615.0, C.byref(h.sys), C.byref(h.ret))
+        lib.sep_angle_harmonic(h.atoms, 0, 1.9, 866.0, C.byref(h.sys), C.byref(h.ret))
+        lib.sep_torsion_Ryckaert(h.atoms, 0, rb, C.byref(h.sys), C.byref(h.ret))
+        lib.sep_nosehoover(h.atoms, 4.0, C.byref(h.alpha), 0.1, C.byref(h.sys))
+        lib.sep_leapfrog(h.atoms, C.byref(h.sys), C.byref(h.ret))
+    h.sync()
+    st = ora.LeapState(s.x, s.v, s.m)
+    alpha = 0.0
+    nsub = [ora.nsubbox(2.5, 0.25, s.L[k]) for k in range(3)]
+    flag, nbuild = 1, 0
+    blist = np.asarray(s.bonds)[:, 1:].reshape(-1)
+    alist = np.asarray(s.angles)[:, 1:].reshape(-1)
+    dlist = np.asarray(s.dihedrals)[:, 1:].reshape(-1)
+    for _ in range(nsteps):
+        if flag:
+            cs, cn = ora.llist(st.x, s.L, nsub, 2.5, 0.25, ora.EXCL_SAMEMOL, mol)
+            nbuild += 1
+        f, e, _ = ora.pair_forces(st.x, s.types, s.L, "CC", ora.POT_LJSHIFT, None, 2.5, cs, cn)
+        fb, eb = ora.stretch_harmonic(blist, 0, 0.4, 33615.0, st.x, s.L)[:2]
+        fa, ea = ora.angles(alist, 0, 1.9, 866.0, False, st.x, s.L)[:2]
+        ft, et = ora.torsion_rb(dlist, 0, RB, st.x, s.L)[:2]
+        f, alpha = ora.nosehoover(st.v, s.m, f + fb + fa + ft, 4.0, alpha, 0.1, 0.002)
+        flag, md, ek, kP = ora.leapfrog(st, f, s.L, 0.002, 0.25, 0.0)
+    assert nbuild >= 2  # the trajectory crosses at least one skin-triggered rebuild
+    dx = h.view["x"] - st.x
+    dx -= s.L * np.round(dx / s.L)
+    assert np.abs(dx).max() < 1e-5
+    assert rel_l2(h.view["v"], st.v) < 1e-5
+    assert abs(h.alpha.value - alpha) < 1e-5 * max(1e-3, abs(alpha))
+    eref = e + eb + ea + et
+    assert abs(h.ret.epot - eref) < 1e-5 * (abs(e) + abs(eb) + abs(ea) + abs(et))
+    assert abs(h.ret.ekin - ek) < 1e-5 * abs(ek)
+    h.close()
