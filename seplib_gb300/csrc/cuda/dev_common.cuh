@@ -118,9 +118,11 @@ struct sepdev {
 
 	// reductions
 	long long *slots;       // device, nslots * SLOT_FIELDS
-	long long *h_slots;     // pinned mirror
+	long long *h_slots;     // pinned, mapped mirror (host address)
+	long long *hd_slots;    // the same memory, device address
 	unsigned *flags;        // device status word [0] overflow, [1] max count, [2..3] scratch
-	unsigned *h_flags;      // pinned mirror
+	unsigned *h_flags;      // pinned, mapped mirror (host address)
+	unsigned *hd_flags;     // the same memory, device address
 	int nslots;
 
 	sepdev_pairset *d_ps;   // device copy of the current pair set

@@ -823,7 +823,7 @@ extern "C" int sepdev_build_list(sepdev *d, double rlist, int excl, int trigger)
 
 // The same without waiting: the list is marked unchecked.  A step kernel
 // skips its work when the build overflowed (flags[0]); the next read of
-// the flags with the step's sums (sepdev_slots_read) clears the mark, and
+// the flags with the step's sums (sepdev_slots_take) clears the mark, and
 // every other consumer confirms the list first (sepdev_list_confirm).
 extern "C" int sepdev_build_list_deferred(sepdev *d, double rlist, int excl, int trigger)
 {

@@ -64,8 +64,10 @@ extern "C" int sepdev_create(sepdev **out, long n)
 	d->nslots = 16;
 	DA(d->slots, (size_t)d->nslots * SLOT_FIELDS);
 	DA(d->flags, 4);
-	CK(cudaMallocHost((void **)&d->h_slots, sizeof(long long) * d->nslots * SLOT_FIELDS));
-	CK(cudaMallocHost((void **)&d->h_flags, sizeof(unsigned) * 4));
+	CK(cudaHostAlloc((void **)&d->h_slots, sizeof(long long) * d->nslots * SLOT_FIELDS, cudaHostAllocMapped));
+	CK(cudaHostAlloc((void **)&d->h_flags, sizeof(unsigned) * 4, cudaHostAllocMapped));
+	CK(cudaHostGetDevicePointer((void **)&d->hd_slots, d->h_slots, 0));
+	CK(cudaHostGetDevicePointer((void **)&d->hd_flags, d->h_flags, 0));
 	CK(cudaMemsetAsync(d->slots, 0, sizeof(long long) * d->nslots * SLOT_FIELDS, d->st));
 	CK(cudaMemsetAsync(d->flags, 0, sizeof(unsigned) * 4, d->st));
 	CK(cudaMemsetAsync(d->frc, 0, sizeof(float4) * n, d->st));
@@ -308,13 +310,29 @@ extern "C" int sepdev_slots_reset(sepdev *d)
 	return SEPDEV_OK;
 }
 
-extern "C" int sepdev_slots_read(sepdev *d, int nslots, double *out, unsigned *flags)
+// One block hands the accumulator slots and the status word to the host:
+// it writes them into pinned host memory mapped into the device's address
+// space (no copy engine, one launch), then clears the slots for the next
+// step, unless keep is set and the overflow bit is: a fused step that found
+// its list overflowed did nothing, and the slots filled before it (bonded
+// terms, say) stay for its second run.  A thread clears only the fields it
+// has read itself, so no barrier is needed.
+__global__ void k_slots_take(long long *slots, int nread, int nall, const unsigned *flags,
+			     long long *hslots, unsigned *hflags, int keep)
 {
-	if (nslots > d->nslots) return SEPDEV_EINVAL;
-	if (nslots > 0)
-		CK(cudaMemcpyAsync(d->h_slots, d->slots, sizeof(long long) * nslots * SLOT_FIELDS,
-				   cudaMemcpyDeviceToHost, d->st));
-	CK(cudaMemcpyAsync(d->h_flags, d->flags, sizeof(unsigned) * 4, cudaMemcpyDeviceToHost, d->st));
+	const unsigned f0 = __ldcg(flags);
+	for (int i = threadIdx.x; i < nread * SLOT_FIELDS; i += blockDim.x) hslots[i] = __ldcg(slots + i);
+	if (threadIdx.x < 4) hflags[threadIdx.x] = __ldcg(flags + threadIdx.x);
+	if (keep && (f0 & 1u)) return;
+	for (int i = threadIdx.x; i < nall * SLOT_FIELDS; i += blockDim.x) slots[i] = 0;
+}
+
+extern "C" int sepdev_slots_take(sepdev *d, int nslots, double *out, unsigned *flags, int keep_on_overflow)
+{
+	if (nslots < 0 || nslots > d->nslots) return SEPDEV_EINVAL;
+	k_slots_take<<<1, 512, 0, d->st>>>(d->slots, nslots, d->nslots, d->flags, d->hd_slots, d->hd_flags,
+					   keep_on_overflow);
+	CKL(d);
 	CK(cudaStreamSynchronize(d->st));
 	// an unchecked list that did not overflow is settled by this read
 	if (d->list_unchecked && !(d->h_flags[0] & 1u)) d->list_unchecked = 0;

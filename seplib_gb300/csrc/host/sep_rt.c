@@ -473,9 +473,10 @@ static int read_slots(rt_ctx *c, sepsys *sys, int lf_slot, int step_may_skip)
 	if (!c->dev) return 0;
 	double vals[16 * SLOT_FIELDS];
 	unsigned flags[4];
-	rt_check(sepdev_slots_read(c->dev, c->nslots, vals, flags), "slot read-back");
-	/* a deferred step on a list whose build overflowed did nothing: leave
-	 * the slots and the operations for its second run */
+	/* the read-back clears the slots, except after a deferred step on a
+	 * list whose build overflowed: that step did nothing, and the slots and
+	 * the operations stay for its second run */
+	rt_check(sepdev_slots_take(c->dev, c->nslots, vals, flags, step_may_skip), "slot read-back");
 	if (step_may_skip && (flags[0] & 1u)) return 1;
 	for (int k = 0; k < c->nops; k++) {
 		const rt_op *o = &c->ops[k];
@@ -521,7 +522,6 @@ static int read_slots(rt_ctx *c, sepsys *sys, int lf_slot, int step_may_skip)
 	}
 	c->nops = 0;
 	c->nslots = 0;
-	rt_check(sepdev_slots_reset(c->dev), "slot reset");
 	return 0;
 }
 

@@ -134,8 +134,10 @@ int sepdev_set_table(sepdev *d, int table, int nt, double r2min, double dr2,
 
 /* ---- accumulator slots ---- */
 int sepdev_slots_reset(sepdev *d);              /* zero all slots (async) */
-int sepdev_slots_read(sepdev *d, int nslots, double *out, unsigned *flags);
-	/* synchronous: out[nslots*SLOT_FIELDS] as doubles (MAXD2 decoded), flags = status word */
+/* Synchronous: out[nslots*SLOT_FIELDS] as doubles (MAXD2 decoded), flags =
+ * status word; then all slots are zeroed, except when keep_on_overflow is
+ * set and flags[0] & 1 (a deferred step that skipped its work). */
+int sepdev_slots_take(sepdev *d, int nslots, double *out, unsigned *flags, int keep_on_overflow);
 
 /* ---- neighbour list ---- */
 /* Rebuild the cell order and the full neighbour list with cut-off rlist.
@@ -143,7 +145,7 @@ int sepdev_slots_read(sepdev *d, int nslots, double *out, unsigned *flags);
 int sepdev_build_list(sepdev *d, double rlist, int excl, int trigger);
 /* The same without waiting for the capacity check: the list is marked
  * unchecked.  sepdev_step_deferred runs on it (skipping its work if the
- * build overflowed), sepdev_slots_read settles it when its flags show no
+ * build overflowed), sepdev_slots_take settles it when its flags show no
  * overflow, every other consumer confirms it first (synchronous). */
 int sepdev_build_list_deferred(sepdev *d, double rlist, int excl, int trigger);
 int sepdev_list_confirm(sepdev *d);
@@ -176,7 +178,7 @@ int sepdev_step_obs(sepdev *d, const sepdev_pairset *ps, int accumulate, double 
 		    int nh, double alpha, int pair_slot, int lf_slot, int observe);
 
 /* sepdev_step on a list that may be unchecked (sepdev_build_list_deferred);
- * if flags[0] & 1 at the following sepdev_slots_read, the step did nothing:
+ * if flags[0] & 1 at the following sepdev_slots_take, the step did nothing:
  * sepdev_step_retract, sepdev_list_confirm, and run it again. */
 int sepdev_step_deferred(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
 			 int nh, double alpha, int pair_slot, int lf_slot);
