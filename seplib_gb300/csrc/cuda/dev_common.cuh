@@ -123,6 +123,8 @@ struct sepdev {
 	unsigned *flags;        // device status word [0] overflow, [1] max count, [2..3] scratch
 	unsigned *h_flags;      // pinned, mapped mirror (host address)
 	unsigned *hd_flags;     // the same memory, device address
+	unsigned *take_arrive;  // device: arrival count of a step kernel that hands its sums over
+	int take_ready;         // slots a step kernel handed over for the next read (-1: none)
 	int nslots;
 
 	sepdev_pairset *d_ps;   // device copy of the current pair set

@@ -48,6 +48,56 @@ __device__ __forceinline__ void decide_abort(const DecideArgs &a)
 	}
 }
 
+// Hand-over of a step's sums to the host without a copy engine: the
+// accumulator slots and the status word are written into pinned host memory
+// mapped into the device's address space, then the slots are cleared for
+// the next step -- unless keep is set and the status word's overflow bit is
+// (a fused step on an overflowed list did nothing, and the slots filled
+// before it stay for its second run).  A thread clears only the fields it
+// has read itself, so no barrier is needed.
+struct TakeArgs {
+	long long *h;          // host mirror of the slots (device address); NULL: no hand-over
+	unsigned *hf;          // host mirror of the status word (device address)
+	unsigned *arrive;      // blocks of the launch that have finished
+	long long *slots;
+	const unsigned *flags;
+	int nread, nall, keep;
+};
+
+__device__ __forceinline__ void take_copy(const TakeArgs &t, int tid, int nthr)
+{
+	const unsigned f0 = __ldcg(t.flags);
+	for (int k = tid; k < t.nread * SLOT_FIELDS; k += nthr) t.h[k] = __ldcg(t.slots + k);
+	if (tid < 4) t.hf[tid] = __ldcg(t.flags + tid);
+	if (t.keep && (f0 & 1u)) return;
+	for (int k = tid; k < t.nall * SLOT_FIELDS; k += nthr) t.slots[k] = 0;
+}
+
+// At the end of a fused step kernel of the C-API path, after the block's
+// accumulator atomics (issued by thread 0): warp 0 of the last block to
+// arrive hands the sums over.  Every lane of warp 0 must reach this call.
+__device__ __forceinline__ void step_take_exit(const TakeArgs &t)
+{
+	if (!t.h || threadIdx.x >= 32) return;
+	unsigned last = 0;
+	if (threadIdx.x == 0) {
+		__threadfence();
+		last = atomicAdd(t.arrive, 1u) == gridDim.x - 1;
+	}
+	last = __shfl_sync(0xffffffffu, last, 0);
+	if (!last) return;
+	__threadfence();
+	take_copy(t, threadIdx.x, 32);
+	if (threadIdx.x == 0) *t.arrive = 0;
+}
+
+// The step skipped its work (overflowed list): no block adds to the slots,
+// so warp 0 of block 0 hands over what the slots and the status word hold.
+__device__ __forceinline__ void step_take_skip(const TakeArgs &t)
+{
+	if (t.h && blockIdx.x == 0 && threadIdx.x < 32) take_copy(t, threadIdx.x, 32);
+}
+
 // Called by the 32 lanes of one warp: lane k takes accumulator field k
 // (SLOT_FIELDS == 32) with one coalesced read; lane 0 then updates the
 // thermostat and makes the decision.

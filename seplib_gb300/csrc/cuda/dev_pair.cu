@@ -175,7 +175,10 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 	extern __shared__ sepdev_pot spot[];
 	if (FUSED) step_decide_entry(a.dec);
 	if (a.flags && (a.flags[0] & 1u)) {           // list overflow: leave the state untouched
-		if (FUSED) step_decide_skip(a.dec);
+		if (FUSED) {
+			step_decide_skip(a.dec);
+			step_take_skip(a.take);
+		}
 		return;
 	}
 	int ntypes = 1;
@@ -334,6 +337,7 @@ __global__ void __launch_bounds__(256) k_pair(long n, PairArgs a)
 		for (int k = 0; k < NM; k++) { q[NCH + 15 + k] = to_fx(0.5f * wm[k]); fld[NCH + 15 + k] = moff + k; }
 		block_to_slot_fx<NCH + 15 + NM>(q, fld, ps, d2, (int)off + SLOT_MAXD2);
 		step_decide_exit(a.dec);
+		step_take_exit(a.take);
 	}
 }
 
@@ -458,7 +462,10 @@ __global__ void __launch_bounds__(256, 4) k_lj(long n, PairArgs a)
 {
 	if (FUSED) step_decide_entry(a.dec);
 	if (a.flags && (a.flags[0] & 1u)) {
-		if (FUSED) step_decide_skip(a.dec);
+		if (FUSED) {
+			step_decide_skip(a.dec);
+			step_take_skip(a.take);
+		}
 		return;
 	}
 	constexpr int PPW = 32 / TEAM;
@@ -520,6 +527,7 @@ __global__ void __launch_bounds__(256, 4) k_lj(long n, PairArgs a)
 		kin_fields<15>(kq, off, 7, q, fld);
 		block_to_slot_fx<15>(q, fld, ps, d2, off + SLOT_MAXD2);
 		step_decide_exit(a.dec);
+		step_take_exit(a.take);
 	}
 }
 
@@ -597,6 +605,7 @@ void sepdev_fill_args(sepdev *d, PairArgs &a, const sepdev_pairset *ps, double d
 	a.flags = NULL;
 	a.skip_obs = 0;
 	memset(&a.dec, 0, sizeof a.dec);
+	memset(&a.take, 0, sizeof a.take);
 }
 
 // Batched systems: one fused step (LJ forces, Nose-Hoover friction,
@@ -871,12 +880,14 @@ extern "C" int sepdev_pair_forces(sepdev *d, const sepdev_pairset *ps, int accum
 
 // the fused step on a list that may still be unchecked: the kernel skips its
 // work (positions, velocities, forces and sums untouched) when the build
-// overflowed; the caller reads the flags with the step's sums
+// overflowed; the caller reads the flags with the step's sums.  take_n >= 0:
+// the kernel's last block also hands slots [0, take_n) and the flags to the
+// host (kept on overflow), for the sepdev_slots_take that follows.
 static int step_launch_checked(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt, int nh,
-			       double alpha, int pair_slot, int lf_slot, int observe)
+			       double alpha, int pair_slot, int lf_slot, int observe, int take_n)
 {
 	if (!d->list_valid || pair_slot < 0 || pair_slot >= d->nslots || lf_slot < 0 ||
-	    lf_slot >= d->nslots)
+	    lf_slot >= d->nslots || take_n > d->nslots)
 		return SEPDEV_EINVAL;
 	int rc;
 	if ((rc = sepdev_upload_pairset(d, ps))) return rc;
@@ -884,15 +895,26 @@ static int step_launch_checked(sepdev *d, const sepdev_pairset *ps, int accumula
 	sepdev_fill_args(d, a, ps, dt, nh, alpha, accumulate, pair_slot, lf_slot, d->cur);
 	a.skip_obs = !observe;
 	if (d->list_unchecked) a.flags = d->flags;
+	if (take_n >= 0) {
+		a.take.h = d->hd_slots;
+		a.take.hf = d->hd_flags;
+		a.take.arrive = d->take_arrive;
+		a.take.slots = d->slots;
+		a.take.flags = d->flags;
+		a.take.nread = take_n;
+		a.take.nall = d->nslots;
+		a.take.keep = 1;
+	}
 	if ((rc = sepdev_launch_pair(d, ps, a, true))) return rc;
+	d->take_ready = take_n;
 	d->cur ^= 1;
 	return SEPDEV_OK;
 }
 
 extern "C" int sepdev_step_deferred(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
-				    int nh, double alpha, int pair_slot, int lf_slot)
+				    int nh, double alpha, int pair_slot, int lf_slot, int take_n)
 {
-	return step_launch_checked(d, ps, accumulate, dt, nh, alpha, pair_slot, lf_slot, 1);
+	return step_launch_checked(d, ps, accumulate, dt, nh, alpha, pair_slot, lf_slot, 1, take_n);
 }
 
 // a deferred step that found the list overflowed did nothing: its buffer
@@ -908,7 +930,7 @@ extern "C" int sepdev_step_obs(sepdev *d, const sepdev_pairset *ps, int accumula
 	if (!d->list_valid) return SEPDEV_EINVAL;
 	int rc;
 	if ((rc = sepdev_list_confirm(d))) return rc;
-	return step_launch_checked(d, ps, accumulate, dt, nh, alpha, pair_slot, lf_slot, observe);
+	return step_launch_checked(d, ps, accumulate, dt, nh, alpha, pair_slot, lf_slot, observe, -1);
 }
 
 extern "C" int sepdev_step(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,

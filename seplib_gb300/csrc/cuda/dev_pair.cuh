@@ -53,6 +53,7 @@ struct PairArgs {
 	int pslot, lslot;
 	const unsigned *flags;
 	DecideArgs dec;            // graph loop: decision at the end of a fused step
+	TakeArgs take;             // C-API step: the sums handed to the host at its end
 	int skip_obs;              // fused step whose energy and virial nobody reads
 	// molecular virial (k_pair<..., MOLV>): molecule of each slot, centres of
 	// mass of this pass, per-atom intermolecular force (user order)

@@ -4,6 +4,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include "dev_common.cuh"
+#include "dev_decide.cuh"
 
 static char g_err[512];
 
@@ -64,12 +65,15 @@ extern "C" int sepdev_create(sepdev **out, long n)
 	d->nslots = 16;
 	DA(d->slots, (size_t)d->nslots * SLOT_FIELDS);
 	DA(d->flags, 4);
+	DA(d->take_arrive, 1);
+	d->take_ready = -1;
 	CK(cudaHostAlloc((void **)&d->h_slots, sizeof(long long) * d->nslots * SLOT_FIELDS, cudaHostAllocMapped));
 	CK(cudaHostAlloc((void **)&d->h_flags, sizeof(unsigned) * 4, cudaHostAllocMapped));
 	CK(cudaHostGetDevicePointer((void **)&d->hd_slots, d->h_slots, 0));
 	CK(cudaHostGetDevicePointer((void **)&d->hd_flags, d->h_flags, 0));
 	CK(cudaMemsetAsync(d->slots, 0, sizeof(long long) * d->nslots * SLOT_FIELDS, d->st));
 	CK(cudaMemsetAsync(d->flags, 0, sizeof(unsigned) * 4, d->st));
+	CK(cudaMemsetAsync(d->take_arrive, 0, sizeof(unsigned), d->st));
 	CK(cudaMemsetAsync(d->frc, 0, sizeof(float4) * n, d->st));
 	d->team = 1;
 	d->groups = 2;
@@ -100,7 +104,7 @@ extern "C" void sepdev_destroy(sepdev *d)
 			d->gid_b, d->inv, d->charge, d->charge_b, d->mol, d->mol_b, d->cellof,
 			d->celloff, d->cellcount, d->cellstart, d->perm, d->nl, d->ncnt, d->exb_start,
 			d->exb_idx, d->exa_start, d->exa_idx, d->bonds, d->angles, d->diheds_abcd,
-			d->dihed_type, d->inc_start, d->inc_term, d->term_out, d->slots, d->flags,
+			d->dihed_type, d->inc_start, d->inc_term, d->term_out, d->slots, d->flags, d->take_arrive,
 			d->d_ps, d->flush_buf, d->hio_scr, d->x0, d->tscr};
 	for (size_t k = 0; k < sizeof bufs / sizeof bufs[0]; k++)
 		if (bufs[k]) cudaFree(bufs[k]);
@@ -310,30 +314,38 @@ extern "C" int sepdev_slots_reset(sepdev *d)
 	return SEPDEV_OK;
 }
 
-// One block hands the accumulator slots and the status word to the host:
-// it writes them into pinned host memory mapped into the device's address
-// space (no copy engine, one launch), then clears the slots for the next
-// step, unless keep is set and the overflow bit is: a fused step that found
-// its list overflowed did nothing, and the slots filled before it (bonded
-// terms, say) stay for its second run.  A thread clears only the fields it
-// has read itself, so no barrier is needed.
-__global__ void k_slots_take(long long *slots, int nread, int nall, const unsigned *flags,
-			     long long *hslots, unsigned *hflags, int keep)
+// The read-back as a kernel of its own (one block; see take_copy).
+__global__ void k_slots_take(TakeArgs t)
 {
-	const unsigned f0 = __ldcg(flags);
-	for (int i = threadIdx.x; i < nread * SLOT_FIELDS; i += blockDim.x) hslots[i] = __ldcg(slots + i);
-	if (threadIdx.x < 4) hflags[threadIdx.x] = __ldcg(flags + threadIdx.x);
-	if (keep && (f0 & 1u)) return;
-	for (int i = threadIdx.x; i < nall * SLOT_FIELDS; i += blockDim.x) slots[i] = 0;
+	take_copy(t, threadIdx.x, blockDim.x);
 }
 
 extern "C" int sepdev_slots_take(sepdev *d, int nslots, double *out, unsigned *flags, int keep_on_overflow)
 {
 	if (nslots < 0 || nslots > d->nslots) return SEPDEV_EINVAL;
-	k_slots_take<<<1, 512, 0, d->st>>>(d->slots, nslots, d->nslots, d->flags, d->hd_slots, d->hd_flags,
-					   keep_on_overflow);
-	CKL(d);
-	CK(cudaStreamSynchronize(d->st));
+	const int ready = d->take_ready;
+	d->take_ready = -1;
+	if (ready >= 0) {
+		// the step kernel handed its slots over (and cleared them unless its
+		// list overflowed); a read of other slots would find them cleared
+		if (ready != nslots) return SEPDEV_EINVAL;
+		CK(cudaStreamSynchronize(d->st));
+		if (!keep_on_overflow && (d->h_flags[0] & 1u))
+			CK(cudaMemsetAsync(d->slots, 0, sizeof(long long) * d->nslots * SLOT_FIELDS, d->st));
+	} else {
+		TakeArgs t;
+		t.h = d->hd_slots;
+		t.hf = d->hd_flags;
+		t.arrive = NULL;
+		t.slots = d->slots;
+		t.flags = d->flags;
+		t.nread = nslots;
+		t.nall = d->nslots;
+		t.keep = keep_on_overflow;
+		k_slots_take<<<1, 512, 0, d->st>>>(t);
+		CKL(d);
+		CK(cudaStreamSynchronize(d->st));
+	}
 	// an unchecked list that did not overflow is settled by this read
 	if (d->list_unchecked && !(d->h_flags[0] & 1u)) d->list_unchecked = 0;
 	for (int s = 0; s < nslots; s++)

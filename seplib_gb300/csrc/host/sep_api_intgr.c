@@ -52,7 +52,8 @@ void sep_leapfrog(seppart *ptr, sepsys *sys, sepret *retval)
 		fr = c->friction;
 		fa = c->friction_alpha;
 		pslot = c->pass_slot;
-		rt_check(sepdev_step_deferred(c->dev, &ps, acc, sys->dt, fr, fa, pslot, lf), "fused step");
+		rt_check(sepdev_step_deferred(c->dev, &ps, acc, sys->dt, fr, fa, pslot, lf, c->nslots),
+			 "fused step");
 		c->nterms = 0;
 		c->coul_on = 0;
 		c->pass_slot = -1;
@@ -73,7 +74,8 @@ void sep_leapfrog(seppart *ptr, sepsys *sys, sepret *retval)
 			sepdev_step_retract(c->dev);
 			rt_check(sepdev_list_confirm(c->dev), "neighbour-list build");
 			rt_pass_mol_slot(c);
-			rt_check(sepdev_step_deferred(c->dev, &ps, acc, sys->dt, fr, fa, pslot, lf), "fused step");
+			rt_check(sepdev_step_deferred(c->dev, &ps, acc, sys->dt, fr, fa, pslot, lf, c->nslots),
+				 "fused step");
 		}
 	} else {
 		rt_read_slots(c, sys, lf);

@@ -179,9 +179,12 @@ int sepdev_step_obs(sepdev *d, const sepdev_pairset *ps, int accumulate, double 
 
 /* sepdev_step on a list that may be unchecked (sepdev_build_list_deferred);
  * if flags[0] & 1 at the following sepdev_slots_take, the step did nothing:
- * sepdev_step_retract, sepdev_list_confirm, and run it again. */
+ * sepdev_step_retract, sepdev_list_confirm, and run it again.  take_n >= 0:
+ * the step kernel itself hands slots [0, take_n) and the flags to the host
+ * at its end, and the next sepdev_slots_take (which must ask for take_n
+ * slots, with keep_on_overflow) only waits for it. */
 int sepdev_step_deferred(sepdev *d, const sepdev_pairset *ps, int accumulate, double dt,
-			 int nh, double alpha, int pair_slot, int lf_slot);
+			 int nh, double alpha, int pair_slot, int lf_slot, int take_n);
 void sepdev_step_retract(sepdev *d);
 
 /* f -= alpha m v on the stored forces. */
