@@ -258,7 +258,7 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 	const int cap = a.maxnb;
 	const float rl = sqrtf(a.rl2), rlm = rl * 1.0001f;
 	int cnt = 0, flushed = 0;     // entries found / entries written out (multiple of 4)
-	bool me = false, local = false, filt = false;
+	bool me = false, local = false;
 	float mx = 0.f, my = 0.f, mz = 0.f;
 	float bx0 = 0.f, bx1 = 0.f, by0 = 0.f, by1 = 0.f, bz0 = 0.f, bz1 = 0.f;
 	int4 ref = pi;
@@ -379,17 +379,19 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 		bx0 = warp_min_f(me ? mx : 3.0e38f, FULL); bx1 = warp_max_f(me ? mx : -3.0e38f, FULL);
 		by0 = warp_min_f(me ? my : 3.0e38f, FULL); by1 = warp_max_f(me ? my : -3.0e38f, FULL);
 		bz0 = warp_min_f(me ? mz : 3.0e38f, FULL); bz1 = warp_max_f(me ? mz : -3.0e38f, FULL);
-		// A wrapped region (small boxes) can still drop candidates farther
-		// than rlist from the run's bounding box, taken in the frame of the
-		// run's first particle, when no lane can meet a candidate's other
-		// image within rlist: half the box minus the run's reach from that
-		// particle exceeds rlist on every axis.  rlm carries a margin for
-		// the roundings, so the filter only removes candidates the test
-		// would reject, and the list is the same with or without it.
-		filt = WRAPFAST && !local &&
-		       0.5f * a.fs[0] * 4294967296.f - fmaxf(-bx0, bx1) > rlm &&
-		       0.5f * a.fs[1] * 4294967296.f - fmaxf(-by0, by1) > rlm &&
-		       0.5f * a.fs[2] * 4294967296.f - fmaxf(-bz0, bz1) > rlm;
+		// A wrapped region (small boxes) drops candidates whose periodic
+		// distance from the run's bounding box is rlist or more: per axis
+		// the gap between the candidate's offset and the box's interval,
+		// over the nearest image (offsets and the interval lie within half
+		// a box of the run's first particle, so |o - centre| < L and the
+		// nearer image is at L - |o - centre|).  Every member's minimum-image
+		// separation is at least that distance on each axis.  rlm carries a
+		// margin for the roundings, so the filter only removes candidates
+		// the test would reject, and the list is the same with or without it.
+		const float cxm = 0.5f * (bx0 + bx1), hxm = 0.5f * (bx1 - bx0);
+		const float cym = 0.5f * (by0 + by1), hym = 0.5f * (by1 - by0);
+		const float czm = 0.5f * (bz0 + bz1), hzm = 0.5f * (bz1 - bz0);
+		const float Lx = a.fs[0] * 4294967296.f, Ly = a.fs[1] * 4294967296.f, Lz = a.fs[2] * 4294967296.f;
 		int sA0, sA1, sB0 = 0, sB1 = 0;
 		if (xhi - xlo + 3 >= nc0) { sA0 = 0; sA1 = nc0; }
 		else {
@@ -459,16 +461,14 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 				} else {
 					q = make_float4(__int_as_float(pj.x), __int_as_float(pj.y), __int_as_float(pj.z),
 							__int_as_float(jcur));
-					if (filt) {
-						const float ox = sep_hi(pj.x, ref.x, a.fs[0]);
-						const float oy = sep_hi(pj.y, ref.y, a.fs[1]);
-						const float oz = sep_hi(pj.z, ref.z, a.fs[2]);
-						const float ex = fmaxf(fmaxf(bx0 - ox, ox - bx1), 0.f);
-						const float ey = fmaxf(fmaxf(by0 - oy, oy - by1), 0.f);
-						const float ez = fmaxf(fmaxf(bz0 - oz, oz - bz1), 0.f);
-						keep = ex < rlm && ey < rlm && ez < rlm &&
-						       fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < rlm * rlm;
-					}
+					const float dx = fabsf(sep_hi(pj.x, ref.x, a.fs[0]) - cxm);
+					const float dy = fabsf(sep_hi(pj.y, ref.y, a.fs[1]) - cym);
+					const float dz = fabsf(sep_hi(pj.z, ref.z, a.fs[2]) - czm);
+					const float ex = fmaxf(fminf(dx, Lx - dx) - hxm, 0.f);
+					const float ey = fmaxf(fminf(dy, Ly - dy) - hym, 0.f);
+					const float ez = fmaxf(fminf(dz, Lz - dz) - hzm, 0.f);
+					keep = ex < rlm && ey < rlm && ez < rlm &&
+					       fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < rlm * rlm;
 				}
 			}
 			const unsigned kb = __ballot_sync(FULL, keep);
