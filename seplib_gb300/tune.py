@@ -11,11 +11,14 @@ sep_gpu_set_tuning):
   cellf   cell edge of the list build over the list cut-off (1.0 or 1.2):
           fewer, larger cells give longer candidate runs and more tests.
 
-Classes: systems of n <= 1024, n <= 8192 and larger.  The two small classes
-are timed as batches (sepb_run_timed) of independent systems of their sizes,
-drawn as the replica-sweep workload draws them; the large class as one
-256000-particle fcc system (sep_gpu_run_timed, every step observed).  Every
-trial flushes the L2 before each step.  The chosen table is applied to
+Classes: systems of n <= 1024, n <= 8192, n <= 65536 and larger.  The two
+small classes are timed as batches (sepb_run_timed) of independent systems
+of their sizes, drawn as the replica-sweep workload draws them; the larger
+ones each as one fcc system of their size (sep_gpu_run_timed, every step
+observed): 32000 particles (fcc 20^3, the scale of the 32000-bead butane
+workload, whose single system leaves most of the GPU's warps empty at one
+lane per particle) and 256000 (fcc 40^3).  Every trial flushes the L2
+before each step.  The chosen table is applied to
 the library and cached as JSON (next to the built library, keyed by the GPU
 and the library file), so later processes load it instead of re-timing.
 """
@@ -27,7 +30,8 @@ import time
 from . import LIB_PATH, NCLASS, GpuTiming, Tuning, configs, sepapi as A
 from .batch import Batch
 
-CLASSES = (1024, 8192)
+CLASSES = (1024, 8192, 65536)
+BATCH_MAX = 8192        # classes up to this size are timed as batches
 TEAMS = (1, 2)
 GROUPS = (1, 2)
 CELLF = (1.0, 1.2)
@@ -93,13 +97,26 @@ def _single_trial(lib, s, steps, warm):
     return tm.ms_steps / steps
 
 
+def mid_ncell(lo, hi):
+    """fcc cells per edge of a bounded class's single-system trial: 4 ncell^3
+    particles at or just below the middle of the class (and inside it)"""
+    k = int((0.5 * (lo + hi) / 4.0) ** (1.0 / 3.0))
+    while 4 * k ** 3 < lo:
+        k += 1
+    return k
+
+
 def workloads(classes=CLASSES, nsys=64, ncell=40, seed=11):
-    """the trial workload of each class: (kind, payload)"""
+    """the trial workload of each class: (kind, payload); ncell sizes the
+    last (unbounded) class's fcc system"""
     out = []
     lo = 108
     for hi in classes:
-        systems, _, temps = configs.replica_sweep(nsys=nsys, seed=seed, nmin=lo, nmax=hi)
-        out.append(("batch", (systems, temps)))
+        if hi <= BATCH_MAX:
+            systems, _, temps = configs.replica_sweep(nsys=nsys, seed=seed, nmin=lo, nmax=hi)
+            out.append(("batch", (systems, temps)))
+        else:
+            out.append(("single", configs.plain_lj_large(mid_ncell(lo, hi), seed=2)))
         lo = hi + 1
     out.append(("single", configs.plain_lj_large(ncell, seed=2)))
     return out

@@ -104,7 +104,7 @@ def test_tuner_choice_batch_equals_single(table):
     """the tuner (short trials) picks a table; batched systems of every class
     still reproduce the single-system runs bit for bit"""
     lib = table
-    rec = tune.tune(lib, steps=6, warm=2, nsys=8, ncell=16, repeats=1)
+    rec = tune.tune(lib, steps=6, warm=2, nsys=8, ncell=26, repeats=1)
     assert len(rec["chosen"]) == len(tune.CLASSES) + 1
     assert all(tuple(c) in tune.candidates() for c in rec["chosen"])
     cur = tune.current(lib)
@@ -112,13 +112,15 @@ def test_tuner_choice_batch_equals_single(table):
     print("tuned:", rec["chosen"], "%.1f s" % rec["seconds"])
     systems, _, temps = cfg.replica_sweep(nsys=5, seed=12, nmin=400, nmax=2500)
     _batch_equals_single(lib, systems, temps, 33)
-    # the large class on the single-system path: within the FP64 bars
+    # a single system of a class above the batched ones takes that class's
+    # parameters
     big = liquid(ncell=13, seed=6)
-    assert big.n > tune.CLASSES[-1]
+    k = sum(big.n > hi for hi in tune.CLASSES)
+    assert tune.CLASSES[k - 1] < big.n <= tune.CLASSES[k]
     h = Handle(lib, big, skin=SKIN)
     h.forces()
     h.sync()
     info = GpuInfo()
     assert lib.sep_gpu_info_get(h.atoms, C.byref(info)) == 0
-    assert [info.team, info.groups, info.cellf] == list(rec["chosen"][-1])
+    assert [info.team, info.groups, info.cellf] == list(rec["chosen"][k])
     h.close()

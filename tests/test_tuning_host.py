@@ -56,6 +56,10 @@ def test_driver_words():
     assert words == ["3", "1024", "1", "2", "1.0", "8192", "2", "1", "1.2", "0", "2", "2", "1.0"]
 
 
+CHOSEN = [(2, 2, 1.0), (1, 2, 1.2), (2, 1, 1.0), (1, 1, 1.0), (2, 2, 1.2), (1, 1, 1.2), (2, 1, 1.2),
+          (1, 2, 1.0)]
+
+
 def test_cache_roundtrip(saved, tmp_path, monkeypatch):
     """load_or_tune times once, writes the table next to the library (here a
     temporary path) and later calls load it for the same GPU and build."""
@@ -63,7 +67,7 @@ def test_cache_roundtrip(saved, tmp_path, monkeypatch):
 
     def fake_tune(lib, **kw):
         calls.append(kw)
-        chosen = [(2, 2, 1.0), (1, 2, 1.2), (1, 1, 1.0)]
+        chosen = CHOSEN[:len(tune.CLASSES) + 1]
         tune.apply(lib, list(tune.CLASSES), chosen)
         return dict(classes=list(tune.CLASSES), chosen=[list(c) for c in chosen], trials=[], seconds=0.0)
 
@@ -75,7 +79,7 @@ def test_cache_roundtrip(saved, tmp_path, monkeypatch):
     rec2 = tune.load_or_tune(saved, path=path)
     assert rec2["source"] == "cache" and len(calls) == 1
     cur = tune.current(saved)
-    assert [(c["team"], c["groups"], c["cellf"]) for c in cur] == [(2, 2, 1.0), (1, 2, 1.2), (1, 1, 1.0)]
+    assert [(c["team"], c["groups"], c["cellf"]) for c in cur] == CHOSEN[:len(tune.CLASSES) + 1]
     # a different build (key) is timed again
     import json
     with open(path) as fh:
