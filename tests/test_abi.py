@@ -14,8 +14,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 INC = os.path.join(ROOT, "include")
 LIBDIR = os.path.join(ROOT, "seplib_gb300", "lib")
-REF_PRGS = "/root/reference/prgs"
-REF_INC = "/root/reference/include"
+# the reference's sources: the location the oracle's Makefile reads them
+# from (REF), overridable through SEPLIB_REFERENCE, as for the oracle build
+REF = os.environ.get("SEPLIB_REFERENCE") or next(
+    (ln.split("?=", 1)[1].strip() for ln in open(os.path.join(ROOT, "oracle", "Makefile"))
+     if ln.startswith("REF ?=")), "")
+REF_PRGS = os.path.join(REF, "prgs")
+REF_INC = os.path.join(REF, "include")
 
 
 def declared_functions():
