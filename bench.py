@@ -118,7 +118,14 @@ def allmax(world, x):
 
 
 def workload_config(args, n):
+    """The workload and its timing conditions: the same object on the GPU arm's
+    line and on the reference arm's, so the two describe one comparison (what
+    each arm measured beyond it goes to its own keys)."""
     nbar = 4.0 / 3.0 * math.pi * (RC + SKIN) ** 3 * RHO
+    # bytes a step touches: the list entries in use (groups of four, the
+    # last one padded) and the per-particle state the fused step reads and
+    # writes
+    wset = n * (4 * 4 * math.ceil(nbar / 4 + 0.5) + 164)
     return {
         "workload": "plain LJ NVT fcc %d^3 cells, N=%d, rho*=%.4f, T*=%.1f, Nose-Hoover T0=%.1f Q=%.0f, "
                     "shifted LJ rc=%.1f, skin %.1f, dt=%.3f" % (args.ncell, n, RHO, TEMP, T0, TAU, RC, SKIN, DT),
@@ -126,6 +133,9 @@ def workload_config(args, n):
         "nbar_full_list": round(nbar, 2),
         "algorithmic_bytes_per_particle_step": round(4 * nbar + 128, 1),
         "parallelism": "replicas (one independent system per GPU)",
+        "l2": ("GPU arm: %d MiB written before every timed step, outside the timed spans (a step "
+               "touches about %.0f MiB, L2 %d MiB); the reference arm runs on the host cores"
+               % (FLUSH_BYTES >> 20, wset / 2 ** 20, L2_BYTES >> 20)),
     }
 
 
@@ -600,45 +610,40 @@ def main():
                "sample": "%d MD steps of the full N=%d system (oracle port of the reference's "
                          "threaded linked-cell LJ path, FP64), %.1f s" % (steps, n, el)}
 
-    # bytes a step touches: the list entries in use (groups of four) and the
-    # per-particle state the fused step reads and writes
-    wset = n * (4 * 4 * math.ceil(info.list_mean / 4 + 0.5) + 164)
     if rank == 0:
         cfgd = workload_config(args, n)
-        cfgd["l2"] = ("flushed: %d MiB written before every timed step, outside the timed spans "
-                      "(a step touches about %.0f MiB, L2 %d MiB)" % (FLUSH_BYTES >> 20, wset / 2 ** 20,
-                                                                     L2_BYTES >> 20))
-        cfgd["timing"] = ("value: sep_gpu_run_timed, graphs of 64 unrolled steps (list rebuild when "
-                          "due, fused step, decision), one CUDA event pair around each step, summed "
-                          "(the event nodes' own cost is inside the spans)")
-        cfgd["unflushed_graph_launches"] = {
+        det = {}
+        det["timing"] = ("value: sep_gpu_run_timed, graphs of 64 unrolled steps (list rebuild when "
+                         "due, fused step, decision), one CUDA event pair around each step, summed "
+                         "(the event nodes' own cost is inside the spans)")
+        det["unflushed_graph_launches"] = {
             "value": world * n * args.steps / t_whole, "unit": "particle-steps/s",
             "list_rebuilds": segw["rebuilds"],
             "what": "the same steps without the flush, one event pair around each launched graph of "
                     "up to 64 steps (L2 keeps part of a step's data for the next)"}
-        cfgd["graph_loop_no_flush"] = {
+        det["graph_loop_no_flush"] = {
             "value": graph_loop_pss, "unit": "particle-steps/s", "list_rebuilds": segg["rebuilds"],
             "steps": g_steps,
             "what": "sep_gpu_run, one CUDA graph with a WHILE node, L2 not flushed (production loop; "
                     "energy and virial summed on the last step only, as sep_gpu_run returns)"}
-        cfgd["observed"] = ("value and roofline: every timed step sums its energy and virial, as a "
-                            "loop of sep_force_pairs / sep_leapfrog calls does")
-        cfgd["kernel_params"] = {"team": info.team, "groups": info.groups, "cellf": info.cellf}
-        cfgd["tuning"] = {"what": "kernel parameters by system size (n <= classes[k]; the last "
-                                  "entry: larger), each [team, groups, cellf], from the autotuner "
-                                  "(seplib_gb300/tune.py)",
-                          "classes": tuning["classes"], "chosen": tuning["chosen"],
-                          "source": tuning["source"], "tune_seconds": tuning.get("seconds")}
-        cfgd["list_mean_full"] = round(info.list_mean, 2)
-        cfgd["list_rebuilds_in_timed_steps"] = rebuilds
-        cfgd["final_state"] = {"epot_per_particle": epot_pp, "temperature": temp}
+        det["observed"] = ("value and roofline: every timed step sums its energy and virial, as a "
+                           "loop of sep_force_pairs / sep_leapfrog calls does")
+        det["kernel_params"] = {"team": info.team, "groups": info.groups, "cellf": info.cellf}
+        det["tuning"] = {"what": "kernel parameters by system size (n <= classes[k]; the last "
+                                 "entry: larger), each [team, groups, cellf], from the autotuner "
+                                 "(seplib_gb300/tune.py)",
+                         "classes": tuning["classes"], "chosen": tuning["chosen"],
+                         "source": tuning["source"], "tune_seconds": tuning.get("seconds")}
+        det["list_mean_full"] = round(info.list_mean, 2)
+        det["list_rebuilds_in_timed_steps"] = rebuilds
+        det["final_state"] = {"epot_per_particle": epot_pp, "temperature": temp}
         line = {
             "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 pair / fixed-point x / f64-exact sums",
             "data": "synthetic (seeded fcc lattice, Maxwell-Boltzmann velocities)",
-            "config": cfgd,
+            "config": cfgd, "details": det,
             "e2e": {"value": e2e_val, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e_steps, "list_rebuilds": e2e_run["rebuilds"],
                     "first_step_ms": 1e3 * e2e_run["first_step_s"],
