@@ -236,21 +236,45 @@ __device__ __forceinline__ float warp_max_f(float v, unsigned mask)
 // loop that tests them from shared memory.
 // PERM: the particles are not in cell order; a cell's members are the
 // slots perm[cellstart[c] .. cellstart[c + 1]) (the adjoint's fixed slots).
-template <bool WRAPFAST, bool MOLX = false, bool PERM = false>
+// TB = 2: two lanes per particle, a tile of 16 particles per warp (twice
+// the warps, for systems too small to fill the GPU).  Lane p (p < 16) and
+// lane p + 16 hold particle i0 + p and split every staged chunk: lane p
+// tests its first half, lane p + 16 the second half into spare rows of its
+// own column, and lane p then appends those hits after its own.  A
+// particle's list is therefore the same, entry for entry, as with one lane.
+template <bool WRAPFAST, bool MOLX = false, bool PERM = false, int TB = 1>
 __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, float4 *sp, int *ring,
 					   int *spm = nullptr)
 {
+	static_assert(TB == 1 || TB == 2, "one or two lanes per particle");
 	const unsigned FULL = 0xffffffffu;
 	const int lane = threadIdx.x & 31;
+	const int hh = TB == 2 ? lane >> 4 : 0;          // which half of the particle's lane pair
 	if (i0 >= n) return;
-	const long i = i0 + lane;
+	const long i = i0 + (TB == 2 ? (lane & 15) : lane);
 	const bool act = i < n;
+	const bool own = act && hh == 0;                   // the lane that writes the particle's list
 	const int4 pi = a.pos[act ? i : i0];
 	const int nc0 = a.nc[0], nc1 = a.nc[1], nc2 = a.nc[2];
 	const int cx = (int)__umulhi((unsigned)pi.x, (unsigned)nc0);
 	const int cy = (int)__umulhi((unsigned)pi.y, (unsigned)nc1);
 	const int cz = (int)__umulhi((unsigned)pi.z, (unsigned)nc2);
 	const int row = cy + nc1 * cz;
+	// TB = 2: lane l also holds particle l of the parent tile (the 32
+	// particles one lane per particle would take), whose run in a row fixes
+	// the staged segments, their order, the frame of the offsets and the
+	// in-box test exactly as with one lane per particle
+	int4 ppi = pi;
+	int pcx = cx, prow = row;
+	bool pact = act;
+	if (TB == 2) {
+		const long P = (i0 & ~31L) + lane;
+		pact = P < n;
+		ppi = a.pos[pact ? P : i0];
+		pcx = (int)__umulhi((unsigned)ppi.x, (unsigned)nc0);
+		prow = (int)__umulhi((unsigned)ppi.y, (unsigned)nc1) +
+		       nc1 * (int)__umulhi((unsigned)ppi.z, (unsigned)nc2);
+	}
 	int4 *gbase = (int4 *)(a.nl + nl_index(i, 0, a.maxnb));   // this lane's group 0
 	const int gi = act ? a.gid[i] : -1, mi = act ? a.mol[i] : -1;
 	const int lo1 = nc1 >= 3 ? -1 : 0, hi1 = nc1 >= 2 ? 1 : 0;
@@ -270,10 +294,10 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 	auto flush = [&]() {
 		const int top = cnt < cap ? cnt : cap;
 		const int g0 = flushed >> 2, g1 = (top + 3) >> 2;
-		const int gmin = __reduce_min_sync(FULL, act ? g0 : 0x7fffffff);
-		const int gmax = __reduce_max_sync(FULL, act ? g1 : 0);
+		const int gmin = __reduce_min_sync(FULL, own ? g0 : 0x7fffffff);
+		const int gmax = __reduce_max_sync(FULL, own ? g1 : 0);
 		for (int g = gmin; g < gmax; g++) {
-			if (act && g >= g0 && g < g1) {
+			if (own && g >= g0 && g < g1) {
 				const int r = (4 * g) & (BT_RING - 1), b0 = 4 * g;
 				// a group past the count is padded with the particle itself
 				// (separation zero), so readers take whole groups of four
@@ -293,47 +317,57 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 	auto test = [&](int fill) {
 		__syncwarp();
 		// entries not yet written out must stay in the ring through this chunk
-		const int span = __reduce_max_sync(FULL, act ? cnt - flushed : 0);
+		const int span = __reduce_max_sync(FULL, own ? cnt - flushed : 0);
 		if (span + fill > BT_RING) flush();
+		// this lane's share of the chunk, and where its hits go: after the
+		// particle's entries, or (second lane of a pair) from row 0 of its
+		// own column, which holds no particle's entries
+		int c0 = 0, c1 = fill, w = cnt;
+		if (TB == 2) {
+			const int half = (fill + 1) >> 1;
+			c0 = hh ? half : 0;
+			c1 = hh ? fill : half;
+			w = hh ? 0 : cnt;
+		}
 		if (me) {
 			if (MOLX && local) {
 #pragma unroll 4
-				for (int c = 0; c < fill; c++) {
+				for (int c = c0; c < c1; c++) {
 					const float4 q = sp[c];
 					const float dx = mx - q.x, dy = my - q.y, dz = mz - q.z;
 					const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 					const int j = __float_as_int(q.w);
 					const bool hit = inlist(r2) & !((mi != -1) & (mi == spm[c]));
-					ring[(cnt & (BT_RING - 1)) * 32 + lane] = j;
-					cnt += hit ? 1 : 0;
+					ring[(w & (BT_RING - 1)) * 32 + lane] = j;
+					w += hit ? 1 : 0;
 				}
 			} else if (local && a.excl == SEPDEV_EXCL_NONE) {
 #pragma unroll 4
-				for (int c = 0; c < fill; c++) {
+				for (int c = c0; c < c1; c++) {
 					const float4 q = sp[c];
 					const float dx = mx - q.x, dy = my - q.y, dz = mz - q.z;
 					const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 					const int j = __float_as_int(q.w);
 					const bool hit = inlist(r2);
-					ring[(cnt & (BT_RING - 1)) * 32 + lane] = j;
-					cnt += hit ? 1 : 0;
+					ring[(w & (BT_RING - 1)) * 32 + lane] = j;
+					w += hit ? 1 : 0;
 				}
 			} else if (WRAPFAST && a.excl == SEPDEV_EXCL_NONE) {
 				// minimum-image separations per candidate, appended in
 				// candidate order without branches (as the local form)
 #pragma unroll 4
-				for (int c = 0; c < fill; c++) {
+				for (int c = c0; c < c1; c++) {
 					const float4 q = sp[c];
 					const float dx = sep_hi(pi.x, __float_as_int(q.x), a.fs[0]);
 					const float dy = sep_hi(pi.y, __float_as_int(q.y), a.fs[1]);
 					const float dz = sep_hi(pi.z, __float_as_int(q.z), a.fs[2]);
 					const int j = __float_as_int(q.w);
 					const bool hit = inlist(dx * dx + dy * dy + dz * dz);
-					ring[(cnt & (BT_RING - 1)) * 32 + lane] = j;
-					cnt += hit ? 1 : 0;
+					ring[(w & (BT_RING - 1)) * 32 + lane] = j;
+					w += hit ? 1 : 0;
 				}
 			} else {
-				for (int c = 0; c < fill; c++) {
+				for (int c = c0; c < c1; c++) {
 					const float4 q = sp[c];
 					const int j = __float_as_int(q.w);
 					float dx, dy, dz;
@@ -345,10 +379,19 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 					}
 					if (!(dx * dx + dy * dy + dz * dz < a.rl2) || j == (int)i) continue;
 					if (a.excl != SEPDEV_EXCL_NONE && excluded(j)) continue;
-					ring[(cnt & (BT_RING - 1)) * 32 + lane] = j;
-					cnt++;
+					ring[(w & (BT_RING - 1)) * 32 + lane] = j;
+					w++;
 				}
 			}
+		}
+		if (TB == 1 || hh == 0) cnt = w;
+		if (TB == 2) {
+			// the second lane's hits follow the first lane's, in chunk order
+			__syncwarp();
+			const int m = __shfl_down_sync(FULL, me && hh ? w : 0, 16);
+			if (me && hh == 0)
+				for (int k = 0; k < m; k++, cnt++)
+					ring[(cnt & (BT_RING - 1)) * 32 + lane] = ring[k * 32 + lane + 16];
 		}
 		__syncwarp();
 	};
@@ -361,17 +404,20 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 		me = (mine >> lane) & 1u;
 		// the run's cells along x: in cell order its first and last lanes;
 		// over index-only cell lists the lanes are in no order (min, max)
+		const unsigned pm = TB == 2 ? __ballot_sync(FULL, pact && prow == rrow) : mine;
 		const int xlo = PERM ? (int)__reduce_min_sync(FULL, me ? (unsigned)cx : 0xffffffffu)
-				     : __shfl_sync(FULL, cx, __ffs(mine) - 1);
+				     : __shfl_sync(FULL, pcx, __ffs(pm) - 1);
 		const int xhi = PERM ? (int)__reduce_max_sync(FULL, me ? (unsigned)cx : 0u)
-				     : __shfl_sync(FULL, cx, 31 - __clz(mine));
+				     : __shfl_sync(FULL, pcx, 31 - __clz(pm));
 		const int ry = rrow % nc1, rz = rrow / nc1;
 		// the staged region spans (xhi - xlo + 3) x 3 x 3 cells; when that is
 		// under half the box on every axis, separations need no wrapping
 		local = 2 * (xhi - xlo + 3) < nc0 && 6 < nc1 && 6 < nc2;
-		ref.x = __shfl_sync(FULL, pi.x, leader);
-		ref.y = __shfl_sync(FULL, pi.y, leader);
-		ref.z = __shfl_sync(FULL, pi.z, leader);
+		// the frame: the run's first particle
+		const int rl0 = TB == 2 ? __ffs(pm) - 1 : leader;
+		ref.x = __shfl_sync(FULL, ppi.x, rl0);
+		ref.y = __shfl_sync(FULL, ppi.y, rl0);
+		ref.z = __shfl_sync(FULL, ppi.z, rl0);
 		mx = sep_hi(pi.x, ref.x, a.fs[0]);
 		my = sep_hi(pi.y, ref.y, a.fs[1]);
 		mz = sep_hi(pi.z, ref.z, a.fs[2]);
@@ -483,31 +529,35 @@ __device__ __forceinline__ void build_tile(long n, const BuildArgs &a, long i0, 
 	}
 	__syncwarp();
 	flush();
-	if (act) {
+	if (own) {
 		a.ncnt[i] = cnt < cap ? cnt : cap;
 		if (cnt > cap) atomicOr(&a.flags[0], 1u);
 	}
-	const unsigned mxc = __reduce_max_sync(FULL, act ? (unsigned)cnt : 0u);
+	const unsigned mxc = __reduce_max_sync(FULL, own ? (unsigned)cnt : 0u);
 	if (lane == 0) atomicMax(&a.flags[1], mxc);
 }
 
+template <int TB>
 __global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles(long n, BuildArgs a)
 {
 	__shared__ float4 sp_all[BT_WARPS][BT_CAP];
 	__shared__ int ring_all[BT_WARPS][BT_RING * 32];
 	const int w = threadIdx.x >> 5;
-	build_tile<false>(n, a, ((long)blockIdx.x * BT_WARPS + w) * 32, sp_all[w], ring_all[w]);
+	build_tile<false, false, false, TB>(n, a, ((long)blockIdx.x * BT_WARPS + w) * (32 / TB), sp_all[w],
+					    ring_all[w]);
 }
 
 // Same-molecule exclusions (the butane-type workloads): molecule indices
 // staged with the candidates.
+template <int TB>
 __global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles_mol(long n, BuildArgs a)
 {
 	__shared__ float4 sp_all[BT_WARPS][BT_CAP];
 	__shared__ int spm_all[BT_WARPS][BT_CAP];
 	__shared__ int ring_all[BT_WARPS][BT_RING * 32];
 	const int w = threadIdx.x >> 5;
-	build_tile<false, true>(n, a, ((long)blockIdx.x * BT_WARPS + w) * 32, sp_all[w], ring_all[w], spm_all[w]);
+	build_tile<false, true, false, TB>(n, a, ((long)blockIdx.x * BT_WARPS + w) * (32 / TB), sp_all[w],
+					   ring_all[w], spm_all[w]);
 }
 
 // Batched systems: each warp builds its tile with its own system's cell grid
@@ -611,13 +661,19 @@ static int grow(sepdev *d, void **p, size_t bytes, size_t *cap)
 	return SEPDEV_OK;
 }
 
+// the system's team size (lanes per particle) also sets the build's lanes
+// per particle; the lists are the same either way
 static int launch_build(sepdev *d, const BuildArgs &a)
 {
-	const int grid = grid_for((d->n + 31) / 32, BT_WARPS);
-	if (a.excl == SEPDEV_EXCL_SAMEMOL)
-		k_build_tiles_mol<<<grid, BT_WARPS * 32, 0, d->st>>>(d->n, a);
-	else
-		k_build_tiles<<<grid, BT_WARPS * 32, 0, d->st>>>(d->n, a);
+	const int tb = d->team == 2 ? 2 : 1, per = 32 / tb;
+	const int grid = grid_for((d->n + per - 1) / per, BT_WARPS);
+	if (a.excl == SEPDEV_EXCL_SAMEMOL) {
+		if (tb == 2) k_build_tiles_mol<2><<<grid, BT_WARPS * 32, 0, d->st>>>(d->n, a);
+		else k_build_tiles_mol<1><<<grid, BT_WARPS * 32, 0, d->st>>>(d->n, a);
+	} else {
+		if (tb == 2) k_build_tiles<2><<<grid, BT_WARPS * 32, 0, d->st>>>(d->n, a);
+		else k_build_tiles<1><<<grid, BT_WARPS * 32, 0, d->st>>>(d->n, a);
+	}
 	CKL(d);
 	return SEPDEV_OK;
 }
