@@ -35,6 +35,24 @@ int sepdev_grow_list_to(sepdev *d, int maxnb);
 
 // ---- the rebuild of flagged systems ----------------------------------------
 
+// one block per system: a flagged system appends its 32-slot warps to the
+// list of warps the batched list build steps through (a fixed grid, so the
+// build of a few systems runs as a few well-filled waves instead of a warp
+// per slot group of every system, most leaving at once).  A warp's list
+// depends on nothing but the warp, so the order of the list changes no
+// result.
+__global__ void kb_compact(const BatchSys *sys, const unsigned *flag, int *fw, int *cnt)
+{
+	const int s = blockIdx.x;
+	if (!flag[s]) return;                          // uniform over the block
+	const BatchSys S = sys[s];
+	const int nw = S.npad / 32;
+	__shared__ int base;
+	if (threadIdx.x == 0) base = atomicAdd(cnt, nw);
+	__syncthreads();
+	for (int k = threadIdx.x; k < nw; k += blockDim.x) fw[base + k] = S.off / 32 + k;
+}
+
 __global__ void kb_bin(const BatchSys *sys, const int *wsys, int nwarps, const unsigned *flag,
 		       const int4 *pos, int *cellof, int *celloff, int *count)
 {
@@ -304,7 +322,7 @@ extern "C" void sepb_destroy(sepb *b)
 	if (b->exec) cudaGraphExecDestroy(b->exec);
 	if (b->graph) cudaGraphDestroy(b->graph);
 	void *dv[] = {b->sys, b->wsys, b->csys, b->flag, b->cellcount, b->cellstart, b->slots, b->bs, b->run,
-		      b->flush_buf, b->wstep};
+		      b->flush_buf, b->wstep, b->fw, b->fcnt};
 	for (size_t k = 0; k < sizeof dv / sizeof dv[0]; k++)
 		if (dv[k]) cudaFree(dv[k]);
 	if (b->h_bs) cudaFreeHost(b->h_bs);
@@ -398,6 +416,8 @@ static sepb *batch_make(int nsys, const int *npart, const double *L, double rc, 
 	BCK(cudaMemcpy(b->wstep, hstep.data(), sizeof(int4) * b->nstepw, cudaMemcpyHostToDevice));
 	BCK(cudaMalloc((void **)&b->csys, sizeof(int) * b->ncells));
 	BCK(cudaMalloc((void **)&b->flag, sizeof(unsigned) * nsys));
+	BCK(cudaMalloc((void **)&b->fw, sizeof(int) * b->nwarps));
+	BCK(cudaMalloc((void **)&b->fcnt, sizeof(int)));
 	BCK(cudaMalloc((void **)&b->cellcount, sizeof(int) * b->ncells));
 	BCK(cudaMalloc((void **)&b->cellstart, sizeof(int) * b->ncells));
 	BCK(cudaMalloc((void **)&b->slots, sizeof(long long) * SLOT_FIELDS * nsys));
@@ -676,10 +696,12 @@ int batch_rebuild_launch(sepb *b, int parity)
 	BGather g = gather_args(b, parity);
 	kb_gather<<<grid_for(nt, B), B, 0, d->st>>>(g);
 	kb_copyback<<<grid_for(nt, B), B, 0, d->st>>>(g);
+	CK(cudaMemsetAsync(b->fcnt, 0, sizeof(int), d->st));
+	kb_compact<<<b->nsys, 128, 0, d->st>>>(b->sys, b->flag, b->fw, b->fcnt);
 	CKL(d);
 	CK(cudaMemsetAsync(d->flags, 0, sizeof(unsigned) * 2, d->st));
 	return sepdev_batch_build(d, parity, b->cellstart, b->sys, b->wsys, b->nwarps, b->flag,
-				  (float)((b->rc + b->skin) * (b->rc + b->skin)), NULL);
+				  (float)((b->rc + b->skin) * (b->rc + b->skin)), NULL, b->fw, b->fcnt);
 }
 
 int batch_step_launch(sepb *b, int parity, const BatchDecide &dec)

@@ -70,9 +70,12 @@ struct BatchDecide {
 int sepdev_batch_step(sepdev *d, const PairArgs &a, const BatchSys *sys, const int4 *wstep, int nwarps,
 		      const BatchState *bs, const BatchRun *run, long long *slots, const BatchDecide &dec,
 		      int typed);
-// perm != NULL: the cell lists hold slot indices (particles not moved)
+// perm != NULL: the cell lists hold slot indices (particles not moved);
+// fw != NULL: the flagged systems' warps (fcnt of them) to build, else every
+// warp of a flagged system
 int sepdev_batch_build(sepdev *d, int parity, const int *cellstart, const BatchSys *sys,
-		       const int *wsys, int nwarps, const unsigned *flag, float rl2, const int *perm);
+		       const int *wsys, int nwarps, const unsigned *flag, float rl2, const int *perm,
+		       const int *fw = nullptr, const int *fcnt = nullptr);
 
 // host-side batch (dev_batch.cu); the adjoint (dev_adj.cu) builds on it
 struct sepb {
@@ -95,6 +98,7 @@ struct sepb {
 	int4 *wstep;               // per warp of the step kernel: system, first slot, team, groups
 	int nstepw;
 	unsigned *flag;
+	int *fw, *fcnt;            // warps of the flagged systems (kb_compact), for the list build, and their count
 	int *cellcount, *cellstart;
 	long long *slots;
 	BatchState *bs;            // device

@@ -562,22 +562,31 @@ __global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles_mol(long n, Build
 
 // Batched systems: each warp builds its tile with its own system's cell grid
 // and box, and only for systems whose rebuild flag is set.
+// fw (with its count fcnt) lists the flagged systems' warps: a fixed grid
+// steps through it; without it, a warp per 32 slots of every system, the
+// unflagged ones leaving at once
 __global__ void __launch_bounds__(BT_WARPS * 32) k_build_tiles_batch(BuildArgs a, const BatchSys *sys,
 								    const int *wsys, int nwarps,
-								    const unsigned *flag)
+								    const unsigned *flag, const int *fw,
+								    const int *fcnt)
 {
 	__shared__ float4 sp_all[BT_WARPS][BT_CAP];
 	__shared__ int ring_all[BT_WARPS][BT_RING * 32];
 	const int w = threadIdx.x >> 5;
-	const long wg = (long)blockIdx.x * BT_WARPS + w;
-	if (wg >= nwarps) return;
-	const int s = wsys[wg];
-	if (!flag[s]) return;
-	const BatchSys S = sys[s];
-	BuildArgs b = a;
-	b.cellstart = a.cellstart + S.coff;
-	for (int k = 0; k < 3; k++) { b.nc[k] = S.nc[k]; b.fs[k] = S.fs; }
-	build_tile<true>(S.off + S.n, b, wg * 32, sp_all[w], ring_all[w]);
+	auto tile = [&](long wg) {
+		const BatchSys S = sys[wsys[wg]];
+		BuildArgs b = a;
+		b.cellstart = a.cellstart + S.coff;
+		for (int k = 0; k < 3; k++) { b.nc[k] = S.nc[k]; b.fs[k] = S.fs; }
+		build_tile<true>(S.off + S.n, b, wg * 32, sp_all[w], ring_all[w]);
+	};
+	if (fw) {
+		for (long k = (long)blockIdx.x * BT_WARPS + w; k < *fcnt; k += (long)gridDim.x * BT_WARPS) tile(fw[k]);
+	} else {
+		const long wg = (long)blockIdx.x * BT_WARPS + w;
+		if (wg >= nwarps || !flag[wsys[wg]]) return;
+		tile(wg);
+	}
 }
 
 // The same over index-only cell lists (particles not moved: the adjoint).
@@ -792,7 +801,8 @@ int sepdev_build_args(sepdev *d, BuildArgs *a, int parity)
 }
 
 int sepdev_batch_build(sepdev *d, int parity, const int *cellstart, const BatchSys *sys,
-		       const int *wsys, int nwarps, const unsigned *flag, float rl2, const int *perm)
+		       const int *wsys, int nwarps, const unsigned *flag, float rl2, const int *perm,
+		       const int *fw, const int *fcnt)
 {
 	BuildArgs a;
 	memset(&a, 0, sizeof a);
@@ -810,8 +820,11 @@ int sepdev_batch_build(sepdev *d, int parity, const int *cellstart, const BatchS
 	if (perm)
 		k_build_tiles_batch_perm<<<grid_for(nwarps, BT_WARPS), BT_WARPS * 32, 0, d->st>>>(a, sys, wsys, nwarps,
 												   flag);
+	else if (fw)
+		k_build_tiles_batch<<<6 * d->nsm, BT_WARPS * 32, 0, d->st>>>(a, sys, wsys, nwarps, flag, fw, fcnt);
 	else
-		k_build_tiles_batch<<<grid_for(nwarps, BT_WARPS), BT_WARPS * 32, 0, d->st>>>(a, sys, wsys, nwarps, flag);
+		k_build_tiles_batch<<<grid_for(nwarps, BT_WARPS), BT_WARPS * 32, 0, d->st>>>(a, sys, wsys, nwarps, flag,
+											     NULL, NULL);
 	CKL(d);
 	return SEPDEV_OK;
 }
