@@ -165,6 +165,39 @@ def test_tabulated_user_potential(gpu_lib, ora):
     h.close()
 
 
+def test_butane_lists_one_and_two_lanes_per_bead(gpu_lib, tmp_path):
+    """the same-molecule list build with one lane per bead and with two (the
+    team size of the system's class): the same pair set, and forces at the
+    reference's bar either way"""
+    from seplib_gb300 import Tuning, tune
+    old = Tuning()
+    gpu_lib.sep_gpu_get_tuning(C.byref(old))
+    g = gold("butane_small")
+    got = {}
+    try:
+        for team in (1, 2):
+            tune.apply(gpu_lib, [], [(team, 2, 1.0)])
+            s, h = load_butane(gpu_lib, g, tmp_path)
+            lib = gpu_lib
+            lib.sep_reset_retval(C.byref(h.ret))
+            lib.sep_reset_force(h.atoms, C.byref(h.sys))
+            lib.sep_force_pairs(h.atoms, b"CC", 2.5, h.fun(), C.byref(h.sys), C.byref(h.ret),
+                                A.SEP_EXCL_SAME_MOL)
+            lib.sep_stretch_harmonic(h.atoms, 0, 0.4, 33615.0, C.byref(h.sys), C.byref(h.ret))
+            lib.sep_angle_harmonic(h.atoms, 0, 1.9, 866.0, C.byref(h.sys), C.byref(h.ret))
+            lib.sep_torsion_Ryckaert(h.atoms, 0, (C.c_double * 6)(*RB), C.byref(h.sys), C.byref(h.ret))
+            h.sync()
+            got[team] = (pairset(gpu_pairs(lib, h.atoms, 400000)), h.view["f"].copy(), h.ret.epot)
+            h.close()
+    finally:
+        assert gpu_lib.sep_gpu_set_tuning(C.byref(old)) == 0
+    assert got[1][0] == got[2][0]
+    e = float(g["e_all"])
+    for team in (1, 2):
+        assert rel_l2(got[team][1], g["f_all"]) < 1e-5
+        assert abs(got[team][2] - e) < 1e-5 * abs(e)
+
+
 def test_butane_nvt_trajectory(gpu_lib, ora, tmp_path):
     """ten steps of the butane loop (prgs/prg2.c order) against the oracle"""
     g = gold("butane_small")
