@@ -45,6 +45,34 @@ def test_pair_set_matches_fp64(gpu_lib, ora):
     h.close()
 
 
+@pytest.mark.parametrize("ncell,rho,team", [(5, 0.85, 1), (6, 0.75, 2), (7, 0.9, 1), (9, 0.8442, 2),
+                                            (11, 0.8442, 1)])
+def test_pair_set_small_boxes(gpu_lib, ora, ncell, rho, team):
+    """boxes of 2 to 6 list cells a side, where a tile's staged region wraps
+    around the box (the periodic bounding-box prefilter and the
+    minimum-image test loops), with one and with two lanes per particle in
+    the build: the FP64 pair set within rc + skin, boundary pairs aside"""
+    from seplib_gb300 import Tuning, tune
+    old = Tuning()
+    gpu_lib.sep_gpu_get_tuning(C.byref(old))
+    try:
+        tune.apply(gpu_lib, [], [(team, 2, 1.0)])
+        s = cfg.plain_lj_large(ncell=ncell, seed=11, rho=rho)
+        s.x = np.mod(s.x + np.random.default_rng(ncell).normal(0, 0.08, s.x.shape), s.L)
+        h = Handle(gpu_lib, s, skin=0.3)
+        h.forces()
+        got = gpu_pairs(gpu_lib, h.atoms, 100 * s.n)
+        h.close()
+    finally:
+        assert gpu_lib.sep_gpu_set_tuning(C.byref(old)) == 0
+    assert 2 <= int(s.L[0] // 2.8) <= 6
+    ref = ora.pairs_brute(s.x, s.L, 2.8)
+    near = boundary_mask(s.x, s.L, ref, 2.8)
+    assert pairset(ref[~near]) - pairset(got) == set()
+    extra = pairset(got) - pairset(ref)
+    assert extra <= pairset(got[boundary_mask(s.x, s.L, got, 2.8)])
+
+
 def test_single_step_forces(gpu_lib, ora):
     s = small()
     # perturb the lattice so forces are not all zero
