@@ -87,17 +87,27 @@ def cluster_system(seed=17):
     return cfg.System(x=x, v=np.zeros((n, 3)), L=L, types=np.full(n, b"A", "S1"), m=np.ones(n), z=np.zeros(n))
 
 
-def test_list_overflow_in_a_step(gpu_lib, ora):
+@pytest.mark.parametrize("team", [1, 2])
+def test_list_overflow_in_a_step(gpu_lib, ora, team):
     """The list is built without waiting for its capacity check; a fused step
     on a list that overflowed does nothing, and sep_leapfrog grows the list
     and runs the step again: one step from the cluster system against the
-    FP64 oracle's step."""
+    FP64 oracle's step, with one and with two lanes per particle in the step
+    and the build."""
+    from seplib_gb300 import Tuning, tune
+    old = Tuning()
+    gpu_lib.sep_gpu_get_tuning(C.byref(old))
     s = cluster_system()
-    h = Handle(gpu_lib, s, skin=0.3)
-    h.step()
-    h.sync()
+    try:
+        tune.apply(gpu_lib, [], [(team, 2, 1.0)])
+        h = Handle(gpu_lib, s, skin=0.3)
+        h.step()
+        h.sync()
+    finally:
+        assert gpu_lib.sep_gpu_set_tuning(C.byref(old)) == 0
     info = seplib_gb300.GpuInfo()
     gpu_lib.sep_gpu_info_get(h.atoms, C.byref(info))
+    assert info.team == team
     est = 1.35 * 4.18879020479 * 2.8 ** 3 * s.n / np.prod(s.L) + 32
     assert info.list_max > est and info.list_capacity >= info.list_max
     r = ora.run_lj(s.x, s.v, s.m, s.types, s.L, ora.POT_LJSHIFT, None, 2.5, 0.3, 0.005, 1)
