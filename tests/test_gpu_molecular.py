@@ -273,31 +273,40 @@ def test_butane_full_size_forces(gpu_lib, ora, tmp_path):
     h.close()
 
 
-def test_butane_full_size_nvt_trajectory(gpu_lib, ora, tmp_path):
+@pytest.mark.parametrize("team", [1, 2])
+def test_butane_full_size_nvt_trajectory(gpu_lib, ora, tmp_path, team):
     """the molecular workload at full size (8000 butane chains, 32000 beads)
     over 20 steps of the prgs/prg2.c loop, list rebuilds included, against
-    the same call sequence in FP64"""
+    the same call sequence in FP64; with one lane per bead and with two (the
+    autotuner's choice for this size) in the step and the list build"""
+    from seplib_gb300 import Tuning, tune
+    old = Tuning()
+    gpu_lib.sep_gpu_get_tuning(C.byref(old))
     s = cfg.butane(nmol=8000, rho=0.6, seed=3)
     s.x = np.mod(s.x + np.random.default_rng(17).normal(0, 0.02, s.x.shape), s.L)
     top = tmp_path / "b8000.top"
     cfg.write_top(str(top), s)
-    h = Handle(gpu_lib, s, update=A.SEP_LLIST_NEIGHBLIST, dt=0.002)
     lib = gpu_lib
-    lib.sep_read_topology_file(h.atoms, str(top).encode(), C.byref(h.sys), b"q")
-    mol = h.view["molindex"].copy()
     rb = (C.c_double * 6)(*RB)
     nsteps = 20
-    for _ in range(nsteps):
-        lib.sep_reset_retval(C.byref(h.ret))
-        lib.sep_reset_force(h.atoms, C.byref(h.sys))
-        lib.sep_force_pairs(h.atoms, b"CC", 2.5, h.fun(), C.byref(h.sys), C.byref(h.ret),
-                            A.SEP_EXCL_SAME_MOL)
-        lib.sep_stretch_harmonic(h.atoms, 0, 0.4, 33615.0, C.byref(h.sys), C.byref(h.ret))
-        lib.sep_angle_harmonic(h.atoms, 0, 1.9, 866.0, C.byref(h.sys), C.byref(h.ret))
-        lib.sep_torsion_Ryckaert(h.atoms, 0, rb, C.byref(h.sys), C.byref(h.ret))
-        lib.sep_nosehoover(h.atoms, 4.0, C.byref(h.alpha), 0.1, C.byref(h.sys))
-        lib.sep_leapfrog(h.atoms, C.byref(h.sys), C.byref(h.ret))
-    h.sync()
+    try:
+        tune.apply(gpu_lib, [], [(team, 2, 1.0)])
+        h = Handle(gpu_lib, s, update=A.SEP_LLIST_NEIGHBLIST, dt=0.002)
+        lib.sep_read_topology_file(h.atoms, str(top).encode(), C.byref(h.sys), b"q")
+        mol = h.view["molindex"].copy()
+        for _ in range(nsteps):
+            lib.sep_reset_retval(C.byref(h.ret))
+            lib.sep_reset_force(h.atoms, C.byref(h.sys))
+            lib.sep_force_pairs(h.atoms, b"CC", 2.5, h.fun(), C.byref(h.sys), C.byref(h.ret),
+                                A.SEP_EXCL_SAME_MOL)
+            lib.sep_stretch_harmonic(h.atoms, 0, 0.4, 33615.0, C.byref(h.sys), C.byref(h.ret))
+            lib.sep_angle_harmonic(h.atoms, 0, 1.9, 866.0, C.byref(h.sys), C.byref(h.ret))
+            lib.sep_torsion_Ryckaert(h.atoms, 0, rb, C.byref(h.sys), C.byref(h.ret))
+            lib.sep_nosehoover(h.atoms, 4.0, C.byref(h.alpha), 0.1, C.byref(h.sys))
+            lib.sep_leapfrog(h.atoms, C.byref(h.sys), C.byref(h.ret))
+        h.sync()
+    finally:
+        assert gpu_lib.sep_gpu_set_tuning(C.byref(old)) == 0
     st = ora.LeapState(s.x, s.v, s.m)
     alpha = 0.0
     nsub = [ora.nsubbox(2.5, 0.25, s.L[k]) for k in range(3)]
