@@ -266,7 +266,9 @@ def run_reference(args, rank, world):
         return
     s = configs.plain_lj_large(args.ncell, seed=2)
     threads = os.cpu_count() or 1
-    steps = max(1, args.cpu_steps or max(3, min(args.steps, 40)))
+    # the K timed steps of the GPU arm's run, at most 400 (about 30 s on the
+    # host cores at ~75 ms per step of the full system)
+    steps = max(1, args.cpu_steps or min(args.steps, 400))
     cpu_leg(s, max(1, args.warmup // 100), threads)        # warm-up (page-in, thread pool)
     val, el = cpu_leg(s, steps, threads)
     line = {"metric": "particle-steps/s", "value": val, "unit": "particle-steps/s", "n_gpus": 0,
